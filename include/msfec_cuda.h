@@ -1,0 +1,192 @@
+/*
+ * msfec_cuda.h - C ABI of the GB300 (sm_103a) MsFEC multiscale basis builder.
+ *
+ * One call builds, for a batch of coarse hexahedral cells, the multiscale
+ * basis (all coarse-basis right-hand sides of every cell solved at once) and
+ * the coarse Galerkin element matrix K_H = Phi^T K Phi and load F_H = Phi^T f.
+ * It replaces the per-cell basis objects of konsim83/MPI-MSFEC:
+ *
+ *   Q::QBasis            include/Q/q_basis.h:62-305, source/Q/q_basis.cc
+ *   NedRT::NedRTBasis    include/Ned_RT/ned_rt_basis.h:81-348,
+ *                        source/Ned_RT/ned_rt_basis.cc
+ *
+ * Conventions (identical for every entry point):
+ *  - Coarse cells are axis-aligned boxes msfec_cell{origin, size, depth};
+ *    the local problem lives on the depth-times uniformly refined box
+ *    (reference QBasis::make_grid, q_basis.cc:95-102: general_cell +
+ *    refine_global(n_refine_local)), n = 2^depth fine cells per edge.
+ *  - Fine-cell arrays: per coarse cell n^3 values, lexicographic (x fastest),
+ *    concatenated over the batch in batch order.
+ *  - Coarse numbering follows deal.II GeometryInfo<3>: vertex v = x + 2y + 4z;
+ *    K_H is row-major [cell][test][trial].
+ *  - Q1 basis Phi: per cell 8 planes (one per coarse vertex) of (n+1)^3 nodal
+ *    values, node = i + (n+1)(j + (n+1)k).
+ *  - Every call returns msfec_status; nothing aborts or traps. Per-cell
+ *    convergence is reported in msfec_cell_report.
+ *  - A handle owns its device buffers and one CUDA stream; it is not
+ *    thread-safe. Host-buffer entry points are synchronous; *_device entry
+ *    points are asynchronous on the handle's stream.
+ */
+#ifndef MSFEC_CUDA_H
+#define MSFEC_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum msfec_status {
+  MSFEC_SUCCESS = 0,
+  MSFEC_ERROR_INVALID_ARGUMENT = 1,
+  MSFEC_ERROR_CUDA = 2,
+  MSFEC_ERROR_OUT_OF_MEMORY = 3,
+  /* A local solve missed its tolerance; outputs are written, see reports.
+     Replaces deal.II's SolverControl::NoConvergence (q_basis.cc:337). */
+  MSFEC_ERROR_NOT_CONVERGED = 4,
+  MSFEC_ERROR_NOT_SUPPORTED = 5,
+  /* NaN/Inf or non-positive coefficient in the input. */
+  MSFEC_ERROR_NUMERICAL = 6,
+  /* Call order violated (e.g. basis requested before any build). */
+  MSFEC_ERROR_INVALID_STATE = 7
+} msfec_status;
+
+typedef enum msfec_precision {
+  /* Plain FP64 PCG for every local solve. */
+  MSFEC_PRECISION_FP64 = 0,
+  /* FP32 PCG inner solves wrapped in FP64 iterative refinement. */
+  MSFEC_PRECISION_MIXED = 1
+} msfec_precision;
+
+/* Load f(x) of the local problems; evaluated on the device at the 2x2x2
+   Gauss points of every fine cell, like the reference's RightHandSideParsed
+   (source/equation_data/eqn_rhs.cc:57-106) at QGauss<3>(2) points. */
+typedef enum msfec_load_kind {
+  MSFEC_LOAD_ZERO = 0,
+  MSFEC_LOAD_CONSTANT = 1,    /* f = p0 */
+  MSFEC_LOAD_SIN_PRODUCT = 2  /* f = p0 sin(p1 pi x) sin(p1 pi y) sin(p1 pi z) */
+} msfec_load_kind;
+
+typedef struct msfec_load {
+  int32_t kind; /* msfec_load_kind */
+  int32_t reserved;
+  double params[4];
+} msfec_load;
+
+typedef struct msfec_config {
+  int32_t device;     /* CUDA device ordinal */
+  int32_t precision;  /* msfec_precision */
+  /* Local solve stops when ||r||_2 <= rtol * ||K_IB g||_2 (the residual norm
+     the reference's zero initial guess starts from), per right-hand side. */
+  double rtol;
+  /* MIXED only: relative residual reduction of each FP32 inner solve. */
+  double inner_rtol;
+  int32_t max_iter;    /* Krylov iterations per inner solve */
+  int32_t max_refine;  /* MIXED: FP64 refinement steps; FP64: verification rounds */
+  int32_t verbose;
+  int32_t reserved;
+} msfec_config;
+
+typedef struct msfec_cell {
+  double origin[3];
+  double size[3];
+  int32_t depth; /* local refinement levels, 1..5 */
+  int32_t reserved;
+} msfec_cell;
+
+typedef struct msfec_cell_report {
+  int32_t iterations;  /* Krylov iterations summed over refinement steps, max over RHS */
+  int32_t refinements; /* FP64 residual evaluations */
+  int32_t converged;   /* 1 if every RHS of the cell met rtol */
+  int32_t reserved;
+  double residual;     /* max over RHS of ||r||_2 / ||K_IB g||_2 */
+} msfec_cell_report;
+
+typedef struct msfec_handle msfec_handle;
+
+/* Fills cfg with defaults: device 0, MIXED, rtol 1e-12, inner_rtol 1e-5,
+   max_iter 2000, max_refine 6. */
+void msfec_config_default(msfec_config *cfg);
+
+msfec_status msfec_create(msfec_handle **handle, const msfec_config *cfg);
+void msfec_destroy(msfec_handle *handle);
+const char *msfec_status_string(msfec_status status);
+/* Text of the last error seen by this handle (CUDA error or argument check). */
+const char *msfec_last_error(const msfec_handle *handle);
+
+/* Use an external CUDA stream (cudaStream_t passed as void*) for all work of
+   this handle; NULL restores the handle's own stream. */
+msfec_status msfec_set_stream(msfec_handle *handle, void *stream);
+msfec_status msfec_set_precision(msfec_handle *handle, int32_t precision);
+
+/*
+ * Q1 basis build from host buffers (synchronous).
+ * Replaces QBasis::run (q_basis.cc:518-603) for every cell of the batch,
+ * followed by get_global_element_matrix / get_global_element_rhs
+ * (q_basis.cc:361-373).
+ *   a        diffusion coefficient per fine cell (> 0), FP64
+ *   reaction reaction coefficient per fine cell, or NULL for none (the
+ *            reference's ReactionRate is zero, eqn_coeff_R.cc:7-14)
+ *   KH       [ncells][8][8], FH [ncells][8], reports [ncells] or NULL
+ * The basis stays on the device until the next build (msfec_q1_get_basis).
+ */
+msfec_status msfec_q1_build(msfec_handle *handle, int32_t ncells,
+                            const msfec_cell *cells, const double *a,
+                            const double *reaction, const msfec_load *load,
+                            double *KH, double *FH, msfec_cell_report *reports);
+
+/*
+ * Same as msfec_q1_build with every array in device memory; asynchronous on
+ * the handle's stream. cells is a HOST array (it sizes the work queue).
+ */
+msfec_status msfec_q1_build_device(msfec_handle *handle, int32_t ncells,
+                                   const msfec_cell *cells, const double *d_a,
+                                   const double *d_reaction,
+                                   const msfec_load *load, double *d_KH,
+                                   double *d_FH, msfec_cell_report *d_reports);
+
+/* Per-phase device time of the last build, measured with CUDA events on the
+   handle's stream when timing is enabled (the reference's TimerOutput scopes,
+   source/Q/q_global.cc:21-24). Milliseconds; -1 when not measured. */
+typedef struct msfec_timings {
+  float solve_ms;    /* persistent local-solver kernel */
+  float galerkin_ms; /* Phi^T K Phi / Phi^T f contraction */
+  float total_ms;    /* whole build on the device, H2D/D2H excluded */
+  int32_t solve_launches;
+  int32_t kernel_launches; /* kernels this build launched */
+} msfec_timings;
+
+msfec_status msfec_set_timing(msfec_handle *handle, int32_t enable);
+/* Synchronises the handle's stream. */
+msfec_status msfec_get_timings(msfec_handle *handle, msfec_timings *out);
+
+/* Number of doubles of the last Q1 build's basis (sum over cells of
+   8 (n+1)^3), or 0 if none. */
+int64_t msfec_q1_basis_size(const msfec_handle *handle);
+
+/* Copy the last Q1 build's basis to host memory (capacity in doubles). */
+msfec_status msfec_q1_get_basis(msfec_handle *handle, double *Phi,
+                                int64_t capacity);
+
+/* Device pointer of the last Q1 build's basis (read-only, valid until the
+   next build on this handle). */
+const double *msfec_q1_basis_device(const msfec_handle *handle);
+
+/*
+ * Fine-scale reconstruction u = sum_v U_v phi_v of the last Q1 build,
+ * evaluated at points (reference QBasis::set_global_weights,
+ * q_basis.cc:394-416, which forms the same combination on the fine mesh).
+ *   weights  [ncells][8] coarse weights U of every cell of the last build
+ *   cell_of  [npoints] batch index of the cell containing each point
+ *   points   [npoints][3], values [npoints]
+ * Host buffers, synchronous.
+ */
+msfec_status msfec_q1_eval_fine(msfec_handle *handle, const double *weights,
+                                int32_t npoints, const int32_t *cell_of,
+                                const double *points, double *values);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MSFEC_CUDA_H */

@@ -1,0 +1,543 @@
+// C ABI of libmsfec_cuda.so (declared in include/msfec_cuda.h).
+//
+// Host-side job planning for the persistent Q1 kernel: one item per
+// (coarse cell, group of coarse vertices), deep cells split into z-slabs over
+// the CTAs of a thread-block cluster, items sorted deepest first (longest
+// processing time first) so the device work queue ends without a tail.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/msfec_cuda.h"
+#include "q1_common.cuh"
+
+namespace msfec {
+cudaError_t q1_solve_launch_f32_c1(bool has_r, const Q1Params &prm, size_t smem, int grid, cudaStream_t st);
+cudaError_t q1_solve_launch_f32_c8(bool has_r, const Q1Params &prm, size_t smem, int grid, cudaStream_t st);
+cudaError_t q1_solve_launch_f64_c1(bool has_r, const Q1Params &prm, size_t smem, int grid, cudaStream_t st);
+cudaError_t q1_solve_launch_f64_c8(bool has_r, const Q1Params &prm, size_t smem, int grid, cudaStream_t st);
+cudaError_t q1_solve_occupancy_f32_c1(bool has_r, size_t smem, int *out);
+cudaError_t q1_solve_occupancy_f32_c8(bool has_r, size_t smem, int *out);
+cudaError_t q1_solve_occupancy_f64_c1(bool has_r, size_t smem, int *out);
+cudaError_t q1_solve_occupancy_f64_c8(bool has_r, size_t smem, int *out);
+
+static cudaError_t q1_solve_launch(bool fp64, int cluster, bool has_r, const Q1Params &prm, size_t smem, int grid,
+                                   cudaStream_t st) {
+  if (fp64)
+    return cluster > 1 ? q1_solve_launch_f64_c8(has_r, prm, smem, grid, st)
+                       : q1_solve_launch_f64_c1(has_r, prm, smem, grid, st);
+  return cluster > 1 ? q1_solve_launch_f32_c8(has_r, prm, smem, grid, st)
+                     : q1_solve_launch_f32_c1(has_r, prm, smem, grid, st);
+}
+static cudaError_t q1_solve_occupancy(bool fp64, int cluster, bool has_r, size_t smem, int *out) {
+  if (fp64)
+    return cluster > 1 ? q1_solve_occupancy_f64_c8(has_r, smem, out) : q1_solve_occupancy_f64_c1(has_r, smem, out);
+  return cluster > 1 ? q1_solve_occupancy_f32_c8(has_r, smem, out) : q1_solve_occupancy_f32_c1(has_r, smem, out);
+}
+cudaError_t q1_galerkin_launch(const Q1Cell *cells, int ncells, const double *phi, const double *y,
+                               const msfec_load &load, double *KH, double *FH, cudaStream_t stream);
+cudaError_t q1_report_launch(const Q1Stat *stats, int ncells, msfec_cell_report *rep, cudaStream_t stream);
+cudaError_t q1_eval_launch(const Q1Cell *cells, const double *phi, const double *weights, int npoints,
+                           const int *cell_of, const double *pts, double *out, cudaStream_t stream);
+}  // namespace msfec
+
+using namespace msfec;
+
+namespace {
+
+template <typename T>
+struct DevBuf {
+  T *ptr = nullptr;
+  size_t cap = 0;  // elements
+  cudaError_t reserve(size_t count) {
+    if (count <= cap) return cudaSuccess;
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+    const size_t want = std::max<size_t>(count, 1);
+    cudaError_t e = cudaMalloc(&ptr, want * sizeof(T));
+    if (e == cudaSuccess) cap = want;
+    return e;
+  }
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+  }
+};
+
+constexpr int kCluster = 8;
+constexpr int kMaxDepth = 5;
+
+}  // namespace
+
+struct msfec_handle {
+  int device = 0;
+  msfec_config cfg;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  int num_sms = 0;
+  size_t max_smem_optin = 0;
+  std::string last_error;
+  // Q1 state of the last build
+  DevBuf<Q1Cell> cells;
+  DevBuf<Q1Item> items;
+  DevBuf<Q1Unit> units;
+  DevBuf<int> queue;
+  DevBuf<double> phi, y;
+  DevBuf<Q1Stat> stats;
+  // host-API staging
+  DevBuf<double> a, react, KH, FH;
+  DevBuf<msfec_cell_report> rep;
+  DevBuf<double> eval_w, eval_pts, eval_out;
+  DevBuf<int> eval_cell;
+  int q1_ncells = 0;
+  int64_t q1_basis_doubles = 0;
+  std::vector<Q1Cell> h_cells;
+  // per-phase timing (CUDA events on the handle's stream)
+  bool timing = false;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  bool ev_recorded = false;
+  int last_launches = 0;
+};
+
+namespace {
+
+msfec_status fail(msfec_handle *h, msfec_status s, const std::string &msg) {
+  if (h) h->last_error = msg;
+  return s;
+}
+
+msfec_status cuda_fail(msfec_handle *h, cudaError_t e, const char *where) {
+  std::string msg = std::string(where) + ": " + cudaGetErrorString(e);
+  return fail(h, e == cudaErrorMemoryAllocation ? MSFEC_ERROR_OUT_OF_MEMORY : MSFEC_ERROR_CUDA, msg);
+}
+
+#define MSFEC_CUDA_TRY(h, call)                          \
+  do {                                                   \
+    cudaError_t e__ = (call);                            \
+    if (e__ != cudaSuccess) return cuda_fail(h, e__, #call); \
+  } while (0)
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
+bool cell_ok(const msfec_cell &c) {
+  if (c.depth < 1 || c.depth > kMaxDepth) return false;
+  for (int d = 0; d < 3; ++d) {
+    if (!std::isfinite(c.origin[d]) || !std::isfinite(c.size[d]) || !(c.size[d] > 0.0)) return false;
+  }
+  return true;
+}
+
+bool load_ok(const msfec_load *l) {
+  if (!l) return true;
+  if (l->kind < MSFEC_LOAD_ZERO || l->kind > MSFEC_LOAD_SIN_PRODUCT) return false;
+  for (int i = 0; i < 4; ++i)
+    if (!std::isfinite(l->params[i])) return false;
+  return true;
+}
+
+struct Q1Plan {
+  std::vector<Q1Cell> cells;
+  std::vector<Q1Item> items;
+  std::vector<Q1Unit> units;
+  int cluster = 1;
+  size_t smem = 0;
+  int64_t nodes = 0;   // sum (n+1)^3
+  int64_t fine = 0;    // sum n^3
+};
+
+// Items per cell depth. Mixed precision: shallow cells (all 8 RHS in one
+// CTA), depth 4 in 4 CTAs x 2 RHS, depth 5 as 8 z-slab items of 1 RHS each
+// (cluster of 8). Plain FP64 (twice the register/shared footprint): depth 4
+// and 5 as z-slab items.
+void plan_items(int depth, bool fp64, int &nitems, int &nrhs, bool &slab) {
+  if (depth <= 3) {
+    nitems = 1;
+    nrhs = 8;
+    slab = false;
+  } else if (depth == 4) {
+    nitems = 4;
+    nrhs = 2;
+    slab = fp64;
+  } else {
+    nitems = 8;
+    nrhs = 1;
+    slab = true;
+  }
+}
+
+Q1Plan make_q1_plan(int ncells, const msfec_cell *cells, bool fp64, bool has_r) {
+  Q1Plan p;
+  p.cells.resize(ncells);
+  for (int c = 0; c < ncells; ++c) {
+    Q1Cell &q = p.cells[c];
+    const int n = 1 << cells[c].depth;
+    for (int d = 0; d < 3; ++d) {
+      q.origin[d] = cells[c].origin[d];
+      q.h[d] = cells[c].size[d] / n;
+    }
+    q.depth = cells[c].depth;
+    q.n = n;
+    q.coef_off = p.fine;
+    q.node_off = p.nodes;
+    p.fine += (int64_t)n * n * n;
+    p.nodes += (int64_t)(n + 1) * (n + 1) * (n + 1);
+  }
+  // cells ordered deepest first (stable), items in that order
+  std::vector<int> order(ncells);
+  for (int c = 0; c < ncells; ++c) order[c] = c;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cells[x].depth > cells[y].depth; });
+  bool any_slab = false;
+  for (int c : order) {
+    int ni, nr;
+    bool slab;
+    plan_items(cells[c].depth, fp64, ni, nr, slab);
+    any_slab = any_slab || slab;
+    for (int t = 0; t < ni; ++t) p.items.push_back(Q1Item{c, t * nr, nr, slab ? 1 : 0});
+  }
+  p.cluster = any_slab ? kCluster : 1;
+  // units: slab items alone; independent items grouped by `cluster` (same depth)
+  size_t i = 0;
+  while (i < p.items.size()) {
+    if (p.items[i].slab) {
+      p.units.push_back(Q1Unit{(int)i, 1, 1, 0});
+      ++i;
+      continue;
+    }
+    const int depth = cells[p.items[i].cell].depth;
+    size_t j = i;
+    while (j < p.items.size() && (int)(j - i) < p.cluster && !p.items[j].slab &&
+           cells[p.items[j].cell].depth == depth)
+      ++j;
+    p.units.push_back(Q1Unit{(int)i, (int)(j - i), 0, 0});
+    i = j;
+  }
+  for (const Q1Item &it : p.items) {
+    const int n = 1 << cells[it.cell].depth;
+    const Q1Smem L = q1_smem_layout(n, it.nrhs, it.slab ? p.cluster : 1, has_r, fp64 ? 8 : 4);
+    p.smem = std::max(p.smem, L.total);
+  }
+  return p;
+}
+
+msfec_status q1_build_impl(msfec_handle *h, int ncells, const msfec_cell *cells, const double *d_a,
+                           const double *d_react, const msfec_load *load, double *d_KH, double *d_FH,
+                           msfec_cell_report *d_rep) {
+  const bool fp64 = h->cfg.precision == MSFEC_PRECISION_FP64;
+  const bool has_r = d_react != nullptr;
+  Q1Plan plan = make_q1_plan(ncells, cells, fp64, has_r);
+  if (plan.smem + 8192 > h->max_smem_optin)
+    return fail(h, MSFEC_ERROR_NOT_SUPPORTED, "shared memory plan exceeds the device limit");
+  cudaStream_t st = h->stream;
+  MSFEC_CUDA_TRY(h, h->cells.reserve(plan.cells.size()));
+  MSFEC_CUDA_TRY(h, h->items.reserve(plan.items.size()));
+  MSFEC_CUDA_TRY(h, h->units.reserve(plan.units.size()));
+  MSFEC_CUDA_TRY(h, h->queue.reserve(1));
+  MSFEC_CUDA_TRY(h, h->phi.reserve((size_t)plan.nodes * 8));
+  MSFEC_CUDA_TRY(h, h->y.reserve((size_t)plan.nodes * 8));
+  MSFEC_CUDA_TRY(h, h->stats.reserve((size_t)ncells * 8));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->cells.ptr, plan.cells.data(), plan.cells.size() * sizeof(Q1Cell),
+                                    cudaMemcpyHostToDevice, st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->items.ptr, plan.items.data(), plan.items.size() * sizeof(Q1Item),
+                                    cudaMemcpyHostToDevice, st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->units.ptr, plan.units.data(), plan.units.size() * sizeof(Q1Unit),
+                                    cudaMemcpyHostToDevice, st));
+  MSFEC_CUDA_TRY(h, cudaMemsetAsync(h->queue.ptr, 0, sizeof(int), st));
+  Q1Params prm;
+  prm.cells = h->cells.ptr;
+  prm.items = h->items.ptr;
+  prm.units = h->units.ptr;
+  prm.n_units = (int)plan.units.size();
+  prm.queue = h->queue.ptr;
+  prm.a = d_a;
+  prm.react = d_react;
+  prm.phi = h->phi.ptr;
+  prm.y = h->y.ptr;
+  prm.stats = h->stats.ptr;
+  prm.rtol = h->cfg.rtol;
+  prm.inner_rtol = h->cfg.inner_rtol;
+  prm.max_iter = h->cfg.max_iter;
+  prm.max_refine = h->cfg.max_refine;
+  int occ = 0;
+  MSFEC_CUDA_TRY(h, q1_solve_occupancy(fp64, plan.cluster, has_r, plan.smem, &occ));
+  if (occ <= 0) return fail(h, MSFEC_ERROR_NOT_SUPPORTED, "local solver kernel cannot be resident");
+  int grid;
+  if (plan.cluster > 1) {
+    const int nclusters = std::min<int>((int)plan.units.size(), occ);
+    grid = nclusters * plan.cluster;
+  } else {
+    grid = std::min<int>((int)plan.units.size(), occ * h->num_sms);
+  }
+  grid = std::max(grid, plan.cluster);
+  if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[0], st));
+  MSFEC_CUDA_TRY(h, q1_solve_launch(fp64, plan.cluster, has_r, prm, plan.smem, grid, st));
+  if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[1], st));
+  msfec_load ld;
+  if (load) {
+    ld = *load;
+  } else {
+    std::memset(&ld, 0, sizeof(ld));
+  }
+  MSFEC_CUDA_TRY(h, q1_galerkin_launch(h->cells.ptr, ncells, h->phi.ptr, h->y.ptr, ld, d_KH, d_FH, st));
+  if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[2], st));
+  if (d_rep) MSFEC_CUDA_TRY(h, q1_report_launch(h->stats.ptr, ncells, d_rep, st));
+  if (h->timing) {
+    MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[3], st));
+    h->ev_recorded = true;
+  }
+  h->last_launches = d_rep ? 3 : 2;
+  h->q1_ncells = ncells;
+  h->q1_basis_doubles = plan.nodes * 8;
+  h->h_cells = plan.cells;
+  return MSFEC_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" {
+
+void msfec_config_default(msfec_config *cfg) {
+  if (!cfg) return;
+  std::memset(cfg, 0, sizeof(*cfg));
+  cfg->device = 0;
+  cfg->precision = MSFEC_PRECISION_MIXED;
+  cfg->rtol = 1e-12;
+  cfg->inner_rtol = 1e-5;
+  cfg->max_iter = 2000;
+  cfg->max_refine = 6;
+  cfg->verbose = 0;
+}
+
+const char *msfec_status_string(msfec_status s) {
+  switch (s) {
+    case MSFEC_SUCCESS: return "success";
+    case MSFEC_ERROR_INVALID_ARGUMENT: return "invalid argument";
+    case MSFEC_ERROR_CUDA: return "CUDA error";
+    case MSFEC_ERROR_OUT_OF_MEMORY: return "out of device memory";
+    case MSFEC_ERROR_NOT_CONVERGED: return "local solve did not converge";
+    case MSFEC_ERROR_NOT_SUPPORTED: return "not supported";
+    case MSFEC_ERROR_NUMERICAL: return "non-finite or non-positive coefficient";
+    case MSFEC_ERROR_INVALID_STATE: return "invalid call order";
+  }
+  return "unknown status";
+}
+
+const char *msfec_last_error(const msfec_handle *h) { return h ? h->last_error.c_str() : "null handle"; }
+
+msfec_status msfec_create(msfec_handle **out, const msfec_config *cfg) {
+  if (!out) return MSFEC_ERROR_INVALID_ARGUMENT;
+  *out = nullptr;
+  msfec_config c;
+  if (cfg)
+    c = *cfg;
+  else
+    msfec_config_default(&c);
+  if (c.precision != MSFEC_PRECISION_FP64 && c.precision != MSFEC_PRECISION_MIXED) return MSFEC_ERROR_INVALID_ARGUMENT;
+  if (!(c.rtol > 0.0) || !(c.inner_rtol > 0.0) || c.inner_rtol >= 1.0 || c.max_iter < 1 || c.max_refine < 1)
+    return MSFEC_ERROR_INVALID_ARGUMENT;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || c.device < 0 || c.device >= ndev) return MSFEC_ERROR_CUDA;
+  msfec_handle *h = new msfec_handle();
+  h->device = c.device;
+  h->cfg = c;
+  DeviceGuard g(c.device);
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, c.device) != cudaSuccess || cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete h;
+    return MSFEC_ERROR_CUDA;
+  }
+  h->stream = h->own_stream;
+  h->num_sms = prop.multiProcessorCount;
+  h->max_smem_optin = prop.sharedMemPerBlockOptin;
+  *out = h;
+  return MSFEC_SUCCESS;
+}
+
+void msfec_destroy(msfec_handle *h) {
+  if (!h) return;
+  {
+    DeviceGuard g(h->device);
+    cudaStreamSynchronize(h->stream);
+    h->cells.release();
+    h->items.release();
+    h->units.release();
+    h->queue.release();
+    h->phi.release();
+    h->y.release();
+    h->stats.release();
+    h->a.release();
+    h->react.release();
+    h->KH.release();
+    h->FH.release();
+    h->rep.release();
+    h->eval_w.release();
+    h->eval_pts.release();
+    h->eval_out.release();
+    h->eval_cell.release();
+    for (auto &e : h->ev)
+      if (e) cudaEventDestroy(e);
+    if (h->own_stream) cudaStreamDestroy(h->own_stream);
+  }
+  delete h;
+}
+
+msfec_status msfec_set_stream(msfec_handle *h, void *stream) {
+  if (!h) return MSFEC_ERROR_INVALID_ARGUMENT;
+  h->stream = stream ? (cudaStream_t)stream : h->own_stream;
+  return MSFEC_SUCCESS;
+}
+
+msfec_status msfec_set_precision(msfec_handle *h, int32_t precision) {
+  if (!h || (precision != MSFEC_PRECISION_FP64 && precision != MSFEC_PRECISION_MIXED))
+    return MSFEC_ERROR_INVALID_ARGUMENT;
+  h->cfg.precision = precision;
+  return MSFEC_SUCCESS;
+}
+
+msfec_status msfec_q1_build_device(msfec_handle *h, int32_t ncells, const msfec_cell *cells, const double *d_a,
+                                   const double *d_reaction, const msfec_load *load, double *d_KH, double *d_FH,
+                                   msfec_cell_report *d_reports) {
+  if (!h) return MSFEC_ERROR_INVALID_ARGUMENT;
+  if (ncells < 0 || (ncells > 0 && (!cells || !d_a || !d_KH || !d_FH)))
+    return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "null pointer or negative cell count");
+  for (int c = 0; c < ncells; ++c)
+    if (!cell_ok(cells[c])) return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "cell " + std::to_string(c) + " invalid");
+  if (!load_ok(load)) return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "invalid load");
+  if (ncells == 0) {
+    h->q1_ncells = 0;
+    h->q1_basis_doubles = 0;
+    h->h_cells.clear();
+    return MSFEC_SUCCESS;
+  }
+  DeviceGuard g(h->device);
+  return q1_build_impl(h, ncells, cells, d_a, d_reaction, load, d_KH, d_FH, d_reports);
+}
+
+msfec_status msfec_q1_build(msfec_handle *h, int32_t ncells, const msfec_cell *cells, const double *a,
+                            const double *reaction, const msfec_load *load, double *KH, double *FH,
+                            msfec_cell_report *reports) {
+  if (!h) return MSFEC_ERROR_INVALID_ARGUMENT;
+  if (ncells < 0 || (ncells > 0 && (!cells || !a || !KH || !FH)))
+    return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "null pointer or negative cell count");
+  int64_t nfine = 0;
+  for (int c = 0; c < ncells; ++c) {
+    if (!cell_ok(cells[c])) return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "cell " + std::to_string(c) + " invalid");
+    const int64_t n = 1LL << cells[c].depth;
+    nfine += n * n * n;
+  }
+  if (!load_ok(load)) return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "invalid load");
+  for (int64_t e = 0; e < nfine; ++e) {
+    if (!(a[e] > 0.0) || !std::isfinite(a[e])) return fail(h, MSFEC_ERROR_NUMERICAL, "coefficient a not positive/finite");
+    if (reaction && (!(reaction[e] >= 0.0) || !std::isfinite(reaction[e])))
+      return fail(h, MSFEC_ERROR_NUMERICAL, "reaction coefficient negative or non-finite");
+  }
+  if (ncells == 0) return msfec_q1_build_device(h, 0, cells, nullptr, nullptr, load, nullptr, nullptr, nullptr);
+  DeviceGuard g(h->device);
+  cudaStream_t st = h->stream;
+  MSFEC_CUDA_TRY(h, h->a.reserve(nfine));
+  if (reaction) MSFEC_CUDA_TRY(h, h->react.reserve(nfine));
+  MSFEC_CUDA_TRY(h, h->KH.reserve((size_t)ncells * 64));
+  MSFEC_CUDA_TRY(h, h->FH.reserve((size_t)ncells * 8));
+  MSFEC_CUDA_TRY(h, h->rep.reserve(ncells));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->a.ptr, a, nfine * sizeof(double), cudaMemcpyHostToDevice, st));
+  if (reaction)
+    MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->react.ptr, reaction, nfine * sizeof(double), cudaMemcpyHostToDevice, st));
+  msfec_status s = q1_build_impl(h, ncells, cells, h->a.ptr, reaction ? h->react.ptr : nullptr, load, h->KH.ptr,
+                                 h->FH.ptr, h->rep.ptr);
+  if (s != MSFEC_SUCCESS) return s;
+  std::vector<msfec_cell_report> rep(ncells);
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(KH, h->KH.ptr, (size_t)ncells * 64 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(FH, h->FH.ptr, (size_t)ncells * 8 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(rep.data(), h->rep.ptr, (size_t)ncells * sizeof(msfec_cell_report),
+                                    cudaMemcpyDeviceToHost, st));
+  MSFEC_CUDA_TRY(h, cudaStreamSynchronize(st));
+  if (reports) std::memcpy(reports, rep.data(), rep.size() * sizeof(msfec_cell_report));
+  for (const auto &r : rep)
+    if (!r.converged) return fail(h, MSFEC_ERROR_NOT_CONVERGED, "at least one local solve missed rtol");
+  return MSFEC_SUCCESS;
+}
+
+msfec_status msfec_set_timing(msfec_handle *h, int32_t enable) {
+  if (!h) return MSFEC_ERROR_INVALID_ARGUMENT;
+  DeviceGuard g(h->device);
+  if (enable && !h->ev[0])
+    for (auto &e : h->ev) MSFEC_CUDA_TRY(h, cudaEventCreate(&e));
+  h->timing = enable != 0;
+  h->ev_recorded = false;
+  return MSFEC_SUCCESS;
+}
+
+msfec_status msfec_get_timings(msfec_handle *h, msfec_timings *out) {
+  if (!h || !out) return MSFEC_ERROR_INVALID_ARGUMENT;
+  out->solve_ms = out->galerkin_ms = out->total_ms = -1.0f;
+  out->solve_launches = h->ev_recorded ? 1 : 0;
+  out->kernel_launches = h->last_launches;
+  if (!h->ev_recorded) return MSFEC_SUCCESS;
+  DeviceGuard g(h->device);
+  MSFEC_CUDA_TRY(h, cudaEventSynchronize(h->ev[3]));
+  MSFEC_CUDA_TRY(h, cudaEventElapsedTime(&out->solve_ms, h->ev[0], h->ev[1]));
+  MSFEC_CUDA_TRY(h, cudaEventElapsedTime(&out->galerkin_ms, h->ev[1], h->ev[2]));
+  MSFEC_CUDA_TRY(h, cudaEventElapsedTime(&out->total_ms, h->ev[0], h->ev[3]));
+  return MSFEC_SUCCESS;
+}
+
+int64_t msfec_q1_basis_size(const msfec_handle *h) { return h ? h->q1_basis_doubles : 0; }
+
+const double *msfec_q1_basis_device(const msfec_handle *h) {
+  return (h && h->q1_basis_doubles > 0) ? h->phi.ptr : nullptr;
+}
+
+msfec_status msfec_q1_get_basis(msfec_handle *h, double *Phi, int64_t capacity) {
+  if (!h || !Phi) return MSFEC_ERROR_INVALID_ARGUMENT;
+  if (h->q1_basis_doubles <= 0) return fail(h, MSFEC_ERROR_INVALID_STATE, "no Q1 basis built yet");
+  if (capacity < h->q1_basis_doubles) return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "capacity too small");
+  DeviceGuard g(h->device);
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(Phi, h->phi.ptr, h->q1_basis_doubles * sizeof(double), cudaMemcpyDeviceToHost,
+                                    h->stream));
+  MSFEC_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  return MSFEC_SUCCESS;
+}
+
+msfec_status msfec_q1_eval_fine(msfec_handle *h, const double *weights, int32_t npoints, const int32_t *cell_of,
+                                const double *points, double *values) {
+  if (!h) return MSFEC_ERROR_INVALID_ARGUMENT;
+  if (h->q1_basis_doubles <= 0) return fail(h, MSFEC_ERROR_INVALID_STATE, "no Q1 basis built yet");
+  if (npoints < 0 || (npoints > 0 && (!weights || !cell_of || !points || !values)))
+    return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "null pointer or negative point count");
+  for (int p = 0; p < npoints; ++p)
+    if (cell_of[p] < 0 || cell_of[p] >= h->q1_ncells)
+      return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "cell_of out of range");
+  if (npoints == 0) return MSFEC_SUCCESS;
+  DeviceGuard g(h->device);
+  cudaStream_t st = h->stream;
+  MSFEC_CUDA_TRY(h, h->eval_w.reserve((size_t)h->q1_ncells * 8));
+  MSFEC_CUDA_TRY(h, h->eval_pts.reserve((size_t)npoints * 3));
+  MSFEC_CUDA_TRY(h, h->eval_out.reserve(npoints));
+  MSFEC_CUDA_TRY(h, h->eval_cell.reserve(npoints));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->eval_w.ptr, weights, (size_t)h->q1_ncells * 8 * sizeof(double),
+                                    cudaMemcpyHostToDevice, st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->eval_pts.ptr, points, (size_t)npoints * 3 * sizeof(double),
+                                    cudaMemcpyHostToDevice, st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->eval_cell.ptr, cell_of, (size_t)npoints * sizeof(int), cudaMemcpyHostToDevice, st));
+  MSFEC_CUDA_TRY(h, q1_eval_launch(h->cells.ptr, h->phi.ptr, h->eval_w.ptr, npoints, h->eval_cell.ptr,
+                                   h->eval_pts.ptr, h->eval_out.ptr, st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(values, h->eval_out.ptr, (size_t)npoints * sizeof(double), cudaMemcpyDeviceToHost, st));
+  MSFEC_CUDA_TRY(h, cudaStreamSynchronize(st));
+  return MSFEC_SUCCESS;
+}
+
+}  // extern "C"

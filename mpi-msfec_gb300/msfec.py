@@ -1,0 +1,256 @@
+"""ctypes binding of libmsfec_cuda.so (C ABI in include/msfec_cuda.h).
+
+Python-side view of the C ABI used by tests, the benchmark and
+``__graft_entry__``; the product interface for C++ callers is the header
+itself and the QBasis-compatible shim under host/. Loading fails loudly when
+the library has not been built: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libmsfec_cuda.so")
+
+SUCCESS = 0
+ERROR_INVALID_ARGUMENT = 1
+ERROR_CUDA = 2
+ERROR_OUT_OF_MEMORY = 3
+ERROR_NOT_CONVERGED = 4
+ERROR_NOT_SUPPORTED = 5
+ERROR_NUMERICAL = 6
+ERROR_INVALID_STATE = 7
+
+PRECISION_FP64 = 0
+PRECISION_MIXED = 1
+
+LOAD_ZERO, LOAD_CONSTANT, LOAD_SIN_PRODUCT = 0, 1, 2
+
+# Every symbol the public header declares (checked by the CPU test suite).
+EXPORTED = [
+    "msfec_config_default", "msfec_create", "msfec_destroy", "msfec_status_string",
+    "msfec_last_error", "msfec_set_stream", "msfec_set_precision", "msfec_q1_build",
+    "msfec_q1_build_device", "msfec_q1_basis_size", "msfec_q1_get_basis",
+    "msfec_q1_basis_device", "msfec_q1_eval_fine", "msfec_set_timing", "msfec_get_timings",
+]
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int32), ("precision", ctypes.c_int32), ("rtol", ctypes.c_double),
+                ("inner_rtol", ctypes.c_double), ("max_iter", ctypes.c_int32),
+                ("max_refine", ctypes.c_int32), ("verbose", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
+class Cell(ctypes.Structure):
+    _fields_ = [("origin", ctypes.c_double * 3), ("size", ctypes.c_double * 3),
+                ("depth", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class Load(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("params", ctypes.c_double * 4)]
+
+
+class CellReport(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int32), ("refinements", ctypes.c_int32),
+                ("converged", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("residual", ctypes.c_double)]
+
+
+class Timings(ctypes.Structure):
+    _fields_ = [("solve_ms", ctypes.c_float), ("galerkin_ms", ctypes.c_float),
+                ("total_ms", ctypes.c_float), ("solve_launches", ctypes.c_int32),
+                ("kernel_launches", ctypes.c_int32)]
+
+
+CELL_DTYPE = np.dtype([("origin", "<f8", (3,)), ("size", "<f8", (3,)), ("depth", "<i4"),
+                       ("reserved", "<i4")])
+REPORT_DTYPE = np.dtype([("iterations", "<i4"), ("refinements", "<i4"), ("converged", "<i4"),
+                         ("reserved", "<i4"), ("residual", "<f8")])
+assert CELL_DTYPE.itemsize == ctypes.sizeof(Cell)
+assert REPORT_DTYPE.itemsize == ctypes.sizeof(CellReport)
+
+_lib = None
+_vp = ctypes.c_void_p
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+def load_library(path: str = LIB_PATH):
+    """Load the CUDA library; raises if it is missing (build it first)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"libmsfec_cuda.so not built ({path}); run __graft_entry__.build()")
+    L = ctypes.CDLL(path)
+    L.msfec_config_default.argtypes = [ctypes.POINTER(Config)]
+    L.msfec_config_default.restype = None
+    L.msfec_create.argtypes = [ctypes.POINTER(_vp), ctypes.POINTER(Config)]
+    L.msfec_create.restype = ctypes.c_int
+    L.msfec_destroy.argtypes = [_vp]
+    L.msfec_destroy.restype = None
+    L.msfec_status_string.argtypes = [ctypes.c_int]
+    L.msfec_status_string.restype = ctypes.c_char_p
+    L.msfec_last_error.argtypes = [_vp]
+    L.msfec_last_error.restype = ctypes.c_char_p
+    L.msfec_set_stream.argtypes = [_vp, _vp]
+    L.msfec_set_stream.restype = ctypes.c_int
+    L.msfec_set_precision.argtypes = [_vp, ctypes.c_int32]
+    L.msfec_set_precision.restype = ctypes.c_int
+    L.msfec_q1_build.argtypes = [_vp, ctypes.c_int32, _vp, _dp, _dp, ctypes.POINTER(Load), _dp, _dp, _vp]
+    L.msfec_q1_build.restype = ctypes.c_int
+    L.msfec_q1_build_device.argtypes = [_vp, ctypes.c_int32, _vp, _vp, _vp, ctypes.POINTER(Load), _vp,
+                                        _vp, _vp]
+    L.msfec_q1_build_device.restype = ctypes.c_int
+    L.msfec_q1_basis_size.argtypes = [_vp]
+    L.msfec_q1_basis_size.restype = ctypes.c_int64
+    L.msfec_q1_get_basis.argtypes = [_vp, _dp, ctypes.c_int64]
+    L.msfec_q1_get_basis.restype = ctypes.c_int
+    L.msfec_q1_basis_device.argtypes = [_vp]
+    L.msfec_q1_basis_device.restype = _vp
+    L.msfec_q1_eval_fine.argtypes = [_vp, _dp, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32), _dp, _dp]
+    L.msfec_q1_eval_fine.restype = ctypes.c_int
+    L.msfec_set_timing.argtypes = [_vp, ctypes.c_int32]
+    L.msfec_set_timing.restype = ctypes.c_int
+    L.msfec_get_timings.argtypes = [_vp, ctypes.POINTER(Timings)]
+    L.msfec_get_timings.restype = ctypes.c_int
+    _lib = L
+    return L
+
+
+class MsfecError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"msfec status {status}: {msg}")
+        self.status = status
+
+
+def make_cells(origins, sizes, depths):
+    origins = np.asarray(origins, dtype=np.float64).reshape(-1, 3)
+    sizes = np.asarray(sizes, dtype=np.float64).reshape(-1, 3)
+    depths = np.asarray(depths, dtype=np.int32).reshape(-1)
+    cells = np.zeros(depths.shape[0], dtype=CELL_DTYPE)
+    cells["origin"] = origins
+    cells["size"] = sizes
+    cells["depth"] = depths
+    return cells
+
+
+def make_load(kind=LOAD_ZERO, params=(0.0, 0.0, 0.0, 0.0)):
+    ld = Load()
+    ld.kind = int(kind)
+    for i, p in enumerate(list(params) + [0.0] * (4 - len(params))):
+        ld.params[i] = float(p)
+    return ld
+
+
+def _d(a):
+    return None if a is None else a.ctypes.data_as(_dp)
+
+
+class Handle:
+    """One msfec handle (device buffers + stream)."""
+
+    def __init__(self, precision=PRECISION_MIXED, device=0, rtol=None, inner_rtol=None,
+                 max_iter=None, max_refine=None):
+        L = load_library()
+        cfg = Config()
+        L.msfec_config_default(ctypes.byref(cfg))
+        cfg.device = device
+        cfg.precision = precision
+        if rtol is not None:
+            cfg.rtol = rtol
+        if inner_rtol is not None:
+            cfg.inner_rtol = inner_rtol
+        if max_iter is not None:
+            cfg.max_iter = max_iter
+        if max_refine is not None:
+            cfg.max_refine = max_refine
+        self.cfg = cfg
+        h = _vp()
+        st = L.msfec_create(ctypes.byref(h), ctypes.byref(cfg))
+        if st != SUCCESS:
+            raise MsfecError(st, L.msfec_status_string(st).decode())
+        self._h = h
+        self._lib = L
+
+    @property
+    def ptr(self):
+        return self._h
+
+    def close(self):
+        if self._h:
+            self._lib.msfec_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def last_error(self):
+        return self._lib.msfec_last_error(self._h).decode()
+
+    def check(self, st, allow=()):
+        if st != SUCCESS and st not in allow:
+            raise MsfecError(st, self._lib.msfec_status_string(st).decode() + ": " + self.last_error())
+        return st
+
+    def set_stream(self, stream_handle):
+        return self.check(self._lib.msfec_set_stream(self._h, _vp(stream_handle or 0)))
+
+    def set_precision(self, precision):
+        return self.check(self._lib.msfec_set_precision(self._h, int(precision)))
+
+    def q1_build(self, cells, a, reaction=None, load=None, allow_unconverged=False):
+        """Host-buffer Q1 build. Returns (KH [c,8,8], FH [c,8], reports, status)."""
+        cells = np.ascontiguousarray(cells, dtype=CELL_DTYPE)
+        nc = cells.shape[0]
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        reaction = None if reaction is None else np.ascontiguousarray(reaction, dtype=np.float64)
+        KH = np.zeros((nc, 8, 8))
+        FH = np.zeros((nc, 8))
+        rep = np.zeros(nc, dtype=REPORT_DTYPE)
+        ld = load if load is not None else make_load()
+        st = self._lib.msfec_q1_build(self._h, nc, cells.ctypes.data_as(_vp), _d(a), _d(reaction),
+                                      ctypes.byref(ld), _d(KH), _d(FH), rep.ctypes.data_as(_vp))
+        self.check(st, allow=(ERROR_NOT_CONVERGED,) if allow_unconverged else ())
+        return KH, FH, rep, st
+
+    def q1_build_device(self, cells, d_a, d_reaction, load, d_KH, d_FH, d_reports):
+        """Device-pointer Q1 build (asynchronous on the handle's stream)."""
+        cells = np.ascontiguousarray(cells, dtype=CELL_DTYPE)
+        st = self._lib.msfec_q1_build_device(self._h, cells.shape[0], cells.ctypes.data_as(_vp),
+                                             _vp(d_a), _vp(d_reaction or 0), ctypes.byref(load),
+                                             _vp(d_KH), _vp(d_FH), _vp(d_reports or 0))
+        return self.check(st)
+
+    def set_timing(self, enable=True):
+        return self.check(self._lib.msfec_set_timing(self._h, 1 if enable else 0))
+
+    def timings(self):
+        t = Timings()
+        self.check(self._lib.msfec_get_timings(self._h, ctypes.byref(t)))
+        return {"solve_ms": t.solve_ms, "galerkin_ms": t.galerkin_ms, "total_ms": t.total_ms,
+                "solve_launches": t.solve_launches, "kernel_launches": t.kernel_launches}
+
+    def q1_basis(self):
+        n = self._lib.msfec_q1_basis_size(self._h)
+        out = np.zeros(n)
+        self.check(self._lib.msfec_q1_get_basis(self._h, _d(out), n))
+        return out
+
+    def q1_eval_fine(self, weights, cell_of, points):
+        weights = np.ascontiguousarray(weights, dtype=np.float64)
+        cell_of = np.ascontiguousarray(cell_of, dtype=np.int32)
+        points = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros(points.shape[0])
+        st = self._lib.msfec_q1_eval_fine(self._h, _d(weights), points.shape[0],
+                                          cell_of.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                          _d(points), _d(out))
+        self.check(st)
+        return out

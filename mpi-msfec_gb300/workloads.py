@@ -1,0 +1,86 @@
+"""Seeded synthetic inputs of the MsFEC basis-build workloads.
+
+The reference measures on no public dataset; every input here is synthetic
+and seeded (numpy PCG64), identical on x86_64 and aarch64:
+
+  q1_lognormal   coarse m^3 cells of the unit cube, depth L, log a ~ N(0,1)
+                 i.i.d. per fine cell, optional reaction r, f = sin(pi x)
+                 sin(pi y) sin(pi z)         (coarse 4^3, L = 3: the small
+                 Q1 case; coarse 8^3, L = 4: the adjoint case)
+  q1_uneven      coarse 16^3, L ~ U{2,3,4,5} per cell, a = (1 + 0.9
+                 sin(2 pi x/eps) sin(2 pi y/eps) sin(2 pi z/eps)) exp(0.5 xi_c),
+                 eps = 1/64, xi_c ~ N(0,1) per coarse cell, sampled at
+                 fine-cell centres                     (batched uneven Q1)
+Coarse cells are listed lexicographically (x fastest); fine-cell arrays per
+coarse cell are lexicographic too.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from msfec import CELL_DTYPE, LOAD_SIN_PRODUCT, make_load
+
+
+def coarse_grid(m, depths, lo=0.0, hi=1.0):
+    """m^3 coarse cells of [lo, hi]^3 (x fastest); depths scalar or per cell."""
+    H = (hi - lo) / m
+    idx = np.arange(m ** 3)
+    ci, cj, ck = idx % m, (idx // m) % m, idx // (m * m)
+    cells = np.zeros(m ** 3, dtype=CELL_DTYPE)
+    cells["origin"] = lo + H * np.stack([ci, cj, ck], axis=1)
+    cells["size"] = H
+    cells["depth"] = np.broadcast_to(np.asarray(depths, dtype=np.int32), (m ** 3,))
+    return cells
+
+
+def fine_counts(cells):
+    n = 1 << cells["depth"].astype(np.int64)
+    return n ** 3, (n + 1) ** 3
+
+
+def work_dof_rhs(cells, rhs=8):
+    """Fine DoF x RHS of a Q1 build: sum over cells of (n+1)^3 * 8."""
+    return int(np.sum(fine_counts(cells)[1]) * rhs)
+
+
+def fine_centres(cells):
+    """Fine-cell centres (x, y, z) concatenated over cells, per-cell lexicographic."""
+    out = []
+    for c in cells:
+        n = 1 << int(c["depth"])
+        h = c["size"] / n
+        t = np.arange(n) + 0.5
+        z, y, x = np.meshgrid(t, t, t, indexing="ij")
+        out.append(np.stack([c["origin"][0] + x.ravel() * h[0], c["origin"][1] + y.ravel() * h[1],
+                             c["origin"][2] + z.ravel() * h[2]], axis=1))
+    return np.concatenate(out, axis=0)
+
+
+def q1_lognormal(m=4, depth=3, seed=1, reaction=True):
+    rng = np.random.default_rng(seed)
+    cells = coarse_grid(m, depth)
+    nf = int(np.sum(fine_counts(cells)[0]))
+    a = np.exp(rng.standard_normal(nf))
+    r = np.ones(nf) if reaction else None
+    load = make_load(LOAD_SIN_PRODUCT, (1.0, 1.0, 0.0, 0.0))
+    return cells, a, r, load
+
+
+def q1_uneven(m=16, seed=3, eps=1.0 / 64.0, depths=(2, 3, 4, 5)):
+    rng = np.random.default_rng(seed)
+    cells = coarse_grid(m, 2)
+    cells["depth"] = rng.choice(np.asarray(depths, dtype=np.int32), size=m ** 3)
+    xi = rng.standard_normal(m ** 3)
+    a_parts = []
+    for c in range(m ** 3):
+        n = 1 << int(cells["depth"][c])
+        h = cells["size"][c][0] / n
+        t = (np.arange(n) + 0.5) * h
+        sx = np.sin(2 * np.pi * (cells["origin"][c][0] + t) / eps)
+        sy = np.sin(2 * np.pi * (cells["origin"][c][1] + t) / eps)
+        sz = np.sin(2 * np.pi * (cells["origin"][c][2] + t) / eps)
+        osc = 1.0 + 0.9 * sz[:, None, None] * sy[None, :, None] * sx[None, None, :]
+        a_parts.append((osc * np.exp(0.5 * xi[c])).ravel())
+    a = np.concatenate(a_parts)
+    load = make_load(LOAD_SIN_PRODUCT, (1.0, 1.0, 0.0, 0.0))
+    return cells, a, None, load

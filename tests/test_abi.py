@@ -1,0 +1,39 @@
+"""The C-ABI library loads and exports every symbol include/msfec_cuda.h declares."""
+import ctypes
+import os
+import re
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    text = open(os.path.join(REPO, "include", "msfec_cuda.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(msfec_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_expected_api():
+    import msfec
+    assert sorted(msfec.EXPORTED) == declared_functions()
+
+
+def test_library_exports_every_declared_symbol():
+    import msfec_build
+    lib = msfec_build.build()
+    L = ctypes.CDLL(lib)
+    for name in declared_functions():
+        assert hasattr(L, name), name
+
+
+def test_status_strings_and_defaults_without_gpu():
+    import msfec
+    L = msfec.load_library()
+    cfg = msfec.Config()
+    L.msfec_config_default(ctypes.byref(cfg))
+    assert cfg.precision == msfec.PRECISION_MIXED and cfg.rtol == 1e-12 and cfg.max_refine >= 1
+    for s in range(8):
+        assert L.msfec_status_string(s)
+    # argument checks happen before any device work
+    assert L.msfec_create(None, None) == msfec.ERROR_INVALID_ARGUMENT
