@@ -105,7 +105,7 @@ typedef struct msfec_cell_report {
 
 typedef struct msfec_handle msfec_handle;
 
-/* Fills cfg with defaults: device 0, MIXED, rtol 1e-12, inner_rtol 1e-5,
+/* Fills cfg with defaults: device 0, MIXED, rtol 1e-12, inner_rtol 1e-6,
    max_iter 2000, max_refine 6. */
 void msfec_config_default(msfec_config *cfg);
 

@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdio>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -283,6 +284,11 @@ msfec_status q1_build_impl(msfec_handle *h, int ncells, const msfec_cell *cells,
     grid = std::min<int>((int)plan.units.size(), occ * h->num_sms);
   }
   grid = std::max(grid, plan.cluster);
+  if (h->cfg.verbose)
+    fprintf(stderr,
+            "[msfec] q1 plan: %d cells, %zu items, %zu units, cluster %d, smem %zu B, occupancy %d, grid %d, %s\n",
+            ncells, plan.items.size(), plan.units.size(), plan.cluster, plan.smem, occ, grid,
+            fp64 ? "fp64" : "mixed");
   if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[0], st));
   MSFEC_CUDA_TRY(h, q1_solve_launch(fp64, plan.cluster, has_r, prm, plan.smem, grid, st));
   if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[1], st));
@@ -316,7 +322,7 @@ void msfec_config_default(msfec_config *cfg) {
   cfg->device = 0;
   cfg->precision = MSFEC_PRECISION_MIXED;
   cfg->rtol = 1e-12;
-  cfg->inner_rtol = 1e-5;
+  cfg->inner_rtol = 1e-6;
   cfg->max_iter = 2000;
   cfg->max_refine = 6;
   cfg->verbose = 0;

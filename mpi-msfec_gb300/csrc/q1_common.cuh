@@ -78,15 +78,16 @@ __host__ __device__ inline int q1_planes_per_cta(int n, int nslab) {
 
 // Dynamic shared memory of one item (bytes), identical on host and device.
 struct Q1Smem {
-  size_t slab_off, caf_off, raf_off, x_off, dv_off, total;
+  size_t slab_off, caf_off, raf_off, x_off, p_off, s_off, dv_off, total;
 };
 
 __host__ __device__ inline size_t q1_align(size_t v) { return (v + 255) & ~(size_t)255; }
 
 // slab: (PS+2) planes of (n+1)^2 nodes x R, sized for FP64 staging (the
 //       Krylov search direction of precision T aliases it);
-// caf/raf: float coefficient layers k0-1 .. k0+PS-1; x: owned nodes x R (T);
-// dv: Jacobi scaling per owned node (float).
+// caf/raf: float coefficient layers k0-1 .. k0+PS-1; x, p, s: owned nodes x R
+// (T; iterate, search direction and its image s = K p); dv: Jacobi scaling
+// per owned node (float).
 __host__ __device__ inline Q1Smem q1_smem_layout(int n, int R, int nslab, bool has_r, int tsize) {
   const int PS = q1_planes_per_cta(n, nslab);
   const int m = n - 1;
@@ -101,6 +102,10 @@ __host__ __device__ inline Q1Smem q1_smem_layout(int n, int R, int nslab, bool h
   s.raf_off = off;
   if (has_r) off = q1_align(off + ncf * sizeof(float));
   s.x_off = off;
+  off = q1_align(off + (size_t)PS * m * m * R * tsize);
+  s.p_off = off;
+  off = q1_align(off + (size_t)PS * m * m * R * tsize);
+  s.s_off = off;
   off = q1_align(off + (size_t)PS * m * m * R * tsize);
   s.dv_off = off;
   off = q1_align(off + (size_t)PS * m * m * sizeof(float));

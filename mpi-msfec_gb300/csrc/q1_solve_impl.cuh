@@ -31,11 +31,33 @@ namespace msfec {
 namespace q1impl {
 
 struct Q1Shared {
+  // reduction slots: per warp, then per (parity, source CTA) of the cluster
   double warp[kQ1Warps][kRedVals][8];
   double part[2][kQ1MaxCluster][kRedVals][8];
+  float fwarp[kQ1Warps][kRedVals][8];
+  float fpart[2][kQ1MaxCluster][kRedVals][8];
   double cst[2][8];  // element pattern constants: stiffness, mass
   int unit;
 };
+
+template <typename VT>
+__device__ __forceinline__ VT *red_warp(Q1Shared &sh) {
+  if constexpr (sizeof(VT) == 4)
+    return &sh.fwarp[0][0][0];
+  else
+    return &sh.warp[0][0][0];
+}
+template <typename VT>
+__device__ __forceinline__ VT *red_part(Q1Shared &sh) {
+  if constexpr (sizeof(VT) == 4)
+    return &sh.fpart[0][0][0][0];
+  else
+    return &sh.part[0][0][0][0];
+}
+__device__ __forceinline__ int warp_slot(int w, int t, int q) { return (w * kRedVals + t) * 8 + q; }
+__device__ __forceinline__ int part_slot(int par, int r, int t, int q) {
+  return ((par * kQ1MaxCluster + r) * kRedVals + t) * 8 + q;
+}
 
 // Stiffness (unit coefficient) and mass entries of the Q1 element on a box,
 // indexed by the pattern of differing coordinates pat = dx + 2 dy + 4 dz
@@ -210,10 +232,12 @@ __device__ __forceinline__ void column_apply_f64(const double *__restrict__ ps, 
   }
 }
 
-// Residual-pass apply at one interior node for all R right-hand sides:
-// y = K v, and (BND) yb = the part of K v coming from lattice-boundary
-// neighbours (K_IB g when v carries the Dirichlet data).
-template <typename TA, int R, bool HAS_R, bool BND, typename TV, typename LoadA, typename LoadR>
+// Residual-pass apply at one node for all R right-hand sides: y = K v, and
+// (BND) yb = the part of K v coming from lattice-boundary neighbours (K_IB g
+// when v carries the Dirichlet data). GUARD: lattice-boundary node, the
+// loaders return 0 for absent cells and absent neighbours are skipped.
+template <typename TA, int R, bool HAS_R, bool BND, bool GUARD = false, typename TV, typename LoadA,
+          typename LoadR>
 __device__ __forceinline__ void node_apply(const TV *__restrict__ vs, int n, int kk, int i, int j, int k,
                                            LoadA lda, LoadR ldr, const double (&c)[8], const double (&mm)[8],
                                            TA (&y)[R], TA (&yb)[R]) {
@@ -241,6 +265,9 @@ __device__ __forceinline__ void node_apply(const TV *__restrict__ vs, int n, int
           wgt += (TA)mm[pat] * Rr;
         }
         const int ni = i + dx - 1, nj = j + dy - 1, nk = k + dz - 1;
+        if constexpr (GUARD) {
+          if (ni < 0 || nj < 0 || nk < 0 || ni > n || nj > n || nk > n) continue;
+        }
         const bool nb_bnd = BND && (ni == 0 || nj == 0 || nk == 0 || ni == n || nj == n || nk == n);
         const TV *src = vs + (((size_t)(kk + dz - 1) * N1 + nj) * N1 + ni) * R;
 #pragma unroll
@@ -264,21 +291,24 @@ __device__ __forceinline__ void xsync() {
 
 // Publish per-CTA totals (threads < R hold rhs = threadIdx.x) into every
 // peer's slot row, synchronise, and return this thread's rhs total (rank
-// order summation: bitwise identical in every CTA of the cluster).
-template <bool SLAB, int NV, int R>
-__device__ __forceinline__ void publish_and_sum(Q1Shared &sh, int &parity, const double (&s)[NV], int rank,
-                                                int nslab, double (&out)[NV]) {
+// order summation: bitwise identical in every CTA of the cluster). VT is the
+// accumulation type: float inside the FP32 Krylov loop (no FP64 pipe use),
+// double for FP64 residuals and the plain FP64 path.
+template <typename VT, bool SLAB, int NV, int R>
+__device__ __forceinline__ void publish_and_sum(Q1Shared &sh, int &parity, const VT (&s)[NV], int rank,
+                                                int nslab, VT (&out)[NV]) {
+  VT *part = red_part<VT>(sh);
   if ((int)threadIdx.x < R) {
     if constexpr (SLAB) {
       cg::cluster_group cluster = cg::this_cluster();
       for (int r = 0; r < nslab; ++r) {
-        Q1Shared *rs = cluster.map_shared_rank(&sh, r);
+        VT *rp = cluster.map_shared_rank(part, r);
 #pragma unroll
-        for (int t = 0; t < NV; ++t) rs->part[parity][rank][t][threadIdx.x] = s[t];
+        for (int t = 0; t < NV; ++t) rp[part_slot(parity, rank, t, threadIdx.x)] = s[t];
       }
     } else {
 #pragma unroll
-      for (int t = 0; t < NV; ++t) sh.part[parity][0][t][threadIdx.x] = s[t];
+      for (int t = 0; t < NV; ++t) part[part_slot(parity, 0, t, threadIdx.x)] = s[t];
     }
   }
   xsync<SLAB>();
@@ -286,58 +316,62 @@ __device__ __forceinline__ void publish_and_sum(Q1Shared &sh, int &parity, const
   const int nrows = SLAB ? nslab : 1;
 #pragma unroll
   for (int t = 0; t < NV; ++t) {
-    double acc = 0.0;
-    for (int r = 0; r < nrows; ++r) acc += sh.part[parity][r][t][rho];
+    VT acc = VT(0);
+    for (int r = 0; r < nrows; ++r) acc += part[part_slot(parity, r, t, rho)];
     out[t] = acc;
   }
   parity ^= 1;
 }
 
 // Reduction when every thread holds partials of ITS rhs (rho = tid % R).
-template <bool SLAB, int NV, int R>
-__device__ __forceinline__ void reduce_own(Q1Shared &sh, int &parity, double (&v)[NV], int rank, int nslab,
-                                           double (&out)[NV]) {
+template <typename VT, bool SLAB, int NV, int R>
+__device__ __forceinline__ void reduce_own(Q1Shared &sh, int &parity, VT (&v)[NV], int rank, int nslab,
+                                           VT (&out)[NV]) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  VT *ws = red_warp<VT>(sh);
 #pragma unroll
   for (int off = 16; off >= R; off >>= 1)
 #pragma unroll
     for (int t = 0; t < NV; ++t) v[t] += __shfl_xor_sync(0xffffffffu, v[t], off);
   if (lane < R)
 #pragma unroll
-    for (int t = 0; t < NV; ++t) sh.warp[warp][t][lane] = v[t];
+    for (int t = 0; t < NV; ++t) ws[warp_slot(warp, t, lane)] = v[t];
   __syncthreads();
-  double s[NV];
+  VT s[NV];
 #pragma unroll
-  for (int t = 0; t < NV; ++t) s[t] = 0.0;
+  for (int t = 0; t < NV; ++t) s[t] = VT(0);
   if ((int)threadIdx.x < R)
+#pragma unroll
     for (int w = 0; w < kQ1Warps; ++w)
 #pragma unroll
-      for (int t = 0; t < NV; ++t) s[t] += sh.warp[w][t][threadIdx.x];
-  publish_and_sum<SLAB, NV, R>(sh, parity, s, rank, nslab, out);
+      for (int t = 0; t < NV; ++t) s[t] += ws[warp_slot(w, t, threadIdx.x)];
+  publish_and_sum<VT, SLAB, NV, R>(sh, parity, s, rank, nslab, out);
 }
 
-// Reduction when every thread holds partials of ALL R rhs.
+// Reduction when every thread holds partials of ALL R rhs (FP64 residuals).
 template <bool SLAB, int NV, int R>
 __device__ __forceinline__ void reduce_all(Q1Shared &sh, int &parity, double (&v)[NV][R], int rank, int nslab,
                                            double (&out)[NV]) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  double *ws = red_warp<double>(sh);
 #pragma unroll
   for (int t = 0; t < NV; ++t)
 #pragma unroll
     for (int q = 0; q < R; ++q) {
 #pragma unroll
       for (int off = 16; off >= 1; off >>= 1) v[t][q] += __shfl_xor_sync(0xffffffffu, v[t][q], off);
-      if (lane == 0) sh.warp[warp][t][q] = v[t][q];
+      if (lane == 0) ws[warp_slot(warp, t, q)] = v[t][q];
     }
   __syncthreads();
   double s[NV];
 #pragma unroll
   for (int t = 0; t < NV; ++t) s[t] = 0.0;
   if ((int)threadIdx.x < R)
+#pragma unroll
     for (int w = 0; w < kQ1Warps; ++w)
 #pragma unroll
-      for (int t = 0; t < NV; ++t) s[t] += sh.warp[w][t][threadIdx.x];
-  publish_and_sum<SLAB, NV, R>(sh, parity, s, rank, nslab, out);
+      for (int t = 0; t < NV; ++t) s[t] += ws[warp_slot(w, t, threadIdx.x)];
+  publish_and_sum<double, SLAB, NV, R>(sh, parity, s, rank, nslab, out);
 }
 
 template <typename T, int R, int UMAX, int PMAX, bool HAS_R, bool SLAB>
@@ -359,6 +393,8 @@ __device__ void solve_item(const Q1Params &prm, Q1Shared &sh, unsigned char *sme
   float *caf = reinterpret_cast<float *>(smem + L.caf_off);
   float *raf = reinterpret_cast<float *>(smem + L.raf_off);
   T *xs = reinterpret_cast<T *>(smem + L.x_off);
+  T *ps = reinterpret_cast<T *>(smem + L.p_off);
+  T *ss = reinterpret_cast<T *>(smem + L.s_off);
   float *dvs = reinterpret_cast<float *>(smem + L.dv_off);
   const int tid = threadIdx.x;
   const int rho = tid % R;
@@ -530,17 +566,22 @@ __device__ void solve_item(const Q1Params &prm, Q1Shared &sh, unsigned char *sme
     if (all_conv || ir >= prm.max_refine) break;
 
     // ---------------- Krylov phase (precision T) ----------------
+    // Chronopoulos-Gear PCG: one apply w = K u (u = D^-1 r) and ONE fused
+    // reduction (gamma = r.u, delta = w.u, r.r) per iteration; p and s = K p
+    // follow by recurrence, so an iteration crosses two barriers (reduction,
+    // halo of u). Accumulation is in T: no FP64 instruction in the FP32 loop.
     const double tol_abs2 = prm.rtol * prm.rtol * bnorm2;
     const double target2 = kMixed ? fmax(prm.inner_rtol * prm.inner_rtol * rnorm2, 0.01 * tol_abs2) : 0.25 * tol_abs2;
     bool active = !conv && (rnorm2 > target2);
-    // r into registers; x = 0; p-slab = 0 (boundary and halo planes stay zero)
+    const T target2t = (T)target2;
+    // r into registers; x = p = s = 0; u-slab = 0 (boundary and halo planes stay zero)
 #pragma unroll
     for (int s = 0; s < UMAX; ++s)
 #pragma unroll
       for (int pk = 0; pk < PMAX; ++pk)
         if (cval[s] && pk < P) r[s][pk] = xs[own_idx(s, pk) * R + rho];
     __syncthreads();
-    for (size_t e = tid; e < own_nodes * R; e += kQ1Threads) xs[e] = T(0);
+    for (size_t e = tid; e < own_nodes * R; e += kQ1Threads) xs[e] = ps[e] = ss[e] = T(0);
     for (size_t e = tid; e < slab_nodes * R; e += kQ1Threads) slab_t[e] = T(0);
     // Peers push halo planes into this slab next: every slab must be zeroed
     // (and done serving the residual phase) first.
@@ -553,114 +594,88 @@ __device__ void solve_item(const Q1Params &prm, Q1Shared &sh, unsigned char *sme
         ct[t] = (T)cd[t];
         mmt[t] = (T)mmd[t];
       }
-      auto write_p = [&](int s, int pk, T pv) {
-        slab_t[slab_idx(s, pk)] = pv;
+      auto write_u = [&](int s, int pk, T uv) {
+        slab_t[slab_idx(s, pk)] = uv;
         if constexpr (SLAB) {
           if (pk == 0 && rank > 0) {
             T *rem = cg::this_cluster().map_shared_rank(slab_t, rank - 1);
-            rem[(((size_t)(PS + 1) * N1 + cj[s]) * N1 + ci[s]) * R + rho] = pv;
+            rem[(((size_t)(PS + 1) * N1 + cj[s]) * N1 + ci[s]) * R + rho] = uv;
           }
           if (pk == P - 1 && rank < nslab - 1) {
             T *rem = cg::this_cluster().map_shared_rank(slab_t, rank + 1);
-            rem[((size_t)cj[s] * N1 + ci[s]) * R + rho] = pv;
+            rem[((size_t)cj[s] * N1 + ci[s]) * R + rho] = uv;
           }
         }
       };
-      // p = z = D^-1 r
-      double part[1] = {0.0};
 #pragma unroll
       for (int s = 0; s < UMAX; ++s) {
         if (!cval[s]) continue;
 #pragma unroll
         for (int pk = 0; pk < PMAX; ++pk)
-          if (pk < P) {
-            const T z = (T)dvs[own_idx(s, pk)] * r[s][pk];
-            part[0] += (double)(r[s][pk] * z);
-            write_p(s, pk, active ? z : T(0));
-          }
+          if (pk < P) write_u(s, pk, active ? (T)dvs[own_idx(s, pk)] * r[s][pk] : T(0));
       }
-      double rz;
-      {
-        double tot[1];
-        reduce_own<SLAB, 1, R>(sh, parity, part, rank, nslab, tot);  // also publishes p and halos
-        rz = tot[0];
-      }
+      xsync<SLAB>();
+      T gamma_old = T(1), alpha_old = T(1);
       for (int iter = 0; iter < prm.max_iter; ++iter) {
-        // q = K p, p.q
-        double pq_part[1] = {0.0};
+        // w = K u (kept in q), partial gamma, delta, r.r
+        T part[3] = {T(0), T(0), T(0)};
 #pragma unroll
         for (int s = 0; s < UMAX; ++s) {
           if (!cval[s]) continue;
-          T cv[PMAX];
+          T uc[PMAX];
           if constexpr (kMixed)
-            column_apply_f32<R, PMAX, HAS_R>(slab_t, caf, raf, n, rho, ci[s], cj[s], P, ct, mmt, q[s], cv);
+            column_apply_f32<R, PMAX, HAS_R>(slab_t, caf, raf, n, rho, ci[s], cj[s], P, ct, mmt, q[s], uc);
           else
-            column_apply_f64<R, PMAX, HAS_R>(slab_t, ag, rg, n, rho, ci[s], cj[s], P, ct, mmt, q[s], cv);
-#pragma unroll
-          for (int pk = 0; pk < PMAX; ++pk)
-            if (pk < P) pq_part[0] += (double)(cv[pk] * q[s][pk]);
-        }
-        double pq;
-        {
-          double tot[1];
-          reduce_own<SLAB, 1, R>(sh, parity, pq_part, rank, nslab, tot);
-          pq = tot[0];
-        }
-        double alpha = 0.0;
-        if (active) {
-          if (!(pq > 0.0) || !isfinite(pq) || !isfinite(rz)) {
-            active = false;
-            flags |= 1;
-          } else {
-            alpha = rz / pq;
-            ++its;
-          }
-        }
-        // x += alpha p, r -= alpha q, z = D^-1 r
-        const T al = (T)alpha;
-        double upd[2] = {0.0, 0.0};
-#pragma unroll
-        for (int s = 0; s < UMAX; ++s) {
-          if (!cval[s]) continue;
+            column_apply_f64<R, PMAX, HAS_R>(slab_t, ag, rg, n, rho, ci[s], cj[s], P, ct, mmt, q[s], uc);
 #pragma unroll
           for (int pk = 0; pk < PMAX; ++pk)
             if (pk < P) {
-              const size_t oi = own_idx(s, pk);
-              const T pv = slab_t[slab_idx(s, pk)];
-              xs[oi * R + rho] += al * pv;
-              r[s][pk] -= al * q[s][pk];
-              const T z = (T)dvs[oi] * r[s][pk];
-              upd[0] += (double)(r[s][pk] * z);
-              upd[1] += (double)(r[s][pk] * r[s][pk]);
+              part[0] += r[s][pk] * uc[pk];
+              part[1] += q[s][pk] * uc[pk];
+              part[2] += r[s][pk] * r[s][pk];
             }
         }
-        double rz_new, rr;
-        {
-          double tot[2];
-          reduce_own<SLAB, 2, R>(sh, parity, upd, rank, nslab, tot);
-          rz_new = tot[0];
-          rr = tot[1];
-        }
-        double beta = 0.0;
+        T tot[3];
+        reduce_own<T, SLAB, 3, R>(sh, parity, part, rank, nslab, tot);
+        T alpha = T(0), beta = T(0);
         if (active) {
-          beta = rz_new / rz;
-          rz = rz_new;
-          if (rr <= target2) active = false;
+          const T gamma = tot[0], delta = tot[1], rr = tot[2];
+          if (rr <= target2t) {
+            active = false;
+          } else {
+            beta = iter == 0 ? T(0) : gamma / gamma_old;
+            const T denom = iter == 0 ? delta : delta - beta * gamma / alpha_old;
+            if (!(denom > T(0)) || !(gamma > T(0)) || !isfinite(denom) || !isfinite(gamma)) {
+              active = false;
+              flags |= 1;
+            } else {
+              alpha = gamma / denom;
+              gamma_old = gamma;
+              alpha_old = alpha;
+              ++its;
+            }
+          }
         }
         if (__syncthreads_or(active) == 0) break;
-        // p = z + beta p
-        const T be = (T)beta;
+        // p = u + beta p, s = w + beta s, x += alpha p, r -= alpha s, u = D^-1 r
+        if (active) {
 #pragma unroll
-        for (int s = 0; s < UMAX; ++s) {
-          if (!cval[s]) continue;
+          for (int s = 0; s < UMAX; ++s) {
+            if (!cval[s]) continue;
 #pragma unroll
-          for (int pk = 0; pk < PMAX; ++pk)
-            if (pk < P) {
-              const size_t si = slab_idx(s, pk);
-              const T z = (T)dvs[own_idx(s, pk)] * r[s][pk];
-              const T pold = slab_t[si];
-              write_p(s, pk, active ? z + be * pold : pold);
-            }
+            for (int pk = 0; pk < PMAX; ++pk)
+              if (pk < P) {
+                const size_t oi = own_idx(s, pk);
+                const size_t vi = oi * R + rho;
+                const T pv = slab_t[slab_idx(s, pk)] + beta * ps[vi];
+                const T sv = q[s][pk] + beta * ss[vi];
+                ps[vi] = pv;
+                ss[vi] = sv;
+                xs[vi] += alpha * pv;
+                r[s][pk] -= alpha * sv;
+                write_u(s, pk, (T)dvs[oi] * r[s][pk]);
+              }
+          }
         }
         xsync<SLAB>();
       }
@@ -678,15 +693,15 @@ __device__ void solve_item(const Q1Params &prm, Q1Shared &sh, unsigned char *sme
   }
 
   // ---------------- boundary rows of y = K phi ----------------
-  // phi is staged in slab_d by the last (FP64) residual phase.
+  // FP64 27-point apply at lattice-boundary nodes with absent cells and
+  // neighbours padded out; phi is staged in slab_d by the last residual phase.
   {
     const int nside = P * 4 * n;  // perimeter nodes of the owned planes
     const int nfirst = (P > 0 && first) ? (int)N1sq : 0;
     const int nlast = last ? (int)N1sq : 0;
     const int nb = (P > 0) ? nside + nfirst + nlast : 0;
-    for (int e = tid; e < nb * R; e += kQ1Threads) {
-      const int r_e = e / nb;
-      int b = e % nb;
+    for (int e = tid; e < nb; e += kQ1Threads) {
+      int b = e;
       int i, j, kk;
       if (b < nside) {
         kk = b / (4 * n) + 1;
@@ -716,23 +731,20 @@ __device__ void solve_item(const Q1Params &prm, Q1Shared &sh, unsigned char *sme
         j = b / N1;
       }
       const int k = k0 - 1 + kk;
-      double acc = 0.0;
-      for (int oz = 0; oz < 2; ++oz)
-        for (int oy = 0; oy < 2; ++oy)
-          for (int ox = 0; ox < 2; ++ox) {
-            const int ex = i - 1 + ox, ey = j - 1 + oy, ez = k - 1 + oz;
-            if (ex < 0 || ey < 0 || ez < 0 || ex >= n || ey >= n || ez >= n) continue;
-            const size_t ce = ((size_t)(ez - (k0 - 1)) * n + ey) * n + ex;
-            const double ae = __ldg(ag + ce);
-            const double re = HAS_R ? __ldg(rg + ce) : 0.0;
-            const int l = (1 - ox) + 2 * (1 - oy) + 4 * (1 - oz);  // local vertex of the node in the cell
-            for (int u = 0; u < 8; ++u) {
-              const int nx = ex + (u & 1), ny = ey + ((u >> 1) & 1), nz = ez + (u >> 2);
-              const double pv = slab_d[(((size_t)(nz - (k0 - 1)) * N1 + ny) * N1 + nx) * R + r_e];
-              acc += (ae * cd[l ^ u] + re * mmd[l ^ u]) * pv;
-            }
-          }
-      y_c[(size_t)(it.rhs0 + r_e) * nn + ((size_t)k * N1 + j) * N1 + i] = acc;
+      auto pad = [&](const double *base, int l, int o) -> double {
+        const int ex = i - 1 + ((o == 1 || o == n + 1) ? 1 : 0);
+        const int ey = j - 1 + (o >= n ? 1 : 0);
+        const int ez = k0 - 1 + l;
+        if (ex < 0 || ey < 0 || ez < 0 || ex >= n || ey >= n || ez >= n) return 0.0;
+        return __ldg(base + ((ptrdiff_t)l * n + ey) * n + ex);
+      };
+      double yv[R], yb[R];
+      node_apply<double, R, HAS_R, false, true>(
+          slab_d, n, kk, i, j, k, [&](int l, int o) { return pad(ag, l, o); },
+          [&](int l, int o) { return HAS_R ? pad(rg, l, o) : 0.0; }, cd, mmd, yv, yb);
+      const size_t gnode = ((size_t)k * N1 + j) * N1 + i;
+#pragma unroll
+      for (int t = 0; t < R; ++t) y_c[(size_t)(it.rhs0 + t) * nn + gnode] = yv[t];
     }
   }
   if (rank == 0 && tid < R) {

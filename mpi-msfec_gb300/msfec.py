@@ -155,7 +155,7 @@ class Handle:
     """One msfec handle (device buffers + stream)."""
 
     def __init__(self, precision=PRECISION_MIXED, device=0, rtol=None, inner_rtol=None,
-                 max_iter=None, max_refine=None):
+                 max_iter=None, max_refine=None, verbose=0):
         L = load_library()
         cfg = Config()
         L.msfec_config_default(ctypes.byref(cfg))
@@ -169,6 +169,7 @@ class Handle:
             cfg.max_iter = max_iter
         if max_refine is not None:
             cfg.max_refine = max_refine
+        cfg.verbose = int(verbose or os.environ.get("MSFEC_VERBOSE", "0"))
         self.cfg = cfg
         h = _vp()
         st = L.msfec_create(ctypes.byref(h), ctypes.byref(cfg))
