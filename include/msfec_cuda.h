@@ -65,7 +65,10 @@ typedef enum msfec_precision {
 typedef enum msfec_load_kind {
   MSFEC_LOAD_ZERO = 0,
   MSFEC_LOAD_CONSTANT = 1,    /* f = p0 */
-  MSFEC_LOAD_SIN_PRODUCT = 2  /* f = p0 sin(p1 pi x) sin(p1 pi y) sin(p1 pi z) */
+  MSFEC_LOAD_SIN_PRODUCT = 2, /* f = p0 sin(p1 pi x) sin(p1 pi y) sin(p1 pi z) */
+  /* vector load of the mixed (Ned_RT) problem, w = p1 pi:
+     f = p0 (sin(w y) sin(w z), sin(w z) sin(w x), sin(w x) sin(w y)) */
+  MSFEC_LOAD_VEC_TRIG = 3
 } msfec_load_kind;
 
 typedef struct msfec_load {
@@ -86,6 +89,10 @@ typedef struct msfec_config {
   int32_t max_refine;  /* MIXED: FP64 refinement steps; FP64: verification rounds */
   int32_t verbose;
   int32_t reserved;
+  /* Ned_RT local solves stop when ||r||_2 <= nedrt_rtol * ||f_I - A_IB g||_2.
+     The mixed local system has condition number ~1e4 at depth 3, so 1e-14
+     is needed for a 1e-10 basis error. */
+  double nedrt_rtol;
 } msfec_config;
 
 typedef struct msfec_cell {
@@ -106,7 +113,7 @@ typedef struct msfec_cell_report {
 typedef struct msfec_handle msfec_handle;
 
 /* Fills cfg with defaults: device 0, MIXED, rtol 1e-12, inner_rtol 1e-6,
-   max_iter 2000, max_refine 6. */
+   max_iter 2000, max_refine 6, nedrt_rtol 1e-14. */
 void msfec_config_default(msfec_config *cfg);
 
 msfec_status msfec_create(msfec_handle **handle, const msfec_config *cfg);
@@ -185,6 +192,45 @@ const double *msfec_q1_basis_device(const msfec_handle *handle);
 msfec_status msfec_q1_eval_fine(msfec_handle *handle, const double *weights,
                                 int32_t npoints, const int32_t *cell_of,
                                 const double *points, double *values);
+
+/*
+ * Ned_RT (lowest-order Nedelec sigma x Raviart-Thomas u) basis build from
+ * host buffers (synchronous). Replaces NedRTBasis::run
+ * (source/Ned_RT/ned_rt_basis.cc:1279-1428) for every cell of the batch,
+ * followed by get_global_element_matrix / get_global_element_rhs
+ * (ned_rt_basis.cc:1262-1273).
+ *   ainv6  A^-1 per fine cell, 6 doubles (a00 a11 a22 a01 a02 a12), SPD
+ *          (the reference's DiffusionInverse_A, eqn_coeff_A.cc:193-242)
+ *   bdiv   B per fine cell (> 0): the div-div weight (Diffusion_B,
+ *          eqn_coeff_B.cc:72-114); the reaction term of the reference is zero
+ *   load   MSFEC_LOAD_ZERO or MSFEC_LOAD_VEC_TRIG (global load, F_H only)
+ *   KH     [ncells][18][18]: rows/cols 0..11 coarse edges (GeometryInfo<3>
+ *          line order), 12..17 coarse faces; FH [ncells][18] (edge rows 0)
+ * Coarse Nedelec / RT functions are normalised to unit line integral / unit
+ * flux along the positive axis (deal.II FE_Nedelec(0) / FE_RaviartThomas(0)).
+ * Depth 1..4.
+ */
+msfec_status msfec_nedrt_build(msfec_handle *handle, int32_t ncells,
+                               const msfec_cell *cells, const double *ainv6,
+                               const double *bdiv, const msfec_load *load,
+                               double *KH, double *FH,
+                               msfec_cell_report *reports);
+
+/* Device-pointer variant (asynchronous on the handle's stream); cells on the host. */
+msfec_status msfec_nedrt_build_device(msfec_handle *handle, int32_t ncells,
+                                      const msfec_cell *cells,
+                                      const double *d_ainv6,
+                                      const double *d_bdiv,
+                                      const msfec_load *load, double *d_KH,
+                                      double *d_FH,
+                                      msfec_cell_report *d_reports);
+
+/* Basis of the last Ned_RT build: per cell 18 rows (coarse basis order) of
+   NE + NF fine DoFs (edges x|y|z then faces x|y|z, lexicographic), sigma and u
+   of every basis function. Size in doubles, and copy to host. */
+int64_t msfec_nedrt_basis_size(const msfec_handle *handle);
+msfec_status msfec_nedrt_get_basis(msfec_handle *handle, double *Phi,
+                                   int64_t capacity);
 
 #ifdef __cplusplus
 }

@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "../../include/msfec_cuda.h"
+#include "nedrt_common.cuh"
 #include "q1_common.cuh"
 
 namespace msfec {
@@ -44,6 +45,10 @@ cudaError_t q1_galerkin_launch(const Q1Cell *cells, int ncells, const double *ph
 cudaError_t q1_report_launch(const Q1Stat *stats, int ncells, msfec_cell_report *rep, cudaStream_t stream);
 cudaError_t q1_eval_launch(const Q1Cell *cells, const double *phi, const double *weights, int npoints,
                            const int *cell_of, const double *pts, double *out, cudaStream_t stream);
+cudaError_t nedrt_solve_launch(bool fp64, const NRParams &prm, size_t smem, int grid, cudaStream_t st);
+cudaError_t nedrt_galerkin_launch(const NRCell *cells, int ncells, const double *phi, const double *y,
+                                  const msfec_load &load, double *KH, double *FH, msfec_cell_report *rep,
+                                  const NRStat *stats, cudaStream_t st);
 }  // namespace msfec
 
 using namespace msfec;
@@ -96,6 +101,14 @@ struct msfec_handle {
   DevBuf<msfec_cell_report> rep;
   DevBuf<double> eval_w, eval_pts, eval_out;
   DevBuf<int> eval_cell;
+  // Ned_RT state of the last build
+  DevBuf<NRCell> nr_cells;
+  DevBuf<NRItem> nr_items;
+  DevBuf<double> nr_phi, nr_y;
+  DevBuf<NRStat> nr_stats;
+  DevBuf<float> nr_scratch;
+  DevBuf<double> nr_ainv, nr_bdiv, nr_KH, nr_FH;
+  int64_t nr_basis_doubles = 0;
   int q1_ncells = 0;
   int64_t q1_basis_doubles = 0;
   std::vector<Q1Cell> h_cells;
@@ -145,7 +158,7 @@ bool cell_ok(const msfec_cell &c) {
 
 bool load_ok(const msfec_load *l) {
   if (!l) return true;
-  if (l->kind < MSFEC_LOAD_ZERO || l->kind > MSFEC_LOAD_SIN_PRODUCT) return false;
+  if (l->kind < MSFEC_LOAD_ZERO || l->kind > MSFEC_LOAD_VEC_TRIG) return false;
   for (int i = 0; i < 4; ++i)
     if (!std::isfinite(l->params[i])) return false;
   return true;
@@ -312,6 +325,103 @@ msfec_status q1_build_impl(msfec_handle *h, int ncells, const msfec_cell *cells,
   return MSFEC_SUCCESS;
 }
 
+
+constexpr int kNRMaxDepth = 4;
+constexpr size_t kNRSmemLimit = 200 * 1024;
+
+msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cells, const double *d_ainv,
+                              const double *d_bdiv, const msfec_load *load, double *d_KH, double *d_FH,
+                              msfec_cell_report *d_rep) {
+  const bool fp64 = h->cfg.precision == MSFEC_PRECISION_FP64;
+  std::vector<NRCell> hc(ncells);
+  int64_t fine = 0, dofs = 0;
+  int nmax = 0;
+  for (int c = 0; c < ncells; ++c) {
+    NRCell &q = hc[c];
+    const int n = 1 << cells[c].depth;
+    for (int d = 0; d < 3; ++d) {
+      q.origin[d] = cells[c].origin[d];
+      q.h[d] = cells[c].size[d] / n;
+    }
+    q.depth = cells[c].depth;
+    q.n = n;
+    q.coef_off = fine;
+    q.dof_off = dofs;
+    int NEx, NFx, NE, NF;
+    nr_counts(n, NEx, NFx, NE, NF);
+    fine += (int64_t)n * n * n;
+    dofs += NE + NF;
+    nmax = std::max(nmax, n);
+  }
+  // items: (cell, basis), deepest cells first
+  std::vector<int> order(ncells);
+  for (int c = 0; c < ncells; ++c) order[c] = c;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cells[x].depth > cells[y].depth; });
+  std::vector<NRItem> items;
+  items.reserve((size_t)ncells * 18);
+  for (int c : order)
+    for (int b = 0; b < 18; ++b) items.push_back(NRItem{c, b});
+  const size_t ws_floats = nr_workspace_floats(nmax, fp64 ? 8 : 4);
+  const bool use_smem = ws_floats * 4 <= kNRSmemLimit;
+  const size_t smem = use_smem ? ws_floats * 4 : 0;
+  cudaStream_t st = h->stream;
+  const int grid = std::min<int>((int)items.size(), h->num_sms);
+  MSFEC_CUDA_TRY(h, h->nr_cells.reserve(ncells));
+  MSFEC_CUDA_TRY(h, h->nr_items.reserve(items.size()));
+  MSFEC_CUDA_TRY(h, h->queue.reserve(1));
+  MSFEC_CUDA_TRY(h, h->nr_phi.reserve((size_t)dofs * 18));
+  MSFEC_CUDA_TRY(h, h->nr_y.reserve((size_t)dofs * 18));
+  MSFEC_CUDA_TRY(h, h->nr_stats.reserve((size_t)ncells * 18));
+  if (!use_smem) MSFEC_CUDA_TRY(h, h->nr_scratch.reserve(ws_floats * grid));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->nr_cells.ptr, hc.data(), hc.size() * sizeof(NRCell), cudaMemcpyHostToDevice, st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->nr_items.ptr, items.data(), items.size() * sizeof(NRItem),
+                                    cudaMemcpyHostToDevice, st));
+  MSFEC_CUDA_TRY(h, cudaMemsetAsync(h->queue.ptr, 0, sizeof(int), st));
+  NRParams prm;
+  prm.cells = h->nr_cells.ptr;
+  prm.items = h->nr_items.ptr;
+  prm.n_items = (int)items.size();
+  prm.queue = h->queue.ptr;
+  prm.ainv6 = d_ainv;
+  prm.bdiv = d_bdiv;
+  prm.phi = h->nr_phi.ptr;
+  prm.y = h->nr_y.ptr;
+  prm.stats = h->nr_stats.ptr;
+  prm.scratch = use_smem ? nullptr : h->nr_scratch.ptr;
+  prm.scratch_floats = ws_floats;
+  prm.use_smem = use_smem ? 1 : 0;
+  prm.rtol = h->cfg.nedrt_rtol;
+  prm.inner_rtol = h->cfg.inner_rtol;
+  prm.max_iter = std::max(h->cfg.max_iter, 20000);
+  prm.max_refine = h->cfg.max_refine;
+  if (h->cfg.verbose)
+    fprintf(stderr, "[msfec] nedrt plan: %d cells, %zu items, workspace %zu floats (%s), grid %d, %s\n", ncells,
+            items.size(), ws_floats, use_smem ? "shared" : "global", grid, fp64 ? "fp64" : "mixed");
+  if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[0], st));
+  MSFEC_CUDA_TRY(h, nedrt_solve_launch(fp64, prm, smem, grid, st));
+  if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[1], st));
+  msfec_load ld;
+  if (load) {
+    ld = *load;
+  } else {
+    std::memset(&ld, 0, sizeof(ld));
+  }
+  MSFEC_CUDA_TRY(h, nedrt_galerkin_launch(h->nr_cells.ptr, ncells, h->nr_phi.ptr, h->nr_y.ptr, ld, d_KH, d_FH, d_rep,
+                                          h->nr_stats.ptr, st));
+  if (h->timing) {
+    MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[2], st));
+    MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[3], st));
+    h->ev_recorded = true;
+  }
+  h->last_launches = d_rep ? 3 : 2;
+  h->nr_basis_doubles = dofs * 18;
+  return MSFEC_SUCCESS;
+}
+
+bool nr_load_ok(const msfec_load *l) {
+  return !l || l->kind == MSFEC_LOAD_ZERO || l->kind == MSFEC_LOAD_VEC_TRIG;
+}
+
 }  // namespace
 
 extern "C" {
@@ -326,6 +436,7 @@ void msfec_config_default(msfec_config *cfg) {
   cfg->max_iter = 2000;
   cfg->max_refine = 6;
   cfg->verbose = 0;
+  cfg->nedrt_rtol = 1e-14;
 }
 
 const char *msfec_status_string(msfec_status s) {
@@ -353,7 +464,8 @@ msfec_status msfec_create(msfec_handle **out, const msfec_config *cfg) {
   else
     msfec_config_default(&c);
   if (c.precision != MSFEC_PRECISION_FP64 && c.precision != MSFEC_PRECISION_MIXED) return MSFEC_ERROR_INVALID_ARGUMENT;
-  if (!(c.rtol > 0.0) || !(c.inner_rtol > 0.0) || c.inner_rtol >= 1.0 || c.max_iter < 1 || c.max_refine < 1)
+  if (!(c.rtol > 0.0) || !(c.inner_rtol > 0.0) || c.inner_rtol >= 1.0 || c.max_iter < 1 || c.max_refine < 1 ||
+      !(c.nedrt_rtol > 0.0))
     return MSFEC_ERROR_INVALID_ARGUMENT;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || c.device < 0 || c.device >= ndev) return MSFEC_ERROR_CUDA;
@@ -394,6 +506,16 @@ void msfec_destroy(msfec_handle *h) {
     h->eval_pts.release();
     h->eval_out.release();
     h->eval_cell.release();
+    h->nr_cells.release();
+    h->nr_items.release();
+    h->nr_phi.release();
+    h->nr_y.release();
+    h->nr_stats.release();
+    h->nr_scratch.release();
+    h->nr_ainv.release();
+    h->nr_bdiv.release();
+    h->nr_KH.release();
+    h->nr_FH.release();
     for (auto &e : h->ev)
       if (e) cudaEventDestroy(e);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
@@ -543,6 +665,86 @@ msfec_status msfec_q1_eval_fine(msfec_handle *h, const double *weights, int32_t 
                                    h->eval_pts.ptr, h->eval_out.ptr, st));
   MSFEC_CUDA_TRY(h, cudaMemcpyAsync(values, h->eval_out.ptr, (size_t)npoints * sizeof(double), cudaMemcpyDeviceToHost, st));
   MSFEC_CUDA_TRY(h, cudaStreamSynchronize(st));
+  return MSFEC_SUCCESS;
+}
+
+msfec_status msfec_nedrt_build_device(msfec_handle *h, int32_t ncells, const msfec_cell *cells, const double *d_ainv6,
+                                      const double *d_bdiv, const msfec_load *load, double *d_KH, double *d_FH,
+                                      msfec_cell_report *d_reports) {
+  if (!h) return MSFEC_ERROR_INVALID_ARGUMENT;
+  if (ncells < 0 || (ncells > 0 && (!cells || !d_ainv6 || !d_bdiv || !d_KH || !d_FH)))
+    return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "null pointer or negative cell count");
+  for (int c = 0; c < ncells; ++c)
+    if (!cell_ok(cells[c]) || cells[c].depth > kNRMaxDepth)
+      return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "cell " + std::to_string(c) + " invalid (Ned_RT depth 1..4)");
+  if (!load_ok(load) || !nr_load_ok(load)) return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "invalid Ned_RT load");
+  if (ncells == 0) {
+    h->nr_basis_doubles = 0;
+    return MSFEC_SUCCESS;
+  }
+  DeviceGuard g(h->device);
+  return nedrt_build_impl(h, ncells, cells, d_ainv6, d_bdiv, load, d_KH, d_FH, d_reports);
+}
+
+msfec_status msfec_nedrt_build(msfec_handle *h, int32_t ncells, const msfec_cell *cells, const double *ainv6,
+                               const double *bdiv, const msfec_load *load, double *KH, double *FH,
+                               msfec_cell_report *reports) {
+  if (!h) return MSFEC_ERROR_INVALID_ARGUMENT;
+  if (ncells < 0 || (ncells > 0 && (!cells || !ainv6 || !bdiv || !KH || !FH)))
+    return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "null pointer or negative cell count");
+  int64_t nfine = 0;
+  for (int c = 0; c < ncells; ++c) {
+    if (!cell_ok(cells[c]) || cells[c].depth > kNRMaxDepth)
+      return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "cell " + std::to_string(c) + " invalid (Ned_RT depth 1..4)");
+    const int64_t n = 1LL << cells[c].depth;
+    nfine += n * n * n;
+  }
+  if (!load_ok(load) || !nr_load_ok(load)) return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "invalid Ned_RT load");
+  for (int64_t e = 0; e < nfine; ++e) {
+    const double *a = ainv6 + 6 * e;
+    // SPD check of the 3x3 A^-1 (leading principal minors) and B > 0
+    const double m1 = a[0], m2 = a[0] * a[1] - a[3] * a[3];
+    const double m3 = a[0] * (a[1] * a[2] - a[5] * a[5]) - a[3] * (a[3] * a[2] - a[5] * a[4]) +
+                      a[4] * (a[3] * a[5] - a[1] * a[4]);
+    bool ok = m1 > 0.0 && m2 > 0.0 && m3 > 0.0 && bdiv[e] > 0.0 && std::isfinite(bdiv[e]);
+    for (int q = 0; q < 6; ++q) ok = ok && std::isfinite(a[q]);
+    if (!ok) return fail(h, MSFEC_ERROR_NUMERICAL, "A^-1 not SPD / finite or B not positive at fine cell " + std::to_string(e));
+  }
+  if (ncells == 0) return msfec_nedrt_build_device(h, 0, cells, nullptr, nullptr, load, nullptr, nullptr, nullptr);
+  DeviceGuard g(h->device);
+  cudaStream_t st = h->stream;
+  MSFEC_CUDA_TRY(h, h->nr_ainv.reserve(nfine * 6));
+  MSFEC_CUDA_TRY(h, h->nr_bdiv.reserve(nfine));
+  MSFEC_CUDA_TRY(h, h->nr_KH.reserve((size_t)ncells * 324));
+  MSFEC_CUDA_TRY(h, h->nr_FH.reserve((size_t)ncells * 18));
+  MSFEC_CUDA_TRY(h, h->rep.reserve(ncells));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->nr_ainv.ptr, ainv6, nfine * 6 * sizeof(double), cudaMemcpyHostToDevice, st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->nr_bdiv.ptr, bdiv, nfine * sizeof(double), cudaMemcpyHostToDevice, st));
+  msfec_status s = nedrt_build_impl(h, ncells, cells, h->nr_ainv.ptr, h->nr_bdiv.ptr, load, h->nr_KH.ptr, h->nr_FH.ptr,
+                                    h->rep.ptr);
+  if (s != MSFEC_SUCCESS) return s;
+  std::vector<msfec_cell_report> rep(ncells);
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(KH, h->nr_KH.ptr, (size_t)ncells * 324 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(FH, h->nr_FH.ptr, (size_t)ncells * 18 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(rep.data(), h->rep.ptr, (size_t)ncells * sizeof(msfec_cell_report),
+                                    cudaMemcpyDeviceToHost, st));
+  MSFEC_CUDA_TRY(h, cudaStreamSynchronize(st));
+  if (reports) std::memcpy(reports, rep.data(), rep.size() * sizeof(msfec_cell_report));
+  for (const auto &r : rep)
+    if (!r.converged) return fail(h, MSFEC_ERROR_NOT_CONVERGED, "at least one Ned_RT local solve missed nedrt_rtol");
+  return MSFEC_SUCCESS;
+}
+
+int64_t msfec_nedrt_basis_size(const msfec_handle *h) { return h ? h->nr_basis_doubles : 0; }
+
+msfec_status msfec_nedrt_get_basis(msfec_handle *h, double *Phi, int64_t capacity) {
+  if (!h || !Phi) return MSFEC_ERROR_INVALID_ARGUMENT;
+  if (h->nr_basis_doubles <= 0) return fail(h, MSFEC_ERROR_INVALID_STATE, "no Ned_RT basis built yet");
+  if (capacity < h->nr_basis_doubles) return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "capacity too small");
+  DeviceGuard g(h->device);
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(Phi, h->nr_phi.ptr, h->nr_basis_doubles * sizeof(double), cudaMemcpyDeviceToHost,
+                                    h->stream));
+  MSFEC_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
   return MSFEC_SUCCESS;
 }
 

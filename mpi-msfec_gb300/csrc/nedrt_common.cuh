@@ -1,0 +1,82 @@
+// Shared types of the Nedelec x Raviart-Thomas multiscale basis build (sm_103a).
+//
+// Fine DoF numbering per coarse cell (n = 2^depth fine cells per edge):
+//   edges [x | y | z], x-edge (i<n, j<=n, k<=n) -> i + n(j + (n+1)k), y-edge
+//   (i<=n, j<n, k<=n) -> NEx + i + (n+1)(j + n k), z-edge (i<=n, j<=n, k<n)
+//   -> 2NEx + i + (n+1)(j + (n+1)k); faces [x | y | z] after the NE edges,
+//   x-face (i<=n, j<n, k<n) -> i + (n+1)(j + n k), y-face (i<n, j<=n, k<n)
+//   -> NFx + i + n(j + (n+1)k), z-face (i<n, j<n, k<=n) -> 2NFx + i + n(j + n k).
+// Coarse basis b: 0..11 coarse edges in deal.II GeometryInfo<3> line order,
+// 12..17 coarse faces in face order.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace msfec {
+
+constexpr int kNRThreads = 512;
+constexpr int kNRWarps = kNRThreads / 32;
+
+struct NRCell {
+  double origin[3];
+  double h[3];
+  int depth;
+  int n;
+  long long coef_off;  // first fine cell in ainv6 / bdiv
+  long long dof_off;   // sum of previous cells' DoF counts; Phi base = 18 * dof_off
+};
+
+struct NRItem {
+  int cell;
+  int basis;  // 0..17
+};
+
+struct NRStat {
+  int iters;
+  int refinements;
+  int converged;
+  int flags;
+  double rel_residual;
+};
+
+struct NRParams {
+  const NRCell *cells;
+  const NRItem *items;
+  int n_items;
+  int *queue;
+  const double *ainv6;  // [fine][6]: a00 a11 a22 a01 a02 a12 of A^-1
+  const double *bdiv;   // [fine]
+  double *phi;          // [18][ndof] per cell
+  double *y;            // [18][ndof] per cell: A P_b (primary block of basis b)
+  NRStat *stats;        // [cell][18]
+  float *scratch;       // global workspace when the item does not fit shared memory
+  size_t scratch_floats;  // per CTA
+  int use_smem;
+  double rtol;
+  double inner_rtol;
+  int max_iter;
+  int max_refine;
+};
+
+__host__ __device__ inline void nr_counts(int n, int &NEx, int &NFx, int &NE, int &NF) {
+  NEx = n * (n + 1) * (n + 1);
+  NFx = (n + 1) * n * n;
+  NE = 3 * NEx;
+  NF = 3 * NFx;
+}
+
+// Workspace (floats) of one item: preconditioner (float) + 7 Krylov vectors
+// of precision T (tsize bytes), all over the full DoF set, plus float copies of
+// the coefficients (7 per fine cell).
+__host__ __device__ inline size_t nr_workspace_floats(int n, int tsize) {
+  int NEx, NFx, NE, NF;
+  nr_counts(n, NEx, NFx, NE, NF);
+  const size_t N = (size_t)NE + NF;
+  const size_t al = 64;
+  const size_t Np = (N + al - 1) / al * al;
+  const size_t nc = (size_t)n * n * n;
+  return Np + 7 * Np * (size_t)(tsize / 4) + (7 * nc + al - 1) / al * al;
+}
+
+}  // namespace msfec

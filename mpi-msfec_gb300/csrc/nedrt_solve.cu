@@ -1,0 +1,786 @@
+// Persistent batched Nedelec x Raviart-Thomas local solver (sm_103a).
+//
+// Restates, for every coarse cell x coarse basis function (12 edge + 6 face),
+// the reference's mixed local problem (konsim83/MPI-MSFEC):
+//   NedRTBasis::assemble_system   source/Ned_RT/ned_rt_basis.cc:361-576
+//     local matrix (A^-1 sigma, tau) - (u, curl tau) + (curl sigma, v) + (B div u, div v)
+//   setup_basis_dofs_curl / _div  ned_rt_basis.cc:224-359 (boundary data = coarse
+//     Nedelec / RT function, zero for the other field)
+//   run solve loop                ned_rt_basis.cc:1338-1381
+//   solve_iterative (Schur CG + ILU/GMRES there) ned_rt_basis.cc:636-847
+// The saddle-point system is solved with MINRES preconditioned by
+// diag(M)^-1 (+) diag(D + C^T diag(M)^-1 C)^-1 on the interior DoFs, FP32 inside
+// FP64 iterative refinement (MINRES in FP64 for the plain FP64 path); the
+// operator is applied matrix-free, cell by cell, from the per-cell A^-1 / B and
+// closed-form element tables, accumulating into shared memory with atomics.
+// The last FP64 pass writes y_b = A P_b (P_b the primary block of basis b:
+// sigma of an edge basis, u of a face basis) for the Galerkin product of
+// NedRTBasis::assemble_global_element_matrix (ned_rt_basis.cc:849-948).
+#include "../../include/msfec_cuda.h"
+#include "nedrt_common.cuh"
+
+namespace msfec {
+namespace nrimpl {
+
+struct NRShared {
+  double wred[kNRWarps][3];
+  double G[3][3][4][4];  // edge-mass geometry: M_e = sum_pq A^-1_pq G[p][q]
+  double C[12][6];       // (curl tau_l, v_f) on the fine cell
+  float Gf[3][3][4][4];
+  float Cf[12][6];
+  int item;
+};
+
+struct NRGeom {
+  int n, NEx, NFx, NE, NF, N;
+};
+
+__device__ __forceinline__ double psi(int a, double t) { return a ? t : 1.0 - t; }
+__device__ __forceinline__ double sgn(int a) { return a ? 1.0 : -1.0; }
+__device__ __forceinline__ double m1(int a, int b) { return a == b ? 1.0 / 3.0 : 1.0 / 6.0; }
+
+// The two axes other than p, in increasing order.
+__device__ __forceinline__ void other_axes(int p, int &o1, int &o2) {
+  o1 = p == 0 ? 1 : 0;
+  o2 = p == 2 ? 1 : 2;
+}
+
+// Position (0/1) along axis `ax` of local edge l4 (0..3) of direction p.
+__device__ __forceinline__ int edge_pos(int p, int l4, int ax) {
+  int o1, o2;
+  other_axes(p, o1, o2);
+  return ax == o1 ? (l4 & 1) : (l4 >> 1);
+}
+
+// Closed forms of the 2x2x2-Gauss integrals of lowest-order Nedelec / RT
+// functions on a box with sides h (exact: polynomial degree <= 3 per axis).
+__device__ double table_G(const double h[3], int p, int q, int l4, int m4) {
+  if (p == q) {
+    int o1, o2;
+    other_axes(p, o1, o2);
+    return h[o1] * h[o2] / h[p] * m1(l4 & 1, m4 & 1) * m1(l4 >> 1, m4 >> 1);
+  }
+  const int r = 3 - p - q;
+  return 0.25 * h[r] * m1(edge_pos(p, l4, r), edge_pos(q, m4, r));
+}
+
+__device__ double table_C(const double h[3], int l, int f) {
+  const int p = l >> 2, l4 = l & 3;
+  const int fd = f >> 1, fa = f & 1;
+  if (fd == p) return 0.0;
+  const double hx = h[0], hy = h[1], hz = h[2];
+  const int a0 = l4 & 1, a1 = l4 >> 1;  // positions along the two other axes
+  if (p == 0) {  // (b, c) = (y, z)
+    if (fd == 1) return sgn(a1) * hy * m1(a0, fa) / (hx * hz);
+    return -sgn(a0) * hz * m1(a1, fa) / (hx * hy);
+  }
+  if (p == 1) {  // (a, c) = (x, z)
+    if (fd == 0) return -sgn(a1) * hx * m1(a0, fa) / (hy * hz);
+    return sgn(a0) * hz * m1(a1, fa) / (hx * hy);
+  }
+  // p == 2, (a, b) = (x, y)
+  if (fd == 0) return sgn(a1) * hx * m1(a0, fa) / (hy * hz);
+  return -sgn(a0) * hy * m1(a1, fa) / (hx * hz);
+}
+
+__device__ __forceinline__ void cell_dofs(const NRGeom &g, int c, int (&e)[12], int (&f)[6]) {
+  const int n = g.n;
+  const int i = c % n, j = (c / n) % n, k = c / (n * n);
+  auto ex = [&](int a, int b, int cc) { return a + n * (b + (n + 1) * cc); };
+  auto ey = [&](int a, int b, int cc) { return g.NEx + a + (n + 1) * (b + n * cc); };
+  auto ez = [&](int a, int b, int cc) { return 2 * g.NEx + a + (n + 1) * (b + (n + 1) * cc); };
+  e[0] = ex(i, j, k);
+  e[1] = ex(i, j + 1, k);
+  e[2] = ex(i, j, k + 1);
+  e[3] = ex(i, j + 1, k + 1);
+  e[4] = ey(i, j, k);
+  e[5] = ey(i + 1, j, k);
+  e[6] = ey(i, j, k + 1);
+  e[7] = ey(i + 1, j, k + 1);
+  e[8] = ez(i, j, k);
+  e[9] = ez(i + 1, j, k);
+  e[10] = ez(i, j + 1, k);
+  e[11] = ez(i + 1, j + 1, k);
+  f[0] = g.NE + i + (n + 1) * (j + n * k);
+  f[1] = g.NE + (i + 1) + (n + 1) * (j + n * k);
+  f[2] = g.NE + g.NFx + i + n * (j + (n + 1) * k);
+  f[3] = g.NE + g.NFx + i + n * ((j + 1) + (n + 1) * k);
+  f[4] = g.NE + 2 * g.NFx + i + n * (j + n * k);
+  f[5] = g.NE + 2 * g.NFx + i + n * (j + n * (k + 1));
+}
+
+// (dir, i, j, k) of DoF d; returns true for a lattice-boundary DoF.
+__device__ bool dof_geometry(const NRGeom &g, int d, int &dir, int &i, int &j, int &k) {
+  const int n = g.n;
+  if (d < g.NE) {
+    dir = d / g.NEx;
+    const int t = d % g.NEx;
+    if (dir == 0) {
+      i = t % n; j = (t / n) % (n + 1); k = t / (n * (n + 1));
+      return j == 0 || j == n || k == 0 || k == n;
+    }
+    if (dir == 1) {
+      i = t % (n + 1); j = (t / (n + 1)) % n; k = t / ((n + 1) * n);
+      return i == 0 || i == n || k == 0 || k == n;
+    }
+    i = t % (n + 1); j = (t / (n + 1)) % (n + 1); k = t / ((n + 1) * (n + 1));
+    return i == 0 || i == n || j == 0 || j == n;
+  }
+  const int fidx = d - g.NE;
+  dir = 3 + fidx / g.NFx;
+  const int t = fidx % g.NFx;
+  if (dir == 3) {
+    i = t % (n + 1); j = (t / (n + 1)) % n; k = t / ((n + 1) * n);
+    return i == 0 || i == n;
+  }
+  if (dir == 4) {
+    i = t % n; j = (t / n) % (n + 1); k = t / (n * (n + 1));
+    return j == 0 || j == n;
+  }
+  i = t % n; j = (t / n) % n; k = t / (n * n);
+  return k == 0 || k == n;
+}
+
+// DoF value of coarse basis b (the reference's BasisNedelec / BasisRaviartThomas,
+// include/functions/basis_nedelec.tpp:38-85, basis_raviart_thomas.tpp:38-88, on
+// an axis-aligned coarse box): line integral along the fine edge / flux
+// through the fine face, exact since the coarse spaces nest in the fine ones.
+__device__ double coarse_dof(int b, int dir, int i, int j, int k, int n) {
+  if (b < 12) {
+    // GeometryInfo<3> lines: (direction, position along the two other axes)
+    const int ld[12] = {1, 1, 0, 0, 1, 1, 0, 0, 2, 2, 2, 2};
+    const int lp[12] = {0, 1, 0, 1, 0, 1, 0, 1, 0, 1, 0, 1};
+    const int lq[12] = {0, 0, 0, 0, 1, 1, 1, 1, 0, 0, 1, 1};
+    if (dir != ld[b]) return 0.0;
+    const int t1 = dir == 0 ? j : i;
+    const int t2 = dir == 2 ? j : k;
+    return psi(lp[b], (double)t1 / n) * psi(lq[b], (double)t2 / n) / n;
+  }
+  const int fd = (b - 12) >> 1, fa = (b - 12) & 1;
+  if (dir != 3 + fd) return 0.0;
+  const int pos = fd == 0 ? i : (fd == 1 ? j : k);
+  return psi(fa, (double)pos / n) / ((double)n * n);
+}
+
+// (v_f, curl N_b) for the 6 local faces of fine cell (i,j,k): the curl
+// right-hand side of an edge basis (full_rhs, ned_rt_basis.cc:502-511),
+// curl N_b as in BasisNedelecCurl (basis_nedelec_curl.tpp:106-147).
+__device__ void curl_rhs_cell(int b, int i, int j, int k, int n, const double h[3], double (&out)[6]) {
+  const int ld[12] = {1, 1, 0, 0, 1, 1, 0, 0, 2, 2, 2, 2};
+  const int lp[12] = {0, 1, 0, 1, 0, 1, 0, 1, 0, 1, 0, 1};
+  const int lq[12] = {0, 0, 0, 0, 1, 1, 1, 1, 0, 0, 1, 1};
+  const int d = ld[b], p = lp[b], q = lq[b];
+  const double Hx = h[0] * n, Hy = h[1] * n, Hz = h[2] * n;
+  const double gq = 0.5 / sqrt(3.0);
+  const double qp[2] = {0.5 - gq, 0.5 + gq};
+  const double jxw = 0.125 * h[0] * h[1] * h[2];
+  for (int t = 0; t < 6; ++t) out[t] = 0.0;
+  for (int qz = 0; qz < 2; ++qz)
+    for (int qy = 0; qy < 2; ++qy)
+      for (int qx = 0; qx < 2; ++qx) {
+        const double X = (i + qp[qx]) / n, Y = (j + qp[qy]) / n, Z = (k + qp[qz]) / n;
+        double cx = 0.0, cy = 0.0, cz = 0.0;
+        if (d == 0) {
+          cy = psi(p, Y) * sgn(q) / (Hx * Hz);
+          cz = -sgn(p) * psi(q, Z) / (Hx * Hy);
+        } else if (d == 1) {
+          cx = -psi(p, X) * sgn(q) / (Hy * Hz);
+          cz = sgn(p) * psi(q, Z) / (Hx * Hy);
+        } else {
+          cx = psi(p, X) * sgn(q) / (Hy * Hz);
+          cy = -sgn(p) * psi(q, Y) / (Hx * Hz);
+        }
+        const double xl = qp[qx], yl = qp[qy], zl = qp[qz];
+        out[0] += jxw * (1.0 - xl) / (h[1] * h[2]) * cx;
+        out[1] += jxw * xl / (h[1] * h[2]) * cx;
+        out[2] += jxw * (1.0 - yl) / (h[0] * h[2]) * cy;
+        out[3] += jxw * yl / (h[0] * h[2]) * cy;
+        out[4] += jxw * (1.0 - zl) / (h[0] * h[1]) * cz;
+        out[5] += jxw * zl / (h[0] * h[1]) * cz;
+      }
+}
+
+// Element operator of one fine cell: out += A_e z_e (18 DoFs), atomically.
+// MASK: 0 none, 1 keep only lattice-boundary values of z (lift of the
+// Dirichlet data), 2 keep only edge values, 3 keep only face values.
+template <typename TA, typename TV, typename TO, int MASK>
+__device__ __forceinline__ void cell_apply(const NRGeom &g, const TV *__restrict__ z, TO *out, const TA (&G)[3][3][4][4],
+                                           const TA (&C)[12][6], const TA (&ai)[6], TA bdiv, TA invV,
+                                           const int (&e)[12], const int (&f)[6], const bool (&eb)[12],
+                                           const bool (&fb)[6]) {
+  TA ze[12], zf[6];
+#pragma unroll
+  for (int l = 0; l < 12; ++l) {
+    const bool keep = MASK == 0 || (MASK == 1 && eb[l]) || MASK == 2;
+    ze[l] = keep ? (TA)z[e[l]] : TA(0);
+  }
+#pragma unroll
+  for (int t = 0; t < 6; ++t) {
+    const bool keep = MASK == 0 || (MASK == 1 && fb[t]) || MASK == 3;
+    zf[t] = keep ? (TA)z[f[t]] : TA(0);
+  }
+  const TA A[3][3] = {{ai[0], ai[3], ai[4]}, {ai[3], ai[1], ai[5]}, {ai[4], ai[5], ai[2]}};
+  TA ye[12];
+#pragma unroll
+  for (int l = 0; l < 12; ++l) ye[l] = TA(0);
+#pragma unroll
+  for (int p = 0; p < 3; ++p)
+#pragma unroll
+    for (int q = 0; q < 3; ++q)
+#pragma unroll
+      for (int l4 = 0; l4 < 4; ++l4) {
+        TA t = TA(0);
+#pragma unroll
+        for (int m4 = 0; m4 < 4; ++m4) t += G[p][q][l4][m4] * ze[4 * q + m4];
+        ye[4 * p + l4] += A[p][q] * t;
+      }
+  TA div = TA(0);
+#pragma unroll
+  for (int t = 0; t < 6; ++t) div += (t & 1) ? zf[t] : -zf[t];
+  const TA bd = bdiv * invV * div;
+#pragma unroll
+  for (int l = 0; l < 12; ++l) {
+    TA s = ye[l];
+#pragma unroll
+    for (int t = 0; t < 6; ++t) s -= C[l][t] * zf[t];
+    atomicAdd(out + e[l], (TO)s);
+  }
+#pragma unroll
+  for (int t = 0; t < 6; ++t) {
+    TA s = (t & 1) ? bd : -bd;
+#pragma unroll
+    for (int l = 0; l < 12; ++l) s += C[l][t] * ze[l];
+    atomicAdd(out + f[t], (TO)s);
+  }
+}
+
+template <typename VT, int NV>
+__device__ __forceinline__ void block_sum(NRShared &sh, VT (&v)[NV], VT (&out)[NV]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int t = 0; t < NV; ++t) {
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) v[t] += __shfl_xor_sync(0xffffffffu, v[t], off);
+  }
+  __syncthreads();  // previous readers of wred are done
+  if (lane == 0)
+#pragma unroll
+    for (int t = 0; t < NV; ++t) sh.wred[warp][t] = (double)v[t];
+  __syncthreads();
+#pragma unroll
+  for (int t = 0; t < NV; ++t) {
+    VT s = VT(0);
+#pragma unroll
+    for (int w = 0; w < kNRWarps; ++w) s += (VT)sh.wred[w][t];
+    out[t] = s;
+  }
+}
+
+template <typename T>
+__device__ void solve_item(const NRParams &prm, NRShared &sh, float *ws, int item_id) {
+  const NRItem it = prm.items[item_id];
+  const NRCell Cc = prm.cells[it.cell];
+  NRGeom g;
+  g.n = Cc.n;
+  nr_counts(g.n, g.NEx, g.NFx, g.NE, g.NF);
+  g.N = g.NE + g.NF;
+  const int n = g.n, N = g.N;
+  const int nc = n * n * n;
+  const int bb = it.basis;
+  const int tid = threadIdx.x;
+  constexpr bool kMixed = sizeof(T) == 4;
+  const double invV = 1.0 / (Cc.h[0] * Cc.h[1] * Cc.h[2]);
+  const size_t Np = ((size_t)N + 63) / 64 * 64;
+  // workspace carve (floats)
+  float *pd = ws;
+  T *zin = reinterpret_cast<T *>(ws + Np);
+  T *az = zin + Np;
+  T *vP = az + Np;  // v_{j-1}
+  T *vC = vP + Np;  // v_j
+  T *wP = vC + Np;
+  T *wC = wP + Np;
+  T *xk = wC + Np;
+  float *cf = ws + Np + 7 * Np * (sizeof(T) / 4);
+  double *dacc = reinterpret_cast<double *>(ws + Np);  // FP64 residual accumulator, aliases zin..
+  float *facc = ws + Np;
+  const double *ag = prm.ainv6 + 6 * Cc.coef_off;
+  const double *bg = prm.bdiv + Cc.coef_off;
+  double *phi = prm.phi + 18 * Cc.dof_off + (size_t)bb * N;
+  double *yout = prm.y + 18 * Cc.dof_off + (size_t)bb * N;
+
+  // tables
+  for (int t = tid; t < 144 + 72; t += kNRThreads) {
+    if (t < 144) {
+      const int p = t / 48, q = (t / 16) % 3, l4 = (t / 4) % 4, m4 = t % 4;
+      const double v = table_G(Cc.h, p, q, l4, m4);
+      sh.G[p][q][l4][m4] = v;
+      sh.Gf[p][q][l4][m4] = (float)v;
+    } else {
+      const int u = t - 144, l = u / 6, f = u % 6;
+      const double v = table_C(Cc.h, l, f);
+      sh.C[l][f] = v;
+      sh.Cf[l][f] = (float)v;
+    }
+  }
+  for (int c = tid; c < nc; c += kNRThreads) {
+#pragma unroll
+    for (int q = 0; q < 6; ++q) cf[7 * c + q] = (float)ag[6 * (size_t)c + q];
+    cf[7 * c + 6] = (float)bg[c];
+  }
+  for (int d = tid; d < N; d += kNRThreads) pd[d] = 0.0f;
+  __syncthreads();
+
+  // ---- block-Jacobi preconditioner: diag(M) on edges, then the lumped Schur
+  // diagonal D_ff + sum_l C_lf^2 / M_ll on faces (cell-local approximation).
+  for (int c = tid; c < nc; c += kNRThreads) {
+    int e[12], f[6];
+    cell_dofs(g, c, e, f);
+    const float *a = cf + 7 * c;
+    const float Ad[3] = {a[0], a[1], a[2]};
+#pragma unroll
+    for (int l = 0; l < 12; ++l) atomicAdd(pd + e[l], Ad[l >> 2] * sh.Gf[l >> 2][l >> 2][l & 3][l & 3]);
+  }
+  __syncthreads();
+  for (int c = tid; c < nc; c += kNRThreads) {
+    int e[12], f[6];
+    cell_dofs(g, c, e, f);
+    const float bdv = cf[7 * c + 6];
+    float me[12];
+#pragma unroll
+    for (int l = 0; l < 12; ++l) me[l] = pd[e[l]];
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      float s = bdv * (float)invV;
+#pragma unroll
+      for (int l = 0; l < 12; ++l) s += sh.Cf[l][t] * sh.Cf[l][t] / me[l];
+      atomicAdd(pd + f[t], s);
+    }
+  }
+  __syncthreads();
+  for (int d = tid; d < N; d += kNRThreads) {
+    int dir, i, j, k;
+    const bool bnd = dof_geometry(g, d, dir, i, j, k);
+    pd[d] = bnd ? 0.0f : 1.0f / pd[d];
+  }
+  __syncthreads();
+
+  double bnorm2 = 0.0, rnorm2 = 0.0;
+  int conv = 0, its = 0, flags = 0, nref = 0;
+
+  for (int ir = 0;; ++ir) {
+    const bool fp32_res = kMixed && ir == 0;
+    // ---------------- residual r = f - A phi on the interior ----------------
+    if (ir == 0) {
+      // phi0 = coarse function on every DoF (satisfies the boundary data)
+      for (int d = tid; d < N; d += kNRThreads) {
+        int dir, i, j, k;
+        dof_geometry(g, d, dir, i, j, k);
+        phi[d] = coarse_dof(bb, dir, i, j, k, n);
+      }
+      __syncthreads();
+    }
+    double part[2] = {0.0, 0.0};
+    for (int pass = (ir == 0 ? 0 : 1); pass < 2; ++pass) {
+      // pass 0: lift of the boundary data only (scale of the stopping test)
+      if (fp32_res) {
+        for (int d = tid; d < N; d += kNRThreads) facc[d] = 0.0f;
+      } else {
+        for (int d = tid; d < N; d += kNRThreads) dacc[d] = 0.0;
+      }
+      __syncthreads();
+      for (int c = tid; c < nc; c += kNRThreads) {
+        int e[12], f[6];
+        cell_dofs(g, c, e, f);
+        bool eb[12], fb[6];
+#pragma unroll
+        for (int l = 0; l < 12; ++l) {
+          int dir, i, j, k;
+          eb[l] = dof_geometry(g, e[l], dir, i, j, k);
+        }
+#pragma unroll
+        for (int t = 0; t < 6; ++t) {
+          int dir, i, j, k;
+          fb[t] = dof_geometry(g, f[t], dir, i, j, k);
+        }
+        double rc[6];
+        if (bb < 12) {
+          curl_rhs_cell(bb, c % n, (c / n) % n, c / (n * n), n, Cc.h, rc);
+        }
+        if (fp32_res) {
+          const float *a = cf + 7 * c;
+          const float ai[6] = {a[0], a[1], a[2], a[3], a[4], a[5]};
+          if (pass == 0)
+            cell_apply<float, double, float, 1>(g, phi, facc, sh.Gf, sh.Cf, ai, a[6], (float)invV, e, f, eb, fb);
+          else
+            cell_apply<float, double, float, 0>(g, phi, facc, sh.Gf, sh.Cf, ai, a[6], (float)invV, e, f, eb, fb);
+          if (bb < 12)
+#pragma unroll
+            for (int t = 0; t < 6; ++t) atomicAdd(facc + f[t], (float)-rc[t]);
+        } else {
+          const double *a = ag + 6 * (size_t)c;
+          const double ai[6] = {a[0], a[1], a[2], a[3], a[4], a[5]};
+          if (pass == 0)
+            cell_apply<double, double, double, 1>(g, phi, dacc, sh.G, sh.C, ai, bg[c], invV, e, f, eb, fb);
+          else
+            cell_apply<double, double, double, 0>(g, phi, dacc, sh.G, sh.C, ai, bg[c], invV, e, f, eb, fb);
+          if (bb < 12)
+#pragma unroll
+            for (int t = 0; t < 6; ++t) atomicAdd(dacc + f[t], -rc[t]);
+        }
+      }
+      __syncthreads();
+      // r = -(A phi - f) on interior DoFs (boundary: 0), kept in vC
+      for (int d = tid; d < N; d += kNRThreads) {
+        const bool interior = pd[d] > 0.0f;
+        const double r = interior ? -(fp32_res ? (double)facc[d] : dacc[d]) : 0.0;
+        part[pass] += r * r;
+        if (pass == 1) vC[d] = (T)r;  // read after the next barrier; aliasing is disjoint (vC past acc)
+      }
+      __syncthreads();
+    }
+    {
+      double tot[2];
+      block_sum<double, 2>(sh, part, tot);
+      if (ir == 0) bnorm2 = tot[0];
+      rnorm2 = tot[1];
+    }
+    ++nref;
+    conv = !fp32_res && (rnorm2 <= prm.rtol * prm.rtol * bnorm2);
+    if (conv || ir >= prm.max_refine) break;
+
+    // ---------------- MINRES on A_II d = r, precision T ----------------
+    // (Paige-Saunders recurrences in the form of Elman, Silvester & Wathen,
+    // preconditioned by pd; x0 = 0.)
+    for (int d = tid; d < N; d += kNRThreads) {
+      vP[d] = T(0);
+      wP[d] = T(0);
+      wC[d] = T(0);
+      xk[d] = T(0);
+      az[d] = T(0);
+    }
+    T gam;  // gamma_1
+    {
+      T p1[1] = {T(0)};
+      for (int d = tid; d < N; d += kNRThreads) {
+        const T z = (T)pd[d] * vC[d];
+        zin[d] = z;
+        p1[0] += z * vC[d];
+      }
+      T t1[1];
+      block_sum<T, 1>(sh, p1, t1);
+      gam = sqrt(t1[0]);
+    }
+    const T eta0 = gam;
+    T eta = gam, gam_prev = T(1), c_prev = T(1), cc = T(1), s_prev = T(0), ss = T(0);
+    const double tol_abs = prm.rtol * sqrt(bnorm2);
+    // inner target on |eta| (preconditioned residual): relative reduction for
+    // the mixed path, the outer tolerance (mapped through eta0/||r||) for FP64.
+    const T target = kMixed ? (T)(prm.inner_rtol * (double)eta0)
+                            : (T)(0.1 * tol_abs * (double)eta0 / fmax(sqrt(rnorm2), 1e-300));
+    bool active = gam > T(0) && isfinite((double)gam);
+    if (active) {
+      const T inv = T(1) / gam;
+      for (int d = tid; d < N; d += kNRThreads) {
+        zin[d] *= inv;
+        vC[d] *= inv;  // v_1 normalised consistently with z_1
+      }
+    }
+    // v is carried unnormalised in the recurrence below: v_{j+1} = A z_j -
+    // (delta/gamma_j) v_j - (gamma_j/gamma_{j-1}) v_{j-1} with z_j = P v_j / gamma_j.
+    // Using normalised vC (= v_j / gamma_j) the update reads
+    // vnew = A z_j - delta vC - gamma_j vP, z_{j+1} = P vnew, gamma_{j+1} = sqrt(z.vnew).
+    __syncthreads();
+    for (int iter = 0; active && iter < prm.max_iter; ++iter) {
+      // az = A zin
+      for (int c = tid; c < nc; c += kNRThreads) {
+        int e[12], f[6];
+        cell_dofs(g, c, e, f);
+        const bool eb[12] = {}, fb[6] = {};
+        if constexpr (kMixed) {
+          const float *a = cf + 7 * c;
+          const float ai[6] = {a[0], a[1], a[2], a[3], a[4], a[5]};
+          cell_apply<float, float, float, 0>(g, zin, az, sh.Gf, sh.Cf, ai, a[6], (float)invV, e, f, eb, fb);
+        } else {
+          const double *a = ag + 6 * (size_t)c;
+          const double ai[6] = {a[0], a[1], a[2], a[3], a[4], a[5]};
+          cell_apply<double, double, double, 0>(g, zin, az, sh.G, sh.C, ai, bg[c], invV, e, f, eb, fb);
+        }
+      }
+      __syncthreads();
+      T delta;
+      {
+        T p1[1] = {T(0)};
+        for (int d = tid; d < N; d += kNRThreads)
+          if (pd[d] > 0.0f) p1[0] += az[d] * zin[d];
+        T t1[1];
+        block_sum<T, 1>(sh, p1, t1);
+        delta = t1[0];
+      }
+      // vnew -> vP slot, gamma_{j+1}
+      T gnew;
+      {
+        T p1[1] = {T(0)};
+        for (int d = tid; d < N; d += kNRThreads) {
+          T vn = T(0);
+          if (pd[d] > 0.0f) vn = az[d] - delta * vC[d] - gam * vP[d];
+          vP[d] = vn;
+          p1[0] += (T)pd[d] * vn * vn;
+        }
+        T t1[1];
+        block_sum<T, 1>(sh, p1, t1);
+        gnew = sqrt(fmax(t1[0], T(0)));
+      }
+      const T a0 = cc * delta - c_prev * ss * gam;
+      const T a1 = sqrt(a0 * a0 + gnew * gnew);
+      const T a2 = ss * delta + c_prev * cc * gam;
+      const T a3 = s_prev * gam;
+      if (!(a1 > T(0)) || !isfinite((double)a1)) {
+        flags |= 1;
+        break;
+      }
+      const T cn = a0 / a1, sn = gnew / a1;
+      const T step = cn * eta;
+      const T ginv = gnew > T(0) ? T(1) / gnew : T(0);
+      // w_{j+1} = (z_j - a3 w_{j-1} - a2 w_j) / a1 -> wP slot; x += c eta w;
+      // next: zin = P vnew / gnew, vC <- vnew / gnew, vP <- old vC (scaled by 1)
+      for (int d = tid; d < N; d += kNRThreads) {
+        const T wn = (zin[d] - a3 * wP[d] - a2 * wC[d]) / a1;
+        wP[d] = wC[d];
+        wC[d] = wn;
+        xk[d] += step * wn;
+        const T vnew = vP[d];
+        vP[d] = vC[d];
+        vC[d] = vnew * ginv;
+        zin[d] = (T)pd[d] * vnew * ginv;
+        az[d] = T(0);
+      }
+      ++its;
+      eta = -sn * eta;
+      gam_prev = gam;
+      gam = gnew;
+      c_prev = cc;
+      cc = cn;
+      s_prev = ss;
+      ss = sn;
+      (void)gam_prev;
+      if (fabs((double)eta) <= (double)target || gnew == T(0)) active = false;
+      __syncthreads();
+    }
+    // ---------------- phi_I += x (FP64, HBM) ----------------
+    for (int d = tid; d < N; d += kNRThreads)
+      if (pd[d] > 0.0f) phi[d] += (double)xk[d];
+    __syncthreads();
+  }
+
+  // ---------------- y_b = A P_b (FP64), P_b = primary block of basis b ----------------
+  for (int d = tid; d < N; d += kNRThreads) dacc[d] = 0.0;
+  __syncthreads();
+  for (int c = tid; c < nc; c += kNRThreads) {
+    int e[12], f[6];
+    cell_dofs(g, c, e, f);
+    const bool eb[12] = {}, fb[6] = {};
+    const double *a = ag + 6 * (size_t)c;
+    const double ai[6] = {a[0], a[1], a[2], a[3], a[4], a[5]};
+    if (bb < 12)
+      cell_apply<double, double, double, 2>(g, phi, dacc, sh.G, sh.C, ai, bg[c], invV, e, f, eb, fb);
+    else
+      cell_apply<double, double, double, 3>(g, phi, dacc, sh.G, sh.C, ai, bg[c], invV, e, f, eb, fb);
+  }
+  __syncthreads();
+  for (int d = tid; d < N; d += kNRThreads) yout[d] = dacc[d];
+  if (tid == 0) {
+    NRStat st;
+    st.iters = its;
+    st.refinements = nref;
+    st.converged = conv;
+    st.flags = flags;
+    st.rel_residual = bnorm2 > 0.0 ? sqrt(rnorm2 / bnorm2) : sqrt(rnorm2);
+    prm.stats[(size_t)it.cell * 18 + bb] = st;
+  }
+  __syncthreads();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kNRThreads, 1) nedrt_solve_kernel(NRParams prm) {
+  extern __shared__ __align__(256) unsigned char smem[];
+  __shared__ NRShared sh;
+  float *ws = prm.use_smem ? reinterpret_cast<float *>(smem) : prm.scratch + (size_t)blockIdx.x * prm.scratch_floats;
+  for (;;) {
+    if (threadIdx.x == 0) sh.item = atomicAdd(prm.queue, 1);
+    __syncthreads();
+    const int item = sh.item;
+    if (item >= prm.n_items) break;
+    solve_item<T>(prm, sh, ws, item);
+  }
+}
+
+constexpr int kGalThreads = 256;
+constexpr int kGalWarps = kGalThreads / 32;
+
+__device__ __forceinline__ void dmma(double &c0, double &c1, double a, double b) {
+  asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};\n"
+               : "+d"(c0), "+d"(c1)
+               : "d"(a), "d"(b));
+}
+
+// Average of sin(w x) over fine cell `cell` along one axis (2-point Gauss).
+__device__ double gauss_sin_avg(double x0, double h, int cell, double w) {
+  const double gq = 0.5 / sqrt(3.0);
+  return 0.5 * (sin(w * (x0 + (cell + 0.5 - gq) * h)) + sin(w * (x0 + (cell + 0.5 + gq) * h)));
+}
+
+// K_H[i][j] = P_i . y_j over all DoFs (P_i: primary block of basis i), on
+// the FP64 tensor pipe (m8n8k4 tiles of the 24x24 padded product);
+// F_H[12+f] = u_f . (v, f) (reference ned_rt_basis.cc:937-944).
+__global__ void __launch_bounds__(kGalThreads) nedrt_galerkin_kernel(const NRCell *__restrict__ cells,
+                                                                     const double *__restrict__ phi,
+                                                                     const double *__restrict__ y, msfec_load load,
+                                                                     double *__restrict__ KH, double *__restrict__ FH) {
+  __shared__ double red[kGalWarps][24 * 24];
+  __shared__ double redf[kGalWarps][8];
+  __shared__ double stab[3][65];  // 1D Gauss averages of sin per axis
+  const int c = blockIdx.x;
+  const NRCell C = cells[c];
+  NRGeom g;
+  g.n = C.n;
+  nr_counts(g.n, g.NEx, g.NFx, g.NE, g.NF);
+  g.N = g.NE + g.NF;
+  const int n = g.n, N = g.N;
+  const bool has_load = load.kind == MSFEC_LOAD_VEC_TRIG;
+  const double w = load.params[1] * M_PI;
+  for (int t = threadIdx.x; t < 3 * n; t += kGalThreads) {
+    const int d = t / n, i = t % n;
+    stab[d][i] = has_load ? gauss_sin_avg(C.origin[d], C.h[d], i, w) : 0.0;
+  }
+  __syncthreads();
+  const double *P = phi + 18 * C.dof_off;
+  const double *Y = y + 18 * C.dof_off;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int gr = lane >> 2, t4 = lane & 3;
+  double acc[3][3][2];
+#pragma unroll
+  for (int I = 0; I < 3; ++I)
+#pragma unroll
+    for (int J = 0; J < 3; ++J) acc[I][J][0] = acc[I][J][1] = 0.0;
+  for (int base = warp * 4; base < N; base += kGalWarps * 4) {
+    const int d = base + t4;
+    const bool ok = d < N;
+    const bool is_edge = d < g.NE;
+    double a[3], b[3];
+#pragma unroll
+    for (int I = 0; I < 3; ++I) {
+      const int row = 8 * I + gr;
+      const bool prim = row < 18 && ((row < 12) == is_edge);
+      a[I] = (ok && prim) ? __ldcs(P + (size_t)row * N + d) : 0.0;
+      b[I] = (ok && row < 18) ? __ldcs(Y + (size_t)row * N + d) : 0.0;
+    }
+#pragma unroll
+    for (int I = 0; I < 3; ++I)
+#pragma unroll
+      for (int J = 0; J < 3; ++J) dmma(acc[I][J][0], acc[I][J][1], a[I], b[J]);
+  }
+  // F_H: face rows only (edge rows of the reference's global_element_rhs stay 0)
+  {
+    double f6[6] = {0, 0, 0, 0, 0, 0};
+    if (has_load)
+      for (int d = g.NE + threadIdx.x; d < N; d += kGalThreads) {
+        int dir, i, j, k;
+        dof_geometry(g, d, dir, i, j, k);
+        const int fd = dir - 3;
+        const int pos = fd == 0 ? i : (fd == 1 ? j : k);
+        const double nadj = (pos == 0 || pos == n) ? 1.0 : 2.0;
+        double s1, s2;
+        if (fd == 0) {
+          s1 = stab[1][j];
+          s2 = stab[2][k];
+        } else if (fd == 1) {
+          s1 = stab[2][k];
+          s2 = stab[0][i];
+        } else {
+          s1 = stab[0][i];
+          s2 = stab[1][j];
+        }
+        const double bl = load.params[0] * 0.5 * C.h[fd] * nadj * s1 * s2;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) f6[q] += P[(size_t)(12 + q) * N + d] * bl;
+      }
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+      double v = f6[q];
+#pragma unroll
+      for (int off = 16; off >= 1; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+      if (lane == 0) redf[warp][q] = v;
+    }
+  }
+#pragma unroll
+  for (int I = 0; I < 3; ++I)
+#pragma unroll
+    for (int J = 0; J < 3; ++J) {
+      const int row = 8 * I + gr;
+      red[warp][row * 24 + 8 * J + 2 * t4] = acc[I][J][0];
+      red[warp][row * 24 + 8 * J + 2 * t4 + 1] = acc[I][J][1];
+    }
+  __syncthreads();
+  for (int t = threadIdx.x; t < 18 * 18; t += kGalThreads) {
+    const int i = t / 18, j = t % 18;
+    double s = 0.0;
+    for (int wv = 0; wv < kGalWarps; ++wv) s += red[wv][i * 24 + j];
+    KH[(size_t)c * 324 + t] = s;
+  }
+  if (threadIdx.x < 18) {
+    double s = 0.0;
+    if (threadIdx.x >= 12)
+      for (int wv = 0; wv < kGalWarps; ++wv) s += redf[wv][threadIdx.x - 12];
+    FH[(size_t)c * 18 + threadIdx.x] = s;
+  }
+}
+
+__global__ void nedrt_report_kernel(const NRStat *__restrict__ stats, int ncells, msfec_cell_report *rep) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncells) return;
+  msfec_cell_report r;
+  r.iterations = 0;
+  r.refinements = 0;
+  r.converged = 1;
+  r.reserved = 0;
+  r.residual = 0.0;
+  for (int v = 0; v < 18; ++v) {
+    const NRStat s = stats[(size_t)c * 18 + v];
+    r.iterations = max(r.iterations, s.iters);
+    r.refinements = max(r.refinements, s.refinements);
+    r.converged = r.converged && s.converged && !(s.flags & 1);
+    r.residual = fmax(r.residual, s.rel_residual);
+    if (!isfinite(s.rel_residual)) r.residual = s.rel_residual;
+  }
+  rep[c] = r;
+}
+
+}  // namespace nrimpl
+
+cudaError_t nedrt_solve_launch(bool fp64, const NRParams &prm, size_t smem, int grid, cudaStream_t st) {
+  if (fp64) {
+    auto k = nrimpl::nedrt_solve_kernel<double>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k<<<grid, kNRThreads, smem, st>>>(prm);
+  } else {
+    auto k = nrimpl::nedrt_solve_kernel<float>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k<<<grid, kNRThreads, smem, st>>>(prm);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t nedrt_galerkin_launch(const NRCell *cells, int ncells, const double *phi, const double *y,
+                                  const msfec_load &load, double *KH, double *FH, msfec_cell_report *rep,
+                                  const NRStat *stats, cudaStream_t st) {
+  if (ncells <= 0) return cudaSuccess;
+  nrimpl::nedrt_galerkin_kernel<<<ncells, nrimpl::kGalThreads, 0, st>>>(cells, phi, y, load, KH, FH);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || !rep) return e;
+  nrimpl::nedrt_report_kernel<<<(ncells + 127) / 128, 128, 0, st>>>(stats, ncells, rep);
+  return cudaGetLastError();
+}
+
+}  // namespace msfec

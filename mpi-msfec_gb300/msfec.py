@@ -27,7 +27,7 @@ ERROR_INVALID_STATE = 7
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
 
-LOAD_ZERO, LOAD_CONSTANT, LOAD_SIN_PRODUCT = 0, 1, 2
+LOAD_ZERO, LOAD_CONSTANT, LOAD_SIN_PRODUCT, LOAD_VEC_TRIG = 0, 1, 2, 3
 
 # Every symbol the public header declares (checked by the CPU test suite).
 EXPORTED = [
@@ -35,6 +35,8 @@ EXPORTED = [
     "msfec_last_error", "msfec_set_stream", "msfec_set_precision", "msfec_q1_build",
     "msfec_q1_build_device", "msfec_q1_basis_size", "msfec_q1_get_basis",
     "msfec_q1_basis_device", "msfec_q1_eval_fine", "msfec_set_timing", "msfec_get_timings",
+    "msfec_nedrt_build", "msfec_nedrt_build_device", "msfec_nedrt_basis_size",
+    "msfec_nedrt_get_basis",
 ]
 
 
@@ -42,7 +44,7 @@ class Config(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("precision", ctypes.c_int32), ("rtol", ctypes.c_double),
                 ("inner_rtol", ctypes.c_double), ("max_iter", ctypes.c_int32),
                 ("max_refine", ctypes.c_int32), ("verbose", ctypes.c_int32),
-                ("reserved", ctypes.c_int32)]
+                ("reserved", ctypes.c_int32), ("nedrt_rtol", ctypes.c_double)]
 
 
 class Cell(ctypes.Structure):
@@ -114,6 +116,16 @@ def load_library(path: str = LIB_PATH):
     L.msfec_q1_basis_device.restype = _vp
     L.msfec_q1_eval_fine.argtypes = [_vp, _dp, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32), _dp, _dp]
     L.msfec_q1_eval_fine.restype = ctypes.c_int
+    L.msfec_nedrt_build.argtypes = [_vp, ctypes.c_int32, _vp, _dp, _dp, ctypes.POINTER(Load), _dp, _dp,
+                                    _vp]
+    L.msfec_nedrt_build.restype = ctypes.c_int
+    L.msfec_nedrt_build_device.argtypes = [_vp, ctypes.c_int32, _vp, _vp, _vp, ctypes.POINTER(Load), _vp,
+                                           _vp, _vp]
+    L.msfec_nedrt_build_device.restype = ctypes.c_int
+    L.msfec_nedrt_basis_size.argtypes = [_vp]
+    L.msfec_nedrt_basis_size.restype = ctypes.c_int64
+    L.msfec_nedrt_get_basis.argtypes = [_vp, _dp, ctypes.c_int64]
+    L.msfec_nedrt_get_basis.restype = ctypes.c_int
     L.msfec_set_timing.argtypes = [_vp, ctypes.c_int32]
     L.msfec_set_timing.restype = ctypes.c_int
     L.msfec_get_timings.argtypes = [_vp, ctypes.POINTER(Timings)]
@@ -155,7 +167,7 @@ class Handle:
     """One msfec handle (device buffers + stream)."""
 
     def __init__(self, precision=PRECISION_MIXED, device=0, rtol=None, inner_rtol=None,
-                 max_iter=None, max_refine=None, verbose=0):
+                 max_iter=None, max_refine=None, verbose=0, nedrt_rtol=None):
         L = load_library()
         cfg = Config()
         L.msfec_config_default(ctypes.byref(cfg))
@@ -169,6 +181,8 @@ class Handle:
             cfg.max_iter = max_iter
         if max_refine is not None:
             cfg.max_refine = max_refine
+        if nedrt_rtol is not None:
+            cfg.nedrt_rtol = nedrt_rtol
         cfg.verbose = int(verbose or os.environ.get("MSFEC_VERBOSE", "0"))
         self.cfg = cfg
         h = _vp()
@@ -238,6 +252,34 @@ class Handle:
         self.check(self._lib.msfec_get_timings(self._h, ctypes.byref(t)))
         return {"solve_ms": t.solve_ms, "galerkin_ms": t.galerkin_ms, "total_ms": t.total_ms,
                 "solve_launches": t.solve_launches, "kernel_launches": t.kernel_launches}
+
+    def nedrt_build(self, cells, ainv6, bdiv, load=None, allow_unconverged=False):
+        """Host-buffer Ned_RT build. Returns (KH [c,18,18], FH [c,18], reports, status)."""
+        cells = np.ascontiguousarray(cells, dtype=CELL_DTYPE)
+        nc = cells.shape[0]
+        ainv6 = np.ascontiguousarray(ainv6, dtype=np.float64)
+        bdiv = np.ascontiguousarray(bdiv, dtype=np.float64)
+        KH = np.zeros((nc, 18, 18))
+        FH = np.zeros((nc, 18))
+        rep = np.zeros(nc, dtype=REPORT_DTYPE)
+        ld = load if load is not None else make_load()
+        st = self._lib.msfec_nedrt_build(self._h, nc, cells.ctypes.data_as(_vp), _d(ainv6), _d(bdiv),
+                                         ctypes.byref(ld), _d(KH), _d(FH), rep.ctypes.data_as(_vp))
+        self.check(st, allow=(ERROR_NOT_CONVERGED,) if allow_unconverged else ())
+        return KH, FH, rep, st
+
+    def nedrt_build_device(self, cells, d_ainv6, d_bdiv, load, d_KH, d_FH, d_reports):
+        cells = np.ascontiguousarray(cells, dtype=CELL_DTYPE)
+        st = self._lib.msfec_nedrt_build_device(self._h, cells.shape[0], cells.ctypes.data_as(_vp),
+                                                _vp(d_ainv6), _vp(d_bdiv), ctypes.byref(load),
+                                                _vp(d_KH), _vp(d_FH), _vp(d_reports or 0))
+        return self.check(st)
+
+    def nedrt_basis(self):
+        n = self._lib.msfec_nedrt_basis_size(self._h)
+        out = np.zeros(n)
+        self.check(self._lib.msfec_nedrt_get_basis(self._h, _d(out), n))
+        return out
 
     def q1_basis(self):
         n = self._lib.msfec_q1_basis_size(self._h)

@@ -11,6 +11,13 @@ and seeded (numpy PCG64), identical on x86_64 and aarch64:
                  sin(2 pi x/eps) sin(2 pi y/eps) sin(2 pi z/eps)) exp(0.5 xi_c),
                  eps = 1/64, xi_c ~ N(0,1) per coarse cell, sampled at
                  fine-cell centres                     (batched uneven Q1)
+  nedrt_tensor   coarse m^3 cells, depth L, A_e = R_e diag(e^g1, e^g2, e^g3) R_e^T
+                 per fine cell, g ~ N(0,1), R_e Haar-random rotation (QR of a
+                 Gaussian 3x3, sign-fixed, det +1); B = 1 - 0.9 sin(2 pi 14 x)
+                 at fine-cell centres (the reference's example div-div
+                 coefficient, example_parameters/prm_ned_rt_test-01.prm);
+                 f = (sin pi y sin pi z, sin pi z sin pi x, sin pi x sin pi y)
+                 (coarse 8^3, L = 3: the small mixed case; 16^3, L = 4: large)
 Coarse cells are listed lexicographically (x fastest); fine-cell arrays per
 coarse cell are lexicographic too.
 """
@@ -18,7 +25,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from msfec import CELL_DTYPE, LOAD_SIN_PRODUCT, make_load
+from msfec import CELL_DTYPE, LOAD_SIN_PRODUCT, LOAD_VEC_TRIG, make_load
 
 
 def coarse_grid(m, depths, lo=0.0, hi=1.0):
@@ -84,3 +91,36 @@ def q1_uneven(m=16, seed=3, eps=1.0 / 64.0, depths=(2, 3, 4, 5)):
     a = np.concatenate(a_parts)
     load = make_load(LOAD_SIN_PRODUCT, (1.0, 1.0, 0.0, 0.0))
     return cells, a, None, load
+
+
+def haar_rotations(rng, count):
+    """Haar-random rotations: QR of Gaussian 3x3 with the sign of diag(R) fixed, det +1."""
+    G = rng.standard_normal((count, 3, 3))
+    Q, Rm = np.linalg.qr(G)
+    d = np.sign(np.diagonal(Rm, axis1=1, axis2=2))
+    d[d == 0] = 1.0
+    Q = Q * d[:, None, :]
+    det = np.linalg.det(Q)
+    Q[:, :, 0] *= np.sign(det)[:, None]
+    return Q
+
+
+def nedrt_tensor(m=8, depth=3, seed=2, kb=14.0):
+    """Ned_RT workload; returns cells, A^-1 as [fine, 6] (a00 a11 a22 a01 a02 a12), B, load."""
+    rng = np.random.default_rng(seed)
+    cells = coarse_grid(m, depth)
+    nf = int(np.sum(fine_counts(cells)[0]))
+    g = rng.standard_normal((nf, 3))
+    Rr = haar_rotations(rng, nf)
+    ainv = np.einsum("cij,cj,ckj->cik", Rr, np.exp(-g), Rr)
+    ainv6 = np.stack([ainv[:, 0, 0], ainv[:, 1, 1], ainv[:, 2, 2], ainv[:, 0, 1], ainv[:, 0, 2],
+                      ainv[:, 1, 2]], 1)
+    x = fine_centres(cells)[:, 0]
+    bdiv = 1.0 - 0.9 * np.sin(2 * np.pi * kb * x)
+    load = make_load(LOAD_VEC_TRIG, (1.0, 1.0, 0.0, 0.0))
+    return cells, ainv6, bdiv, load
+
+
+def nedrt_work_dof_rhs(cells):
+    n = 1 << cells["depth"].astype(np.int64)
+    return int(np.sum(3 * n * (n + 1) ** 2 + 3 * n * n * (n + 1)) * 18)

@@ -1,0 +1,352 @@
+"""FP64 CPU oracle, Nedelec x Raviart-Thomas pairing (numpy + scipy SuperLU).
+
+TEST INFRASTRUCTURE ONLY: the checker of the CUDA path in tests/, smoke and the
+CPU baseline of bench.py; the product library never imports it.
+
+Restates the reference's mixed local basis problem (konsim83/MPI-MSFEC):
+  setup_grid / setup_system_matrix  source/Ned_RT/ned_rt_basis.cc:166-222
+  setup_basis_dofs_curl (12 sets)   ned_rt_basis.cc:224-292
+  setup_basis_dofs_div  (6 sets)    ned_rt_basis.cc:294-359
+  assemble_system                   ned_rt_basis.cc:361-576 (local matrix :488-496,
+                                     curl rhs :502-511, global load :500)
+  solve_direct (UMFPACK)            ned_rt_basis.cc:578-634 -> SuperLU here,
+                                     one factorisation shared by the 18 solves
+  assemble_global_element_matrix    ned_rt_basis.cc:849-948
+  coarse shape functions            include/functions/basis_nedelec.tpp:38-85,
+                                     basis_raviart_thomas.tpp:38-88,
+                                     basis_nedelec_curl.tpp:38-147
+Lowest-order Nedelec sigma on fine edges, RT0 u on fine faces of the
+uniformly refined axis-aligned coarse box. DoF functionals (pinned by the
+reference's golden Nedelec projection output): edge DoF = line integral of
+the tangential component along the positive axis; face DoF = flux through the
+face in the positive axis direction. The element integrals use the
+reference's QGauss<3>(degree + 2) = 2x2x2 Gauss rule (exact here: the
+coefficients are constant per fine cell).
+
+Sign conventions of the block system, identical to the reference:
+  [ M   -C ] [sigma]   [f0]      M_ij = (A^-1 tau_j, tau_i),  C_ij = (curl tau_i, v_j)
+  [ C^T  D ] [  u  ] = [f1]      D_ij = (B div v_j, div v_i)
+Coarse basis order: 12 edges in deal.II GeometryInfo<3> line order, then 6
+faces in face order (line l / face f <-> coarse DoF l / 12 + f).
+
+Fine DoF numbering (lexicographic, not deal.II's): x-edges (i<n, j<=n, k<=n)
+i + n(j + (n+1)k), then y-edges, z-edges; x-faces (i<=n, j<n, k<n), y-, z-faces.
+"""
+from __future__ import annotations
+
+import numpy as np
+import scipy.sparse as sp
+import scipy.sparse.linalg as spla
+
+_G = 0.5 / np.sqrt(3.0)
+QP = np.array([0.5 - _G, 0.5 + _G])
+
+# coarse lines in GeometryInfo<3> order: (direction, fixed local coords of the two others)
+#   x-edge (dir 0): (b, c) = (y, z) position; y-edge (dir 1): (a, c); z-edge (dir 2): (a, b)
+COARSE_LINES = [(1, (0, 0)), (1, (1, 0)), (0, (0, 0)), (0, (1, 0)),
+                (1, (0, 1)), (1, (1, 1)), (0, (0, 1)), (0, (1, 1)),
+                (2, (0, 0)), (2, (1, 0)), (2, (0, 1)), (2, (1, 1))]
+# coarse faces: (normal direction, position 0/1)
+COARSE_FACES = [(0, 0), (0, 1), (1, 0), (1, 1), (2, 0), (2, 1)]
+
+LOAD_VEC_ZERO, LOAD_VEC_TRIG = 0, 3
+
+
+def _psi(a, t):
+    return t if a else 1.0 - t
+
+
+def _dpsi(a):
+    return 1.0 if a else -1.0
+
+
+def local_functions(h):
+    """Values/curls of the 12 local edge functions and values/divergences of the
+    6 local face functions at the 8 Gauss points of a box with sides h.
+
+    Local edge order: x-edges (b,c) in (0,0),(1,0),(0,1),(1,1); y-edges (a,c);
+    z-edges (a,b). Local face order: x0, x1, y0, y1, z0, z1."""
+    hx, hy, hz = h
+    pts, wts = [], []
+    for qz in range(2):
+        for qy in range(2):
+            for qx in range(2):
+                pts.append((QP[qx], QP[qy], QP[qz]))
+                wts.append(0.125 * hx * hy * hz)
+    pts = np.array(pts)
+    E = np.zeros((12, 8, 3))
+    CE = np.zeros((12, 8, 3))
+    F = np.zeros((6, 8, 3))
+    DF = np.zeros((6, 8))
+    pairs = [(0, 0), (1, 0), (0, 1), (1, 1)]
+    for q, (x, y, z) in enumerate(pts):
+        for l, (b, c) in enumerate(pairs):
+            E[l, q, 0] = _psi(b, y) * _psi(c, z) / hx
+            CE[l, q] = [0.0, _psi(b, y) * _dpsi(c) / (hx * hz), -_dpsi(b) * _psi(c, z) / (hx * hy)]
+        for l, (a, c) in enumerate(pairs):
+            E[4 + l, q, 1] = _psi(a, x) * _psi(c, z) / hy
+            CE[4 + l, q] = [-_psi(a, x) * _dpsi(c) / (hy * hz), 0.0, _dpsi(a) * _psi(c, z) / (hx * hy)]
+        for l, (a, b) in enumerate(pairs):
+            E[8 + l, q, 2] = _psi(a, x) * _psi(b, y) / hz
+            CE[8 + l, q] = [_psi(a, x) * _dpsi(b) / (hy * hz), -_dpsi(a) * _psi(b, y) / (hx * hz), 0.0]
+        for a in range(2):
+            F[a, q, 0] = _psi(a, x) / (hy * hz)
+            F[2 + a, q, 1] = _psi(a, y) / (hx * hz)
+            F[4 + a, q, 2] = _psi(a, z) / (hx * hy)
+            DF[a, q] = DF[2 + a, q] = DF[4 + a, q] = _dpsi(a) / (hx * hy * hz)
+    return pts, np.array(wts), E, CE, F, DF
+
+
+def counts(n):
+    ne = n * (n + 1) ** 2
+    nf = (n + 1) * n * n
+    return 3 * ne, 3 * nf
+
+
+def cell_dofs(n):
+    """Global edge / face indices of every fine cell (lexicographic cells)."""
+    Ex = n * (n + 1) ** 2
+    Fx = (n + 1) * n * n
+    c = np.arange(n ** 3)
+    i, j, k = c % n, (c // n) % n, c // (n * n)
+
+    def ex(i, j, k): return i + n * (j + (n + 1) * k)
+    def ey(i, j, k): return Ex + i + (n + 1) * (j + n * k)
+    def ez(i, j, k): return 2 * Ex + i + (n + 1) * (j + (n + 1) * k)
+    def fx(i, j, k): return i + (n + 1) * (j + n * k)
+    def fy(i, j, k): return Fx + i + n * (j + (n + 1) * k)
+    def fz(i, j, k): return 2 * Fx + i + n * (j + n * k)
+
+    eidx = np.stack([ex(i, j, k), ex(i, j + 1, k), ex(i, j, k + 1), ex(i, j + 1, k + 1),
+                     ey(i, j, k), ey(i + 1, j, k), ey(i, j, k + 1), ey(i + 1, j, k + 1),
+                     ez(i, j, k), ez(i + 1, j, k), ez(i, j + 1, k), ez(i + 1, j + 1, k)], 1)
+    fidx = np.stack([fx(i, j, k), fx(i + 1, j, k), fy(i, j, k), fy(i, j + 1, k),
+                     fz(i, j, k), fz(i, j, k + 1)], 1)
+    return eidx, fidx
+
+
+def edge_geometry(n):
+    """(direction, i, j, k) of every fine edge in the global numbering."""
+    Ex = n * (n + 1) ** 2
+    t = np.arange(Ex)
+    out = []
+    out.append((0, t % n, (t // n) % (n + 1), t // (n * (n + 1))))
+    out.append((1, t % (n + 1), (t // (n + 1)) % n, t // ((n + 1) * n)))
+    out.append((2, t % (n + 1), (t // (n + 1)) % (n + 1), t // ((n + 1) ** 2)))
+    return out
+
+
+def face_geometry(n):
+    Fx = (n + 1) * n * n
+    s = np.arange(Fx)
+    out = []
+    out.append((0, s % (n + 1), (s // (n + 1)) % n, s // ((n + 1) * n)))
+    out.append((1, s % n, (s // n) % (n + 1), s // (n * (n + 1))))
+    out.append((2, s % n, (s // n) % n, s // (n * n)))
+    return out
+
+
+def boundary_mask(n):
+    NE, NF = counts(n)
+    bnd = np.zeros(NE + NF, dtype=bool)
+    off = 0
+    for d, i, j, k in edge_geometry(n):
+        other = [(j, k), (i, k), (i, j)][d]
+        bnd[off:off + len(i)] = (other[0] == 0) | (other[0] == n) | (other[1] == 0) | (other[1] == n)
+        off += len(i)
+    for d, i, j, k in face_geometry(n):
+        pos = (i, j, k)[d]
+        bnd[off:off + len(i)] = (pos == 0) | (pos == n)
+        off += len(i)
+    return bnd
+
+
+def element_matrices(h, ainv, bdiv):
+    """Per-cell blocks: Me [c,12,12] (A^-1 mass), Ce [12,6] (curl tau, v), De [c,6,6]."""
+    _, wts, E, CE, F, DF = local_functions(h)
+    Me = np.einsum("q,iqa,cab,jqb->cij", wts, E, ainv, E)
+    Ce = np.einsum("q,iqa,jqa->ij", wts, CE, F)
+    De = np.einsum("q,iq,jq->ij", wts, DF, DF)[None] * bdiv[:, None, None]
+    return Me, Ce, De
+
+
+def assemble(n, size, ainv, bdiv):
+    """Unconstrained block matrix [[M, -C], [C^T, D]] (scipy CSR)."""
+    h = np.asarray(size, dtype=np.float64) / n
+    Me, Ce, De = element_matrices(h, ainv, bdiv)
+    eidx, fidx = cell_dofs(n)
+    NE, NF = counts(n)
+    nc = n ** 3
+    rows, cols, vals = [], [], []
+    for a in range(12):
+        for b in range(12):
+            rows.append(eidx[:, a]); cols.append(eidx[:, b]); vals.append(Me[:, a, b])
+        for b in range(6):
+            rows.append(eidx[:, a]); cols.append(NE + fidx[:, b]); vals.append(np.full(nc, -Ce[a, b]))
+            rows.append(NE + fidx[:, b]); cols.append(eidx[:, a]); vals.append(np.full(nc, Ce[a, b]))
+    for a in range(6):
+        for b in range(6):
+            rows.append(NE + fidx[:, a]); cols.append(NE + fidx[:, b]); vals.append(De[:, a, b])
+    return sp.coo_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
+                         shape=(NE + NF, NE + NF)).tocsr()
+
+
+def coarse_edge_dofs(n, line):
+    """Fine edge DoFs (line integrals) of coarse Nedelec function `line` on the
+    whole fine lattice: the coarse function lies in the fine space (nested
+    lowest-order spaces), so its interpolant reproduces it exactly."""
+    d, (p, q) = COARSE_LINES[line]
+    NE, _ = counts(n)
+    out = np.zeros(NE)
+    off = 0
+    for dd, i, j, k in edge_geometry(n):
+        if dd == d:
+            coords = [(j, k), (i, k), (i, j)][d]
+            out[off:off + len(i)] = _psi(p, coords[0] / n) * _psi(q, coords[1] / n) / n
+        off += len(i)
+    return out
+
+
+def coarse_face_dofs(n, face):
+    """Fine face fluxes of coarse RT function `face` on the whole fine lattice."""
+    d, a = COARSE_FACES[face]
+    _, NF = counts(n)
+    out = np.zeros(NF)
+    off = 0
+    for dd, i, j, k in face_geometry(n):
+        if dd == d:
+            out[off:off + len(i)] = _psi(a, (i, j, k)[d] / n) / (n * n)
+        off += len(i)
+    return out
+
+
+def coarse_curl_rhs(n, size, line):
+    """(v_f, curl N_line) for every fine face f (the reference's full_rhs,
+    ned_rt_basis.cc:502-511): curl of the coarse Nedelec function, i.e.
+    BasisNedelecCurl (basis_nedelec_curl.tpp:106-147), at the fine Gauss points."""
+    H = np.asarray(size, dtype=np.float64)
+    h = H / n
+    pts, wts, E, CE, F, DF = local_functions(h)
+    _, fidx = cell_dofs(n)
+    _, NF = counts(n)
+    d, (p, q) = COARSE_LINES[line]
+    c = np.arange(n ** 3)
+    ci = np.stack([c % n, (c // n) % n, c // (n * n)], 1).astype(np.float64)
+    # coarse-local coordinates of the Gauss points of every fine cell
+    X = (ci[:, None, :] + pts[None, :, :]) / n  # [cell, q, 3] in [0,1]^3
+    curl = np.zeros((n ** 3, 8, 3))
+    Hx, Hy, Hz = H
+    if d == 0:   # (1/Hx) psi_p(Y) psi_q(Z) e_x
+        curl[..., 1] = _psi(p, X[..., 1]) * _dpsi(q) / (Hx * Hz)
+        curl[..., 2] = -_dpsi(p) * _psi(q, X[..., 2]) / (Hx * Hy)
+    elif d == 1:  # (1/Hy) psi_p(X) psi_q(Z) e_y
+        curl[..., 0] = -_psi(p, X[..., 0]) * _dpsi(q) / (Hy * Hz)
+        curl[..., 2] = _dpsi(p) * _psi(q, X[..., 2]) / (Hx * Hy)
+    else:        # (1/Hz) psi_p(X) psi_q(Y) e_z
+        curl[..., 0] = _psi(p, X[..., 0]) * _dpsi(q) / (Hy * Hz)
+        curl[..., 1] = -_dpsi(p) * _psi(q, X[..., 1]) / (Hx * Hz)
+    loc = np.einsum("q,jqa,cqa->cj", wts, F, curl)
+    out = np.zeros(NF)
+    np.add.at(out, fidx.ravel(), loc.ravel())
+    return out
+
+
+def face_load(n, origin, size, kind, params):
+    """(v_f, f) for every fine face: the global load of assemble_system
+    (ned_rt_basis.cc:500), f evaluated at the fine Gauss points.
+    LOAD_VEC_TRIG: f = p0 (sin(w y) sin(w z), sin(w z) sin(w x), sin(w x) sin(w y)), w = p1 pi."""
+    _, NF = counts(n)
+    if kind == LOAD_VEC_ZERO:
+        return np.zeros(NF)
+    H = np.asarray(size, dtype=np.float64)
+    h = H / n
+    pts, wts, E, CE, F, DF = local_functions(h)
+    _, fidx = cell_dofs(n)
+    c = np.arange(n ** 3)
+    ci = np.stack([c % n, (c // n) % n, c // (n * n)], 1).astype(np.float64)
+    P = np.asarray(origin)[None, None, :] + (ci[:, None, :] + pts[None, :, :]) * h[None, None, :]
+    w = params[1] * np.pi
+    s = np.sin(w * P)
+    f = params[0] * np.stack([s[..., 1] * s[..., 2], s[..., 2] * s[..., 0], s[..., 0] * s[..., 1]], -1)
+    loc = np.einsum("q,jqa,cqa->cj", wts, F, f)
+    out = np.zeros(NF)
+    np.add.at(out, fidx.ravel(), loc.ravel())
+    return out
+
+
+def build_cell(origin, size, depth, ainv, bdiv, load_kind=LOAD_VEC_ZERO, load_params=(0, 0, 0, 0),
+               basis="solve"):
+    """One coarse cell. Returns (Phi [18, NE+NF], KH [18,18], FH [18]).
+
+    basis="solve": the multiscale basis (the reference's run loop,
+    ned_rt_basis.cc:1338-1381, direct solver). basis="std": the coarse
+    functions themselves (the reference's set_to_std sanity path,
+    ned_rt_basis.cc:1312-1335 / set_sigma_to_std :1183-1217)."""
+    n = 1 << int(depth)
+    NE, NF = counts(n)
+    A = assemble(n, size, ainv, bdiv)
+    bnd = boundary_mask(n)
+    I = np.where(~bnd)[0]
+    B = np.where(bnd)[0]
+    Phi = np.zeros((18, NE + NF))
+    rhs_all = np.zeros((NE + NF, 18))
+    for l in range(12):
+        g = np.zeros(NE + NF)
+        g[:NE] = coarse_edge_dofs(n, l)
+        Phi[l] = g
+        rhs_all[NE:, l] = coarse_curl_rhs(n, size, l)
+    for f in range(6):
+        g = np.zeros(NE + NF)
+        g[NE:] = coarse_face_dofs(n, f)
+        Phi[12 + f] = g
+    if basis == "solve":
+        G = Phi.copy()
+        G[:, I] = 0.0  # Dirichlet data only
+        R = rhs_all[I, :] - A[I][:, B] @ G[:, B].T
+        lu = spla.splu(A[I][:, I].tocsc())
+        X = lu.solve(R)
+        Phi = G
+        Phi[:, I] = X.T
+    # Galerkin with the unconstrained matrix, primary blocks only (:849-948)
+    P = np.zeros_like(Phi)
+    P[:12, :NE] = Phi[:12, :NE]
+    P[12:, NE:] = Phi[12:, NE:]
+    Y = (A @ P.T).T
+    KH = P @ Y.T
+    bu = face_load(n, origin, size, load_kind, load_params)
+    FH = np.zeros(18)
+    FH[12:] = Phi[12:, NE:] @ bu
+    return Phi, KH, FH
+
+
+def build(cells, ainv, bdiv, load_kind=LOAD_VEC_ZERO, load_params=(0, 0, 0, 0), want_phi=True,
+          basis="solve"):
+    """Batch over coarse cells; ainv [sum n^3, 3, 3], bdiv [sum n^3]."""
+    KH, FH, PH = [], [], []
+    off = 0
+    for c in cells:
+        n = 1 << int(c["depth"])
+        sl = slice(off, off + n ** 3)
+        off += n ** 3
+        phi, kh, fh = build_cell(c["origin"], c["size"], c["depth"], ainv[sl], bdiv[sl], load_kind,
+                                 load_params, basis)
+        KH.append(kh)
+        FH.append(fh)
+        if want_phi:
+            PH.append(phi)
+    return {"KH": np.array(KH), "FH": np.array(FH), "Phi": PH if want_phi else None}
+
+
+def ainv_to_sym6(ainv):
+    """[c,3,3] -> [c,6] (a00, a11, a22, a01, a02, a12), the ABI layout."""
+    return np.stack([ainv[:, 0, 0], ainv[:, 1, 1], ainv[:, 2, 2], ainv[:, 0, 1], ainv[:, 0, 2],
+                     ainv[:, 1, 2]], 1)
+
+
+def sym6_to_ainv(s):
+    out = np.zeros((s.shape[0], 3, 3))
+    out[:, 0, 0], out[:, 1, 1], out[:, 2, 2] = s[:, 0], s[:, 1], s[:, 2]
+    out[:, 0, 1] = out[:, 1, 0] = s[:, 3]
+    out[:, 0, 2] = out[:, 2, 0] = s[:, 4]
+    out[:, 1, 2] = out[:, 2, 1] = s[:, 5]
+    return out

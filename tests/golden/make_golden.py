@@ -7,6 +7,8 @@
    not on the GPU machine).
 2. q1_*.npz: FP64 oracle (banded-Cholesky mode) K_H / F_H of seeded Q1
    workloads, the parity target of the CUDA path.
+3. nedrt_*.npz: FP64 oracle (sparse direct, SuperLU) K_H / F_H of a seeded
+   Ned_RT workload.
 
 Usage: python tests/golden/make_golden.py [--reference DIR]
 """
@@ -22,6 +24,7 @@ sys.path.insert(0, os.path.join(REPO, "mpi-msfec_gb300"))
 sys.path.insert(0, REPO)
 
 from oracle import oracle  # noqa: E402
+from oracle import nedrt_oracle  # noqa: E402
 import workloads  # noqa: E402
 
 
@@ -61,6 +64,11 @@ def main():
     nf = int(np.sum(workloads.fine_counts(cells)[0]))
     a = np.exp(rng.standard_normal(nf))
     q1_case("q1_mixed_depths_seed7.npz", cells, a, None, load)
+    # Ned_RT: coarse 2^3, depth 2, Haar-rotated log-normal tensor (seed 2)
+    cells, ainv6, bdiv, load = workloads.nedrt_tensor(m=2, depth=2, seed=2)
+    res = nedrt_oracle.build(cells, nedrt_oracle.sym6_to_ainv(ainv6), bdiv, load.kind, list(load.params),
+                             want_phi=False)
+    np.savez_compressed(os.path.join(HERE, "nedrt_tensor_m2_L2_seed2.npz"), KH=res["KH"], FH=res["FH"])
 
 
 if __name__ == "__main__":

@@ -1,0 +1,94 @@
+"""GPU parity of the Ned_RT basis build against the FP64 oracle (C ABI).
+
+The local mixed system is ill-conditioned (kappa ~ 1e4 at depth 3), so even
+the sparse-direct oracle carries errors of order 1e-11 in the basis. Stated,
+measured tolerances (both precisions; mixed = FP32 MINRES + FP64 refinement):
+  K_H, F_H   max abs error <= 1e-9 * max |entry| of the cell
+  basis      max|phi - phi_oracle| <= 1e-8 * max|phi_oracle| per function
+"""
+import os
+
+import numpy as np
+import pytest
+
+import workloads
+from oracle import nedrt_oracle as N
+
+pytestmark = pytest.mark.gpu
+HERE = os.path.dirname(os.path.abspath(__file__))
+TOL_KH = 1e-9
+TOL_PHI = 1e-8
+PRECISIONS = ("mixed", "fp64")
+
+
+def _handle(gpu, precision):
+    return gpu.Handle(precision=gpu.PRECISION_MIXED if precision == "mixed" else gpu.PRECISION_FP64)
+
+
+def _rel(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def _check(gpu, precision, cells, ainv6, bdiv, load, basis=True):
+    h = _handle(gpu, precision)
+    KH, FH, rep, st = h.nedrt_build(cells, ainv6, bdiv, load)
+    assert st == gpu.SUCCESS and rep["converged"].all(), rep
+    ref = N.build(cells, N.sym6_to_ainv(ainv6), bdiv, load.kind, list(load.params), want_phi=basis)
+    errs = []
+    for c in range(len(cells)):
+        e = _rel(KH[c], ref["KH"][c])
+        errs.append(e)
+        assert e <= TOL_KH, (c, e)
+        if np.abs(ref["FH"][c]).max() > 0:
+            assert _rel(FH[c], ref["FH"][c]) <= TOL_KH
+    if basis:
+        phi = h.nedrt_basis()
+        off = 0
+        for c, po in enumerate(ref["Phi"]):
+            pg = phi[off:off + po.size].reshape(po.shape)
+            off += po.size
+            for b in range(18):
+                assert _rel(pg[b], po[b]) <= TOL_PHI, (c, b, _rel(pg[b], po[b]))
+    print(f"{precision}: max K_H rel err {max(errs):.2e}, max iterations {rep['iterations'].max()}")
+    return KH, FH, rep
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_small_tensor_matches_golden(gpu, precision):
+    cells, ainv6, bdiv, load = workloads.nedrt_tensor(m=2, depth=2, seed=2)
+    g = np.load(os.path.join(HERE, "golden", "nedrt_tensor_m2_L2_seed2.npz"))
+    h = _handle(gpu, precision)
+    KH, FH, rep, st = h.nedrt_build(cells, ainv6, bdiv, load)
+    assert st == gpu.SUCCESS and rep["converged"].all()
+    for c in range(len(cells)):
+        assert _rel(KH[c], g["KH"][c]) <= TOL_KH
+        assert _rel(FH[c], g["FH"][c]) <= TOL_KH
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_depth3_basis_matches_oracle(gpu, precision):
+    cells, ainv6, bdiv, load = workloads.nedrt_tensor(m=1, depth=3, seed=3)
+    cells2, a2, b2, _ = workloads.nedrt_tensor(m=1, depth=1, seed=4)
+    _check(gpu, precision, np.concatenate([cells, cells2]), np.concatenate([ainv6, a2]),
+           np.concatenate([bdiv, b2]), load)
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_depth4_global_workspace(gpu, precision):
+    cells, ainv6, bdiv, load = workloads.nedrt_tensor(m=1, depth=4, seed=6)
+    _check(gpu, precision, cells, ainv6, bdiv, load, basis=False)
+
+
+def test_invalid_tensor_rejected(gpu):
+    cells, ainv6, bdiv, load = workloads.nedrt_tensor(m=1, depth=1, seed=1)
+    h = gpu.Handle()
+    bad = ainv6.copy()
+    bad[0, 0] = -1.0
+    with pytest.raises(gpu.MsfecError) as e:
+        h.nedrt_build(cells, bad, bdiv, load)
+    assert e.value.status == gpu.ERROR_NUMERICAL
+    c5 = cells.copy()
+    c5["depth"] = 5
+    with pytest.raises(gpu.MsfecError) as e:
+        h.nedrt_build(c5, ainv6, bdiv, load)
+    assert e.value.status == gpu.ERROR_INVALID_ARGUMENT

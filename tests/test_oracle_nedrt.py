@@ -1,0 +1,112 @@
+"""CPU checks of the Ned_RT FP64 oracle and of the closed-form element tables
+the CUDA kernel uses (restated here in Python from the kernel's formulas)."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import nedrt_oracle as N
+import workloads
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _m1(a, b):
+    return 1.0 / 3.0 if a == b else 1.0 / 6.0
+
+
+def _sgn(a):
+    return 1.0 if a else -1.0
+
+
+def _other(p):
+    return (1 if p == 0 else 0), (1 if p == 2 else 2)
+
+
+def _edge_pos(p, l4, ax):
+    o1, o2 = _other(p)
+    return (l4 & 1) if ax == o1 else (l4 >> 1)
+
+
+def kernel_table_G(h, p, q, l4, m4):
+    """Same closed form as table_G in csrc/nedrt_solve.cu."""
+    if p == q:
+        o1, o2 = _other(p)
+        return h[o1] * h[o2] / h[p] * _m1(l4 & 1, m4 & 1) * _m1(l4 >> 1, m4 >> 1)
+    r = 3 - p - q
+    return 0.25 * h[r] * _m1(_edge_pos(p, l4, r), _edge_pos(q, m4, r))
+
+
+def kernel_table_C(h, l, f):
+    """Same closed form as table_C in csrc/nedrt_solve.cu."""
+    p, l4 = l >> 2, l & 3
+    fd, fa = f >> 1, f & 1
+    if fd == p:
+        return 0.0
+    hx, hy, hz = h
+    a0, a1 = l4 & 1, l4 >> 1
+    if p == 0:
+        return _sgn(a1) * hy * _m1(a0, fa) / (hx * hz) if fd == 1 else -_sgn(a0) * hz * _m1(a1, fa) / (hx * hy)
+    if p == 1:
+        return -_sgn(a1) * hx * _m1(a0, fa) / (hy * hz) if fd == 0 else _sgn(a0) * hz * _m1(a1, fa) / (hx * hy)
+    return _sgn(a1) * hx * _m1(a0, fa) / (hy * hz) if fd == 0 else -_sgn(a0) * hy * _m1(a1, fa) / (hx * hz)
+
+
+def test_kernel_closed_form_tables_match_quadrature():
+    h = np.array([0.3, 0.17, 0.55])
+    for p in range(3):
+        for q in range(3):
+            ainv = np.zeros((1, 3, 3))
+            ainv[0, p, q] = ainv[0, q, p] = 1.0
+            Me, Ce, _ = N.element_matrices(h, ainv, np.ones(1))
+            G = np.array([[kernel_table_G(h, p, q, l4, m4) for m4 in range(4)] for l4 in range(4)])
+            blk = Me[0][4 * p:4 * p + 4, 4 * q:4 * q + 4]
+            assert np.allclose(blk, G, rtol=1e-13, atol=1e-15), (p, q)
+    C = np.array([[kernel_table_C(h, l, f) for f in range(6)] for l in range(12)])
+    assert np.allclose(Ce, C, rtol=1e-13, atol=1e-14)
+
+
+def test_standard_basis_galerkin_is_refinement_invariant():
+    # The reference's set_to_std sanity path (ned_rt_basis.cc:1312-1335): with
+    # constant coefficients the coarse functions' Galerkin matrix does not
+    # depend on the local refinement.
+    H = [0.25, 0.5, 0.125]
+    ref = None
+    for L in (0, 1, 2):
+        n = 1 << L
+        ainv = np.tile(np.array([[2.0, 0.3, 0.1], [0.3, 1.0, -0.2], [0.1, -0.2, 1.5]]), (n ** 3, 1, 1))
+        _, KH, _ = N.build_cell([0, 0, 0], H, L, ainv, np.full(n ** 3, 0.7), basis="std")
+        if ref is None:
+            ref = KH
+        assert np.abs(KH - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+def test_solution_satisfies_the_saddle_point_system():
+    cells, ainv6, bdiv, load = workloads.nedrt_tensor(m=1, depth=2, seed=5)
+    n = 4
+    ainv = N.sym6_to_ainv(ainv6)
+    Phi, KH, FH = N.build_cell(cells["origin"][0], cells["size"][0], 2, ainv, bdiv, load.kind,
+                               list(load.params))
+    A = N.assemble(n, cells["size"][0], ainv, bdiv)
+    bnd = N.boundary_mask(n)
+    NE, NF = N.counts(n)
+    for b in range(18):
+        f = np.zeros(NE + NF)
+        if b < 12:
+            f[NE:] = N.coarse_curl_rhs(n, cells["size"][0], b)
+            g = N.coarse_edge_dofs(n, b)
+            assert np.array_equal(Phi[b][:NE][bnd[:NE]], g[bnd[:NE]])
+        r = f - A @ Phi[b]
+        assert np.abs(r[~bnd]).max() <= 1e-10 * max(np.abs(A @ Phi[b]).max(), 1e-300)
+    # block structure of K_H: K_ef = -K_fe^T, ee and ff symmetric
+    assert np.abs(KH[:12, 12:] + KH[12:, :12].T).max() <= 1e-12 * np.abs(KH).max()
+    assert np.abs(KH[:12, :12] - KH[:12, :12].T).max() <= 1e-12 * np.abs(KH).max()
+    assert np.all(FH[:12] == 0.0)
+
+
+def test_committed_nedrt_fixture_reproduces():
+    g = np.load(os.path.join(HERE, "golden", "nedrt_tensor_m2_L2_seed2.npz"))
+    cells, ainv6, bdiv, load = workloads.nedrt_tensor(m=2, depth=2, seed=2)
+    res = N.build(cells, N.sym6_to_ainv(ainv6), bdiv, load.kind, list(load.params), want_phi=False)
+    assert np.abs(res["KH"] - g["KH"]).max() <= 1e-9 * np.abs(g["KH"]).max()
+    assert np.abs(res["FH"] - g["FH"]).max() <= 1e-9 * np.abs(g["FH"]).max()
