@@ -1,24 +1,30 @@
 #!/usr/bin/env python3
 """Benchmark of the batched MsFEC basis build (fine-DoF x RHS per second).
 
-Default workload: batched uneven-depth Q1 basis build, coarse 16^3 cells of
-the unit cube, local depth L ~ U{2,3,4,5} per cell (seed 3), 8 coarse-basis
-RHS per cell, oscillatory coefficient (eps = 1/64) times a per-cell
-log-normal factor, load sin(pi x) sin(pi y) sin(pi z); mixed precision
-(FP32 PCG + FP64 iterative refinement) with the plain FP64 path timed beside
-it. One step = one full build (local solves + Galerkin K_H, F_H) of every
-cell of this rank's share.
+Headline workload (default): Ned_RT mixed basis build, coarse 8^3 cells of the
+unit cube, 3 local refinement levels (8^3 fine cells, 3672 Nedelec+RT DoFs per
+cell, 12 edge + 6 face coarse-basis RHS), per fine cell A = R diag(e^g) R^T with
+g ~ N(0,1) and R Haar-random (seed 2), B = 1 - 0.9 sin(2 pi 14 x), vector trig
+load. Mixed precision (FP32 MINRES inside FP64 iterative refinement) with the
+plain FP64 path timed beside it. Reported beside the headline: the batched
+uneven-depth Q1 build (coarse 16^3, L ~ U{2..5}, 8 RHS, oscillatory
+coefficient eps = 1/64 times a per-cell log-normal factor).
+
+One step = one full build (all local solves + Galerkin K_H, F_H) of every
+cell of this rank's share; inputs resident in HBM for `value`, host buffers
+through the C ABI (H2D + D2H inside the timed region) for `e2e`.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-N > 1 runs under torchrun: coarse cells are partitioned contiguously by work
-(no data-path collective; only the timing max is reduced), scaling "weak" is
-NOT claimed since the global workload is fixed -> "strong".
+N > 1 (torchrun): coarse cells are partitioned contiguously by work across
+ranks, no data-path collective (only the timing max is reduced); the global
+workload is fixed -> scaling "strong".
 """
 from __future__ import annotations
 
 import argparse
 import json
+import multiprocessing as mp
 import os
 import subprocess
 import sys
@@ -35,6 +41,7 @@ for _p in (PKG, REPO):
 
 METRIC = "fine-DoF·RHS/s of batched basis solves, mixed vs FP64 @1e-10 rel; bwd/fwd time"
 UNIT = "fine-DoF·RHS/s"
+FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12  # 152 SMs x 128 FP32 lanes x FMA x max clock
 
 
 def peaks():
@@ -46,55 +53,82 @@ def peaks():
 
 
 def dist_env():
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return world, rank, local
+    return (int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")),
+            int(os.environ.get("LOCAL_RANK", "0")))
 
 
-def partition(cells, world, rank):
-    """Contiguous cell ranges with balanced fine-DoF x RHS work."""
-    import workloads
-    w = workloads.fine_counts(cells)[1].astype(np.float64)
+# --------------------------------------------------------------------------- workloads
+class Workload:
+    """Cells + coefficients of one build, with per-cell slicing."""
+
+    def __init__(self, name):
+        import workloads
+        self.name = name
+        if name == "nedrt_small":
+            self.kind = "nedrt"
+            self.cells, self.ainv6, self.bdiv, self.load = workloads.nedrt_tensor(m=8, depth=3, seed=2)
+            self.cfg = {"workload": "nedrt_tensor_coarse8^3_L3_18rhs", "coarse_cells": 512, "depth": 3,
+                        "seed": 2, "B": "1-0.9 sin(2 pi 14 x)", "load": "vec trig"}
+        elif name == "nedrt_large":
+            self.kind = "nedrt"
+            self.cells, self.ainv6, self.bdiv, self.load = workloads.nedrt_tensor(m=16, depth=4, seed=5)
+            self.cfg = {"workload": "nedrt_tensor_coarse16^3_L4_18rhs", "coarse_cells": 4096, "depth": 4, "seed": 5}
+        elif name == "q1_uneven":
+            self.kind = "q1"
+            self.cells, self.a, self.r, self.load = workloads.q1_uneven(m=16, seed=3)
+            self.cfg = {"workload": "q1_uneven_coarse16^3_L2-5_8rhs", "coarse_cells": 4096, "depths": [2, 3, 4, 5],
+                        "eps": 1.0 / 64, "seed": 3}
+        elif name == "q1_small":
+            self.kind = "q1"
+            self.cells, self.a, self.r, self.load = workloads.q1_lognormal(m=4, depth=3, seed=1, reaction=True)
+            self.cfg = {"workload": "q1_lognormal_coarse4^3_L3_8rhs_reaction1", "coarse_cells": 64, "seed": 1}
+        elif name == "q1_adjoint_fwd":
+            self.kind = "q1"
+            self.cells, self.a, self.r, self.load = workloads.q1_lognormal(m=8, depth=4, seed=4, reaction=False)
+            self.cfg = {"workload": "q1_lognormal_coarse8^3_L4_8rhs", "coarse_cells": 512, "seed": 4}
+        else:
+            raise SystemExit(f"unknown workload {name}")
+        n = 1 << self.cells["depth"].astype(np.int64)
+        self.nfine = n ** 3
+        self.foff = np.concatenate([[0], np.cumsum(self.nfine)])
+
+    def work(self, lo=0, hi=None):
+        import workloads
+        c = self.cells[lo:hi]
+        return workloads.nedrt_work_dof_rhs(c) if self.kind == "nedrt" else workloads.work_dof_rhs(c)
+
+    def per_cell_work(self):
+        n = 1 << self.cells["depth"].astype(np.int64)
+        if self.kind == "nedrt":
+            return (3 * n * (n + 1) ** 2 + 3 * n * n * (n + 1)) * 18
+        return (n + 1) ** 3 * 8
+
+    def shard(self, lo, hi):
+        f0, f1 = int(self.foff[lo]), int(self.foff[hi])
+        out = {"cells": self.cells[lo:hi]}
+        if self.kind == "nedrt":
+            out["ainv6"] = np.ascontiguousarray(self.ainv6[f0:f1])
+            out["bdiv"] = np.ascontiguousarray(self.bdiv[f0:f1])
+        else:
+            out["a"] = np.ascontiguousarray(self.a[f0:f1])
+            out["r"] = None if self.r is None else np.ascontiguousarray(self.r[f0:f1])
+        return out
+
+
+def partition(wl, world, rank):
+    w = wl.per_cell_work().astype(np.float64)
     cum = np.concatenate([[0.0], np.cumsum(w)])
-    bounds = [int(np.searchsorted(cum, cum[-1] * r / world, side="left")) for r in range(world + 1)]
-    bounds[0], bounds[-1] = 0, len(cells)
-    lo, hi = bounds[rank], bounds[rank + 1]
-    return lo, hi
+    b = [int(np.searchsorted(cum, cum[-1] * r / world, side="left")) for r in range(world + 1)]
+    b[0], b[-1] = 0, len(wl.cells)
+    return b[rank], b[rank + 1]
 
 
-def make_workload(name):
-    import workloads
-    if name == "q1_uneven":
-        cells, a, r, load = workloads.q1_uneven(m=16, seed=3)
-        cfg = {"workload": "q1_uneven_coarse16^3_L2-5_8rhs", "coarse_cells": 4096, "depths": [2, 3, 4, 5],
-               "eps": 1.0 / 64, "seed": 3}
-    elif name == "q1_small":
-        cells, a, r, load = workloads.q1_lognormal(m=4, depth=3, seed=1, reaction=True)
-        cfg = {"workload": "q1_lognormal_coarse4^3_L3_8rhs_reaction1", "coarse_cells": 64, "depths": [3],
-               "seed": 1}
-    elif name == "q1_adjoint_fwd":
-        cells, a, r, load = workloads.q1_lognormal(m=8, depth=4, seed=4, reaction=False)
-        cfg = {"workload": "q1_lognormal_coarse8^3_L4_8rhs", "coarse_cells": 512, "depths": [4], "seed": 4}
-    else:
-        raise SystemExit(f"unknown workload {name}")
-    return cells, a, r, load, cfg
-
-
-def coef_slice(cells, lo, hi):
-    import workloads
-    nf = workloads.fine_counts(cells)[0]
-    off = np.concatenate([[0], np.cumsum(nf)])
-    return int(off[lo]), int(off[hi])
-
-
+# --------------------------------------------------------------------------- clocks
 class ClockSampler:
     """nvidia-smi clock / throttle sampling during the timed region."""
 
     def __init__(self, index):
-        self.index = index
-        self.proc = None
-        self.path = None
+        self.index, self.proc, self.path = index, None, None
 
     def start(self):
         fd, self.path = tempfile.mkstemp(suffix=".csv")
@@ -117,16 +151,19 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except Exception:
             self.proc.kill()
-        rows = []
-        for ln in open(self.path).read().splitlines():
-            parts = [p.strip() for p in ln.split(",")]
-            if len(parts) >= 9:
-                rows.append(parts)
+        rows = [[p.strip() for p in ln.split(",")] for ln in open(self.path).read().splitlines()]
+        rows = [r for r in rows if len(r) >= 9]
         os.unlink(self.path)
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
-        sm = np.array([float(r[1]) for r in rows if r[1].replace(".", "").isdigit()] or [0.0])
-        smax = max(float(r[2]) for r in rows if r[2].replace(".", "").isdigit())
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = np.array([v for v in (num(r[1]) for r in rows) if v is not None] or [0.0])
+        smax = max([v for v in (num(r[2]) for r in rows) if v is not None] or [0.0])
         under = sm[sm > 0.5 * np.max(sm)] if sm.size else sm
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
@@ -134,66 +171,201 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def cpu_sample_cells(cells, target_s, nthreads):
+# --------------------------------------------------------------------------- CPU (oracle)
+def _nedrt_oracle_chunk(args):
+    sys.path.insert(0, REPO)
+    sys.path.insert(0, PKG)
+    from oracle import nedrt_oracle as N
+    cells, ainv6, bdiv, kind, params = args
+    t0 = time.perf_counter()
+    N.build(cells, N.sym6_to_ainv(ainv6), bdiv, kind, params, want_phi=False)
+    return time.perf_counter() - t0
+
+
+def cpu_sample(wl, target_s, nthreads):
     """Stratified sample (every depth represented) sized for ~target_s of CPU work."""
-    depths = sorted(set(int(d) for d in cells["depth"]))
-    # rough per-cell CG+SSOR cost model in seconds on one core (measured: L4 ~ 0.1 s)
-    per_cell = {1: 1e-4, 2: 5e-4, 3: 8e-3, 4: 0.1, 5: 1.6}
+    depths = sorted(set(int(d) for d in wl.cells["depth"]))
+    if wl.kind == "nedrt":
+        per_cell = {1: 5e-3, 2: 3e-2, 3: 0.6, 4: 12.0}
+    else:
+        per_cell = {1: 1e-4, 2: 5e-4, 3: 8e-3, 4: 0.1, 5: 1.6}
     per_depth = target_s * nthreads / max(1, len(depths))
     idx = []
     for d in depths:
-        cand = np.where(cells["depth"] == d)[0]
+        cand = np.where(wl.cells["depth"] == d)[0]
         k = int(max(1, min(len(cand), per_depth / per_cell.get(d, 1.0))))
         idx.extend(cand[:k].tolist())
     return np.array(sorted(idx))
 
 
-def time_oracle(cells, a, r, load, sel, nthreads):
-    from oracle import oracle
-    import workloads
-    nf = workloads.fine_counts(cells)[0]
-    off = np.concatenate([[0], np.cumsum(nf)])
-    asub = np.concatenate([a[off[c]:off[c + 1]] for c in sel])
-    rsub = None if r is None else np.concatenate([r[off[c]:off[c + 1]] for c in sel])
-    sub = cells[sel]
+def time_oracle(wl, sel, nthreads):
+    """The oracle on the selected cells with all host threads: Q1 = C++ CG+SSOR(1.6)
+    (OpenMP over cells, the reference's solve_iterative), Ned_RT = sparse direct
+    (SuperLU per cell, the reference's solve_direct), spawn-started process pool."""
+    sub_cells = wl.cells[sel]
+    if wl.kind == "q1":
+        from oracle import oracle
+        asub = np.concatenate([wl.a[wl.foff[c]:wl.foff[c + 1]] for c in sel])
+        rsub = None if wl.r is None else np.concatenate([wl.r[wl.foff[c]:wl.foff[c + 1]] for c in sel])
+        t0 = time.perf_counter()
+        res = oracle.q1_build(sub_cells["origin"], sub_cells["size"], sub_cells["depth"], asub, rsub,
+                              load_kind=wl.load.kind, load_params=list(wl.load.params),
+                              solver=oracle.SOLVER_CG_SSOR, tol=1e-12, max_iter=1000, want_phi=False,
+                              nthreads=nthreads)
+        dt = time.perf_counter() - t0
+        desc = "CG+SSOR(1.6) 1e-12 per RHS (C++, OpenMP over cells)"
+    else:
+        chunks = []
+        for part in np.array_split(np.asarray(sel), nthreads):
+            if len(part) == 0:
+                continue
+            a6 = np.concatenate([wl.ainv6[wl.foff[c]:wl.foff[c + 1]] for c in part])
+            bd = np.concatenate([wl.bdiv[wl.foff[c]:wl.foff[c + 1]] for c in part])
+            chunks.append((wl.cells[part], a6, bd, wl.load.kind, list(wl.load.params)))
+        ctx = mp.get_context("spawn")
+        saved = {k: os.environ.get(k) for k in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")}
+        for k in saved:
+            os.environ[k] = "1"  # one core per worker process
+        pool = ctx.Pool(len(chunks))
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+        with pool:
+            pool.map(_nedrt_oracle_chunk, chunks[:1])  # warm the workers' imports
+            t0 = time.perf_counter()
+            pool.map(_nedrt_oracle_chunk, chunks)
+            dt = time.perf_counter() - t0
+        desc = "sparse direct (SuperLU, one factorisation per cell, 18 solves), process per core"
+    work = int(np.sum(wl.per_cell_work()[sel]))
+    return work / dt, dt, f"{len(sel)} of {len(wl.cells)} cells (every depth); {desc}; {dt:.1f} s"
+
+
+# --------------------------------------------------------------------------- GPU
+def gpu_run(wl, lo, hi, precision, steps, warmup, local, stream, barrier):
+    """Device-resident builds; returns per-step ms, mean solve / Galerkin ms, launches, reports."""
+    import torch
+    import msfec
+    sh = wl.shard(lo, hi)
+    cells = sh["cells"]
+    nc = len(cells)
+    h = msfec.Handle(precision=precision, device=local)
+    h.set_stream(stream.cuda_stream)
+    h.set_timing(True)
+    nr = 18 if wl.kind == "nedrt" else 8
+    d_KH = torch.zeros((nc, nr, nr), dtype=torch.float64, device="cuda")
+    d_FH = torch.zeros((nc, nr), dtype=torch.float64, device="cuda")
+    d_rep = torch.zeros(max(1, nc) * msfec.REPORT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    if wl.kind == "nedrt":
+        d_x = torch.from_numpy(sh["ainv6"]).cuda()
+        d_y = torch.from_numpy(sh["bdiv"]).cuda()
+
+        def step():
+            h.nedrt_build_device(cells, d_x.data_ptr(), d_y.data_ptr(), wl.load, d_KH.data_ptr(),
+                                 d_FH.data_ptr(), d_rep.data_ptr())
+    else:
+        d_x = torch.from_numpy(sh["a"]).cuda()
+        d_y = None if sh["r"] is None else torch.from_numpy(sh["r"]).cuda()
+
+        def step():
+            h.q1_build_device(cells, d_x.data_ptr(), 0 if d_y is None else d_y.data_ptr(), wl.load,
+                              d_KH.data_ptr(), d_FH.data_ptr(), d_rep.data_ptr())
+    for _ in range(warmup):
+        step()
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    solve_ms, gal_ms, launches = [], [], 0
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+        t = h.timings()
+        solve_ms.append(t["solve_ms"])
+        gal_ms.append(t["galerkin_ms"])
+        launches += t["kernel_launches"]
+    e1.record(stream)
+    barrier()
+    ms = e0.elapsed_time(e1) / steps
+    rep = np.frombuffer(d_rep.cpu().numpy().tobytes(), dtype=msfec.REPORT_DTYPE)[:nc]
+    h.close()
+    return ms, float(np.mean(solve_ms)), float(np.mean(gal_ms)), launches, rep
+
+
+def e2e_run(wl, lo, hi, local, stream, barrier, steps):
+    """Through the host-buffer C ABI: pinned inputs, H2D + build + D2H per step."""
+    import torch
+    import msfec
+    sh = wl.shard(lo, hi)
+    cells = sh["cells"]
+    h = msfec.Handle(precision=msfec.PRECISION_MIXED, device=local)
+    h.set_stream(stream.cuda_stream)
+    pin = lambda a: None if a is None else torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
+    if wl.kind == "nedrt":
+        x, y = pin(sh["ainv6"]), pin(sh["bdiv"])
+        call = lambda: h.nedrt_build(cells, x, y, wl.load)  # noqa: E731
+        h2d = x.nbytes + y.nbytes
+        nr = 18
+    else:
+        x, y = pin(sh["a"]), pin(sh["r"])
+        call = lambda: h.q1_build(cells, x, y, wl.load)  # noqa: E731
+        h2d = x.nbytes + (0 if y is None else y.nbytes)
+        nr = 8
+    call()
+    barrier()
     t0 = time.perf_counter()
-    res = oracle.q1_build(sub["origin"], sub["size"], sub["depth"], asub, rsub, load_kind=load.kind,
-                          load_params=list(load.params), solver=oracle.SOLVER_CG_SSOR, tol=1e-12,
-                          max_iter=1000, want_phi=False, nthreads=nthreads)
-    dt = time.perf_counter() - t0
-    return workloads.work_dof_rhs(sub) / dt, dt, len(sel), res["status"]
+    for _ in range(steps):
+        call()
+    barrier()
+    dt = (time.perf_counter() - t0) / steps
+    h.close()
+    h2d += len(cells) * msfec.CELL_DTYPE.itemsize
+    d2h = len(cells) * (nr * nr + nr) * 8 + len(cells) * msfec.REPORT_DTYPE.itemsize
+    return dt, h2d, d2h
 
 
-def run_reference(args):
-    world, rank, _ = dist_env()
-    if rank != 0:
-        return
-    cells, a, r, load, cfg = make_workload(args.workload)
-    nthreads = os.cpu_count() or 1
-    sel = cpu_sample_cells(cells, args.cpu_seconds / 2.0, nthreads)
-    vals = []
-    for _ in range(args.warmup):
-        time_oracle(cells, a, r, load, sel[: max(1, len(sel) // 8)], nthreads)
-    t_all = []
-    for _ in range(args.steps):
-        v, dt, ncell, st = time_oracle(cells, a, r, load, sel, nthreads)
-        vals.append(v)
-        t_all.append(dt)
-    value = float(np.median(vals))
-    sample = f"{len(sel)} of {len(cells)} cells, every depth represented; CG+SSOR(1.6) 1e-12 per RHS"
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": float(np.median(t_all) * 1e3), "higher_is_better": True,
-            "scaling": "strong", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
-            "impl": "reference",
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": sample},
-            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
+def roofline(wl, lo, hi, solve_ms, gal_ms, rep, kind):
+    """Roofline of the dominant (solver) kernel and of the Galerkin kernel."""
+    peak, peak_kind = peaks()
+    c = wl.cells[lo:hi]
+    n = 1 << c["depth"].astype(np.int64)
+    nfine = int(np.sum(n ** 3))
+    if wl.kind == "nedrt":
+        ndof = int(np.sum(3 * n * (n + 1) ** 2 + 3 * n * n * (n + 1)))
+        nrhs, coef_bytes = 18, 7 * 8
+        # FP32 flops of one MINRES iteration of one item: cell operator (2 x 336 per
+        # fine cell) + vector recurrences (~30 per DoF)
+        flops_iter = 2 * 336 * n ** 3 + 30 * (3 * n * (n + 1) ** 2 + 3 * n * n * (n + 1))
+    else:
+        ndof = int(np.sum((n + 1) ** 3))
+        nrhs, coef_bytes = 8, 8 * (1 if wl.r is None else 2)
+        # FP32 flops per Krylov iteration of one item: 27-point apply (2 x 35) + recurrences (~20)
+        flops_iter = 90 * (n - 1) ** 3
+    # algorithmic HBM bytes of one solver launch: coefficients in, basis and K*basis out (FP64)
+    alg_solve = nfine * coef_bytes + ndof * nrhs * 8 * 2
+    alg_gal = ndof * nrhs * 8 * 2 + len(c) * (nrhs * nrhs + nrhs) * 8
+    iters = rep["iterations"].astype(np.float64)  # max over the cell's RHS (upper estimate)
+    per_cell_flops = flops_iter * iters * (nrhs if wl.kind == "nedrt" else 8)
+    tflops = float(np.sum(per_cell_flops)) / (solve_ms * 1e-3) / 1e12
+    return {"bound": "hbm", "kernel": f"{kind}_solve_kernel (persistent, on-chip Krylov state)",
+            "achieved": alg_solve / (solve_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+            "frac": alg_solve / (solve_ms * 1e-3) / 1e9 / peak, "traffic": None,
+            "algorithmic_bytes": alg_solve, "launch_ms": solve_ms, "peak_source": peak_kind,
+            "note": "Krylov vectors stay in shared memory/registers: HBM carries only coefficients "
+                    "in and basis + K*basis out, so this fraction is low by design; the on-chip "
+                    "FP32 rate below is the binding roofline",
+            "onchip": {"bound": "fp32", "achieved_tflops": tflops, "peak_tflops_nominal": FP32_NOMINAL_TFLOPS,
+                       "frac": tflops / FP32_NOMINAL_TFLOPS,
+                       "flops_model": "per Krylov iteration of one RHS: operator + recurrences, "
+                                      "x iterations (max over the cell's RHS)"},
+            "galerkin": {"kernel": f"{kind}_galerkin_kernel (FP64 DMMA m8n8k4)", "launch_ms": gal_ms,
+                         "achieved": alg_gal / (gal_ms * 1e-3) / 1e9,
+                         "frac": alg_gal / (gal_ms * 1e-3) / 1e9 / peak, "algorithmic_bytes": alg_gal}}
 
 
 def run_ours(args):
     import torch
     import msfec
-    import workloads
 
     world, rank, local = dist_env()
     torch.cuda.set_device(local)
@@ -201,23 +373,7 @@ def run_ours(args):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    cells_all, a_all, r_all, load, cfg = make_workload(args.workload)
-    lo, hi = partition(cells_all, world, rank)
-    flo, fhi = coef_slice(cells_all, lo, hi)
-    cells = cells_all[lo:hi]
-    a = np.ascontiguousarray(a_all[flo:fhi])
-    r = None if r_all is None else np.ascontiguousarray(r_all[flo:fhi])
-    work_local = workloads.work_dof_rhs(cells)
-    work_total = workloads.work_dof_rhs(cells_all)
-    nc = len(cells)
-
     stream = torch.cuda.Stream()
-    d_a = torch.from_numpy(a).cuda()
-    d_r = None if r is None else torch.from_numpy(r).cuda()
-    d_KH = torch.zeros((nc, 8, 8), dtype=torch.float64, device="cuda")
-    d_FH = torch.zeros((nc, 8), dtype=torch.float64, device="cuda")
-    d_rep = torch.zeros(nc * msfec.REPORT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
-    torch.cuda.synchronize()
 
     def barrier():
         torch.cuda.synchronize()
@@ -231,108 +387,93 @@ def run_ours(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
-    def timed_device(precision, steps, warmup):
-        h = msfec.Handle(precision=precision, device=local)
-        h.set_stream(stream.cuda_stream)
-        h.set_timing(True)
-        rp = 0 if d_r is None else d_r.data_ptr()
-        for _ in range(warmup):
-            h.q1_build_device(cells, d_a.data_ptr(), rp, load, d_KH.data_ptr(), d_FH.data_ptr(), d_rep.data_ptr())
-        barrier()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        solve_ms, gal_ms, launches = [], [], 0
-        e0.record(stream)
-        for _ in range(steps):
-            h.q1_build_device(cells, d_a.data_ptr(), rp, load, d_KH.data_ptr(), d_FH.data_ptr(), d_rep.data_ptr())
-            t = h.timings()
-            solve_ms.append(t["solve_ms"])
-            gal_ms.append(t["galerkin_ms"])
-            launches += t["kernel_launches"]
-        e1.record(stream)
-        barrier()
-        ms = e0.elapsed_time(e1) / steps
-        rep = np.frombuffer(d_rep.cpu().numpy().tobytes(), dtype=msfec.REPORT_DTYPE)
-        h.close()
-        return ms, float(np.mean(solve_ms)), float(np.mean(gal_ms)), launches, rep
+    def measure(name, steps, warmup, fp64_steps, with_clocks):
+        wl = Workload(name)
+        lo, hi = partition(wl, world, rank)
+        total = wl.work()
+        sampler = ClockSampler(local)
+        if with_clocks:
+            sampler.start()
+        ms, solve_ms, gal_ms, launches, rep = gpu_run(wl, lo, hi, msfec.PRECISION_MIXED, steps, warmup, local,
+                                                      stream, barrier)
+        clocks = sampler.stop() if with_clocks else None
+        ms = reduce_max(ms)
+        out = {"wl": wl, "lo": lo, "hi": hi, "value": total / (ms * 1e-3), "ms_per_step": ms, "clocks": clocks,
+               "launches": launches, "converged": bool(rep["converged"].all()),
+               "max_iterations": int(rep["iterations"].max()) if len(rep) else 0, "work_dof_rhs": total,
+               "roofline": roofline(wl, lo, hi, solve_ms, gal_ms, rep, wl.kind)}
+        if fp64_steps > 0:
+            ms64, s64, g64, _, rep64 = gpu_run(wl, lo, hi, msfec.PRECISION_FP64, fp64_steps, 1, local, stream,
+                                               barrier)
+            ms64 = reduce_max(ms64)
+            out["fp64_path"] = {"value": total / (ms64 * 1e-3), "ms_per_step": ms64, "solve_ms": s64,
+                                "steps": fp64_steps, "converged": bool(rep64["converged"].all()),
+                                "mixed_over_fp64": ms64 / ms}
+        return out
 
-    # ---- mixed precision (headline) with clocks sampled during the timed region
-    sampler = ClockSampler(local)
-    sampler.start()
-    ms_mixed, solve_ms, gal_ms, launches, rep = timed_device(msfec.PRECISION_MIXED, args.steps, args.warmup)
-    clocks = sampler.stop()
-    ms_mixed = reduce_max(ms_mixed)
-    value = work_total / (ms_mixed * 1e-3)
-
-    # ---- plain FP64 path on the same workload (fewer steps: it is the slow baseline)
-    fp64 = None
-    if not args.skip_fp64:
-        k64 = max(1, min(args.steps, 3))
-        ms64, solve64, gal64, _, rep64 = timed_device(msfec.PRECISION_FP64, k64, 1)
-        ms64 = reduce_max(ms64)
-        fp64 = {"value": work_total / (ms64 * 1e-3), "ms_per_step": ms64, "solve_ms": solve64,
-                "steps": k64, "converged": bool(rep64["converged"].all()),
-                "mixed_over_fp64": (work_total / (ms_mixed * 1e-3)) / (work_total / (ms64 * 1e-3))}
-
-    # ---- end to end through the host-buffer C ABI (pinned host inputs, H2D + D2H inside)
-    h = msfec.Handle(precision=msfec.PRECISION_MIXED, device=local)
-    h.set_stream(stream.cuda_stream)
-    a_pin = torch.from_numpy(a).pin_memory().numpy()
-    r_pin = None if r is None else torch.from_numpy(r).pin_memory().numpy()
-    h.q1_build(cells, a_pin, r_pin, load)
-    barrier()
-    t0 = time.perf_counter()
-    ke = max(1, min(args.steps, 3))
-    for _ in range(ke):
-        KH, FH, rep_e, st = h.q1_build(cells, a_pin, r_pin, load)
-    barrier()
-    e2e_s = reduce_max((time.perf_counter() - t0) / ke)
-    h.close()
-    h2d = a.nbytes + (0 if r is None else r.nbytes) + nc * msfec.CELL_DTYPE.itemsize
-    d2h = KH.nbytes + FH.nbytes + nc * msfec.REPORT_DTYPE.itemsize
-
+    head = measure(args.workload, args.steps, args.warmup, 0 if args.skip_fp64 else max(1, min(args.steps, 2)),
+                   True)
+    wl, lo, hi = head["wl"], head["lo"], head["hi"]
+    e2e_s, h2d, d2h = e2e_run(wl, lo, hi, local, stream, barrier, max(1, min(args.steps, 3)))
+    e2e_s = reduce_max(e2e_s)
+    extras = {}
+    if not args.skip_extra and args.extra:
+        for name in args.extra.split(","):
+            ex = measure(name, max(3, min(args.steps, 5)), 3, 0 if args.skip_fp64 else 2, False)
+            extras[name] = {k: ex[k] for k in ("value", "ms_per_step", "converged", "max_iterations",
+                                               "work_dof_rhs", "roofline", "fp64_path") if k in ex}
+            extras[name]["config"] = ex["wl"].cfg
     if rank != 0:
         if dist is not None:
             dist.destroy_process_group()
         return
-
-    # ---- roofline of the dominant kernel (persistent local solver)
-    peak, peak_kind = peaks()
-    nfine = int(np.sum(workloads.fine_counts(cells)[0]))
-    nnodes = int(np.sum(workloads.fine_counts(cells)[1]))
-    alg_solve = nfine * 8 * (1 if r is None else 2) + nnodes * 8 * 8 * 2  # a(,r) in; phi, y out
-    alg_gal = nnodes * 8 * 8 * 2 + nc * 72 * 8
-    roof = {"bound": "hbm", "kernel": "q1_solve_kernel (persistent PCG, on-chip state)",
-            "achieved": alg_solve / (solve_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
-            "frac": alg_solve / (solve_ms * 1e-3) / 1e9 / peak, "traffic": None,
-            "algorithmic_bytes": alg_solve, "launch_ms": solve_ms, "peak_source": peak_kind,
-            "galerkin": {"kernel": "q1_galerkin_kernel (DMMA)", "launch_ms": gal_ms,
-                         "achieved": alg_gal / (gal_ms * 1e-3) / 1e9, "frac": alg_gal / (gal_ms * 1e-3) / 1e9 / peak,
-                         "algorithmic_bytes": alg_gal}}
-
-    # ---- CPU baseline: oracle CG+SSOR (faithful-iterative) on a bounded sample
     cpu = None
     if not args.skip_cpu:
         nthreads = os.cpu_count() or 1
-        sel = cpu_sample_cells(cells_all, args.cpu_seconds, nthreads)
-        v, dt, ncell, st = time_oracle(cells_all, a_all, r_all, load, sel, nthreads)
-        cpu = {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
-               "sample": f"{ncell} of {len(cells_all)} cells (every depth), CG+SSOR(1.6) 1e-12, {dt:.1f} s"}
-
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True,
+        sel = cpu_sample(wl, args.cpu_seconds, nthreads)
+        v, dt, desc = time_oracle(wl, sel, nthreads)
+        cpu = {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": desc}
+    line = {"metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True,
             "scaling": "strong", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-            "config": dict(cfg, precision="mixed", l2="inputs and basis (>5 GB) exceed L2",
-                           parallelism=f"cells partitioned over {world} GPU(s)"),
-            "roofline": roof, "cpu_baseline": cpu,
-            "e2e": {"value": work_total / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+            "config": dict(wl.cfg, precision="mixed (FP32 Krylov + FP64 refinement)",
+                           l2="inputs + basis exceed L2 (129 MB): Phi and K*Phi are written fresh every step",
+                           parallelism=f"coarse cells partitioned over {world} GPU(s)"),
+            "roofline": head["roofline"], "cpu_baseline": cpu,
+            "e2e": {"value": head["work_dof_rhs"] / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
-            "gpu_launches": int(launches), "clocks": clocks, "fp64_path": fp64,
-            "converged": bool(rep["converged"].all()),
-            "max_iterations": int(rep["iterations"].max()), "work_dof_rhs": work_total}
+            "gpu_launches": int(head["launches"]), "clocks": head["clocks"],
+            "fp64_path": head.get("fp64_path"), "converged": head["converged"],
+            "max_iterations": head["max_iterations"], "work_dof_rhs": head["work_dof_rhs"],
+            "extra": extras}
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    wl = Workload(args.workload)
+    nthreads = os.cpu_count() or 1
+    sel = cpu_sample(wl, args.cpu_seconds / 2.0, nthreads)
+    for _ in range(args.warmup):
+        time_oracle(wl, sel[: max(1, len(sel) // 8)], nthreads)
+    vals, dts = [], []
+    desc = ""
+    for _ in range(args.steps):
+        v, dt, desc = time_oracle(wl, sel, nthreads)
+        vals.append(v)
+        dts.append(dt)
+    value = float(np.median(vals))
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": float(np.median(dts) * 1e3), "higher_is_better": True,
+            "scaling": "strong", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": wl.cfg,
+            "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": desc},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
 
 
 def main():
@@ -341,16 +482,19 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="q1_uneven", choices=["q1_uneven", "q1_small", "q1_adjoint_fwd"])
+    ap.add_argument("--workload", default="nedrt_small",
+                    choices=["nedrt_small", "nedrt_large", "q1_uneven", "q1_small", "q1_adjoint_fwd"])
+    ap.add_argument("--extra", default="q1_uneven", help="comma-separated workloads reported beside the headline")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-extra", action="store_true")
     args = ap.parse_args()
-    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
-    if args.impl == "reference":
-        run_reference(args)
-    else:
+    if args.impl == "ours":
+        args.warmup = max(args.warmup, 3)
         run_ours(args)
+    else:
+        run_reference(args)
 
 
 if __name__ == "__main__":

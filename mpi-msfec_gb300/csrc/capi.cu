@@ -392,7 +392,7 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
   prm.use_smem = use_smem ? 1 : 0;
   prm.rtol = h->cfg.nedrt_rtol;
   prm.inner_rtol = h->cfg.inner_rtol;
-  prm.max_iter = std::max(h->cfg.max_iter, 20000);
+  prm.max_iter = std::max(h->cfg.max_iter, 8000);  // per refinement step (MINRES, kappa ~ 1e4)
   prm.max_refine = h->cfg.max_refine;
   if (h->cfg.verbose)
     fprintf(stderr, "[msfec] nedrt plan: %d cells, %zu items, workspace %zu floats (%s), grid %d, %s\n", ncells,

@@ -8,7 +8,8 @@
 //     Nedelec / RT function, zero for the other field)
 //   run solve loop                ned_rt_basis.cc:1338-1381
 //   solve_iterative (Schur CG + ILU/GMRES there) ned_rt_basis.cc:636-847
-// The saddle-point system is solved with MINRES preconditioned by
+// The saddle-point system is solved (in its symmetric form, face rows negated)
+// with MINRES preconditioned by
 // diag(M)^-1 (+) diag(D + C^T diag(M)^-1 C)^-1 on the interior DoFs, FP32 inside
 // FP64 iterative refinement (MINRES in FP64 for the plain FP64 path); the
 // operator is applied matrix-free, cell by cell, from the per-cell A^-1 / B and
@@ -24,6 +25,7 @@ namespace nrimpl {
 
 struct NRShared {
   double wred[kNRWarps][3];
+  float fred[kNRWarps][3];  // float slots: no FP64 instruction in the FP32 Krylov loop
   double G[3][3][4][4];  // edge-mass geometry: M_e = sum_pq A^-1_pq G[p][q]
   double C[12][6];       // (curl tau_l, v_f) on the fine cell
   float Gf[3][3][4][4];
@@ -262,16 +264,26 @@ __device__ __forceinline__ void block_sum(NRShared &sh, VT (&v)[NV], VT (&out)[N
 #pragma unroll
     for (int off = 16; off >= 1; off >>= 1) v[t] += __shfl_xor_sync(0xffffffffu, v[t], off);
   }
-  __syncthreads();  // previous readers of wred are done
+  __syncthreads();  // previous readers of the slots are done
   if (lane == 0)
 #pragma unroll
-    for (int t = 0; t < NV; ++t) sh.wred[warp][t] = (double)v[t];
+    for (int t = 0; t < NV; ++t) {
+      if constexpr (sizeof(VT) == 4)
+        sh.fred[warp][t] = v[t];
+      else
+        sh.wred[warp][t] = v[t];
+    }
   __syncthreads();
 #pragma unroll
   for (int t = 0; t < NV; ++t) {
     VT s = VT(0);
 #pragma unroll
-    for (int w = 0; w < kNRWarps; ++w) s += (VT)sh.wred[w][t];
+    for (int w = 0; w < kNRWarps; ++w) {
+      if constexpr (sizeof(VT) == 4)
+        s += sh.fred[w][t];
+      else
+        s += sh.wred[w][t];
+    }
     out[t] = s;
   }
 }
@@ -434,7 +446,9 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, float *ws, int ite
         const bool interior = pd[d] > 0.0f;
         const double r = interior ? -(fp32_res ? (double)facc[d] : dacc[d]) : 0.0;
         part[pass] += r * r;
-        if (pass == 1) vC[d] = (T)r;  // read after the next barrier; aliasing is disjoint (vC past acc)
+        // MINRES runs on the symmetric form S A (S = +1 on edges, -1 on faces):
+        // [M -C; -C^T -D] x = S r. vC is disjoint from the accumulator.
+        if (pass == 1) vC[d] = (T)(d < g.NE ? r : -r);
       }
       __syncthreads();
     }
@@ -477,7 +491,7 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, float *ws, int ite
     // the mixed path, the outer tolerance (mapped through eta0/||r||) for FP64.
     const T target = kMixed ? (T)(prm.inner_rtol * (double)eta0)
                             : (T)(0.1 * tol_abs * (double)eta0 / fmax(sqrt(rnorm2), 1e-300));
-    bool active = gam > T(0) && isfinite((double)gam);
+    bool active = gam > T(0) && isfinite(gam);
     if (active) {
       const T inv = T(1) / gam;
       for (int d = tid; d < N; d += kNRThreads) {
@@ -511,7 +525,7 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, float *ws, int ite
       {
         T p1[1] = {T(0)};
         for (int d = tid; d < N; d += kNRThreads)
-          if (pd[d] > 0.0f) p1[0] += az[d] * zin[d];
+          if (pd[d] > 0.0f) p1[0] += (d < g.NE ? az[d] : -az[d]) * zin[d];
         T t1[1];
         block_sum<T, 1>(sh, p1, t1);
         delta = t1[0];
@@ -522,7 +536,7 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, float *ws, int ite
         T p1[1] = {T(0)};
         for (int d = tid; d < N; d += kNRThreads) {
           T vn = T(0);
-          if (pd[d] > 0.0f) vn = az[d] - delta * vC[d] - gam * vP[d];
+          if (pd[d] > 0.0f) vn = (d < g.NE ? az[d] : -az[d]) - delta * vC[d] - gam * vP[d];
           vP[d] = vn;
           p1[0] += (T)pd[d] * vn * vn;
         }
@@ -534,7 +548,7 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, float *ws, int ite
       const T a1 = sqrt(a0 * a0 + gnew * gnew);
       const T a2 = ss * delta + c_prev * cc * gam;
       const T a3 = s_prev * gam;
-      if (!(a1 > T(0)) || !isfinite((double)a1)) {
+      if (!(a1 > T(0)) || !isfinite(a1)) {
         flags |= 1;
         break;
       }
@@ -563,7 +577,7 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, float *ws, int ite
       s_prev = ss;
       ss = sn;
       (void)gam_prev;
-      if (fabs((double)eta) <= (double)target || gnew == T(0)) active = false;
+      if (fabs(eta) <= target || gnew == T(0)) active = false;
       __syncthreads();
     }
     // ---------------- phi_I += x (FP64, HBM) ----------------
