@@ -476,6 +476,23 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def probe(name):
+    """One small build through the host C ABI (the ncu capture target)."""
+    import msfec
+    import workloads
+    h = msfec.Handle(precision=msfec.PRECISION_MIXED)
+    h.set_timing(True)
+    if name == "nedrt_one_cell":
+        cells, ainv6, bdiv, load = workloads.nedrt_tensor(m=1, depth=3, seed=2)
+        KH, FH, rep, st = h.nedrt_build(cells, ainv6, bdiv, load)
+    else:
+        depth, m = (5, 1) if name == "q1_depth5_one_cell" else (3, 2)
+        cells, a, r, load = workloads.q1_lognormal(m=m, depth=depth, seed=9, reaction=False)
+        KH, FH, rep, st = h.q1_build(cells, a, None, load)
+    print(json.dumps({"probe": name, "status": int(st), "timings": h.timings(),
+                      "max_iterations": int(rep["iterations"].max())}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -489,7 +506,12 @@ def main():
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-extra", action="store_true")
+    ap.add_argument("--probe", default=None, choices=["nedrt_one_cell", "q1_depth5_one_cell", "q1_depth3_8cells"],
+                    help="run one small mixed build and exit (the case profiled with ncu --set full)")
     args = ap.parse_args()
+    if args.probe:
+        probe(args.probe)
+        return
     if args.impl == "ours":
         args.warmup = max(args.warmup, 3)
         run_ours(args)

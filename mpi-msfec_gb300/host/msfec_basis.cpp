@@ -1,0 +1,258 @@
+// Implementation of the QBasis / NedRTBasis-compatible host shim (see
+// msfec_basis.hpp). Batches cells, builds them with one C-ABI call, and
+// answers the reference's getters from the batch results.
+#include "msfec_basis.hpp"
+
+#include <cmath>
+#include <cstring>
+
+namespace msfec_host {
+
+static void check(msfec_handle *h, msfec_status s, const char *where) {
+  if (s != MSFEC_SUCCESS)
+    throw BasisError(s, std::string(where) + ": " + msfec_status_string(s) + ": " + (h ? msfec_last_error(h) : ""));
+}
+
+BasisBatch::BasisBatch(int device, int precision) {
+  msfec_config cfg;
+  msfec_config_default(&cfg);
+  cfg.device = device;
+  cfg.precision = precision;
+  check(nullptr, msfec_create(&handle_, &cfg), "msfec_create");
+}
+
+BasisBatch::~BasisBatch() { msfec_destroy(handle_); }
+
+static msfec_cell make_cell(const CoarseCell &c, unsigned depth) {
+  msfec_cell m;
+  std::memset(&m, 0, sizeof(m));
+  for (int d = 0; d < 3; ++d) {
+    m.origin[d] = c.origin[d];
+    m.size[d] = c.size[d];
+  }
+  m.depth = (int32_t)depth;
+  return m;
+}
+
+// Fine-cell centres of a coarse cell in the ABI's lexicographic order.
+template <typename F>
+static void for_each_fine_centre(const msfec_cell &c, F &&f) {
+  const int n = 1 << c.depth;
+  for (int k = 0; k < n; ++k)
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i)
+        f(Point{c.origin[0] + (i + 0.5) * c.size[0] / n, c.origin[1] + (j + 0.5) * c.size[1] / n,
+                c.origin[2] + (k + 0.5) * c.size[2] / n});
+}
+
+namespace Q {
+
+QBasis::QBasis(const ParametersBasis &parameters, const std::string &parameter_filename, const CoarseCell &global_cell,
+               const std::string &first_cell, unsigned local_subdomain, std::shared_ptr<Q1Batch> batch)
+    : parameters_(parameters),
+      parameter_filename_(parameter_filename),
+      cell_(global_cell),
+      first_cell_(first_cell),
+      local_subdomain_(local_subdomain),
+      batch_(std::move(batch)),
+      global_weights_(8, 0.0) {}
+
+void QBasis::run() {
+  if (slot_ < 0) slot_ = batch_->enqueue(cell_, parameters_.n_refine_local);
+}
+
+const FullMatrix &QBasis::get_global_element_matrix() const {
+  if (slot_ < 0) throw BasisError(MSFEC_ERROR_INVALID_STATE, "QBasis: run() was not called");
+  return batch_->matrix(slot_);
+}
+
+const Vector &QBasis::get_global_element_rhs() const {
+  if (slot_ < 0) throw BasisError(MSFEC_ERROR_INVALID_STATE, "QBasis: run() was not called");
+  return batch_->rhs(slot_);
+}
+
+const std::string &QBasis::get_filename_global() { return parameters_.filename_global; }
+
+void QBasis::set_global_weights(const std::vector<double> &global_weights) {
+  if (global_weights.size() != 8) throw BasisError(MSFEC_ERROR_INVALID_ARGUMENT, "QBasis: 8 weights expected");
+  global_weights_ = global_weights;
+}
+
+void QBasis::set_output_flag() { output_flag_ = cell_.id == first_cell_; }
+
+double QBasis::global_solution_value(const Point &x) const {
+  if (slot_ < 0) throw BasisError(MSFEC_ERROR_INVALID_STATE, "QBasis: run() was not called");
+  return batch_->evaluate(slot_, global_weights_, x);
+}
+
+Q1Batch::Q1Batch(Q1Coefficients coeff, int device, int precision) : coeff_(std::move(coeff)), gpu_(device, precision) {}
+
+int Q1Batch::enqueue(const CoarseCell &cell, unsigned depth) {
+  if (built_) {  // a new cell after a build starts a new batch
+    cells_.clear();
+    built_ = false;
+  }
+  cells_.push_back(make_cell(cell, depth));
+  return (int)cells_.size() - 1;
+}
+
+void Q1Batch::flush() {
+  if (built_) return;
+  std::vector<double> a, r;
+  for (const msfec_cell &c : cells_)
+    for_each_fine_centre(c, [&](const Point &p) {
+      a.push_back(coeff_.diffusion(p));
+      if (coeff_.reaction) r.push_back(coeff_.reaction(p));
+    });
+  const int nc = (int)cells_.size();
+  std::vector<double> KH((size_t)nc * 64), FH((size_t)nc * 8);
+  reports_.assign(nc, msfec_cell_report{});
+  check(gpu_.handle(),
+        msfec_q1_build(gpu_.handle(), nc, cells_.data(), a.data(), coeff_.reaction ? r.data() : nullptr, &coeff_.load,
+                       KH.data(), FH.data(), reports_.data()),
+        "msfec_q1_build");
+  KH_.assign(nc, FullMatrix(8, 8));
+  FH_.assign(nc, Vector(8));
+  for (int c = 0; c < nc; ++c) {
+    std::memcpy(KH_[c].data.data(), &KH[(size_t)c * 64], 64 * sizeof(double));
+    std::memcpy(FH_[c].data.data(), &FH[(size_t)c * 8], 8 * sizeof(double));
+  }
+  built_ = true;
+}
+
+const FullMatrix &Q1Batch::matrix(int slot) {
+  flush();
+  return KH_.at(slot);
+}
+
+const Vector &Q1Batch::rhs(int slot) {
+  flush();
+  return FH_.at(slot);
+}
+
+double Q1Batch::evaluate(int slot, const std::vector<double> &w, const Point &x) {
+  flush();
+  std::vector<double> weights((size_t)cells_.size() * 8, 0.0);
+  for (int v = 0; v < 8; ++v) weights[(size_t)slot * 8 + v] = w[v];
+  int32_t cell_of = slot;
+  double out = 0.0;
+  check(gpu_.handle(), msfec_q1_eval_fine(gpu_.handle(), weights.data(), 1, &cell_of, x.data(), &out),
+        "msfec_q1_eval_fine");
+  return out;
+}
+
+}  // namespace Q
+
+namespace NedRT {
+
+NedRTBasis::NedRTBasis(const ParametersBasis &parameters, const std::string &parameter_filename,
+                       const CoarseCell &global_cell, const std::string &first_cell, unsigned local_subdomain,
+                       std::shared_ptr<NedRTBatch> batch)
+    : parameters_(parameters),
+      parameter_filename_(parameter_filename),
+      cell_(global_cell),
+      first_cell_(first_cell),
+      local_subdomain_(local_subdomain),
+      batch_(std::move(batch)),
+      global_weights_(18, 0.0) {}
+
+void NedRTBasis::run() {
+  if (slot_ < 0) slot_ = batch_->enqueue(cell_, parameters_.n_refine_local);
+}
+
+const FullMatrix &NedRTBasis::get_global_element_matrix() const {
+  if (slot_ < 0) throw BasisError(MSFEC_ERROR_INVALID_STATE, "NedRTBasis: run() was not called");
+  return batch_->matrix(slot_);
+}
+
+const Vector &NedRTBasis::get_global_element_rhs() const {
+  if (slot_ < 0) throw BasisError(MSFEC_ERROR_INVALID_STATE, "NedRTBasis: run() was not called");
+  return batch_->rhs(slot_);
+}
+
+const std::string &NedRTBasis::get_filename_global() const { return parameters_.filename_global; }
+
+void NedRTBasis::set_global_weights(const std::vector<double> &global_weights) {
+  if (global_weights.size() != 18) throw BasisError(MSFEC_ERROR_INVALID_ARGUMENT, "NedRTBasis: 18 weights expected");
+  global_weights_ = global_weights;
+}
+
+void NedRTBasis::set_output_flag() { output_flag_ = cell_.id == first_cell_; }
+
+void NedRTBasis::global_solution(std::vector<double> &sigma, std::vector<double> &u) const {
+  if (slot_ < 0) throw BasisError(MSFEC_ERROR_INVALID_STATE, "NedRTBasis: run() was not called");
+  batch_->solution(slot_, global_weights_, sigma, u);
+}
+
+NedRTBatch::NedRTBatch(NedRTCoefficients coeff, int device, int precision)
+    : coeff_(std::move(coeff)), gpu_(device, precision) {}
+
+int NedRTBatch::enqueue(const CoarseCell &cell, unsigned depth) {
+  if (built_) {
+    cells_.clear();
+    built_ = false;
+  }
+  cells_.push_back(make_cell(cell, depth));
+  return (int)cells_.size() - 1;
+}
+
+void NedRTBatch::flush() {
+  if (built_) return;
+  std::vector<double> ainv6, b;
+  for (const msfec_cell &c : cells_)
+    for_each_fine_centre(c, [&](const Point &p) {
+      const std::array<double, 9> m = coeff_.diffusion_inverse(p);
+      const double s[6] = {m[0], m[4], m[8], m[1], m[2], m[5]};
+      ainv6.insert(ainv6.end(), s, s + 6);
+      b.push_back(coeff_.div_weight(p));
+    });
+  const int nc = (int)cells_.size();
+  std::vector<double> KH((size_t)nc * 324), FH((size_t)nc * 18);
+  reports_.assign(nc, msfec_cell_report{});
+  check(gpu_.handle(),
+        msfec_nedrt_build(gpu_.handle(), nc, cells_.data(), ainv6.data(), b.data(), &coeff_.load, KH.data(),
+                          FH.data(), reports_.data()),
+        "msfec_nedrt_build");
+  KH_.assign(nc, FullMatrix(18, 18));
+  FH_.assign(nc, Vector(18));
+  for (int c = 0; c < nc; ++c) {
+    std::memcpy(KH_[c].data.data(), &KH[(size_t)c * 324], 324 * sizeof(double));
+    std::memcpy(FH_[c].data.data(), &FH[(size_t)c * 18], 18 * sizeof(double));
+  }
+  basis_.resize((size_t)msfec_nedrt_basis_size(gpu_.handle()));
+  check(gpu_.handle(), msfec_nedrt_get_basis(gpu_.handle(), basis_.data(), (int64_t)basis_.size()),
+        "msfec_nedrt_get_basis");
+  basis_off_.assign(nc + 1, 0);
+  for (int c = 0; c < nc; ++c) {
+    const size_t n = (size_t)1 << cells_[c].depth;
+    basis_off_[c + 1] = basis_off_[c] + 18 * (3 * n * (n + 1) * (n + 1) + 3 * n * n * (n + 1));
+  }
+  built_ = true;
+}
+
+const FullMatrix &NedRTBatch::matrix(int slot) {
+  flush();
+  return KH_.at(slot);
+}
+
+const Vector &NedRTBatch::rhs(int slot) {
+  flush();
+  return FH_.at(slot);
+}
+
+void NedRTBatch::solution(int slot, const std::vector<double> &w, std::vector<double> &sigma, std::vector<double> &u) {
+  flush();
+  const size_t n = (size_t)1 << cells_[slot].depth;
+  const size_t NE = 3 * n * (n + 1) * (n + 1), NF = 3 * n * n * (n + 1), N = NE + NF;
+  const double *phi = basis_.data() + basis_off_[slot];
+  sigma.assign(NE, 0.0);
+  u.assign(NF, 0.0);
+  // sigma from the 12 edge bases' sigma block, u from the 6 face bases' u block
+  for (int b = 0; b < 12; ++b)
+    for (size_t d = 0; d < NE; ++d) sigma[d] += w[b] * phi[(size_t)b * N + d];
+  for (int b = 12; b < 18; ++b)
+    for (size_t d = 0; d < NF; ++d) u[d] += w[b] * phi[(size_t)b * N + NE + d];
+}
+
+}  // namespace NedRT
+}  // namespace msfec_host

@@ -1,0 +1,220 @@
+// QBasis / NedRTBasis-compatible host shim over the GB300 C ABI.
+//
+// Keeps the public interface of the reference's basis classes so that its
+// global coarse solvers consume the result unchanged:
+//   Q::QBasis          include/Q/q_basis.h:77-139
+//   NedRT::NedRTBasis  include/Ned_RT/ned_rt_basis.h:99-153
+// ctor -> run() -> get_global_element_matrix() / get_global_element_rhs()
+// -> (coarse solve) -> set_global_weights().
+//
+// The reference computes each cell's basis inside run() (serially per MPI
+// rank, source/Q/q_global.cc:83-86). Here run() only enqueues the cell into a
+// shared batch; the first getter on any object of the batch launches ONE
+// batched build through msfec_q1_build / msfec_nedrt_build and distributes
+// K_H, F_H and the basis to every object. deal.II types are replaced by small
+// stand-ins (CoarseCell for the active_cell_iterator, FullMatrix, Vector);
+// coefficients come from callbacks evaluated at fine-cell centres (the
+// reference evaluates its EquationData functions at Gauss points; the GB300
+// path takes one value per fine cell). Errors surface as BasisError carrying
+// the msfec_status (the reference throws SolverControl::NoConvergence).
+#pragma once
+
+#include <array>
+#include <functional>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/msfec_cuda.h"
+
+namespace msfec_host {
+
+using Point = std::array<double, 3>;
+
+struct BasisError : std::runtime_error {
+  msfec_status status;
+  BasisError(msfec_status s, const std::string &what) : std::runtime_error(what), status(s) {}
+};
+
+// Stand-in for Triangulation<3>::active_cell_iterator: an axis-aligned coarse box.
+struct CoarseCell {
+  Point origin{};
+  Point size{};
+  std::string id;  // CellId::to_string() of the reference
+};
+
+// Stand-in for deal.II FullMatrix<double> / Vector<double>.
+struct FullMatrix {
+  unsigned rows = 0, cols = 0;
+  std::vector<double> data;
+  FullMatrix() = default;
+  FullMatrix(unsigned r, unsigned c) : rows(r), cols(c), data((size_t)r * c, 0.0) {}
+  double operator()(unsigned i, unsigned j) const { return data[(size_t)i * cols + j]; }
+  double &operator()(unsigned i, unsigned j) { return data[(size_t)i * cols + j]; }
+  unsigned m() const { return rows; }
+  unsigned n() const { return cols; }
+};
+
+struct Vector {
+  std::vector<double> data;
+  Vector() = default;
+  explicit Vector(unsigned n) : data(n, 0.0) {}
+  double operator()(unsigned i) const { return data[i]; }
+  double &operator()(unsigned i) { return data[i]; }
+  unsigned size() const { return (unsigned)data.size(); }
+};
+
+// The knobs of ParametersBasis the hot path reads (q_parameters.cc:252-262,
+// ned_rt_parameters.h:78-96).
+struct ParametersBasis {
+  unsigned n_refine_local = 3;
+  bool verbose = false;
+  bool use_direct_solver = false;  // accepted for compatibility; the GPU path is iterative
+  int precision = MSFEC_PRECISION_MIXED;
+  std::string filename_global = "multiscale_solution";
+};
+
+// One GPU handle and the pending cells of one batch.
+class BasisBatch {
+ public:
+  explicit BasisBatch(int device = 0, int precision = MSFEC_PRECISION_MIXED);
+  ~BasisBatch();
+  BasisBatch(const BasisBatch &) = delete;
+  BasisBatch &operator=(const BasisBatch &) = delete;
+  msfec_handle *handle() const { return handle_; }
+
+ private:
+  msfec_handle *handle_ = nullptr;
+};
+
+namespace Q {
+
+// Scalar diffusion a(x) > 0, reaction r(x) >= 0 (r may be empty = zero, the
+// reference's ReactionRate), load f as an msfec_load.
+struct Q1Coefficients {
+  std::function<double(const Point &)> diffusion;
+  std::function<double(const Point &)> reaction;
+  msfec_load load{MSFEC_LOAD_ZERO, 0, {0, 0, 0, 0}};
+};
+
+class Q1Batch;
+
+class QBasis {
+ public:
+  QBasis() = delete;
+  QBasis(const ParametersBasis &parameters, const std::string &parameter_filename, const CoarseCell &global_cell,
+         const std::string &first_cell, unsigned local_subdomain, std::shared_ptr<Q1Batch> batch);
+  QBasis(const QBasis &other) = default;
+
+  void run();
+  const FullMatrix &get_global_element_matrix() const;
+  const Vector &get_global_element_rhs() const;
+  const std::string &get_filename_global();
+  void set_global_weights(const std::vector<double> &global_weights);
+  void set_output_flag();
+  // u_h(x) = sum_i w_i phi_i(x) inside this cell (replaces the VTU output of
+  // output_global_solution_in_cell, q_basis.cc:484-513).
+  double global_solution_value(const Point &x) const;
+
+ private:
+  friend class Q1Batch;
+  ParametersBasis parameters_;
+  std::string parameter_filename_;
+  CoarseCell cell_;
+  std::string first_cell_;
+  unsigned local_subdomain_;
+  std::shared_ptr<Q1Batch> batch_;
+  int slot_ = -1;
+  std::vector<double> global_weights_;
+  bool output_flag_ = false;
+};
+
+class Q1Batch : public std::enable_shared_from_this<Q1Batch> {
+ public:
+  Q1Batch(Q1Coefficients coeff, int device = 0, int precision = MSFEC_PRECISION_MIXED);
+  int enqueue(const CoarseCell &cell, unsigned depth);
+  void flush();  // one batched build of every enqueued cell
+  const FullMatrix &matrix(int slot);
+  const Vector &rhs(int slot);
+  double evaluate(int slot, const std::vector<double> &w, const Point &x);
+  const std::vector<msfec_cell_report> &reports() const { return reports_; }
+
+ private:
+  Q1Coefficients coeff_;
+  BasisBatch gpu_;
+  std::vector<msfec_cell> cells_;
+  std::vector<FullMatrix> KH_;
+  std::vector<Vector> FH_;
+  std::vector<msfec_cell_report> reports_;
+  bool built_ = false;
+};
+
+}  // namespace Q
+
+namespace NedRT {
+
+// A^-1(x) (SPD 3x3) and B(x) > 0 at a point (the reference's
+// DiffusionInverse_A and Diffusion_B), vector load as an msfec_load.
+struct NedRTCoefficients {
+  std::function<std::array<double, 9>(const Point &)> diffusion_inverse;
+  std::function<double(const Point &)> div_weight;
+  msfec_load load{MSFEC_LOAD_ZERO, 0, {0, 0, 0, 0}};
+};
+
+class NedRTBatch;
+
+class NedRTBasis {
+ public:
+  NedRTBasis() = delete;
+  NedRTBasis(const ParametersBasis &parameters, const std::string &parameter_filename,
+             const CoarseCell &global_cell, const std::string &first_cell, unsigned local_subdomain,
+             std::shared_ptr<NedRTBatch> batch);
+  NedRTBasis(const NedRTBasis &other) = default;
+
+  void run();
+  const FullMatrix &get_global_element_matrix() const;
+  const Vector &get_global_element_rhs() const;
+  const std::string &get_filename_global() const;
+  void set_global_weights(const std::vector<double> &global_weights);
+  void set_output_flag();
+  // Fine DoF vectors of the local multiscale solution: sigma (edge DoFs) and u
+  // (face DoFs), as NedRTBasis::set_global_weights forms them (:1155-1181).
+  void global_solution(std::vector<double> &sigma, std::vector<double> &u) const;
+
+ private:
+  friend class NedRTBatch;
+  ParametersBasis parameters_;
+  std::string parameter_filename_;
+  CoarseCell cell_;
+  std::string first_cell_;
+  unsigned local_subdomain_;
+  std::shared_ptr<NedRTBatch> batch_;
+  int slot_ = -1;
+  std::vector<double> global_weights_;
+  bool output_flag_ = false;
+};
+
+class NedRTBatch : public std::enable_shared_from_this<NedRTBatch> {
+ public:
+  NedRTBatch(NedRTCoefficients coeff, int device = 0, int precision = MSFEC_PRECISION_MIXED);
+  int enqueue(const CoarseCell &cell, unsigned depth);
+  void flush();
+  const FullMatrix &matrix(int slot);
+  const Vector &rhs(int slot);
+  void solution(int slot, const std::vector<double> &w, std::vector<double> &sigma, std::vector<double> &u);
+
+ private:
+  NedRTCoefficients coeff_;
+  BasisBatch gpu_;
+  std::vector<msfec_cell> cells_;
+  std::vector<FullMatrix> KH_;
+  std::vector<Vector> FH_;
+  std::vector<double> basis_;
+  std::vector<size_t> basis_off_;
+  std::vector<msfec_cell_report> reports_;
+  bool built_ = false;
+};
+
+}  // namespace NedRT
+}  // namespace msfec_host

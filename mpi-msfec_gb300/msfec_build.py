@@ -17,6 +17,10 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libmsfec_cuda.so")
+HOSTLIB = os.path.join(LIBDIR, "libmsfec_host.so")
+EXAMPLE = os.path.join(LIBDIR, "example_q1")
+HOST = os.path.join(HERE, "host")
+CXX = os.environ.get("CXX", "g++")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 NVCC = os.environ.get("NVCC", "nvcc")
@@ -62,9 +66,30 @@ def build(verbose: bool = False) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n" + r.stderr + r.stdout)
+    build_host(objs)
     if verbose:
         print(LIB)
     return LIB
+
+
+def build_host(objs=()):
+    """QBasis/NedRTBasis shim + coarse solver (g++, links the CUDA library) and the example driver."""
+    srcs = [os.path.join(HOST, f) for f in ("msfec_basis.cpp", "coarse_q1.cpp")]
+    deps = srcs + [os.path.join(HOST, "msfec_basis.hpp"), LIB] + glob.glob(os.path.join(INCLUDE, "*.h"))
+    if not os.path.exists(HOSTLIB) or any(os.path.getmtime(d) > os.path.getmtime(HOSTLIB) for d in deps):
+        cmd = [CXX, "-O2", "-std=c++17", "-fPIC", "-shared", "-I", INCLUDE, "-o", HOSTLIB] + srcs + \
+              ["-L", LIBDIR, "-lmsfec_cuda", "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("host shim build failed:\n" + r.stderr)
+    ex = os.path.join(HOST, "example_q1.cpp")
+    if not os.path.exists(EXAMPLE) or os.path.getmtime(ex) > os.path.getmtime(EXAMPLE) or \
+            os.path.getmtime(HOSTLIB) > os.path.getmtime(EXAMPLE):
+        cmd = [CXX, "-O2", "-std=c++17", "-I", INCLUDE, "-o", EXAMPLE, ex, "-L", LIBDIR, "-lmsfec_host",
+               "-lmsfec_cuda", "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("example build failed:\n" + r.stderr)
 
 
 if __name__ == "__main__":

@@ -1,0 +1,73 @@
+"""CPU checks of the host-side coarse Q1 assembly/solve (consumer of K_H, F_H)
+and of the C++ shim library build."""
+import ctypes
+import os
+
+import numpy as np
+import scipy.sparse as sp
+import scipy.sparse.linalg as spla
+
+import workloads
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def host_lib():
+    import msfec_build
+    msfec_build.build()
+    L = ctypes.CDLL(msfec_build.HOSTLIB)
+    dp = ctypes.POINTER(ctypes.c_double)
+    L.msfec_host_q1_coarse_solve.argtypes = [ctypes.c_int, dp, dp, dp, ctypes.c_double, ctypes.c_int,
+                                             ctypes.POINTER(ctypes.c_int)]
+    L.msfec_host_q1_coarse_solve.restype = ctypes.c_int
+    return L
+
+
+def coarse_solve(m, KH, FH):
+    L = host_lib()
+    U = np.zeros((m + 1) ** 3)
+    it = ctypes.c_int(0)
+    dp = ctypes.POINTER(ctypes.c_double)
+    KH = np.ascontiguousarray(KH, dtype=np.float64)
+    FH = np.ascontiguousarray(FH, dtype=np.float64)
+    st = L.msfec_host_q1_coarse_solve(m, KH.ctypes.data_as(dp), FH.ctypes.data_as(dp), U.ctypes.data_as(dp),
+                                      1e-14, 20000, ctypes.byref(it))
+    assert st == 0
+    return U
+
+
+def scipy_coarse(m, KH, FH):
+    M1 = m + 1
+    rows, cols, vals = [], [], []
+    b = np.zeros(M1 ** 3)
+    for c in range(m ** 3):
+        i, j, k = c % m, (c // m) % m, c // (m * m)
+        nodes = [(i + (v & 1)) + M1 * ((j + ((v >> 1) & 1)) + M1 * (k + (v >> 2))) for v in range(8)]
+        for u in range(8):
+            b[nodes[u]] += FH[c, u]
+            for v in range(8):
+                rows.append(nodes[u]); cols.append(nodes[v]); vals.append(KH[c, u, v])
+    K = sp.coo_matrix((vals, (rows, cols)), shape=(M1 ** 3, M1 ** 3)).tocsr()
+    idx = np.arange(M1 ** 3)
+    i, j, k = idx % M1, (idx // M1) % M1, idx // (M1 * M1)
+    I = np.where((i > 0) & (j > 0) & (k > 0) & (i < m) & (j < m) & (k < m))[0]
+    U = np.zeros(M1 ** 3)
+    U[I] = spla.spsolve(K[I][:, I].tocsc(), b[I])
+    return U
+
+
+def test_coarse_solver_matches_scipy(oracle_lib):
+    cells, a, r, load = workloads.q1_lognormal(m=3, depth=2, seed=21, reaction=False)
+    res = oracle_lib.q1_build(cells["origin"], cells["size"], cells["depth"], a, r, load_kind=load.kind,
+                              load_params=list(load.params), want_phi=False)
+    U = coarse_solve(3, res["KH"], res["FH"])
+    Us = scipy_coarse(3, res["KH"], res["FH"])
+    assert np.abs(U - Us).max() <= 1e-11 * np.abs(Us).max()
+
+
+def test_shim_library_and_example_build():
+    import msfec_build
+    msfec_build.build()
+    assert os.path.exists(msfec_build.HOSTLIB) and os.path.exists(msfec_build.EXAMPLE)
+    L = ctypes.CDLL(msfec_build.HOSTLIB)
+    assert hasattr(L, "msfec_host_q1_coarse_solve")
