@@ -363,6 +363,43 @@ def roofline(wl, lo, hi, solve_ms, gal_ms, rep, kind):
                          "frac": alg_gal / (gal_ms * 1e-3) / 1e9 / peak, "algorithmic_bytes": alg_gal}}
 
 
+def adjoint_timing(local, stream, steps=3):
+    """Backward / forward time of the Q1 adjoint on coarse 8^3 x depth 4 (2.1 M fine
+    cells, 512 observation points): forward = msfec_q1_build, backward =
+    msfec_q1_backward reusing the stored basis (host buffers for both)."""
+    import msfec
+    import workloads
+    cells, a, _, load = workloads.q1_lognormal(m=8, depth=4, seed=4, reaction=False)
+    rng = np.random.default_rng(7)
+    npts = 512
+    cell_of = rng.integers(0, len(cells), npts).astype(np.int32)
+    pts = cells["origin"][cell_of] + rng.random((npts, 3)) * cells["size"][cell_of]
+    U = rng.standard_normal((len(cells), 8))
+    lam = rng.standard_normal((len(cells), 8))
+    g = rng.standard_normal(npts)
+    h = msfec.Handle(precision=msfec.PRECISION_MIXED, device=local)
+    h.set_stream(stream.cuda_stream)
+    h.q1_build(cells, a, None, load)
+    h.q1_backward(cells, a, None, load, U, lam, cell_of, pts, g)
+    fw, bw = [], []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        h.q1_build(cells, a, None, load)
+        t1 = time.perf_counter()
+        h.q1_backward(cells, a, None, load, U, lam, cell_of, pts, g, reuse_basis=True)
+        t2 = time.perf_counter()
+        fw.append(t1 - t0)
+        bw.append(t2 - t1)
+    t0 = time.perf_counter()
+    h.q1_backward(cells, a, None, load, U, lam, cell_of, pts, g, reuse_basis=False)
+    recompute = time.perf_counter() - t0
+    h.close()
+    f, b = float(np.median(fw)), float(np.median(bw))
+    return {"workload": "q1_lognormal_coarse8^3_L4, 512 observation points", "forward_ms": f * 1e3,
+            "backward_ms": b * 1e3, "bwd_over_fwd": b / f, "backward_recompute_basis_ms": recompute * 1e3,
+            "note": "host-buffer C ABI for both; backward = 2 adjoint local problems per cell + gradient kernel"}
+
+
 def run_ours(args):
     import torch
     import msfec
@@ -423,6 +460,8 @@ def run_ours(args):
             extras[name] = {k: ex[k] for k in ("value", "ms_per_step", "converged", "max_iterations",
                                                "work_dof_rhs", "roofline", "fp64_path") if k in ex}
             extras[name]["config"] = ex["wl"].cfg
+    if not args.skip_extra and not args.skip_adjoint:
+        extras["adjoint_q1"] = adjoint_timing(local, stream)
     if rank != 0:
         if dist is not None:
             dist.destroy_process_group()
@@ -506,6 +545,7 @@ def main():
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-extra", action="store_true")
+    ap.add_argument("--skip-adjoint", action="store_true")
     ap.add_argument("--probe", default=None, choices=["nedrt_one_cell", "q1_depth5_one_cell", "q1_depth3_8cells"],
                     help="run one small mixed build and exit (the case profiled with ncu --set full)")
     args = ap.parse_args()

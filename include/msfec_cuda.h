@@ -153,6 +153,31 @@ msfec_status msfec_q1_build_device(msfec_handle *handle, int32_t ncells,
                                    const msfec_load *load, double *d_KH,
                                    double *d_FH, msfec_cell_report *d_reports);
 
+/*
+ * Adjoint of the Q1 build: dJ/d(log a) for every fine cell of the batch, for a
+ * misfit J of the coarse multiscale solution u_H = sum_i U_i phi_i evaluated at
+ * points. Host buffers, synchronous. The caller owns the coarse problem:
+ *   U        [ncells][8] coarse solution restricted to each cell (vertex order)
+ *   lambda   [ncells][8] coarse adjoint K_H^-1 dJ/dU restricted to each cell
+ *   points   [npoints][3] in cell cell_of[p]; dJ_du[p] = dJ / d u_H(points[p])
+ *   grad     [fine cells] output, total derivative dJ / d log a_e
+ * Two adjoint local problems per cell (load and observation bubbles) run
+ * through the batched local solver; no basis sensitivity is solved for
+ * because the multiscale basis is K-harmonic. With reuse_basis != 0 the
+ * basis of the last msfec_q1_build on this handle is reused when the batch is
+ * the same (same cells; the caller guarantees the same a); otherwise it is
+ * recomputed first (the reference keeps no basis either: basis objects are
+ * rebuilt per run, q_global.cc:38-87). No counterpart in the reference, which
+ * has no adjoint; it extends QBasis with the gradient of its outputs.
+ */
+msfec_status msfec_q1_backward(msfec_handle *handle, int32_t ncells,
+                               const msfec_cell *cells, const double *a,
+                               const double *reaction, const msfec_load *load,
+                               int32_t reuse_basis, const double *U,
+                               const double *lambda, int32_t npoints,
+                               const int32_t *cell_of, const double *points,
+                               const double *dJ_du, double *grad);
+
 /* Per-phase device time of the last build, measured with CUDA events on the
    handle's stream when timing is enabled (the reference's TimerOutput scopes,
    source/Q/q_global.cc:21-24). Milliseconds; -1 when not measured. */

@@ -45,6 +45,11 @@ cudaError_t q1_galerkin_launch(const Q1Cell *cells, int ncells, const double *ph
 cudaError_t q1_report_launch(const Q1Stat *stats, int ncells, msfec_cell_report *rep, cudaStream_t stream);
 cudaError_t q1_eval_launch(const Q1Cell *cells, const double *phi, const double *weights, int npoints,
                            const int *cell_of, const double *pts, double *out, cudaStream_t stream);
+cudaError_t q1_adjoint_rhs_launch(const Q1Cell *cells, int ncells, const msfec_load &load, int npoints,
+                                  const int *cell_of, const double *pts, const double *gk, double *rhs,
+                                  cudaStream_t st);
+cudaError_t q1_gradient_launch(const Q1Cell *cells, int ncells, const double *a, const double *phi, const double *sol,
+                               const double *U, const double *lam, double *grad, cudaStream_t st);
 cudaError_t nedrt_solve_launch(bool fp64, const NRParams &prm, size_t smem, int grid, cudaStream_t st);
 cudaError_t nedrt_galerkin_launch(const NRCell *cells, int ncells, const double *phi, const double *y,
                                   const msfec_load &load, double *KH, double *FH, msfec_cell_report *rep,
@@ -101,6 +106,10 @@ struct msfec_handle {
   DevBuf<msfec_cell_report> rep;
   DevBuf<double> eval_w, eval_pts, eval_out;
   DevBuf<int> eval_cell;
+  // adjoint buffers
+  DevBuf<double> adj_rhs, adj_sol, adj_U, adj_lam, adj_gk, adj_grad, adj_KH, adj_FH;
+  DevBuf<Q1Item> adj_items;
+  DevBuf<Q1Unit> adj_units;
   // Ned_RT state of the last build
   DevBuf<NRCell> nr_cells;
   DevBuf<NRItem> nr_items;
@@ -221,7 +230,7 @@ Q1Plan make_q1_plan(int ncells, const msfec_cell *cells, bool fp64, bool has_r) 
     bool slab;
     plan_items(cells[c].depth, fp64, ni, nr, slab);
     any_slab = any_slab || slab;
-    for (int t = 0; t < ni; ++t) p.items.push_back(Q1Item{c, t * nr, nr, slab ? 1 : 0});
+    for (int t = 0; t < ni; ++t) p.items.push_back(Q1Item{c, t * nr, nr, slab ? 1 : 0, 0, 0});
   }
   p.cluster = any_slab ? kCluster : 1;
   // units: slab items alone; independent items grouped by `cluster` (same depth)
@@ -281,6 +290,8 @@ msfec_status q1_build_impl(msfec_handle *h, int ncells, const msfec_cell *cells,
   prm.react = d_react;
   prm.phi = h->phi.ptr;
   prm.y = h->y.ptr;
+  prm.src_rhs = nullptr;
+  prm.src_out = nullptr;
   prm.stats = h->stats.ptr;
   prm.rtol = h->cfg.rtol;
   prm.inner_rtol = h->cfg.inner_rtol;
@@ -325,6 +336,104 @@ msfec_status q1_build_impl(msfec_handle *h, int ncells, const msfec_cell *cells,
   return MSFEC_SUCCESS;
 }
 
+
+
+bool same_batch(const msfec_handle *h, int ncells, const msfec_cell *cells) {
+  if (h->q1_ncells != ncells || (int)h->h_cells.size() != ncells) return false;
+  for (int c = 0; c < ncells; ++c) {
+    const Q1Cell &q = h->h_cells[c];
+    if (q.depth != cells[c].depth) return false;
+    for (int d = 0; d < 3; ++d)
+      if (q.origin[d] != cells[c].origin[d] || q.h[d] * q.n != cells[c].size[d]) return false;
+  }
+  return true;
+}
+
+// Adjoint local problems (load bubble mu, observation bubble eta: source items
+// of the persistent solver, planes 0 and 1) and the per-fine-cell gradient.
+msfec_status q1_backward_impl(msfec_handle *h, int ncells, const msfec_cell *cells, const double *d_a,
+                              const double *d_react, const msfec_load *load, const double *d_U, const double *d_lam,
+                              int npoints, const int *d_cell_of, const double *d_pts, const double *d_gk,
+                              double *d_grad) {
+  const bool fp64 = h->cfg.precision == MSFEC_PRECISION_FP64;
+  const bool has_r = d_react != nullptr;
+  Q1Plan plan = make_q1_plan(ncells, cells, fp64, has_r);
+  std::vector<Q1Item> items;
+  std::vector<Q1Unit> units;
+  // keep the items that cover planes 0 and 1, as source items; regroup units
+  for (const Q1Item &it : plan.items)
+    if (it.rhs0 < 2) {
+      Q1Item s = it;
+      s.mode = 1;
+      items.push_back(s);
+    }
+  size_t i = 0;
+  while (i < items.size()) {
+    if (items[i].slab) {
+      units.push_back(Q1Unit{(int)i, 1, 1, 0});
+      ++i;
+      continue;
+    }
+    const int depth = cells[items[i].cell].depth;
+    size_t j = i;
+    while (j < items.size() && (int)(j - i) < plan.cluster && !items[j].slab && cells[items[j].cell].depth == depth) ++j;
+    units.push_back(Q1Unit{(int)i, (int)(j - i), 0, 0});
+    i = j;
+  }
+  cudaStream_t st = h->stream;
+  const size_t planes = (size_t)plan.nodes * 8;
+  MSFEC_CUDA_TRY(h, h->adj_rhs.reserve(planes));
+  MSFEC_CUDA_TRY(h, h->adj_sol.reserve(planes));
+  MSFEC_CUDA_TRY(h, h->adj_items.reserve(items.size()));
+  MSFEC_CUDA_TRY(h, h->adj_units.reserve(units.size()));
+  MSFEC_CUDA_TRY(h, cudaMemsetAsync(h->adj_rhs.ptr, 0, planes * sizeof(double), st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->adj_items.ptr, items.data(), items.size() * sizeof(Q1Item),
+                                    cudaMemcpyHostToDevice, st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->adj_units.ptr, units.data(), units.size() * sizeof(Q1Unit),
+                                    cudaMemcpyHostToDevice, st));
+  MSFEC_CUDA_TRY(h, cudaMemsetAsync(h->queue.ptr, 0, sizeof(int), st));
+  msfec_load ld;
+  if (load) {
+    ld = *load;
+  } else {
+    std::memset(&ld, 0, sizeof(ld));
+  }
+  MSFEC_CUDA_TRY(h, q1_adjoint_rhs_launch(h->cells.ptr, ncells, ld, npoints, d_cell_of, d_pts, d_gk, h->adj_rhs.ptr, st));
+  Q1Params prm;
+  prm.cells = h->cells.ptr;
+  prm.items = h->adj_items.ptr;
+  prm.units = h->adj_units.ptr;
+  prm.n_units = (int)units.size();
+  prm.queue = h->queue.ptr;
+  prm.a = d_a;
+  prm.react = d_react;
+  prm.phi = h->phi.ptr;
+  prm.y = h->y.ptr;
+  prm.src_rhs = h->adj_rhs.ptr;
+  prm.src_out = h->adj_sol.ptr;
+  prm.stats = h->stats.ptr;
+  prm.rtol = h->cfg.rtol;
+  prm.inner_rtol = h->cfg.inner_rtol;
+  prm.max_iter = h->cfg.max_iter;
+  prm.max_refine = h->cfg.max_refine;
+  int occ = 0;
+  MSFEC_CUDA_TRY(h, q1_solve_occupancy(fp64, plan.cluster, has_r, plan.smem, &occ));
+  if (occ <= 0) return fail(h, MSFEC_ERROR_NOT_SUPPORTED, "local solver kernel cannot be resident");
+  int grid = plan.cluster > 1 ? std::min<int>((int)units.size(), occ) * plan.cluster
+                              : std::min<int>((int)units.size(), occ * h->num_sms);
+  grid = std::max(grid, plan.cluster);
+  if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[0], st));
+  MSFEC_CUDA_TRY(h, q1_solve_launch(fp64, plan.cluster, has_r, prm, plan.smem, grid, st));
+  if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[1], st));
+  MSFEC_CUDA_TRY(h, q1_gradient_launch(h->cells.ptr, ncells, d_a, h->phi.ptr, h->adj_sol.ptr, d_U, d_lam, d_grad, st));
+  if (h->timing) {
+    MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[2], st));
+    MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[3], st));
+    h->ev_recorded = true;
+  }
+  h->last_launches = 3;
+  return MSFEC_SUCCESS;
+}
 
 constexpr int kNRMaxDepth = 4;
 constexpr size_t kNRSmemLimit = 200 * 1024;
@@ -506,6 +615,16 @@ void msfec_destroy(msfec_handle *h) {
     h->eval_pts.release();
     h->eval_out.release();
     h->eval_cell.release();
+    h->adj_rhs.release();
+    h->adj_sol.release();
+    h->adj_U.release();
+    h->adj_lam.release();
+    h->adj_gk.release();
+    h->adj_grad.release();
+    h->adj_KH.release();
+    h->adj_FH.release();
+    h->adj_items.release();
+    h->adj_units.release();
     h->nr_cells.release();
     h->nr_items.release();
     h->nr_phi.release();
@@ -665,6 +784,71 @@ msfec_status msfec_q1_eval_fine(msfec_handle *h, const double *weights, int32_t 
                                    h->eval_pts.ptr, h->eval_out.ptr, st));
   MSFEC_CUDA_TRY(h, cudaMemcpyAsync(values, h->eval_out.ptr, (size_t)npoints * sizeof(double), cudaMemcpyDeviceToHost, st));
   MSFEC_CUDA_TRY(h, cudaStreamSynchronize(st));
+  return MSFEC_SUCCESS;
+}
+
+msfec_status msfec_q1_backward(msfec_handle *h, int32_t ncells, const msfec_cell *cells, const double *a,
+                               const double *reaction, const msfec_load *load, int32_t reuse_basis, const double *U,
+                               const double *lambda, int32_t npoints, const int32_t *cell_of, const double *points,
+                               const double *dJ_du, double *grad) {
+  if (!h) return MSFEC_ERROR_INVALID_ARGUMENT;
+  if (ncells <= 0 || !cells || !a || !U || !lambda || !grad || npoints < 0 ||
+      (npoints > 0 && (!cell_of || !points || !dJ_du)))
+    return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "null pointer or invalid count");
+  int64_t nfine = 0;
+  for (int c = 0; c < ncells; ++c) {
+    if (!cell_ok(cells[c])) return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "cell " + std::to_string(c) + " invalid");
+    const int64_t n = 1LL << cells[c].depth;
+    nfine += n * n * n;
+  }
+  for (int p = 0; p < npoints; ++p)
+    if (cell_of[p] < 0 || cell_of[p] >= ncells) return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "cell_of out of range");
+  if (!load_ok(load) || (load && load->kind == MSFEC_LOAD_VEC_TRIG))
+    return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "invalid Q1 load");
+  DeviceGuard g(h->device);
+  cudaStream_t st = h->stream;
+  MSFEC_CUDA_TRY(h, h->a.reserve(nfine));
+  if (reaction) MSFEC_CUDA_TRY(h, h->react.reserve(nfine));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->a.ptr, a, nfine * sizeof(double), cudaMemcpyHostToDevice, st));
+  if (reaction)
+    MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->react.ptr, reaction, nfine * sizeof(double), cudaMemcpyHostToDevice, st));
+  if (!(reuse_basis && same_batch(h, ncells, cells))) {
+    // recompute the basis (no stored basis, or a different batch)
+    MSFEC_CUDA_TRY(h, h->adj_KH.reserve((size_t)ncells * 64));
+    MSFEC_CUDA_TRY(h, h->adj_FH.reserve((size_t)ncells * 8));
+    msfec_status s = q1_build_impl(h, ncells, cells, h->a.ptr, reaction ? h->react.ptr : nullptr, load, h->adj_KH.ptr,
+                                   h->adj_FH.ptr, nullptr);
+    if (s != MSFEC_SUCCESS) return s;
+  }
+  MSFEC_CUDA_TRY(h, h->adj_U.reserve((size_t)ncells * 8));
+  MSFEC_CUDA_TRY(h, h->adj_lam.reserve((size_t)ncells * 8));
+  MSFEC_CUDA_TRY(h, h->adj_gk.reserve(std::max(npoints, 1)));
+  MSFEC_CUDA_TRY(h, h->eval_pts.reserve((size_t)std::max(npoints, 1) * 3));
+  MSFEC_CUDA_TRY(h, h->eval_cell.reserve(std::max(npoints, 1)));
+  MSFEC_CUDA_TRY(h, h->adj_grad.reserve(nfine));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->adj_U.ptr, U, (size_t)ncells * 8 * sizeof(double), cudaMemcpyHostToDevice, st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->adj_lam.ptr, lambda, (size_t)ncells * 8 * sizeof(double), cudaMemcpyHostToDevice,
+                                    st));
+  if (npoints > 0) {
+    MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->adj_gk.ptr, dJ_du, (size_t)npoints * sizeof(double), cudaMemcpyHostToDevice, st));
+    MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->eval_pts.ptr, points, (size_t)npoints * 3 * sizeof(double),
+                                      cudaMemcpyHostToDevice, st));
+    MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->eval_cell.ptr, cell_of, (size_t)npoints * sizeof(int), cudaMemcpyHostToDevice,
+                                      st));
+  }
+  msfec_status s = q1_backward_impl(h, ncells, cells, h->a.ptr, reaction ? h->react.ptr : nullptr, load, h->adj_U.ptr,
+                                    h->adj_lam.ptr, npoints, h->eval_cell.ptr, h->eval_pts.ptr, h->adj_gk.ptr,
+                                    h->adj_grad.ptr);
+  if (s != MSFEC_SUCCESS) return s;
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(grad, h->adj_grad.ptr, nfine * sizeof(double), cudaMemcpyDeviceToHost, st));
+  MSFEC_CUDA_TRY(h, cudaStreamSynchronize(st));
+  // convergence of the adjoint local problems (planes 0 and 1)
+  std::vector<Q1Stat> stats((size_t)ncells * 8);
+  MSFEC_CUDA_TRY(h, cudaMemcpy(stats.data(), h->stats.ptr, stats.size() * sizeof(Q1Stat), cudaMemcpyDeviceToHost));
+  for (int c = 0; c < ncells; ++c)
+    for (int v = 0; v < 2; ++v)
+      if (!stats[(size_t)c * 8 + v].converged)
+        return fail(h, MSFEC_ERROR_NOT_CONVERGED, "adjoint local solve missed rtol");
   return MSFEC_SUCCESS;
 }
 

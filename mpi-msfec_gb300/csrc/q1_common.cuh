@@ -34,6 +34,9 @@ struct Q1Item {
   int rhs0;
   int nrhs;
   int slab;  // 1: z-slab decomposition over every CTA of the cluster
+  int mode;  // 0: basis (Dirichlet data = coarse vertex function, no load);
+             // 1: source (zero Dirichlet data, right-hand side from src_rhs)
+  int pad;
 };
 
 // One dequeue of the persistent kernel, executed by one cluster.
@@ -62,6 +65,8 @@ struct Q1Params {
   const double *react;
   double *phi;
   double *y;
+  const double *src_rhs;  // mode 1: [cell][8][(n+1)^3] right-hand sides (FP64)
+  double *src_out;        // mode 1: solutions, same layout
   Q1Stat *stats;
   double rtol;
   double inner_rtol;

@@ -170,4 +170,142 @@ cudaError_t q1_eval_launch(const Q1Cell *cells, const double *phi, const double 
   return cudaGetLastError();
 }
 
+
+// ---------------------------------------------------------------------------
+// Adjoint of the Q1 multiscale build (dJ/d log a per fine cell).
+//
+// For J(u_H(x_k)) with u_H = sum_i U_i phi_i, K_H U = F_H, coarse adjoint
+// lambda = K_H^-1 dJ/dU, and per coarse cell psi_U = Phi U_e, psi_l = Phi lambda_e:
+//   dJ/d log a_e = -a_e [ (mu + psi_U)_e^T Khat psi_l,e + eta_e^T Khat psi_U,e ]
+// with the adjoint local problems mu = K_II^-1 b_I (load bubble) and
+// eta = K_II^-1 (sum_k g_k E_k)_I (observation bubble, g_k = dJ/du_H(x_k)).
+// The basis derivative terms vanish because (K phi)_I = 0 for every basis
+// function (the energy-minimising property of the multiscale basis), so no
+// basis sensitivities are solved for. Khat = unit-coefficient element
+// stiffness; the reaction (if any) does not depend on a.
+// ---------------------------------------------------------------------------
+namespace {
+
+__global__ void __launch_bounds__(kGalThreads) q1_load_rhs_kernel(const Q1Cell *__restrict__ cells, msfec_load load,
+                                                                  double *__restrict__ rhs) {
+  __shared__ double beta[3][kMaxN1];
+  const int c = blockIdx.x;
+  const Q1Cell C = cells[c];
+  const int n = C.n, N1 = n + 1;
+  const size_t nn = (size_t)N1 * N1 * N1;
+  const bool has_load = load.kind == MSFEC_LOAD_SIN_PRODUCT || load.kind == MSFEC_LOAD_CONSTANT;
+  for (int t = threadIdx.x; t < 3 * N1; t += kGalThreads) {
+    const int d = t / N1, i = t % N1;
+    beta[d][i] = has_load ? q1_load_factor_1d(load.kind, load.params, C.origin[d], C.h[d], n, i) : 0.0;
+  }
+  __syncthreads();
+  double *out = rhs + 8 * C.node_off;  // plane 0: the load vector b
+  for (size_t node = threadIdx.x; node < nn; node += kGalThreads) {
+    const int i = (int)(node % N1), j = (int)((node / N1) % N1), k = (int)(node / ((size_t)N1 * N1));
+    out[node] = has_load ? load.params[0] * beta[0][i] * beta[1][j] * beta[2][k] : 0.0;
+  }
+}
+
+// plane 1: sum_k g_k E_k, E_k the trilinear weights of point k on its fine cell
+__global__ void q1_point_source_kernel(const Q1Cell *__restrict__ cells, int npoints, const int *__restrict__ cell_of,
+                                       const double *__restrict__ pts, const double *__restrict__ gk,
+                                       double *__restrict__ rhs) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npoints) return;
+  const Q1Cell C = cells[cell_of[p]];
+  const int n = C.n, N1 = n + 1;
+  const size_t nn = (size_t)N1 * N1 * N1;
+  int f[3];
+  double xi[3];
+  for (int d = 0; d < 3; ++d) {
+    const double t = (pts[3 * (size_t)p + d] - C.origin[d]) / C.h[d];
+    int fi = (int)floor(t);
+    fi = fi < 0 ? 0 : (fi > n - 1 ? n - 1 : fi);
+    f[d] = fi;
+    xi[d] = t - fi;
+  }
+  double *out = rhs + 8 * C.node_off + nn;
+  for (int corner = 0; corner < 8; ++corner) {
+    const int cx = corner & 1, cy = (corner >> 1) & 1, cz = corner >> 2;
+    const double w = (cx ? xi[0] : 1.0 - xi[0]) * (cy ? xi[1] : 1.0 - xi[1]) * (cz ? xi[2] : 1.0 - xi[2]);
+    atomicAdd(out + ((size_t)(f[2] + cz) * N1 + (f[1] + cy)) * N1 + (f[0] + cx), gk[p] * w);
+  }
+}
+
+__global__ void __launch_bounds__(kGalThreads) q1_gradient_kernel(const Q1Cell *__restrict__ cells,
+                                                                  const double *__restrict__ a,
+                                                                  const double *__restrict__ phi,
+                                                                  const double *__restrict__ sol,
+                                                                  const double *__restrict__ U,
+                                                                  const double *__restrict__ lam,
+                                                                  double *__restrict__ grad) {
+  const int c = blockIdx.x;
+  const Q1Cell C = cells[c];
+  const int n = C.n, N1 = n + 1;
+  const size_t nn = (size_t)N1 * N1 * N1;
+  double kh[8];  // unit-coefficient stiffness by coordinate-difference pattern
+  for (int pat = 0; pat < 8; ++pat) {
+    const int dx = pat & 1, dy = (pat >> 1) & 1, dz = pat >> 2;
+    const double kx = (dx ? -1.0 : 1.0) / C.h[0], ky = (dy ? -1.0 : 1.0) / C.h[1], kz = (dz ? -1.0 : 1.0) / C.h[2];
+    const double mx = C.h[0] * (dx ? 1.0 / 6.0 : 1.0 / 3.0), my = C.h[1] * (dy ? 1.0 / 6.0 : 1.0 / 3.0),
+                 mz = C.h[2] * (dz ? 1.0 / 6.0 : 1.0 / 3.0);
+    kh[pat] = kx * my * mz + mx * ky * mz + mx * my * kz;
+  }
+  double u8[8], l8[8];
+  for (int v = 0; v < 8; ++v) {
+    u8[v] = U[(size_t)c * 8 + v];
+    l8[v] = lam[(size_t)c * 8 + v];
+  }
+  const double *ph = phi + 8 * C.node_off;
+  const double *mu = sol + 8 * C.node_off;
+  const double *eta = mu + nn;
+  const size_t nc = (size_t)n * n * n;
+  for (size_t e = threadIdx.x; e < nc; e += kGalThreads) {
+    const int i = (int)(e % n), j = (int)((e / n) % n), k = (int)(e / ((size_t)n * n));
+    double pu[8], pl[8], pm[8], pe[8];
+    for (int u = 0; u < 8; ++u) {
+      const size_t node = ((size_t)(k + (u >> 2)) * N1 + (j + ((u >> 1) & 1))) * N1 + (i + (u & 1));
+      double su = 0.0, sl = 0.0;
+      for (int v = 0; v < 8; ++v) {
+        const double p = ph[(size_t)v * nn + node];
+        su += u8[v] * p;
+        sl += l8[v] * p;
+      }
+      pu[u] = su;
+      pl[u] = sl;
+      pm[u] = mu[node] + su;
+      pe[u] = eta[node];
+    }
+    double acc = 0.0;
+    for (int u = 0; u < 8; ++u) {
+      double kl = 0.0, ku = 0.0;
+      for (int v = 0; v < 8; ++v) {
+        kl += kh[u ^ v] * pl[v];
+        ku += kh[u ^ v] * pu[v];
+      }
+      acc += pm[u] * kl + pe[u] * ku;
+    }
+    grad[C.coef_off + e] = -a[C.coef_off + e] * acc;
+  }
+}
+
+}  // namespace
+
+cudaError_t q1_adjoint_rhs_launch(const Q1Cell *cells, int ncells, const msfec_load &load, int npoints,
+                                  const int *cell_of, const double *pts, const double *gk, double *rhs,
+                                  cudaStream_t st) {
+  if (ncells > 0) q1_load_rhs_kernel<<<ncells, kGalThreads, 0, st>>>(cells, load, rhs);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  if (npoints > 0) q1_point_source_kernel<<<(npoints + 127) / 128, 128, 0, st>>>(cells, npoints, cell_of, pts, gk, rhs);
+  return cudaGetLastError();
+}
+
+cudaError_t q1_gradient_launch(const Q1Cell *cells, int ncells, const double *a, const double *phi, const double *sol,
+                               const double *U, const double *lam, double *grad, cudaStream_t st) {
+  if (ncells <= 0) return cudaSuccess;
+  q1_gradient_kernel<<<ncells, kGalThreads, 0, st>>>(cells, a, phi, sol, U, lam, grad);
+  return cudaGetLastError();
+}
+
 }  // namespace msfec

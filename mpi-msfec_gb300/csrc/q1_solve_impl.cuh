@@ -9,6 +9,9 @@
 // hand side, and writes y = K phi for the Galerkin product of
 // QBasis::assemble_global_element_matrix (q_basis.cc:262-300).
 //
+// Source items (adjoint local problems) solve K_II x = f_I with zero Dirichlet
+// data and a given right-hand side through the same loop.
+//
 // Execution model: one persistent launch; each cluster dequeues units from a
 // device counter. A unit is either up to CL independent items (one CTA each)
 // or one item split into z-slabs over the CL CTAs of a cluster (deep cells);
@@ -398,8 +401,10 @@ __device__ void solve_item(const Q1Params &prm, Q1Shared &sh, unsigned char *sme
   float *dvs = reinterpret_cast<float *>(smem + L.dv_off);
   const int tid = threadIdx.x;
   const int rho = tid % R;
-  double *phi_c = prm.phi + 8 * C.node_off;
+  const bool src = it.mode == 1;
+  double *phi_c = (src ? prm.src_out : prm.phi) + 8 * C.node_off;
   double *y_c = prm.y + 8 * C.node_off;
+  const double *f_c = src ? prm.src_rhs + 8 * C.node_off : nullptr;
   const double *ag = prm.a + C.coef_off + (size_t)(k0 - 1) * n * n;  // layer 0 of the slab
   const double *rg = HAS_R ? prm.react + C.coef_off + (size_t)(k0 - 1) * n * n : nullptr;
   const int nplanes = P > 0 ? P + 2 : 0;
@@ -480,7 +485,7 @@ __device__ void solve_item(const Q1Params &prm, Q1Shared &sh, unsigned char *sme
       if (mode == 2) {
         val = __ldcg(phi_c + g);
       } else {
-        val = trilinear(v, i, j, k, n);
+        val = src ? 0.0 : trilinear(v, i, j, k, n);
         if ((kk >= 1 && kk <= P) || (kk == 0 && k == 0) || (kk == P + 1 && k == n)) phi_c[g] = val;
       }
       dst[nl * R + r_e] = (TV)val;
@@ -513,6 +518,16 @@ __device__ void solve_item(const Q1Params &prm, Q1Shared &sh, unsigned char *sme
         const int pk = (int)(e / ncol), col = (int)(e % ncol);
         const int i = col % m + 1, j = col / m + 1, k = k0 + pk;
         const size_t gnode = ((size_t)k * N1 + j) * N1 + i;
+        // r = f - K phi (f = 0 for basis items); at ir == 0 also the scale of the
+        // stopping test: ||K_IB g|| (basis items) or ||f_I|| (source items)
+        auto finish = [&](int t, double yv, double yb, bool write_y) {
+          const double f = src ? __ldg(f_c + (size_t)(it.rhs0 + t) * nn + gnode) : 0.0;
+          const double rr = f - yv;
+          xs[e * R + t] = (T)rr;
+          if (ir == 0) part[0][t] += src ? f * f : yb * yb;
+          part[1][t] += rr * rr;
+          if (write_y && !src) y_c[(size_t)(it.rhs0 + t) * nn + gnode] = yv;
+        };
         if (fp32_res) {
           float yv[R], yb[R];
           node_apply<float, R, HAS_R, true>(
@@ -520,11 +535,7 @@ __device__ void solve_item(const Q1Params &prm, Q1Shared &sh, unsigned char *sme
               [&](int l, int o) { return HAS_R ? raf[((size_t)l * n + (j - 1)) * n + (i - 1) + o] : 0.0f; }, cd, mmd,
               yv, yb);
 #pragma unroll
-          for (int t = 0; t < R; ++t) {
-            xs[e * R + t] = (T)(-yv[t]);
-            part[0][t] += (double)yb[t] * (double)yb[t];
-            part[1][t] += (double)yv[t] * (double)yv[t];
-          }
+          for (int t = 0; t < R; ++t) finish(t, (double)yv[t], (double)yb[t], false);
         } else if (ir == 0) {
           double yv[R], yb[R];
           node_apply<double, R, HAS_R, true>(
@@ -533,12 +544,7 @@ __device__ void solve_item(const Q1Params &prm, Q1Shared &sh, unsigned char *sme
               [&](int l, int o) { return HAS_R ? __ldg(rg + ((size_t)l * n + (j - 1)) * n + (i - 1) + o) : 0.0; }, cd,
               mmd, yv, yb);
 #pragma unroll
-          for (int t = 0; t < R; ++t) {
-            xs[e * R + t] = (T)(-yv[t]);
-            part[0][t] += yb[t] * yb[t];
-            part[1][t] += yv[t] * yv[t];
-            y_c[(size_t)(it.rhs0 + t) * nn + gnode] = yv[t];
-          }
+          for (int t = 0; t < R; ++t) finish(t, yv[t], yb[t], true);
         } else {
           double yv[R], yb[R];
           node_apply<double, R, HAS_R, false>(
@@ -547,11 +553,7 @@ __device__ void solve_item(const Q1Params &prm, Q1Shared &sh, unsigned char *sme
               [&](int l, int o) { return HAS_R ? __ldg(rg + ((size_t)l * n + (j - 1)) * n + (i - 1) + o) : 0.0; }, cd,
               mmd, yv, yb);
 #pragma unroll
-          for (int t = 0; t < R; ++t) {
-            xs[e * R + t] = (T)(-yv[t]);
-            part[1][t] += yv[t] * yv[t];
-            y_c[(size_t)(it.rhs0 + t) * nn + gnode] = yv[t];
-          }
+          for (int t = 0; t < R; ++t) finish(t, yv[t], 0.0, true);
         }
       }
       double tot[2];
@@ -699,7 +701,7 @@ __device__ void solve_item(const Q1Params &prm, Q1Shared &sh, unsigned char *sme
     const int nside = P * 4 * n;  // perimeter nodes of the owned planes
     const int nfirst = (P > 0 && first) ? (int)N1sq : 0;
     const int nlast = last ? (int)N1sq : 0;
-    const int nb = (P > 0) ? nside + nfirst + nlast : 0;
+    const int nb = (P > 0 && !src) ? nside + nfirst + nlast : 0;
     for (int e = tid; e < nb; e += kQ1Threads) {
       int b = e;
       int i, j, kk;

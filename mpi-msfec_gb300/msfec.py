@@ -36,7 +36,7 @@ EXPORTED = [
     "msfec_q1_build_device", "msfec_q1_basis_size", "msfec_q1_get_basis",
     "msfec_q1_basis_device", "msfec_q1_eval_fine", "msfec_set_timing", "msfec_get_timings",
     "msfec_nedrt_build", "msfec_nedrt_build_device", "msfec_nedrt_basis_size",
-    "msfec_nedrt_get_basis",
+    "msfec_nedrt_get_basis", "msfec_q1_backward",
 ]
 
 
@@ -126,6 +126,9 @@ def load_library(path: str = LIB_PATH):
     L.msfec_nedrt_basis_size.restype = ctypes.c_int64
     L.msfec_nedrt_get_basis.argtypes = [_vp, _dp, ctypes.c_int64]
     L.msfec_nedrt_get_basis.restype = ctypes.c_int
+    L.msfec_q1_backward.argtypes = [_vp, ctypes.c_int32, _vp, _dp, _dp, ctypes.POINTER(Load), ctypes.c_int32,
+                                    _dp, _dp, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32), _dp, _dp, _dp]
+    L.msfec_q1_backward.restype = ctypes.c_int
     L.msfec_set_timing.argtypes = [_vp, ctypes.c_int32]
     L.msfec_set_timing.restype = ctypes.c_int
     L.msfec_get_timings.argtypes = [_vp, ctypes.POINTER(Timings)]
@@ -252,6 +255,24 @@ class Handle:
         self.check(self._lib.msfec_get_timings(self._h, ctypes.byref(t)))
         return {"solve_ms": t.solve_ms, "galerkin_ms": t.galerkin_ms, "total_ms": t.total_ms,
                 "solve_launches": t.solve_launches, "kernel_launches": t.kernel_launches}
+
+    def q1_backward(self, cells, a, reaction, load, U, lam, cell_of, points, dJ_du, reuse_basis=True):
+        """dJ/d log a per fine cell (msfec_q1_backward)."""
+        cells = np.ascontiguousarray(cells, dtype=CELL_DTYPE)
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        reaction = None if reaction is None else np.ascontiguousarray(reaction, dtype=np.float64)
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        lam = np.ascontiguousarray(lam, dtype=np.float64)
+        cell_of = np.ascontiguousarray(cell_of, dtype=np.int32)
+        points = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+        dJ_du = np.ascontiguousarray(dJ_du, dtype=np.float64)
+        grad = np.zeros(a.shape[0])
+        st = self._lib.msfec_q1_backward(self._h, cells.shape[0], cells.ctypes.data_as(_vp), _d(a), _d(reaction),
+                                         ctypes.byref(load), 1 if reuse_basis else 0, _d(U), _d(lam),
+                                         points.shape[0], cell_of.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                         _d(points), _d(dJ_du), _d(grad))
+        self.check(st)
+        return grad
 
     def nedrt_build(self, cells, ainv6, bdiv, load=None, allow_unconverged=False):
         """Host-buffer Ned_RT build. Returns (KH [c,18,18], FH [c,18], reports, status)."""
