@@ -44,12 +44,12 @@ def global_rhs(m, FH):
 
 
 class MisfitProblem:
-    def __init__(self, msfec, cells, m, load, cell_of, points, data, precision):
+    def __init__(self, msfec, cells, m, load, cell_of, points, data, precision, rtol=None):
         self.msfec, self.cells, self.m, self.load = msfec, cells, m, load
         self.cell_of = np.asarray(cell_of, dtype=np.int32)
         self.points = np.asarray(points, dtype=np.float64)
         self.data = np.asarray(data, dtype=np.float64)
-        self.h = msfec.Handle(precision=precision)
+        self.h = msfec.Handle(precision=precision, rtol=rtol)
         self.nodes = cell_nodes(m)
 
     def forward(self, theta):
