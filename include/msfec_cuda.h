@@ -250,6 +250,38 @@ msfec_status msfec_nedrt_build_device(msfec_handle *handle, int32_t ncells,
                                       double *d_FH,
                                       msfec_cell_report *d_reports);
 
+/*
+ * Allocation-free variant of msfec_nedrt_build_device. No counterpart in the
+ * reference (deal.II allocates per cell inside NedRTBasis::run); it serves
+ * callers that must not allocate device memory while they build: a solver
+ * whose pooling allocator already holds nearly all of HBM, or a rank whose
+ * other streams must not be stalled by the device-wide synchronisation of
+ * cudaMalloc / cudaFree. Same arguments, results and asynchrony as
+ * msfec_nedrt_build_device (identical K_H, F_H, reports), but every internal
+ * buffer comes from one static device pool of 32 MiB per device that is part
+ * of the library image; nothing is allocated on the device (host memory only
+ * to format an error message). A batch whose cell table, basis Phi, Y = A Phi
+ * and status (about 1.06 MB per depth-3 cell, 7.76 MB per depth-4 cell) do not
+ * fit, or that holds more than 4096 cells, is rejected with
+ * MSFEC_ERROR_INVALID_ARGUMENT and a message naming the bytes needed; split
+ * it. Depth-4 cells also take 0.98 MB (mixed) / 1.73 MB (FP64) of MINRES
+ * workspace per concurrent CTA from the pool, so fewer CTAs run when space is
+ * short. The first call on each device looks up the pool's address (and may
+ * load the library's module for it): make that first call before any stream
+ * capture. The basis stays in the pool (msfec_nedrt_get_basis still returns
+ * the last handle-owned build) and is overwritten by the next call. There is
+ * one pool per device and process: calls that overlap in time on the same
+ * device (other threads, handles or streams) race and corrupt each other's
+ * results; serialise them on one stream.
+ */
+msfec_status msfec_nedrt_build_noalloc(msfec_handle *handle, int32_t ncells,
+                                       const msfec_cell *cells,
+                                       const double *d_ainv6,
+                                       const double *d_bdiv,
+                                       const msfec_load *load, double *d_KH,
+                                       double *d_FH,
+                                       msfec_cell_report *d_reports);
+
 /* Basis of the last Ned_RT build: per cell 18 rows (coarse basis order) of
    NE + NF fine DoFs (edges x|y|z then faces x|y|z, lexicographic), sigma and u
    of every basis function. Size in doubles, and copy to host. */

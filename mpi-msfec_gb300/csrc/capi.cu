@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -929,6 +930,237 @@ msfec_status msfec_nedrt_get_basis(msfec_handle *h, double *Phi, int64_t capacit
   MSFEC_CUDA_TRY(h, cudaMemcpyAsync(Phi, h->nr_phi.ptr, h->nr_basis_doubles * sizeof(double), cudaMemcpyDeviceToHost,
                                     h->stream));
   MSFEC_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  return MSFEC_SUCCESS;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free Ned_RT build (msfec_nedrt_build_noalloc).
+//
+// Some callers cannot allocate device memory at the moment they build a
+// basis: a coarse solver whose pooling allocator (RMM, the PyTorch caching
+// allocator) already holds nearly all of HBM, where a stray cudaMalloc fails
+// or fragments the pool; and an MPI rank that overlaps halo exchanges on other
+// streams, where cudaMalloc / cudaFree would synchronise the whole device.
+// For them every buffer of one Ned_RT batch (copied cell list, cell table,
+// work items, queue counter, basis Phi, Y = A Phi, per-item status and the
+// global MINRES workspace of depth-4 cells) is carved out of the file-scope
+// array below, which exists once per device from the moment this module is
+// loaded. The only value that must start at zero, the work-queue counter, is
+// cleared by the plan kernel in stream order. There is one pool per device
+// and process: calls that overlap in time (two host threads, two handles or
+// two streams on one device) race on it.
+namespace {
+
+constexpr size_t kNRStaticPoolBytes = size_t(32) << 20;  // 32 MiB per device
+constexpr int kNRStaticMaxCells = 4096;
+constexpr int kNRStaticMaxDevices = 64;
+constexpr int kNRPlanThreads = 1024;
+
+static __device__ __align__(256) unsigned char g_nr_static_pool[kNRStaticPoolBytes];
+
+struct NRStaticPoolSlot {
+  std::mutex m;
+  unsigned char *ptr = nullptr;
+};
+NRStaticPoolSlot g_nr_static_slots[kNRStaticMaxDevices];
+
+// Device address of this device's pool, looked up once per device with that
+// device current (the caller holds a DeviceGuard). The first lookup may load
+// this module onto the device; later calls only read the cached pointer.
+cudaError_t nr_static_pool(int device, unsigned char **out) {
+  NRStaticPoolSlot &s = g_nr_static_slots[device];
+  std::lock_guard<std::mutex> lk(s.m);
+  if (!s.ptr) {
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_nr_static_pool);
+    if (e != cudaSuccess) return e;
+    s.ptr = static_cast<unsigned char *>(p);
+  }
+  *out = s.ptr;
+  return cudaSuccess;
+}
+
+// Cell table and work items of the batch, built on the device from the copied
+// msfec_cell list: the same NRCell offsets and the same deepest-first item
+// order (stable within a depth) as the host planner of nedrt_build_impl.
+// One block; each thread owns a contiguous run of cells, a block-wide
+// inclusive scan gives the fine-cell offset, the DoF offset and four packed
+// 16-bit per-depth counters (ncells <= 4096 < 2^16).
+__global__ void __launch_bounds__(kNRPlanThreads)
+    nr_static_plan_kernel(const msfec_cell *in, int ncells, NRCell *cells, NRItem *items, int *queue) {
+  __shared__ long long s_fine[kNRPlanThreads], s_dofs[kNRPlanThreads], s_cnt[kNRPlanThreads];
+  const int t = threadIdx.x;
+  const int per = (ncells + kNRPlanThreads - 1) / kNRPlanThreads;
+  const int c0 = min(ncells, t * per), c1 = min(ncells, c0 + per);
+  long long f = 0, d = 0, k = 0;
+  for (int c = c0; c < c1; ++c) {
+    const int dep = in[c].depth, n = 1 << dep;
+    int NEx, NFx, NE, NF;
+    nr_counts(n, NEx, NFx, NE, NF);
+    f += (long long)n * n * n;
+    d += NE + NF;
+    k += 1LL << (16 * (dep - 1));
+  }
+  s_fine[t] = f;
+  s_dofs[t] = d;
+  s_cnt[t] = k;
+  __syncthreads();
+  for (int off = 1; off < kNRPlanThreads; off <<= 1) {
+    long long af = 0, ad = 0, ak = 0;
+    if (t >= off) {
+      af = s_fine[t - off];
+      ad = s_dofs[t - off];
+      ak = s_cnt[t - off];
+    }
+    __syncthreads();
+    s_fine[t] += af;
+    s_dofs[t] += ad;
+    s_cnt[t] += ak;
+    __syncthreads();
+  }
+  long long pf = s_fine[t] - f, pd = s_dofs[t] - d, pk = s_cnt[t] - k;
+  const long long total = s_cnt[kNRPlanThreads - 1];
+  long long first[5] = {0, 0, 0, 0, 0};  // first cell slot of each depth, deepest first
+  long long acc = 0;
+  for (int dep = 4; dep >= 1; --dep) {
+    first[dep] = acc;
+    acc += (total >> (16 * (dep - 1))) & 0xFFFF;
+  }
+  for (int c = c0; c < c1; ++c) {
+    const msfec_cell src = in[c];
+    const int dep = src.depth, n = 1 << dep;
+    NRCell q;
+    for (int a = 0; a < 3; ++a) {
+      q.origin[a] = src.origin[a];
+      q.h[a] = src.size[a] / n;
+    }
+    q.depth = dep;
+    q.n = n;
+    q.coef_off = pf;
+    q.dof_off = pd;
+    cells[c] = q;
+    const long long slot = first[dep] + ((pk >> (16 * (dep - 1))) & 0xFFFF);
+    for (int b = 0; b < 18; ++b) items[slot * 18 + b] = NRItem{c, b};
+    int NEx, NFx, NE, NF;
+    nr_counts(n, NEx, NFx, NE, NF);
+    pf += (long long)n * n * n;
+    pd += NE + NF;
+    pk += 1LL << (16 * (dep - 1));
+  }
+  if (t == 0) *queue = 0;
+}
+
+size_t nr_static_round(size_t bytes) { return (bytes + 255) / 256 * 256; }
+
+}  // namespace
+
+extern "C" {
+
+msfec_status msfec_nedrt_build_noalloc(msfec_handle *h, int32_t ncells, const msfec_cell *cells,
+                                       const double *d_ainv6, const double *d_bdiv, const msfec_load *load,
+                                       double *d_KH, double *d_FH, msfec_cell_report *d_reports) {
+  if (!h) return MSFEC_ERROR_INVALID_ARGUMENT;
+  if (ncells < 0 || (ncells > 0 && (!cells || !d_ainv6 || !d_bdiv || !d_KH || !d_FH)))
+    return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "null pointer or negative cell count");
+  if (ncells > kNRStaticMaxCells)
+    return fail(h, MSFEC_ERROR_INVALID_ARGUMENT,
+                "msfec_nedrt_build_noalloc: " + std::to_string(ncells) + " cells exceed the static limit of " +
+                    std::to_string(kNRStaticMaxCells) + "; split the batch");
+  if (h->device < 0 || h->device >= kNRStaticMaxDevices)
+    return fail(h, MSFEC_ERROR_NOT_SUPPORTED, "msfec_nedrt_build_noalloc: device ordinal beyond 63");
+  int64_t dofs = 0;
+  int nmax = 0;
+  for (int c = 0; c < ncells; ++c) {
+    if (!cell_ok(cells[c]) || cells[c].depth > kNRMaxDepth)
+      return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "cell " + std::to_string(c) + " invalid (Ned_RT depth 1..4)");
+    const int n = 1 << cells[c].depth;
+    int NEx, NFx, NE, NF;
+    nr_counts(n, NEx, NFx, NE, NF);
+    dofs += NE + NF;
+    nmax = std::max(nmax, n);
+  }
+  if (!load_ok(load) || !nr_load_ok(load)) return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "invalid Ned_RT load");
+  if (ncells == 0) return MSFEC_SUCCESS;
+
+  // pool layout, every block 256-byte aligned
+  const bool fp64 = h->cfg.precision == MSFEC_PRECISION_FP64;
+  const size_t nitems = (size_t)ncells * 18;
+  size_t off = 0;
+  auto take = [&off](size_t bytes) {
+    const size_t o = off;
+    off += nr_static_round(bytes);
+    return o;
+  };
+  const size_t o_queue = take(sizeof(int));
+  const size_t o_in = take((size_t)ncells * sizeof(msfec_cell));
+  const size_t o_cells = take((size_t)ncells * sizeof(NRCell));
+  const size_t o_items = take(nitems * sizeof(NRItem));
+  const size_t o_stats = take(nitems * sizeof(NRStat));
+  const size_t o_phi = take((size_t)dofs * 18 * sizeof(double));
+  const size_t o_y = take((size_t)dofs * 18 * sizeof(double));
+  const size_t o_ws = off;
+  const size_t ws_floats = nr_workspace_floats(nmax, fp64 ? 8 : 4);
+  const bool use_smem = ws_floats * 4 <= kNRSmemLimit;
+  const size_t smem = use_smem ? ws_floats * 4 : 0;
+  int grid = std::min<int>((int)nitems, h->num_sms);
+  if (o_ws <= kNRStaticPoolBytes && !use_smem)
+    grid = std::min<int>(grid, (int)((kNRStaticPoolBytes - o_ws) / (ws_floats * 4)));
+  if (o_ws > kNRStaticPoolBytes || grid < 1)
+    return fail(h, MSFEC_ERROR_INVALID_ARGUMENT,
+                "msfec_nedrt_build_noalloc: the batch needs " + std::to_string(o_ws) + " bytes" +
+                    (use_smem ? std::string() : " + " + std::to_string(ws_floats * 4) + " per CTA workspace") +
+                    " of static scratch but the pool holds " + std::to_string(kNRStaticPoolBytes) +
+                    " bytes per device; split the batch");
+
+  DeviceGuard g(h->device);
+  unsigned char *pool = nullptr;
+  {
+    const cudaError_t e = nr_static_pool(h->device, &pool);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaGetSymbolAddress(static Ned_RT pool)");
+  }
+  cudaStream_t st = h->stream;
+  int *queue = reinterpret_cast<int *>(pool + o_queue);
+  msfec_cell *d_in = reinterpret_cast<msfec_cell *>(pool + o_in);
+  NRCell *d_cells = reinterpret_cast<NRCell *>(pool + o_cells);
+  NRItem *d_items = reinterpret_cast<NRItem *>(pool + o_items);
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(d_in, cells, (size_t)ncells * sizeof(msfec_cell), cudaMemcpyHostToDevice, st));
+  nr_static_plan_kernel<<<1, kNRPlanThreads, 0, st>>>(d_in, ncells, d_cells, d_items, queue);
+  MSFEC_CUDA_TRY(h, cudaGetLastError());
+  NRParams prm;
+  prm.cells = d_cells;
+  prm.items = d_items;
+  prm.n_items = (int)nitems;
+  prm.queue = queue;
+  prm.ainv6 = d_ainv6;
+  prm.bdiv = d_bdiv;
+  prm.phi = reinterpret_cast<double *>(pool + o_phi);
+  prm.y = reinterpret_cast<double *>(pool + o_y);
+  prm.stats = reinterpret_cast<NRStat *>(pool + o_stats);
+  prm.scratch = use_smem ? nullptr : reinterpret_cast<float *>(pool + o_ws);
+  prm.scratch_floats = ws_floats;
+  prm.use_smem = use_smem ? 1 : 0;
+  prm.rtol = h->cfg.nedrt_rtol;
+  prm.inner_rtol = h->cfg.inner_rtol;
+  prm.max_iter = std::max(h->cfg.max_iter, 8000);
+  prm.max_refine = h->cfg.max_refine;
+  if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[0], st));
+  MSFEC_CUDA_TRY(h, nedrt_solve_launch(fp64, prm, smem, grid, st));
+  if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[1], st));
+  msfec_load ld;
+  if (load) {
+    ld = *load;
+  } else {
+    std::memset(&ld, 0, sizeof(ld));
+  }
+  MSFEC_CUDA_TRY(h, nedrt_galerkin_launch(d_cells, ncells, prm.phi, prm.y, ld, d_KH, d_FH, d_reports, prm.stats, st));
+  if (h->timing) {
+    MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[2], st));
+    MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[3], st));
+    h->ev_recorded = true;
+  }
+  h->last_launches = d_reports ? 4 : 3;
   return MSFEC_SUCCESS;
 }
 

@@ -36,7 +36,7 @@ EXPORTED = [
     "msfec_q1_build_device", "msfec_q1_basis_size", "msfec_q1_get_basis",
     "msfec_q1_basis_device", "msfec_q1_eval_fine", "msfec_set_timing", "msfec_get_timings",
     "msfec_nedrt_build", "msfec_nedrt_build_device", "msfec_nedrt_basis_size",
-    "msfec_nedrt_get_basis", "msfec_q1_backward",
+    "msfec_nedrt_get_basis", "msfec_q1_backward", "msfec_nedrt_build_noalloc",
 ]
 
 
@@ -294,6 +294,15 @@ class Handle:
         st = self._lib.msfec_nedrt_build_device(self._h, cells.shape[0], cells.ctypes.data_as(_vp),
                                                 _vp(d_ainv6), _vp(d_bdiv), ctypes.byref(load),
                                                 _vp(d_KH), _vp(d_FH), _vp(d_reports or 0))
+        return self.check(st)
+
+    def nedrt_build_noalloc(self, cells, d_ainv6, d_bdiv, load, d_KH, d_FH, d_reports):
+        """msfec_nedrt_build_noalloc: msfec_nedrt_build_device with every internal
+        buffer in the library's static per-device pool (no device allocation)."""
+        cells = np.ascontiguousarray(cells, dtype=CELL_DTYPE)
+        st = self._lib.msfec_nedrt_build_noalloc(self._h, cells.shape[0], cells.ctypes.data_as(_vp),
+                                                 _vp(d_ainv6), _vp(d_bdiv), ctypes.byref(load),
+                                                 _vp(d_KH), _vp(d_FH), _vp(d_reports or 0))
         return self.check(st)
 
     def nedrt_basis(self):
