@@ -12,8 +12,9 @@
 // with MINRES preconditioned by
 // diag(M)^-1 (+) diag(D + C^T diag(M)^-1 C)^-1 on the interior DoFs, FP32 inside
 // FP64 iterative refinement (MINRES in FP64 for the plain FP64 path); the
-// operator is applied matrix-free, cell by cell, from the per-cell A^-1 / B and
-// closed-form element tables, accumulating into shared memory with atomics.
+// operator is applied matrix-free, cell by cell, from the per-cell A^-1 / B in
+// tensor-product form (1D P1 mass factors), accumulating into shared memory
+// with atomics; the closed-form element tables feed the preconditioner.
 // The last FP64 pass writes y_b = A P_b (P_b the primary block of basis b:
 // sigma of an edge basis, u of a face basis) for the Galerkin product of
 // NedRTBasis::assemble_global_element_matrix (ned_rt_basis.cc:849-948).
@@ -23,6 +24,14 @@
 namespace msfec {
 namespace nrimpl {
 
+// Per-item constants of the tensor-product element operator (cell sides h).
+template <typename TA>
+struct NRFactors {
+  TA hd[3];     // h_o1 h_o2 / (36 h_p): diagonal edge-mass block of direction p, per unit A_pp
+  TA hq[3];     // h_r / 24: block coupling the two edge directions other than r, per unit A_pq
+  TA cf[3][3];  // eps(p, fd) h_fd / (6 h_p h_t): edges of direction p against faces of normal fd
+};
+
 struct NRShared {
   double wred[kNRWarps][3];
   float fred[kNRWarps][3];  // float slots: no FP64 instruction in the FP32 Krylov loop
@@ -30,11 +39,15 @@ struct NRShared {
   double C[12][6];       // (curl tau_l, v_f) on the fine cell
   float Gf[3][3][4][4];
   float Cf[12][6];
+  NRFactors<float> Ff;  // tensor-product factors of the current item's cell
+  NRFactors<double> Fd;
+  float fslot[2][kNRWarps];  // per-warp partials of the two fused MINRES reductions
+  double dslot[2][kNRWarps];
   int item;
 };
 
 struct NRGeom {
-  int n, NEx, NFx, NE, NF, N;
+  int n, L, NEx, NFx, NE, NF, N;  // n = 2^L fine cells per edge
 };
 
 __device__ __forceinline__ double psi(int a, double t) { return a ? t : 1.0 - t; }
@@ -87,7 +100,7 @@ __device__ double table_C(const double h[3], int l, int f) {
 
 __device__ __forceinline__ void cell_dofs(const NRGeom &g, int c, int (&e)[12], int (&f)[6]) {
   const int n = g.n;
-  const int i = c % n, j = (c / n) % n, k = c / (n * n);
+  const int i = c & (n - 1), j = (c >> g.L) & (n - 1), k = c >> (2 * g.L);
   auto ex = [&](int a, int b, int cc) { return a + n * (b + (n + 1) * cc); };
   auto ey = [&](int a, int b, int cc) { return g.NEx + a + (n + 1) * (b + n * cc); };
   auto ez = [&](int a, int b, int cc) { return 2 * g.NEx + a + (n + 1) * (b + (n + 1) * cc); };
@@ -202,14 +215,39 @@ __device__ void curl_rhs_cell(int b, int i, int j, int k, int n, const double h[
       }
 }
 
-// Element operator of one fine cell: out += A_e z_e (18 DoFs), atomically.
-// MASK: 0 none, 1 keep only lattice-boundary values of z (lift of the
-// Dirichlet data), 2 keep only edge values, 3 keep only face values.
-template <typename TA, typename TV, typename TO, int MASK>
-__device__ __forceinline__ void cell_apply(const NRGeom &g, const TV *__restrict__ z, TO *out, const TA (&G)[3][3][4][4],
-                                           const TA (&C)[12][6], const TA (&ai)[6], TA bdiv, TA invV,
-                                           const int (&e)[12], const int (&f)[6], const bool (&eb)[12],
-                                           const bool (&fb)[6]) {
+template <typename TA>
+__device__ __forceinline__ void make_factors(const double h[3], NRFactors<TA> &F) {
+#pragma unroll
+  for (int p = 0; p < 3; ++p) {
+    int o1, o2;
+    other_axes(p, o1, o2);
+    F.hd[p] = (TA)(h[o1] * h[o2] / (36.0 * h[p]));
+    F.hq[p] = (TA)(h[p] / 24.0);
+#pragma unroll
+    for (int fd = 0; fd < 3; ++fd) {
+      const int t = 3 - p - fd;
+      const double eps = fd == (p + 1) % 3 ? 1.0 : -1.0;
+      F.cf[p][fd] = fd == p ? TA(0) : (TA)(eps * h[fd] / (6.0 * h[p] * h[t]));
+    }
+  }
+}
+
+// Element operator of one fine cell, out += A_e z_e (18 DoFs, atomically),
+// in tensor-product form instead of tables: the edge-mass block (p, q) is
+// A^-1_pq times the 1D P1 mass m = [2 1; 1 2] / 6 along every axis the two
+// edge directions share (and the cell length along the others: for p == q a
+// Kronecker product m (x) m, for p != q one factor m along the third axis r);
+// the curl block couples edges of direction p with faces of normal fd != p
+// through m along fd and a -+1 difference along the remaining axis t; the
+// div-div block is B/|K| times the outer product of the face signs. Equal to
+// table_G / table_C contracted with z. MASK: 0 none, 1 keep only
+// lattice-boundary values of z (lift of the Dirichlet data), 2 keep only edge
+// values, 3 keep only face values. With DOT set returns
+// sum_d S_d z_d (A_e z_e)_d, S = +1 on edges and -1 on faces.
+template <typename TA, typename TV, typename TO, int MASK, bool DOT>
+__device__ __forceinline__ TA cell_apply_s(const TV *__restrict__ z, TO *out, const NRFactors<TA> &F,
+                                           const TA (&ai)[6], TA bdv, const int (&e)[12], const int (&f)[6],
+                                           const bool (&eb)[12], const bool (&fb)[6]) {
   TA ze[12], zf[6];
 #pragma unroll
   for (int l = 0; l < 12; ++l) {
@@ -222,38 +260,110 @@ __device__ __forceinline__ void cell_apply(const NRGeom &g, const TV *__restrict
     zf[t] = keep ? (TA)z[f[t]] : TA(0);
   }
   const TA A[3][3] = {{ai[0], ai[3], ai[4]}, {ai[3], ai[1], ai[5]}, {ai[4], ai[5], ai[2]}};
-  TA ye[12];
+  TA ye[12], yf[6];
+  // diagonal blocks: m along both other axes (bit 0 and bit 1 of l)
 #pragma unroll
-  for (int l = 0; l < 12; ++l) ye[l] = TA(0);
+  for (int p = 0; p < 3; ++p) {
+    const TA k = A[p][p] * F.hd[p];
+    TA t[4];
+#pragma unroll
+    for (int l = 0; l < 4; ++l) t[l] = TA(2) * ze[4 * p + l] + ze[4 * p + (l ^ 1)];
+#pragma unroll
+    for (int l = 0; l < 4; ++l) ye[4 * p + l] = k * (TA(2) * t[l] + t[l ^ 2]);
+  }
+  // off-diagonal blocks: m along the shared axis r, edge-length integrals elsewhere
 #pragma unroll
   for (int p = 0; p < 3; ++p)
 #pragma unroll
-    for (int q = 0; q < 3; ++q)
+    for (int q = 0; q < 3; ++q) {
+      if (q == p) continue;
+      const int r = 3 - p - q;
+      TA s0 = TA(0), s1 = TA(0);
 #pragma unroll
-      for (int l4 = 0; l4 < 4; ++l4) {
-        TA t = TA(0);
-#pragma unroll
-        for (int m4 = 0; m4 < 4; ++m4) t += G[p][q][l4][m4] * ze[4 * q + m4];
-        ye[4 * p + l4] += A[p][q] * t;
+      for (int m = 0; m < 4; ++m) {
+        if (edge_pos(q, m, r))
+          s1 += ze[4 * q + m];
+        else
+          s0 += ze[4 * q + m];
       }
-  TA div = TA(0);
+      const TA k = A[p][q] * F.hq[r];
+      const TA u0 = TA(2) * s0 + s1, u1 = s0 + TA(2) * s1;
 #pragma unroll
-  for (int t = 0; t < 6; ++t) div += (t & 1) ? zf[t] : -zf[t];
-  const TA bd = bdiv * invV * div;
+      for (int l = 0; l < 4; ++l) ye[4 * p + l] += k * (edge_pos(p, l, r) ? u1 : u0);
+    }
+  // div-div
+  const TA bd = bdv * ((zf[1] - zf[0]) + (zf[3] - zf[2]) + (zf[5] - zf[4]));
+#pragma unroll
+  for (int t = 0; t < 6; ++t) yf[t] = (t & 1) ? bd : -bd;
+  // curl coupling: edge rows get -C z_f, face rows +C^T z_e
+  TA wf[3][2];
+#pragma unroll
+  for (int fd = 0; fd < 3; ++fd) {
+    wf[fd][0] = TA(2) * zf[2 * fd] + zf[2 * fd + 1];
+    wf[fd][1] = zf[2 * fd] + TA(2) * zf[2 * fd + 1];
+  }
+#pragma unroll
+  for (int p = 0; p < 3; ++p)
+#pragma unroll
+    for (int fd = 0; fd < 3; ++fd) {
+      if (fd == p) continue;
+      const int t3 = 3 - p - fd;
+      const TA fac = F.cf[p][fd];
+      TA u0 = TA(0), u1 = TA(0);
+#pragma unroll
+      for (int l = 0; l < 4; ++l) {
+        const bool up = edge_pos(p, l, t3);
+        const TA w = wf[fd][edge_pos(p, l, fd)];
+        ye[4 * p + l] += up ? -fac * w : fac * w;
+        const TA zv = up ? ze[4 * p + l] : -ze[4 * p + l];
+        if (edge_pos(p, l, fd))
+          u1 += zv;
+        else
+          u0 += zv;
+      }
+      yf[2 * fd] += fac * (TA(2) * u0 + u1);
+      yf[2 * fd + 1] += fac * (u0 + TA(2) * u1);
+    }
+  TA dot = TA(0);
 #pragma unroll
   for (int l = 0; l < 12; ++l) {
-    TA s = ye[l];
-#pragma unroll
-    for (int t = 0; t < 6; ++t) s -= C[l][t] * zf[t];
-    atomicAdd(out + e[l], (TO)s);
+    atomicAdd(out + e[l], (TO)ye[l]);
+    if (DOT) dot += ze[l] * ye[l];
   }
 #pragma unroll
   for (int t = 0; t < 6; ++t) {
-    TA s = (t & 1) ? bd : -bd;
-#pragma unroll
-    for (int l = 0; l < 12; ++l) s += C[l][t] * ze[l];
-    atomicAdd(out + f[t], (TO)s);
+    atomicAdd(out + f[t], (TO)yf[t]);
+    if (DOT) dot -= zf[t] * yf[t];
   }
+  return dot;
+}
+
+// Warp-reduce v and store the warp's partial in slot set `slot`; the block
+// total is read with slot_total after the next __syncthreads.
+template <typename VT>
+__device__ __forceinline__ void warp_publish(NRShared &sh, int slot, VT v) {
+#pragma unroll
+  for (int off = 16; off >= 1; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  if ((threadIdx.x & 31) == 0) {
+    if constexpr (sizeof(VT) == 4)
+      sh.fslot[slot][threadIdx.x >> 5] = v;
+    else
+      sh.dslot[slot][threadIdx.x >> 5] = v;
+  }
+}
+
+// Same summation order in every thread: identical decisions block-wide.
+template <typename VT>
+__device__ __forceinline__ VT slot_total(const NRShared &sh, int slot) {
+  VT s = VT(0);
+#pragma unroll
+  for (int w = 0; w < kNRWarps; ++w) {
+    if constexpr (sizeof(VT) == 4)
+      s += sh.fslot[slot][w];
+    else
+      s += sh.dslot[slot][w];
+  }
+  return s;
 }
 
 template <typename VT, int NV>
@@ -288,12 +398,19 @@ __device__ __forceinline__ void block_sum(NRShared &sh, VT (&v)[NV], VT (&out)[N
   }
 }
 
-template <typename T>
-__device__ void solve_item(const NRParams &prm, NRShared &sh, float *ws, int item_id) {
+extern __shared__ __align__(256) unsigned char nr_dyn_smem[];
+
+// One (cell, basis) item. SMEM: the workspace is the dynamic shared memory
+// (known at compile time, so every vector access is a shared-memory access),
+// otherwise this CTA's slot of the global scratch.
+template <typename T, bool SMEM>
+__device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
+  float *ws = SMEM ? reinterpret_cast<float *>(nr_dyn_smem) : prm.scratch + (size_t)blockIdx.x * prm.scratch_floats;
   const NRItem it = prm.items[item_id];
   const NRCell Cc = prm.cells[it.cell];
   NRGeom g;
   g.n = Cc.n;
+  g.L = Cc.depth;
   nr_counts(g.n, g.NEx, g.NFx, g.NE, g.NF);
   g.N = g.NE + g.NF;
   const int n = g.n, N = g.N;
@@ -305,15 +422,21 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, float *ws, int ite
   const size_t Np = ((size_t)N + 63) / 64 * 64;
   // workspace carve (floats)
   float *pd = ws;
-  T *zin = reinterpret_cast<T *>(ws + Np);
-  T *az = zin + Np;
-  T *vP = az + Np;  // v_{j-1}
-  T *vC = vP + Np;  // v_j
-  T *wP = vC + Np;
-  T *wC = wP + Np;
-  T *xk = wC + Np;
+  T *zt = reinterpret_cast<T *>(ws + Np);  // P v~_j (unnormalised), operand of the apply
+  T *az = zt + Np;
+  T *vA = az + Np;  // unnormalised Lanczos vectors v~_j, v~_{j-1} (roles swap)
+  T *vB = vA + Np;
+  T *wA = vB + Np;  // MINRES directions w_{j-1}, w_j (roles swap)
+  T *wB = wA + Np;
+  T *xk = wB + Np;
   float *cf = ws + Np + 7 * Np * (sizeof(T) / 4);
-  double *dacc = reinterpret_cast<double *>(ws + Np);  // FP64 residual accumulator, aliases zin..
+  double *dacc = reinterpret_cast<double *>(ws + Np);  // FP64 residual accumulator, aliases zt..
+  const NRFactors<float> &Ff = sh.Ff;
+  const NRFactors<double> &Fd = sh.Fd;
+  if (tid == 0) {
+    make_factors(Cc.h, sh.Ff);
+    make_factors(Cc.h, sh.Fd);
+  }
   float *facc = ws + Np;
   const double *ag = prm.ainv6 + 6 * Cc.coef_off;
   const double *bg = prm.bdiv + Cc.coef_off;
@@ -422,9 +545,9 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, float *ws, int ite
           const float *a = cf + 7 * c;
           const float ai[6] = {a[0], a[1], a[2], a[3], a[4], a[5]};
           if (pass == 0)
-            cell_apply<float, double, float, 1>(g, phi, facc, sh.Gf, sh.Cf, ai, a[6], (float)invV, e, f, eb, fb);
+            cell_apply_s<float, double, float, 1, false>(phi, facc, Ff, ai, a[6] * (float)invV, e, f, eb, fb);
           else
-            cell_apply<float, double, float, 0>(g, phi, facc, sh.Gf, sh.Cf, ai, a[6], (float)invV, e, f, eb, fb);
+            cell_apply_s<float, double, float, 0, false>(phi, facc, Ff, ai, a[6] * (float)invV, e, f, eb, fb);
           if (bb < 12)
 #pragma unroll
             for (int t = 0; t < 6; ++t) atomicAdd(facc + f[t], (float)-rc[t]);
@@ -432,23 +555,23 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, float *ws, int ite
           const double *a = ag + 6 * (size_t)c;
           const double ai[6] = {a[0], a[1], a[2], a[3], a[4], a[5]};
           if (pass == 0)
-            cell_apply<double, double, double, 1>(g, phi, dacc, sh.G, sh.C, ai, bg[c], invV, e, f, eb, fb);
+            cell_apply_s<double, double, double, 1, false>(phi, dacc, Fd, ai, bg[c] * invV, e, f, eb, fb);
           else
-            cell_apply<double, double, double, 0>(g, phi, dacc, sh.G, sh.C, ai, bg[c], invV, e, f, eb, fb);
+            cell_apply_s<double, double, double, 0, false>(phi, dacc, Fd, ai, bg[c] * invV, e, f, eb, fb);
           if (bb < 12)
 #pragma unroll
             for (int t = 0; t < 6; ++t) atomicAdd(dacc + f[t], -rc[t]);
         }
       }
       __syncthreads();
-      // r = -(A phi - f) on interior DoFs (boundary: 0), kept in vC
+      // r = -(A phi - f) on interior DoFs (boundary: 0), kept in vA
       for (int d = tid; d < N; d += kNRThreads) {
         const bool interior = pd[d] > 0.0f;
         const double r = interior ? -(fp32_res ? (double)facc[d] : dacc[d]) : 0.0;
         part[pass] += r * r;
         // MINRES runs on the symmetric form S A (S = +1 on edges, -1 on faces):
-        // [M -C; -C^T -D] x = S r. vC is disjoint from the accumulator.
-        if (pass == 1) vC[d] = (T)(d < g.NE ? r : -r);
+        // [M -C; -C^T -D] x = S r. vA is disjoint from the accumulator.
+        if (pass == 1) vA[d] = (T)(d < g.NE ? r : -r);
       }
       __syncthreads();
     }
@@ -463,49 +586,53 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, float *ws, int ite
     if (conv || ir >= prm.max_refine) break;
 
     // ---------------- MINRES on A_II d = r, precision T ----------------
-    // (Paige-Saunders recurrences in the form of Elman, Silvester & Wathen,
-    // preconditioned by pd; x0 = 0.)
+    // Preconditioned Lanczos + MINRES (Paige-Saunders recurrences in the form
+    // of Elman, Silvester & Wathen, preconditioner pd, x0 = 0) in two
+    // block-wide phases per iteration, each ending in one barrier:
+    //   phase 1: az = A z~_j cell by cell, fused with delta~ = z~_j^T S A z~_j,
+    //            plus the w / x update of iteration j-1 (it needs a1, which
+    //            depends on gamma_j, known only after phase 2 of j-1);
+    //   phase 2: v~_{j+1} = (S az - delta v~_j) / g_j - gamma_j v~_{j-1} / g_{j-1},
+    //            z~_{j+1} = P v~_{j+1}, gamma_{j+1}^2 = z~_{j+1}^T v~_{j+1}.
+    // The Lanczos vectors are kept unnormalised (v_j = v~_j / g_j, g_j =
+    // gamma_j), so there is no normalisation pass; each phase's reduction is
+    // published per warp and summed by every thread after the barrier.
     for (int d = tid; d < N; d += kNRThreads) {
-      vP[d] = T(0);
-      wP[d] = T(0);
-      wC[d] = T(0);
+      vB[d] = T(0);
+      wA[d] = T(0);
+      wB[d] = T(0);
       xk[d] = T(0);
       az[d] = T(0);
     }
-    T gam;  // gamma_1
+    T *vc = vA, *vp = vB;  // v~_j, v~_{j-1}
+    T *wo = wA, *wc = wB;  // w_{j-1}, w_j
+    T gam;                 // gamma_j
     {
       T p1[1] = {T(0)};
       for (int d = tid; d < N; d += kNRThreads) {
-        const T z = (T)pd[d] * vC[d];
-        zin[d] = z;
-        p1[0] += z * vC[d];
+        const T z = (T)pd[d] * vc[d];
+        zt[d] = z;
+        p1[0] += z * vc[d];
       }
       T t1[1];
       block_sum<T, 1>(sh, p1, t1);
       gam = sqrt(t1[0]);
     }
     const T eta0 = gam;
-    T eta = gam, gam_prev = T(1), c_prev = T(1), cc = T(1), s_prev = T(0), ss = T(0);
+    T eta = gam, c_prev = T(1), cc = T(1), s_prev = T(0), ss = T(0);
+    T gi_c = gam > T(0) ? T(1) / gam : T(0), gi_p = T(0);  // 1/gamma_j, 1/gamma_{j-1}
     const double tol_abs = prm.rtol * sqrt(bnorm2);
     // inner target on |eta| (preconditioned residual): relative reduction for
     // the mixed path, the outer tolerance (mapped through eta0/||r||) for FP64.
     const T target = kMixed ? (T)(prm.inner_rtol * (double)eta0)
                             : (T)(0.1 * tol_abs * (double)eta0 / fmax(sqrt(rnorm2), 1e-300));
     bool active = gam > T(0) && isfinite(gam);
-    if (active) {
-      const T inv = T(1) / gam;
-      for (int d = tid; d < N; d += kNRThreads) {
-        zin[d] *= inv;
-        vC[d] *= inv;  // v_1 normalised consistently with z_1
-      }
-    }
-    // v is carried unnormalised in the recurrence below: v_{j+1} = A z_j -
-    // (delta/gamma_j) v_j - (gamma_j/gamma_{j-1}) v_{j-1} with z_j = P v_j / gamma_j.
-    // Using normalised vC (= v_j / gamma_j) the update reads
-    // vnew = A z_j - delta vC - gamma_j vP, z_{j+1} = P vnew, gamma_{j+1} = sqrt(z.vnew).
+    bool pending = false;  // w / x update of the last iteration not yet applied
+    T p_step = T(0), p_a2 = T(0), p_a3 = T(0), p_ia1 = T(0);
     __syncthreads();
     for (int iter = 0; active && iter < prm.max_iter; ++iter) {
-      // az = A zin
+      // ---- phase 1
+      T dpart = T(0);
       for (int c = tid; c < nc; c += kNRThreads) {
         int e[12], f[6];
         cell_dofs(g, c, e, f);
@@ -513,37 +640,46 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, float *ws, int ite
         if constexpr (kMixed) {
           const float *a = cf + 7 * c;
           const float ai[6] = {a[0], a[1], a[2], a[3], a[4], a[5]};
-          cell_apply<float, float, float, 0>(g, zin, az, sh.Gf, sh.Cf, ai, a[6], (float)invV, e, f, eb, fb);
+          dpart += cell_apply_s<float, float, float, 0, true>(zt, az, Ff, ai, a[6] * (float)invV, e, f, eb, fb);
         } else {
           const double *a = ag + 6 * (size_t)c;
           const double ai[6] = {a[0], a[1], a[2], a[3], a[4], a[5]};
-          cell_apply<double, double, double, 0>(g, zin, az, sh.G, sh.C, ai, bg[c], invV, e, f, eb, fb);
+          dpart += cell_apply_s<double, double, double, 0, true>(zt, az, Fd, ai, bg[c] * invV, e, f, eb, fb);
         }
       }
-      __syncthreads();
-      T delta;
-      {
-        T p1[1] = {T(0)};
-        for (int d = tid; d < N; d += kNRThreads)
-          if (pd[d] > 0.0f) p1[0] += (d < g.NE ? az[d] : -az[d]) * zin[d];
-        T t1[1];
-        block_sum<T, 1>(sh, p1, t1);
-        delta = t1[0];
-      }
-      // vnew -> vP slot, gamma_{j+1}
-      T gnew;
-      {
-        T p1[1] = {T(0)};
+      if (pending) {  // w_j = (z_{j-1} - a3 w_{j-2} - a2 w_{j-1}) / a1, x += c eta w_j
         for (int d = tid; d < N; d += kNRThreads) {
-          T vn = T(0);
-          if (pd[d] > 0.0f) vn = (d < g.NE ? az[d] : -az[d]) - delta * vC[d] - gam * vP[d];
-          vP[d] = vn;
-          p1[0] += (T)pd[d] * vn * vn;
+          const T z = (T)pd[d] * vp[d] * gi_p;
+          const T wn = (z - p_a3 * wo[d] - p_a2 * wc[d]) * p_ia1;
+          wo[d] = wn;
+          xk[d] += p_step * wn;
         }
-        T t1[1];
-        block_sum<T, 1>(sh, p1, t1);
-        gnew = sqrt(fmax(t1[0], T(0)));
+        T *t = wo;
+        wo = wc;
+        wc = t;
       }
+      warp_publish<T>(sh, 0, dpart);
+      __syncthreads();
+      const T delta = slot_total<T>(sh, 0) * gi_c * gi_c;
+      // ---- phase 2
+      T gpart = T(0);
+      const T gg = gam * gi_p;
+      for (int d = tid; d < N; d += kNRThreads) {
+        const float pdd = pd[d];
+        T vn = T(0);
+        if (pdd > 0.0f) {
+          const T a = d < g.NE ? az[d] : -az[d];
+          vn = (a - delta * vc[d]) * gi_c - gg * vp[d];
+        }
+        vp[d] = vn;
+        az[d] = T(0);
+        const T z = (T)pdd * vn;
+        zt[d] = z;
+        gpart += z * vn;
+      }
+      warp_publish<T>(sh, 1, gpart);
+      __syncthreads();
+      const T gnew = sqrt(fmax(slot_total<T>(sh, 1), T(0)));
       const T a0 = cc * delta - c_prev * ss * gam;
       const T a1 = sqrt(a0 * a0 + gnew * gnew);
       const T a2 = ss * delta + c_prev * cc * gam;
@@ -553,33 +689,34 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, float *ws, int ite
         break;
       }
       const T cn = a0 / a1, sn = gnew / a1;
-      const T step = cn * eta;
-      const T ginv = gnew > T(0) ? T(1) / gnew : T(0);
-      // w_{j+1} = (z_j - a3 w_{j-1} - a2 w_j) / a1 -> wP slot; x += c eta w;
-      // next: zin = P vnew / gnew, vC <- vnew / gnew, vP <- old vC (scaled by 1)
-      for (int d = tid; d < N; d += kNRThreads) {
-        const T wn = (zin[d] - a3 * wP[d] - a2 * wC[d]) / a1;
-        wP[d] = wC[d];
-        wC[d] = wn;
-        xk[d] += step * wn;
-        const T vnew = vP[d];
-        vP[d] = vC[d];
-        vC[d] = vnew * ginv;
-        zin[d] = (T)pd[d] * vnew * ginv;
-        az[d] = T(0);
+      p_step = cn * eta;
+      p_a2 = a2;
+      p_a3 = a3;
+      p_ia1 = T(1) / a1;
+      pending = true;
+      {
+        T *t = vc;  // v~_{j+1} becomes current
+        vc = vp;
+        vp = t;
       }
+      gi_p = gi_c;
+      gi_c = gnew > T(0) ? T(1) / gnew : T(0);
       ++its;
       eta = -sn * eta;
-      gam_prev = gam;
       gam = gnew;
       c_prev = cc;
       cc = cn;
       s_prev = ss;
       ss = sn;
-      (void)gam_prev;
       if (fabs(eta) <= target || gnew == T(0)) active = false;
-      __syncthreads();
     }
+    if (pending)
+      for (int d = tid; d < N; d += kNRThreads) {
+        const T z = (T)pd[d] * vp[d] * gi_p;
+        const T wn = (z - p_a3 * wo[d] - p_a2 * wc[d]) * p_ia1;
+        xk[d] += p_step * wn;
+      }
+    __syncthreads();
     // ---------------- phi_I += x (FP64, HBM) ----------------
     for (int d = tid; d < N; d += kNRThreads)
       if (pd[d] > 0.0f) phi[d] += (double)xk[d];
@@ -596,9 +733,9 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, float *ws, int ite
     const double *a = ag + 6 * (size_t)c;
     const double ai[6] = {a[0], a[1], a[2], a[3], a[4], a[5]};
     if (bb < 12)
-      cell_apply<double, double, double, 2>(g, phi, dacc, sh.G, sh.C, ai, bg[c], invV, e, f, eb, fb);
+      cell_apply_s<double, double, double, 2, false>(phi, dacc, Fd, ai, bg[c] * invV, e, f, eb, fb);
     else
-      cell_apply<double, double, double, 3>(g, phi, dacc, sh.G, sh.C, ai, bg[c], invV, e, f, eb, fb);
+      cell_apply_s<double, double, double, 3, false>(phi, dacc, Fd, ai, bg[c] * invV, e, f, eb, fb);
   }
   __syncthreads();
   for (int d = tid; d < N; d += kNRThreads) yout[d] = dacc[d];
@@ -616,15 +753,16 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, float *ws, int ite
 
 template <typename T>
 __global__ void __launch_bounds__(kNRThreads, 1) nedrt_solve_kernel(NRParams prm) {
-  extern __shared__ __align__(256) unsigned char smem[];
   __shared__ NRShared sh;
-  float *ws = prm.use_smem ? reinterpret_cast<float *>(smem) : prm.scratch + (size_t)blockIdx.x * prm.scratch_floats;
   for (;;) {
     if (threadIdx.x == 0) sh.item = atomicAdd(prm.queue, 1);
     __syncthreads();
     const int item = sh.item;
     if (item >= prm.n_items) break;
-    solve_item<T>(prm, sh, ws, item);
+    if (prm.use_smem)
+      solve_item<T, true>(prm, sh, item);
+    else
+      solve_item<T, false>(prm, sh, item);
   }
 }
 
@@ -657,6 +795,7 @@ __global__ void __launch_bounds__(kGalThreads) nedrt_galerkin_kernel(const NRCel
   const NRCell C = cells[c];
   NRGeom g;
   g.n = C.n;
+  g.L = C.depth;
   nr_counts(g.n, g.NEx, g.NFx, g.NE, g.NF);
   g.N = g.NE + g.NF;
   const int n = g.n, N = g.N;
