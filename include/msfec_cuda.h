@@ -187,9 +187,27 @@ typedef struct msfec_timings {
   float total_ms;    /* whole build on the device, H2D/D2H excluded */
   int32_t solve_launches;
   int32_t kernel_launches; /* kernels this build launched */
+  /* 0: launched directly; 1: captured into a new CUDA graph, then launched;
+     2: replayed the cached graph (solve_ms then covers the whole graph) */
+  int32_t graph;
 } msfec_timings;
 
 msfec_status msfec_set_timing(msfec_handle *handle, int32_t enable);
+
+/*
+ * CUDA-graph mode for repeated builds (default off). The refinement loop of
+ * every local solve runs inside the persistent kernel, so one build is a
+ * fixed sequence of device operations (queue reset, solver, Galerkin,
+ * report). With graph mode on, the first build of a batch captures that
+ * sequence into a CUDA graph; a later build of the same kind with the same
+ * cells, load, configuration, stream and buffer pointers skips the host
+ * planner and the plan upload and replays the graph, reading the current
+ * contents of the coefficient buffers (the case of an optimisation or
+ * adjoint loop that updates coefficients in place). Any other build of that
+ * kind re-captures. Results are those of the direct launches. Turning the
+ * mode off drops the cached graphs.
+ */
+msfec_status msfec_set_graph(msfec_handle *handle, int32_t enable);
 /* Synchronises the handle's stream. */
 msfec_status msfec_get_timings(msfec_handle *handle, msfec_timings *out);
 

@@ -85,6 +85,39 @@ struct DevBuf {
 constexpr int kCluster = 8;
 constexpr int kMaxDepth = 5;
 
+// Byte key of a build: every input that shapes the launch sequence and every
+// pointer the sequence reads or writes.
+struct BuildKey {
+  std::vector<unsigned char> bytes;
+  template <typename T>
+  void add(const T &v) {
+    add_raw(&v, sizeof(T));
+  }
+  void add_raw(const void *p, size_t n) {
+    const unsigned char *c = static_cast<const unsigned char *>(p);
+    bytes.insert(bytes.end(), c, c + n);
+  }
+};
+
+// The device-side launch sequence of the last build of one kind (queue reset,
+// persistent solver, Galerkin contraction, report), captured once as a CUDA
+// graph and replayed while the build key is unchanged: repeated builds of one
+// batch with new coefficient values (an optimisation or adjoint loop) skip the
+// host planner, the plan upload and per-kernel launch overhead.
+struct GraphCache {
+  BuildKey key;
+  cudaGraphExec_t exec = nullptr;
+  int launches = 0;
+  bool valid = false;
+  void reset() {
+    if (exec) cudaGraphExecDestroy(exec);
+    exec = nullptr;
+    key.bytes.clear();
+    launches = 0;
+    valid = false;
+  }
+};
+
 }  // namespace
 
 struct msfec_handle {
@@ -127,6 +160,11 @@ struct msfec_handle {
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   bool ev_recorded = false;
   int last_launches = 0;
+  // CUDA-graph replay of the launch sequence (msfec_set_graph)
+  bool graph_mode = false;
+  GraphCache q1_graph, nr_graph;
+  int64_t nr_graph_basis = 0;  // basis size of the Ned_RT build the graph holds
+  int last_graph = 0;  // 0 direct launches, 1 captured a new graph, 2 replayed
 };
 
 namespace {
@@ -157,6 +195,72 @@ struct DeviceGuard {
     if (prev >= 0) cudaSetDevice(prev);
   }
 };
+
+// Launches the instantiated graph of `gc` on the handle's stream; timing
+// events bracket the whole graph (solve_ms = total_ms, galerkin_ms = 0).
+msfec_status launch_graph(msfec_handle *h, GraphCache &gc) {
+  cudaStream_t st = h->stream;
+  cudaError_t e = cudaSuccess;
+  if (h->timing) e = cudaEventRecord(h->ev[0], st);
+  if (e == cudaSuccess) e = cudaGraphLaunch(gc.exec, st);
+  for (int i = 1; i < 4 && e == cudaSuccess && h->timing; ++i) e = cudaEventRecord(h->ev[i], st);
+  if (e != cudaSuccess) {
+    gc.reset();
+    return cuda_fail(h, e, "cudaGraphLaunch");
+  }
+  h->ev_recorded = h->timing;
+  h->last_launches = gc.launches;
+  return MSFEC_SUCCESS;
+}
+
+// Replays the cached graph of `gc` if graph mode is on and its key equals
+// `key`; returns true if it did (the outcome in *status).
+bool replay_graph(msfec_handle *h, GraphCache &gc, const BuildKey &key, msfec_status *status) {
+  if (!h->graph_mode || !gc.valid || gc.key.bytes != key.bytes) return false;
+  *status = launch_graph(h, gc);
+  if (*status == MSFEC_SUCCESS) h->last_graph = 2;
+  return true;
+}
+
+// Runs `seq(timed)` (the device launches of one build: no host
+// synchronisation, no allocation) directly, or in graph mode captures it into
+// `gc` and launches the graph. Only the non-replay path of a build reaches
+// this, and it always drops the previous graph of that kind: the plan buffers
+// the graph reads are rewritten (or reallocated) just before.
+template <typename Seq>
+msfec_status run_sequence(msfec_handle *h, GraphCache &gc, BuildKey &&key, int launches, Seq &&seq) {
+  gc.reset();
+  h->last_launches = launches;
+  if (!h->graph_mode) {
+    const cudaError_t e = seq(h->timing);
+    if (e != cudaSuccess) return cuda_fail(h, e, "build launch sequence");
+    h->ev_recorded = h->timing;
+    h->last_graph = 0;
+    return MSFEC_SUCCESS;
+  }
+  cudaStream_t st = h->stream;
+  cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed);
+  if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamBeginCapture");
+  const cudaError_t e1 = seq(false);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t e2 = cudaStreamEndCapture(st, &graph);
+  if (e1 != cudaSuccess || e2 != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    return cuda_fail(h, e1 != cudaSuccess ? e1 : e2, "graph capture of the build");
+  }
+  e = cudaGraphInstantiate(&gc.exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    gc.exec = nullptr;
+    return cuda_fail(h, e, "cudaGraphInstantiate");
+  }
+  gc.key = std::move(key);
+  gc.launches = launches;
+  gc.valid = true;
+  const msfec_status s = launch_graph(h, gc);
+  if (s == MSFEC_SUCCESS) h->last_graph = 1;
+  return s;
+}
 
 bool cell_ok(const msfec_cell &c) {
   if (c.depth < 1 || c.depth > kMaxDepth) return false;
@@ -258,11 +362,41 @@ Q1Plan make_q1_plan(int ncells, const msfec_cell *cells, bool fp64, bool has_r) 
   return p;
 }
 
+BuildKey build_key(const msfec_handle *h, int kind, int ncells, const msfec_cell *cells, const void *in0,
+                   const void *in1, const msfec_load *load, const void *out0, const void *out1, const void *out2) {
+  BuildKey k;
+  k.add(kind);
+  k.add(h->cfg.precision);
+  k.add(h->cfg.rtol);
+  k.add(h->cfg.inner_rtol);
+  k.add(h->cfg.max_iter);
+  k.add(h->cfg.max_refine);
+  k.add(h->cfg.nedrt_rtol);
+  k.add(h->stream);
+  k.add(ncells);
+  k.add_raw(cells, (size_t)ncells * sizeof(msfec_cell));
+  msfec_load ld{};
+  if (load) ld = *load;
+  k.add(ld);
+  k.add(in0);
+  k.add(in1);
+  k.add(out0);
+  k.add(out1);
+  k.add(out2);
+  return k;
+}
+
 msfec_status q1_build_impl(msfec_handle *h, int ncells, const msfec_cell *cells, const double *d_a,
                            const double *d_react, const msfec_load *load, double *d_KH, double *d_FH,
                            msfec_cell_report *d_rep) {
   const bool fp64 = h->cfg.precision == MSFEC_PRECISION_FP64;
   const bool has_r = d_react != nullptr;
+  BuildKey key;
+  if (h->graph_mode) {
+    key = build_key(h, 1, ncells, cells, d_a, d_react, load, d_KH, d_FH, d_rep);
+    msfec_status rs;
+    if (replay_graph(h, h->q1_graph, key, &rs)) return rs;
+  }
   Q1Plan plan = make_q1_plan(ncells, cells, fp64, has_r);
   if (plan.smem + 8192 > h->max_smem_optin)
     return fail(h, MSFEC_ERROR_NOT_SUPPORTED, "shared memory plan exceeds the device limit");
@@ -280,7 +414,6 @@ msfec_status q1_build_impl(msfec_handle *h, int ncells, const msfec_cell *cells,
                                     cudaMemcpyHostToDevice, st));
   MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->units.ptr, plan.units.data(), plan.units.size() * sizeof(Q1Unit),
                                     cudaMemcpyHostToDevice, st));
-  MSFEC_CUDA_TRY(h, cudaMemsetAsync(h->queue.ptr, 0, sizeof(int), st));
   Q1Params prm;
   prm.cells = h->cells.ptr;
   prm.items = h->items.ptr;
@@ -314,23 +447,25 @@ msfec_status q1_build_impl(msfec_handle *h, int ncells, const msfec_cell *cells,
             "[msfec] q1 plan: %d cells, %zu items, %zu units, cluster %d, smem %zu B, occupancy %d, grid %d, %s\n",
             ncells, plan.items.size(), plan.units.size(), plan.cluster, plan.smem, occ, grid,
             fp64 ? "fp64" : "mixed");
-  if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[0], st));
-  MSFEC_CUDA_TRY(h, q1_solve_launch(fp64, plan.cluster, has_r, prm, plan.smem, grid, st));
-  if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[1], st));
   msfec_load ld;
   if (load) {
     ld = *load;
   } else {
     std::memset(&ld, 0, sizeof(ld));
   }
-  MSFEC_CUDA_TRY(h, q1_galerkin_launch(h->cells.ptr, ncells, h->phi.ptr, h->y.ptr, ld, d_KH, d_FH, st));
-  if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[2], st));
-  if (d_rep) MSFEC_CUDA_TRY(h, q1_report_launch(h->stats.ptr, ncells, d_rep, st));
-  if (h->timing) {
-    MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[3], st));
-    h->ev_recorded = true;
-  }
-  h->last_launches = d_rep ? 3 : 2;
+  auto seq = [&](bool timed) -> cudaError_t {
+    cudaError_t e = cudaMemsetAsync(h->queue.ptr, 0, sizeof(int), st);
+    if (e == cudaSuccess && timed) e = cudaEventRecord(h->ev[0], st);
+    if (e == cudaSuccess) e = q1_solve_launch(fp64, plan.cluster, has_r, prm, plan.smem, grid, st);
+    if (e == cudaSuccess && timed) e = cudaEventRecord(h->ev[1], st);
+    if (e == cudaSuccess) e = q1_galerkin_launch(h->cells.ptr, ncells, h->phi.ptr, h->y.ptr, ld, d_KH, d_FH, st);
+    if (e == cudaSuccess && timed) e = cudaEventRecord(h->ev[2], st);
+    if (e == cudaSuccess && d_rep) e = q1_report_launch(h->stats.ptr, ncells, d_rep, st);
+    if (e == cudaSuccess && timed) e = cudaEventRecord(h->ev[3], st);
+    return e;
+  };
+  const msfec_status s = run_sequence(h, h->q1_graph, std::move(key), d_rep ? 3 : 2, seq);
+  if (s != MSFEC_SUCCESS) return s;
   h->q1_ncells = ncells;
   h->q1_basis_doubles = plan.nodes * 8;
   h->h_cells = plan.cells;
@@ -433,6 +568,7 @@ msfec_status q1_backward_impl(msfec_handle *h, int ncells, const msfec_cell *cel
     h->ev_recorded = true;
   }
   h->last_launches = 3;
+  h->last_graph = 0;
   return MSFEC_SUCCESS;
 }
 
@@ -443,6 +579,15 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
                               const double *d_bdiv, const msfec_load *load, double *d_KH, double *d_FH,
                               msfec_cell_report *d_rep) {
   const bool fp64 = h->cfg.precision == MSFEC_PRECISION_FP64;
+  BuildKey key;
+  if (h->graph_mode) {
+    key = build_key(h, 2, ncells, cells, d_ainv, d_bdiv, load, d_KH, d_FH, d_rep);
+    msfec_status rs;
+    if (replay_graph(h, h->nr_graph, key, &rs)) {
+      if (rs == MSFEC_SUCCESS) h->nr_basis_doubles = h->nr_graph_basis;
+      return rs;
+    }
+  }
   std::vector<NRCell> hc(ncells);
   int64_t fine = 0, dofs = 0;
   int nmax = 0;
@@ -486,7 +631,6 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
   MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->nr_cells.ptr, hc.data(), hc.size() * sizeof(NRCell), cudaMemcpyHostToDevice, st));
   MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->nr_items.ptr, items.data(), items.size() * sizeof(NRItem),
                                     cudaMemcpyHostToDevice, st));
-  MSFEC_CUDA_TRY(h, cudaMemsetAsync(h->queue.ptr, 0, sizeof(int), st));
   NRParams prm;
   prm.cells = h->nr_cells.ptr;
   prm.items = h->nr_items.ptr;
@@ -507,23 +651,27 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
   if (h->cfg.verbose)
     fprintf(stderr, "[msfec] nedrt plan: %d cells, %zu items, workspace %zu floats (%s), grid %d, %s\n", ncells,
             items.size(), ws_floats, use_smem ? "shared" : "global", grid, fp64 ? "fp64" : "mixed");
-  if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[0], st));
-  MSFEC_CUDA_TRY(h, nedrt_solve_launch(fp64, prm, smem, grid, st));
-  if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[1], st));
   msfec_load ld;
   if (load) {
     ld = *load;
   } else {
     std::memset(&ld, 0, sizeof(ld));
   }
-  MSFEC_CUDA_TRY(h, nedrt_galerkin_launch(h->nr_cells.ptr, ncells, h->nr_phi.ptr, h->nr_y.ptr, ld, d_KH, d_FH, d_rep,
-                                          h->nr_stats.ptr, st));
-  if (h->timing) {
-    MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[2], st));
-    MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[3], st));
-    h->ev_recorded = true;
-  }
-  h->last_launches = d_rep ? 3 : 2;
+  auto seq = [&](bool timed) -> cudaError_t {
+    cudaError_t e = cudaMemsetAsync(h->queue.ptr, 0, sizeof(int), st);
+    if (e == cudaSuccess && timed) e = cudaEventRecord(h->ev[0], st);
+    if (e == cudaSuccess) e = nedrt_solve_launch(fp64, prm, smem, grid, st);
+    if (e == cudaSuccess && timed) e = cudaEventRecord(h->ev[1], st);
+    if (e == cudaSuccess)
+      e = nedrt_galerkin_launch(h->nr_cells.ptr, ncells, h->nr_phi.ptr, h->nr_y.ptr, ld, d_KH, d_FH, d_rep,
+                                h->nr_stats.ptr, st);
+    if (e == cudaSuccess && timed) e = cudaEventRecord(h->ev[2], st);
+    if (e == cudaSuccess && timed) e = cudaEventRecord(h->ev[3], st);
+    return e;
+  };
+  const msfec_status s = run_sequence(h, h->nr_graph, std::move(key), d_rep ? 3 : 2, seq);
+  if (s != MSFEC_SUCCESS) return s;
+  h->nr_graph_basis = dofs * 18;
   h->nr_basis_doubles = dofs * 18;
   return MSFEC_SUCCESS;
 }
@@ -636,6 +784,8 @@ void msfec_destroy(msfec_handle *h) {
     h->nr_bdiv.release();
     h->nr_KH.release();
     h->nr_FH.release();
+    h->q1_graph.reset();
+    h->nr_graph.reset();
     for (auto &e : h->ev)
       if (e) cudaEventDestroy(e);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
@@ -729,11 +879,24 @@ msfec_status msfec_set_timing(msfec_handle *h, int32_t enable) {
   return MSFEC_SUCCESS;
 }
 
+msfec_status msfec_set_graph(msfec_handle *h, int32_t enable) {
+  if (!h) return MSFEC_ERROR_INVALID_ARGUMENT;
+  DeviceGuard g(h->device);
+  h->graph_mode = enable != 0;
+  if (!h->graph_mode) {
+    cudaStreamSynchronize(h->stream);
+    h->q1_graph.reset();
+    h->nr_graph.reset();
+  }
+  return MSFEC_SUCCESS;
+}
+
 msfec_status msfec_get_timings(msfec_handle *h, msfec_timings *out) {
   if (!h || !out) return MSFEC_ERROR_INVALID_ARGUMENT;
   out->solve_ms = out->galerkin_ms = out->total_ms = -1.0f;
   out->solve_launches = h->ev_recorded ? 1 : 0;
   out->kernel_launches = h->last_launches;
+  out->graph = h->last_graph;
   if (!h->ev_recorded) return MSFEC_SUCCESS;
   DeviceGuard g(h->device);
   MSFEC_CUDA_TRY(h, cudaEventSynchronize(h->ev[3]));
@@ -1161,6 +1324,7 @@ msfec_status msfec_nedrt_build_noalloc(msfec_handle *h, int32_t ncells, const ms
     h->ev_recorded = true;
   }
   h->last_launches = d_reports ? 4 : 3;
+  h->last_graph = 0;
   return MSFEC_SUCCESS;
 }
 

@@ -37,6 +37,7 @@ EXPORTED = [
     "msfec_q1_basis_device", "msfec_q1_eval_fine", "msfec_set_timing", "msfec_get_timings",
     "msfec_nedrt_build", "msfec_nedrt_build_device", "msfec_nedrt_basis_size",
     "msfec_nedrt_get_basis", "msfec_q1_backward", "msfec_nedrt_build_noalloc",
+    "msfec_set_graph",
 ]
 
 
@@ -66,7 +67,7 @@ class CellReport(ctypes.Structure):
 class Timings(ctypes.Structure):
     _fields_ = [("solve_ms", ctypes.c_float), ("galerkin_ms", ctypes.c_float),
                 ("total_ms", ctypes.c_float), ("solve_launches", ctypes.c_int32),
-                ("kernel_launches", ctypes.c_int32)]
+                ("kernel_launches", ctypes.c_int32), ("graph", ctypes.c_int32)]
 
 
 CELL_DTYPE = np.dtype([("origin", "<f8", (3,)), ("size", "<f8", (3,)), ("depth", "<i4"),
@@ -133,6 +134,8 @@ def load_library(path: str = LIB_PATH):
     L.msfec_set_timing.restype = ctypes.c_int
     L.msfec_get_timings.argtypes = [_vp, ctypes.POINTER(Timings)]
     L.msfec_get_timings.restype = ctypes.c_int
+    L.msfec_set_graph.argtypes = [_vp, ctypes.c_int32]
+    L.msfec_set_graph.restype = ctypes.c_int
     _lib = L
     return L
 
@@ -250,11 +253,16 @@ class Handle:
     def set_timing(self, enable=True):
         return self.check(self._lib.msfec_set_timing(self._h, 1 if enable else 0))
 
+    def set_graph(self, enable=True):
+        """msfec_set_graph: capture / replay the build's launch sequence as a CUDA graph."""
+        return self.check(self._lib.msfec_set_graph(self._h, 1 if enable else 0))
+
     def timings(self):
         t = Timings()
         self.check(self._lib.msfec_get_timings(self._h, ctypes.byref(t)))
         return {"solve_ms": t.solve_ms, "galerkin_ms": t.galerkin_ms, "total_ms": t.total_ms,
-                "solve_launches": t.solve_launches, "kernel_launches": t.kernel_launches}
+                "solve_launches": t.solve_launches, "kernel_launches": t.kernel_launches,
+                "graph": t.graph}
 
     def q1_backward(self, cells, a, reaction, load, U, lam, cell_of, points, dJ_du, reuse_basis=True):
         """dJ/d log a per fine cell (msfec_q1_backward)."""
