@@ -116,11 +116,8 @@ class Workload:
 
 
 def partition(wl, world, rank):
-    w = wl.per_cell_work().astype(np.float64)
-    cum = np.concatenate([[0.0], np.cumsum(w)])
-    b = [int(np.searchsorted(cum, cum[-1] * r / world, side="left")) for r in range(world + 1)]
-    b[0], b[-1] = 0, len(wl.cells)
-    return b[rank], b[rank + 1]
+    import sharding
+    return sharding.partition(wl.per_cell_work(), world, rank)
 
 
 # --------------------------------------------------------------------------- clocks
