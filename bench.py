@@ -240,8 +240,10 @@ def time_oracle(wl, sel, nthreads):
 
 
 # --------------------------------------------------------------------------- GPU
-def gpu_run(wl, lo, hi, precision, steps, warmup, local, stream, barrier):
-    """Device-resident builds; returns per-step ms, mean solve / Galerkin ms, launches, reports."""
+def gpu_run(wl, lo, hi, precision, steps, warmup, local, stream, barrier, tune_info=None):
+    """Device-resident builds; returns per-step ms, mean solve / Galerkin ms, launches, reports.
+    With tune_info (a dict), msfec_autotune first picks the launch shape on a sample of the
+    shard (untimed) and its outcome is stored there."""
     import torch
     import msfec
     sh = wl.shard(lo, hi)
@@ -268,6 +270,17 @@ def gpu_run(wl, lo, hi, precision, steps, warmup, local, stream, barrier):
         def step():
             h.q1_build_device(cells, d_x.data_ptr(), 0 if d_y is None else d_y.data_ptr(), wl.load,
                               d_KH.data_ptr(), d_FH.data_ptr(), d_rep.data_ptr())
+    if tune_info is not None and nc > 0:
+        import sharding
+        k = min(nc, 64 if wl.kind == "nedrt" else 512)  # several waves of items, seconds of trials
+        f = int(sharding.fine_offsets(cells)[k])
+        if wl.kind == "nedrt":
+            c0, c1, kind = sh["ainv6"][:f], sh["bdiv"][:f], msfec.KIND_NEDRT
+        else:
+            c0, c1, kind = sh["a"][:f], None if sh["r"] is None else sh["r"][:f], msfec.KIND_Q1
+        choice, ncand, times = h.autotune(kind, cells[:k], c0, c1, wl.load)
+        tune_info.update({"sample_cells": k, "candidates": ncand, "choice": choice,
+                          "times_ms": [round(t, 3) for t in times]})
     for _ in range(warmup):
         step()
     barrier()
@@ -428,21 +441,23 @@ def run_ours(args):
         sampler = ClockSampler(local)
         if with_clocks:
             sampler.start()
+        tune = {}
         ms, solve_ms, gal_ms, launches, rep = gpu_run(wl, lo, hi, msfec.PRECISION_MIXED, steps, warmup, local,
-                                                      stream, barrier)
+                                                      stream, barrier, tune_info=tune)
         clocks = sampler.stop() if with_clocks else None
         ms = reduce_max(ms)
         out = {"wl": wl, "lo": lo, "hi": hi, "value": total / (ms * 1e-3), "ms_per_step": ms, "clocks": clocks,
                "launches": launches, "converged": bool(rep["converged"].all()),
                "max_iterations": int(rep["iterations"].max()) if len(rep) else 0, "work_dof_rhs": total,
-               "roofline": roofline(wl, lo, hi, solve_ms, gal_ms, rep, wl.kind)}
+               "roofline": roofline(wl, lo, hi, solve_ms, gal_ms, rep, wl.kind), "autotune": tune}
         if fp64_steps > 0:
+            tune64 = {}
             ms64, s64, g64, _, rep64 = gpu_run(wl, lo, hi, msfec.PRECISION_FP64, fp64_steps, 1, local, stream,
-                                               barrier)
+                                               barrier, tune_info=tune64)
             ms64 = reduce_max(ms64)
             out["fp64_path"] = {"value": total / (ms64 * 1e-3), "ms_per_step": ms64, "solve_ms": s64,
                                 "steps": fp64_steps, "converged": bool(rep64["converged"].all()),
-                                "mixed_over_fp64": ms64 / ms}
+                                "mixed_over_fp64": ms64 / ms, "autotune": tune64}
         return out
 
     head = measure(args.workload, args.steps, args.warmup, 0 if args.skip_fp64 else max(1, min(args.steps, 2)),
@@ -455,7 +470,7 @@ def run_ours(args):
         for name in args.extra.split(","):
             ex = measure(name, max(3, min(args.steps, 5)), 3, 0 if args.skip_fp64 else 2, False)
             extras[name] = {k: ex[k] for k in ("value", "ms_per_step", "converged", "max_iterations",
-                                               "work_dof_rhs", "roofline", "fp64_path") if k in ex}
+                                               "work_dof_rhs", "roofline", "fp64_path", "autotune") if k in ex}
             extras[name]["config"] = ex["wl"].cfg
     if not args.skip_extra and not args.skip_adjoint:
         extras["adjoint_q1"] = adjoint_timing(local, stream)
@@ -481,7 +496,7 @@ def run_ours(args):
             "gpu_launches": int(head["launches"]), "clocks": head["clocks"],
             "fp64_path": head.get("fp64_path"), "converged": head["converged"],
             "max_iterations": head["max_iterations"], "work_dof_rhs": head["work_dof_rhs"],
-            "extra": extras}
+            "autotune": head.get("autotune"), "extra": extras}
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

@@ -88,7 +88,10 @@ typedef struct msfec_config {
   int32_t max_iter;    /* Krylov iterations per inner solve */
   int32_t max_refine;  /* MIXED: FP64 refinement steps; FP64: verification rounds */
   int32_t verbose;
-  int32_t reserved;
+  /* Q1 launch shape when a batch mixes cluster (z-slab) and independent
+     items: 0 = autotuned (msfec_autotune) or else one fused launch,
+     1 = one fused launch, 2 = split cluster / non-cluster launches. */
+  int32_t q1_launch;
   /* Ned_RT local solves stop when ||r||_2 <= nedrt_rtol * ||f_I - A_IB g||_2.
      The mixed local system has condition number ~1e4 at depth 3, so 1e-14
      is needed for a 1e-10 basis error. */
@@ -299,6 +302,32 @@ msfec_status msfec_nedrt_build_noalloc(msfec_handle *handle, int32_t ncells,
                                        const msfec_load *load, double *d_KH,
                                        double *d_FH,
                                        msfec_cell_report *d_reports);
+
+/* Problem kinds (msfec_autotune). */
+typedef enum msfec_kind { MSFEC_KIND_Q1 = 1, MSFEC_KIND_NEDRT = 2 } msfec_kind;
+
+/*
+ * Autotuner for launch shapes. Builds the given batch (host buffers, as
+ * msfec_q1_build / msfec_nedrt_build: coef0 = a or ainv6, coef1 = reaction
+ * (may be NULL) or bdiv) twice per candidate in the handle's precision,
+ * times the second build on the device, and keeps the fastest candidate for
+ * later builds of that kind on this handle. Pass a representative sample
+ * (e.g. one or two GPU waves of cells); the call costs 2 builds per
+ * candidate. choice[0] = index of the chosen candidate, choice[1] = number of
+ * candidates; times_ms (NULL or >= 8 floats) receives each candidate's time.
+ *   Q1 (per precision and reaction on/off), when the batch mixes cluster
+ *     (z-slab) items with independent ones: 0 = one launch of the cluster
+ *     kernel over all items, 1 = the cluster kernel over the slab items and
+ *     a non-cluster kernel over the rest, concurrently on two streams.
+ *   Ned_RT (per precision and deepest depth), when the MINRES workspace is
+ *     in global memory (depth 4, or FP64): the number of resident CTAs, i.e.
+ *     of workspace slots in L2: the SM count times 1, 7/8, 6/8, 5/8, 4/8.
+ * Batches with a single candidate return at once (choice = {0, 1}).
+ */
+msfec_status msfec_autotune(msfec_handle *handle, int32_t kind, int32_t ncells,
+                            const msfec_cell *cells, const double *coef0,
+                            const double *coef1, const msfec_load *load,
+                            int32_t *choice, float *times_ms);
 
 /* Basis of the last Ned_RT build: per cell 18 rows (coarse basis order) of
    NE + NF fine DoFs (edges x|y|z then faces x|y|z, lexicographic), sigma and u

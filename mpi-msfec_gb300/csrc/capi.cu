@@ -84,6 +84,7 @@ struct DevBuf {
 
 constexpr int kCluster = 8;
 constexpr int kMaxDepth = 5;
+constexpr int kNRMaxDepthCfg = 4;
 
 // Byte key of a build: every input that shapes the launch sequence and every
 // pointer the sequence reads or writes.
@@ -132,7 +133,7 @@ struct msfec_handle {
   DevBuf<Q1Cell> cells;
   DevBuf<Q1Item> items;
   DevBuf<Q1Unit> units;
-  DevBuf<int> queue;
+  DevBuf<int> queue;  // two work-queue counters; never regrown (captured graphs hold its address)
   DevBuf<double> phi, y;
   DevBuf<Q1Stat> stats;
   // host-API staging
@@ -164,6 +165,12 @@ struct msfec_handle {
   bool graph_mode = false;
   GraphCache q1_graph, nr_graph;
   int64_t nr_graph_basis = 0;  // basis size of the Ned_RT build the graph holds
+  // launch shapes picked by msfec_autotune ([precision][...]; -1 / 0 = default)
+  int q1_split[2][2] = {{-1, -1}, {-1, -1}};  // [precision][has reaction]: 1 = split launches
+  int nr_ctas[2][kNRMaxDepthCfg + 1] = {};    // [precision][deepest depth]: resident CTAs
+  int force_split = -1, force_ctas = 0;       // candidate under trial
+  cudaStream_t aux_stream = nullptr;          // second stream of the split Q1 launch
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int last_graph = 0;  // 0 direct launches, 1 captured a new graph, 2 replayed
 };
 
@@ -284,6 +291,11 @@ struct Q1Plan {
   std::vector<Q1Unit> units;
   int cluster = 1;
   size_t smem = 0;
+  // split: slab units (units[0, n_slab_units)) run in the cluster kernel,
+  // the independent single-item units after them in a non-cluster kernel
+  bool split = false;
+  int n_slab_units = 0;
+  size_t smem_slab = 0, smem_indep = 0;
   int64_t nodes = 0;   // sum (n+1)^3
   int64_t fine = 0;    // sum n^3
 };
@@ -308,7 +320,7 @@ void plan_items(int depth, bool fp64, int &nitems, int &nrhs, bool &slab) {
   }
 }
 
-Q1Plan make_q1_plan(int ncells, const msfec_cell *cells, bool fp64, bool has_r) {
+Q1Plan make_q1_plan(int ncells, const msfec_cell *cells, bool fp64, bool has_r, bool split = false) {
   Q1Plan p;
   p.cells.resize(ncells);
   for (int c = 0; c < ncells; ++c) {
@@ -338,18 +350,24 @@ Q1Plan make_q1_plan(int ncells, const msfec_cell *cells, bool fp64, bool has_r) 
     for (int t = 0; t < ni; ++t) p.items.push_back(Q1Item{c, t * nr, nr, slab ? 1 : 0, 0, 0});
   }
   p.cluster = any_slab ? kCluster : 1;
-  // units: slab items alone; independent items grouped by `cluster` (same depth)
+  bool any_indep = false;
+  for (const Q1Item &it : p.items) any_indep = any_indep || !it.slab;
+  p.split = split && any_slab && any_indep;
+  // units: slab items alone; independent items grouped by `cluster` (same
+  // depth), or one per unit for the non-cluster kernel of a split launch.
+  // Slab items come first (deepest first), so slab units precede the rest.
+  const int group = p.split ? 1 : p.cluster;
   size_t i = 0;
   while (i < p.items.size()) {
     if (p.items[i].slab) {
       p.units.push_back(Q1Unit{(int)i, 1, 1, 0});
+      ++p.n_slab_units;
       ++i;
       continue;
     }
     const int depth = cells[p.items[i].cell].depth;
     size_t j = i;
-    while (j < p.items.size() && (int)(j - i) < p.cluster && !p.items[j].slab &&
-           cells[p.items[j].cell].depth == depth)
+    while (j < p.items.size() && (int)(j - i) < group && !p.items[j].slab && cells[p.items[j].cell].depth == depth)
       ++j;
     p.units.push_back(Q1Unit{(int)i, (int)(j - i), 0, 0});
     i = j;
@@ -358,6 +376,10 @@ Q1Plan make_q1_plan(int ncells, const msfec_cell *cells, bool fp64, bool has_r) 
     const int n = 1 << cells[it.cell].depth;
     const Q1Smem L = q1_smem_layout(n, it.nrhs, it.slab ? p.cluster : 1, has_r, fp64 ? 8 : 4);
     p.smem = std::max(p.smem, L.total);
+    if (it.slab)
+      p.smem_slab = std::max(p.smem_slab, L.total);
+    else
+      p.smem_indep = std::max(p.smem_indep, L.total);
   }
   return p;
 }
@@ -397,14 +419,23 @@ msfec_status q1_build_impl(msfec_handle *h, int ncells, const msfec_cell *cells,
     msfec_status rs;
     if (replay_graph(h, h->q1_graph, key, &rs)) return rs;
   }
-  Q1Plan plan = make_q1_plan(ncells, cells, fp64, has_r);
+  int tuned_split = h->q1_split[fp64 ? 0 : 1][has_r ? 1 : 0];
+  if (h->cfg.q1_launch == 1) tuned_split = 0;
+  if (h->cfg.q1_launch == 2) tuned_split = 1;
+  if (h->force_split >= 0) tuned_split = h->force_split;
+  Q1Plan plan = make_q1_plan(ncells, cells, fp64, has_r, tuned_split == 1);
   if (plan.smem + 8192 > h->max_smem_optin)
     return fail(h, MSFEC_ERROR_NOT_SUPPORTED, "shared memory plan exceeds the device limit");
   cudaStream_t st = h->stream;
+  if (plan.split && !h->aux_stream) {
+    MSFEC_CUDA_TRY(h, cudaStreamCreateWithFlags(&h->aux_stream, cudaStreamNonBlocking));
+    MSFEC_CUDA_TRY(h, cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
+    MSFEC_CUDA_TRY(h, cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
+  }
   MSFEC_CUDA_TRY(h, h->cells.reserve(plan.cells.size()));
   MSFEC_CUDA_TRY(h, h->items.reserve(plan.items.size()));
   MSFEC_CUDA_TRY(h, h->units.reserve(plan.units.size()));
-  MSFEC_CUDA_TRY(h, h->queue.reserve(1));
+  MSFEC_CUDA_TRY(h, h->queue.reserve(2));
   MSFEC_CUDA_TRY(h, h->phi.reserve((size_t)plan.nodes * 8));
   MSFEC_CUDA_TRY(h, h->y.reserve((size_t)plan.nodes * 8));
   MSFEC_CUDA_TRY(h, h->stats.reserve((size_t)ncells * 8));
@@ -431,22 +462,43 @@ msfec_status q1_build_impl(msfec_handle *h, int ncells, const msfec_cell *cells,
   prm.inner_rtol = h->cfg.inner_rtol;
   prm.max_iter = h->cfg.max_iter;
   prm.max_refine = h->cfg.max_refine;
+  // fused: one launch over every unit; split: the cluster kernel over the
+  // slab units on the handle's stream and the non-cluster kernel over the
+  // rest on a second stream, concurrently (the cluster launch leaves SMs
+  // that cannot host a whole 8-CTA cluster idle; the second kernel uses them).
+  Q1Params prm_b = prm;
+  size_t smem_a = plan.smem;
+  int cluster_a = plan.cluster;
+  if (plan.split) {
+    prm.n_units = plan.n_slab_units;
+    prm_b.units = h->units.ptr + plan.n_slab_units;
+    prm_b.n_units = (int)plan.units.size() - plan.n_slab_units;
+    prm_b.queue = h->queue.ptr + 1;
+    smem_a = plan.smem_slab;
+  }
   int occ = 0;
-  MSFEC_CUDA_TRY(h, q1_solve_occupancy(fp64, plan.cluster, has_r, plan.smem, &occ));
+  MSFEC_CUDA_TRY(h, q1_solve_occupancy(fp64, cluster_a, has_r, smem_a, &occ));
   if (occ <= 0) return fail(h, MSFEC_ERROR_NOT_SUPPORTED, "local solver kernel cannot be resident");
   int grid;
-  if (plan.cluster > 1) {
-    const int nclusters = std::min<int>((int)plan.units.size(), occ);
-    grid = nclusters * plan.cluster;
+  if (cluster_a > 1) {
+    const int nclusters = std::min<int>(prm.n_units, occ);
+    grid = nclusters * cluster_a;
   } else {
-    grid = std::min<int>((int)plan.units.size(), occ * h->num_sms);
+    grid = std::min<int>(prm.n_units, occ * h->num_sms);
   }
-  grid = std::max(grid, plan.cluster);
+  grid = std::max(grid, cluster_a);
+  int grid_b = 0;
+  if (plan.split) {
+    int occ_b = 0;
+    MSFEC_CUDA_TRY(h, q1_solve_occupancy(fp64, 1, has_r, plan.smem_indep, &occ_b));
+    if (occ_b <= 0) return fail(h, MSFEC_ERROR_NOT_SUPPORTED, "local solver kernel cannot be resident");
+    grid_b = std::max(1, std::min<int>(prm_b.n_units, occ_b * h->num_sms));
+  }
   if (h->cfg.verbose)
     fprintf(stderr,
-            "[msfec] q1 plan: %d cells, %zu items, %zu units, cluster %d, smem %zu B, occupancy %d, grid %d, %s\n",
-            ncells, plan.items.size(), plan.units.size(), plan.cluster, plan.smem, occ, grid,
-            fp64 ? "fp64" : "mixed");
+            "[msfec] q1 plan: %d cells, %zu items, %zu units, cluster %d, smem %zu B, occupancy %d, grid %d%s, %s\n",
+            ncells, plan.items.size(), plan.units.size(), cluster_a, smem_a, occ, grid,
+            plan.split ? " + split non-cluster launch" : "", fp64 ? "fp64" : "mixed");
   msfec_load ld;
   if (load) {
     ld = *load;
@@ -454,9 +506,18 @@ msfec_status q1_build_impl(msfec_handle *h, int ncells, const msfec_cell *cells,
     std::memset(&ld, 0, sizeof(ld));
   }
   auto seq = [&](bool timed) -> cudaError_t {
-    cudaError_t e = cudaMemsetAsync(h->queue.ptr, 0, sizeof(int), st);
+    cudaError_t e = cudaMemsetAsync(h->queue.ptr, 0, 2 * sizeof(int), st);
     if (e == cudaSuccess && timed) e = cudaEventRecord(h->ev[0], st);
-    if (e == cudaSuccess) e = q1_solve_launch(fp64, plan.cluster, has_r, prm, plan.smem, grid, st);
+    if (plan.split) {
+      if (e == cudaSuccess) e = cudaEventRecord(h->ev_fork, st);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(h->aux_stream, h->ev_fork, 0);
+      if (e == cudaSuccess) e = q1_solve_launch(fp64, cluster_a, has_r, prm, smem_a, grid, st);
+      if (e == cudaSuccess) e = q1_solve_launch(fp64, 1, has_r, prm_b, plan.smem_indep, grid_b, h->aux_stream);
+      if (e == cudaSuccess) e = cudaEventRecord(h->ev_join, h->aux_stream);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(st, h->ev_join, 0);
+    } else if (e == cudaSuccess) {
+      e = q1_solve_launch(fp64, cluster_a, has_r, prm, smem_a, grid, st);
+    }
     if (e == cudaSuccess && timed) e = cudaEventRecord(h->ev[1], st);
     if (e == cudaSuccess) e = q1_galerkin_launch(h->cells.ptr, ncells, h->phi.ptr, h->y.ptr, ld, d_KH, d_FH, st);
     if (e == cudaSuccess && timed) e = cudaEventRecord(h->ev[2], st);
@@ -464,7 +525,7 @@ msfec_status q1_build_impl(msfec_handle *h, int ncells, const msfec_cell *cells,
     if (e == cudaSuccess && timed) e = cudaEventRecord(h->ev[3], st);
     return e;
   };
-  const msfec_status s = run_sequence(h, h->q1_graph, std::move(key), d_rep ? 3 : 2, seq);
+  const msfec_status s = run_sequence(h, h->q1_graph, std::move(key), (d_rep ? 3 : 2) + (plan.split ? 1 : 0), seq);
   if (s != MSFEC_SUCCESS) return s;
   h->q1_ncells = ncells;
   h->q1_basis_doubles = plan.nodes * 8;
@@ -620,10 +681,16 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
   const bool use_smem = ws_floats * 4 <= kNRSmemLimit;
   const size_t smem = use_smem ? ws_floats * 4 : 0;
   cudaStream_t st = h->stream;
-  const int grid = std::min<int>((int)items.size(), h->num_sms);
+  int grid = std::min<int>((int)items.size(), h->num_sms);
+  if (!use_smem) {  // resident CTAs = workspace slots (L2 footprint), possibly autotuned
+    int deepest = 0;
+    while ((1 << deepest) < nmax) ++deepest;
+    const int cap = h->force_ctas > 0 ? h->force_ctas : h->nr_ctas[fp64 ? 0 : 1][std::min(deepest, kNRMaxDepthCfg)];
+    if (cap > 0) grid = std::min(grid, cap);
+  }
   MSFEC_CUDA_TRY(h, h->nr_cells.reserve(ncells));
   MSFEC_CUDA_TRY(h, h->nr_items.reserve(items.size()));
-  MSFEC_CUDA_TRY(h, h->queue.reserve(1));
+  MSFEC_CUDA_TRY(h, h->queue.reserve(2));
   MSFEC_CUDA_TRY(h, h->nr_phi.reserve((size_t)dofs * 18));
   MSFEC_CUDA_TRY(h, h->nr_y.reserve((size_t)dofs * 18));
   MSFEC_CUDA_TRY(h, h->nr_stats.reserve((size_t)ncells * 18));
@@ -723,7 +790,7 @@ msfec_status msfec_create(msfec_handle **out, const msfec_config *cfg) {
     msfec_config_default(&c);
   if (c.precision != MSFEC_PRECISION_FP64 && c.precision != MSFEC_PRECISION_MIXED) return MSFEC_ERROR_INVALID_ARGUMENT;
   if (!(c.rtol > 0.0) || !(c.inner_rtol > 0.0) || c.inner_rtol >= 1.0 || c.max_iter < 1 || c.max_refine < 1 ||
-      !(c.nedrt_rtol > 0.0))
+      !(c.nedrt_rtol > 0.0) || c.q1_launch < 0 || c.q1_launch > 2)
     return MSFEC_ERROR_INVALID_ARGUMENT;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || c.device < 0 || c.device >= ndev) return MSFEC_ERROR_CUDA;
@@ -786,6 +853,10 @@ void msfec_destroy(msfec_handle *h) {
     h->nr_FH.release();
     h->q1_graph.reset();
     h->nr_graph.reset();
+    if (h->aux_stream) cudaStreamSynchronize(h->aux_stream);
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->ev_join) cudaEventDestroy(h->ev_join);
+    if (h->aux_stream) cudaStreamDestroy(h->aux_stream);
     for (auto &e : h->ev)
       if (e) cudaEventDestroy(e);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
@@ -1080,6 +1151,71 @@ msfec_status msfec_nedrt_build(msfec_handle *h, int32_t ncells, const msfec_cell
   if (reports) std::memcpy(reports, rep.data(), rep.size() * sizeof(msfec_cell_report));
   for (const auto &r : rep)
     if (!r.converged) return fail(h, MSFEC_ERROR_NOT_CONVERGED, "at least one Ned_RT local solve missed nedrt_rtol");
+  return MSFEC_SUCCESS;
+}
+
+msfec_status msfec_autotune(msfec_handle *h, int32_t kind, int32_t ncells, const msfec_cell *cells,
+                            const double *coef0, const double *coef1, const msfec_load *load, int32_t *choice,
+                            float *times_ms) {
+  if (!h) return MSFEC_ERROR_INVALID_ARGUMENT;
+  if ((kind != MSFEC_KIND_Q1 && kind != MSFEC_KIND_NEDRT) || ncells <= 0 || !cells || !coef0 ||
+      (kind == MSFEC_KIND_NEDRT && !coef1) || !choice)
+    return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "msfec_autotune: invalid kind, batch or output");
+  const bool fp64 = h->cfg.precision == MSFEC_PRECISION_FP64;
+  int deepest = 0;
+  for (int c = 0; c < ncells; ++c) deepest = std::max(deepest, (int)cells[c].depth);
+  // candidates
+  std::vector<int> cand;
+  if (kind == MSFEC_KIND_Q1) {
+    const Q1Plan p = make_q1_plan(ncells, cells, fp64, coef1 != nullptr, true);
+    cand = p.split ? std::vector<int>{0, 1} : std::vector<int>{0};
+  } else {
+    const int nmax = 1 << std::min(deepest, kNRMaxDepthCfg);
+    const bool smem_ws = nr_workspace_floats(nmax, fp64 ? 8 : 4) * 4 <= kNRSmemLimit;
+    cand.push_back(h->num_sms);
+    if (!smem_ws)
+      for (int k : {7, 6, 5, 4}) cand.push_back(std::max(1, h->num_sms * k / 8));
+  }
+  choice[0] = 0;
+  choice[1] = (int32_t)cand.size();
+  if (cand.size() == 1) return MSFEC_SUCCESS;
+  const bool timing0 = h->timing, graph0 = h->graph_mode;
+  msfec_status s = msfec_set_timing(h, 1);
+  if (s != MSFEC_SUCCESS) return s;
+  h->graph_mode = false;
+  std::vector<double> KH((size_t)ncells * 324), FH((size_t)ncells * 18);
+  float best = 0.0f;
+  for (size_t k = 0; k < cand.size() && s == MSFEC_SUCCESS; ++k) {
+    if (kind == MSFEC_KIND_Q1)
+      h->force_split = cand[k];
+    else
+      h->force_ctas = cand[k];
+    msfec_timings t{};
+    for (int rep = 0; rep < 2 && s == MSFEC_SUCCESS; ++rep) {  // second run timed (first warms)
+      s = kind == MSFEC_KIND_Q1
+              ? msfec_q1_build(h, ncells, cells, coef0, coef1, load, KH.data(), FH.data(), nullptr)
+              : msfec_nedrt_build(h, ncells, cells, coef0, coef1, load, KH.data(), FH.data(), nullptr);
+      if (s == MSFEC_SUCCESS) s = msfec_get_timings(h, &t);
+    }
+    if (s != MSFEC_SUCCESS) break;
+    if (times_ms) times_ms[k] = t.total_ms;
+    if (k == 0 || t.total_ms < best) {
+      best = t.total_ms;
+      choice[0] = (int32_t)k;
+    }
+  }
+  h->force_split = -1;
+  h->force_ctas = 0;
+  h->graph_mode = graph0;
+  msfec_set_timing(h, timing0 ? 1 : 0);
+  if (s != MSFEC_SUCCESS) return s;
+  if (kind == MSFEC_KIND_Q1)
+    h->q1_split[fp64 ? 0 : 1][coef1 ? 1 : 0] = cand[choice[0]];
+  else
+    h->nr_ctas[fp64 ? 0 : 1][std::min(deepest, kNRMaxDepthCfg)] = cand[choice[0]] == h->num_sms ? 0 : cand[choice[0]];
+  if (h->cfg.verbose)
+    fprintf(stderr, "[msfec] autotune kind %d depth %d %s: candidate %d of %zu\n", kind, deepest,
+            fp64 ? "fp64" : "mixed", choice[0], cand.size());
   return MSFEC_SUCCESS;
 }
 

@@ -23,6 +23,7 @@ ERROR_NOT_CONVERGED = 4
 ERROR_NOT_SUPPORTED = 5
 ERROR_NUMERICAL = 6
 ERROR_INVALID_STATE = 7
+KIND_Q1, KIND_NEDRT = 1, 2
 
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
@@ -37,7 +38,7 @@ EXPORTED = [
     "msfec_q1_basis_device", "msfec_q1_eval_fine", "msfec_set_timing", "msfec_get_timings",
     "msfec_nedrt_build", "msfec_nedrt_build_device", "msfec_nedrt_basis_size",
     "msfec_nedrt_get_basis", "msfec_q1_backward", "msfec_nedrt_build_noalloc",
-    "msfec_set_graph",
+    "msfec_set_graph", "msfec_autotune",
 ]
 
 
@@ -45,7 +46,7 @@ class Config(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("precision", ctypes.c_int32), ("rtol", ctypes.c_double),
                 ("inner_rtol", ctypes.c_double), ("max_iter", ctypes.c_int32),
                 ("max_refine", ctypes.c_int32), ("verbose", ctypes.c_int32),
-                ("reserved", ctypes.c_int32), ("nedrt_rtol", ctypes.c_double)]
+                ("q1_launch", ctypes.c_int32), ("nedrt_rtol", ctypes.c_double)]
 
 
 class Cell(ctypes.Structure):
@@ -134,6 +135,9 @@ def load_library(path: str = LIB_PATH):
     L.msfec_set_timing.restype = ctypes.c_int
     L.msfec_get_timings.argtypes = [_vp, ctypes.POINTER(Timings)]
     L.msfec_get_timings.restype = ctypes.c_int
+    L.msfec_autotune.argtypes = [_vp, ctypes.c_int32, ctypes.c_int32, _vp, _vp, _vp, ctypes.POINTER(Load),
+                                 ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_float)]
+    L.msfec_autotune.restype = ctypes.c_int
     L.msfec_set_graph.argtypes = [_vp, ctypes.c_int32]
     L.msfec_set_graph.restype = ctypes.c_int
     _lib = L
@@ -173,7 +177,7 @@ class Handle:
     """One msfec handle (device buffers + stream)."""
 
     def __init__(self, precision=PRECISION_MIXED, device=0, rtol=None, inner_rtol=None,
-                 max_iter=None, max_refine=None, verbose=0, nedrt_rtol=None):
+                 max_iter=None, max_refine=None, verbose=0, nedrt_rtol=None, q1_launch=0):
         L = load_library()
         cfg = Config()
         L.msfec_config_default(ctypes.byref(cfg))
@@ -190,6 +194,7 @@ class Handle:
         if nedrt_rtol is not None:
             cfg.nedrt_rtol = nedrt_rtol
         cfg.verbose = int(verbose or os.environ.get("MSFEC_VERBOSE", "0"))
+        cfg.q1_launch = int(q1_launch)
         self.cfg = cfg
         h = _vp()
         st = L.msfec_create(ctypes.byref(h), ctypes.byref(cfg))
@@ -252,6 +257,19 @@ class Handle:
 
     def set_timing(self, enable=True):
         return self.check(self._lib.msfec_set_timing(self._h, 1 if enable else 0))
+
+    def autotune(self, kind, cells, coef0, coef1, load):
+        """msfec_autotune on a sample batch; returns (choice, n_candidates, times_ms)."""
+        cells = np.ascontiguousarray(cells, dtype=CELL_DTYPE)
+        c0 = np.ascontiguousarray(coef0, dtype=np.float64)
+        c1 = None if coef1 is None else np.ascontiguousarray(coef1, dtype=np.float64)
+        ch = (ctypes.c_int32 * 2)()
+        tm = (ctypes.c_float * 8)()
+        st = self._lib.msfec_autotune(self._h, int(kind), cells.shape[0], cells.ctypes.data_as(_vp),
+                                      c0.ctypes.data_as(_vp), None if c1 is None else c1.ctypes.data_as(_vp),
+                                      ctypes.byref(load), ch, tm)
+        self.check(st)
+        return int(ch[0]), int(ch[1]), [float(tm[k]) for k in range(int(ch[1]))]
 
     def set_graph(self, enable=True):
         """msfec_set_graph: capture / replay the build's launch sequence as a CUDA graph."""

@@ -1,0 +1,64 @@
+"""Launch-shape autotuner (msfec_autotune) and the split Q1 launch.
+
+The split launch (cluster kernel for z-slab items, non-cluster kernel for the
+rest, concurrently on two streams) runs the same per-item solver, so its K_H,
+F_H and reports equal the fused launch bit for bit (the Q1 solver is
+deterministic). The autotuner must return a valid candidate with positive
+times, and builds after tuning must equal the defaults (Q1 bit for bit,
+Ned_RT within 1e-11 relative: shared-memory atomics).
+"""
+import numpy as np
+import pytest
+
+import workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_q1_split_launch_equals_fused(gpu, precision):
+    prec = gpu.PRECISION_MIXED if precision == "mixed" else gpu.PRECISION_FP64
+    cells, a, r, load = workloads.q1_uneven(m=3, seed=4)
+    assert set(np.unique(cells["depth"])) >= {4, 5}
+    out = {}
+    for launch in (1, 2):
+        h = gpu.Handle(precision=prec, q1_launch=launch)
+        KH, FH, rep, st = h.q1_build(cells, a, None, load)
+        assert st == gpu.SUCCESS and rep["converged"].all()
+        out[launch] = (KH, FH, rep)
+        assert h.timings()["kernel_launches"] == (3 if launch == 1 else 4)
+    assert np.array_equal(out[1][0], out[2][0]) and np.array_equal(out[1][1], out[2][1])
+    assert np.array_equal(out[1][2]["iterations"], out[2][2]["iterations"])
+
+
+def test_q1_autotune_then_build(gpu):
+    cells, a, _, load = workloads.q1_uneven(m=3, seed=4)
+    h = gpu.Handle()
+    choice, ncand, times = h.autotune(gpu.KIND_Q1, cells, a, None, load)
+    assert ncand == 2 and choice in (0, 1) and all(t > 0 for t in times), (choice, times)
+    print(f"q1 autotune: fused {times[0]:.2f} ms, split {times[1]:.2f} ms -> {['fused', 'split'][choice]}")
+    KH, FH, rep, st = h.q1_build(cells, a, None, load)
+    KH0, FH0, _, _ = gpu.Handle(q1_launch=1).q1_build(cells, a, None, load)
+    assert np.array_equal(KH, KH0) and np.array_equal(FH, FH0)
+    assert h.timings()["kernel_launches"] == (4 if choice == 1 else 3)
+
+
+def test_nedrt_autotune_global_workspace(gpu):
+    # FP64 depth 3: the workspace lives in global memory, so CTA counts are tuned
+    cells, ainv6, bdiv, load = workloads.nedrt_tensor(m=2, depth=3, seed=2)
+    h = gpu.Handle(precision=gpu.PRECISION_FP64)
+    choice, ncand, times = h.autotune(gpu.KIND_NEDRT, cells, ainv6, bdiv, load)
+    assert ncand == 5 and 0 <= choice < 5 and all(t > 0 for t in times), (choice, times)
+    print("nedrt autotune (fp64, depth 3):", [f"{t:.1f}" for t in times], "->", choice)
+    KH, FH, rep, st = h.nedrt_build(cells, ainv6, bdiv, load)
+    assert st == gpu.SUCCESS and rep["converged"].all()
+    KH0, _, _, _ = gpu.Handle(precision=gpu.PRECISION_FP64).nedrt_build(cells, ainv6, bdiv, load)
+    for c in range(len(cells)):
+        assert _rel(KH[c], KH0[c]) <= 1e-11
+    # shared-memory workspace (mixed, depth 3): a single candidate, no trial builds
+    h2 = gpu.Handle()
+    assert h2.autotune(gpu.KIND_NEDRT, cells, ainv6, bdiv, load)[:2] == (0, 1)
