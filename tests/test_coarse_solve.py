@@ -1,9 +1,10 @@
-"""CPU checks of the host-side coarse Q1 assembly/solve (consumer of K_H, F_H)
-and of the C++ shim library build."""
+"""CPU checks of the host-side coarse Q1 and Ned_RT assembly/solve (consumers
+of K_H, F_H) and of the C++ shim library build."""
 import ctypes
 import os
 
 import numpy as np
+import pytest
 import scipy.sparse as sp
 import scipy.sparse.linalg as spla
 
@@ -20,6 +21,8 @@ def host_lib():
     L.msfec_host_q1_coarse_solve.argtypes = [ctypes.c_int, dp, dp, dp, ctypes.c_double, ctypes.c_int,
                                              ctypes.POINTER(ctypes.c_int)]
     L.msfec_host_q1_coarse_solve.restype = ctypes.c_int
+    L.msfec_host_nedrt_coarse_solve.argtypes = L.msfec_host_q1_coarse_solve.argtypes
+    L.msfec_host_nedrt_coarse_solve.restype = ctypes.c_int
     return L
 
 
@@ -70,4 +73,47 @@ def test_shim_library_and_example_build():
     msfec_build.build()
     assert os.path.exists(msfec_build.HOSTLIB) and os.path.exists(msfec_build.EXAMPLE)
     L = ctypes.CDLL(msfec_build.HOSTLIB)
-    assert hasattr(L, "msfec_host_q1_coarse_solve")
+    assert hasattr(L, "msfec_host_q1_coarse_solve") and hasattr(L, "msfec_host_nedrt_coarse_solve")
+
+
+def nedrt_coarse_solve(m, KH, FH, rtol=1e-13):
+    L = host_lib()
+    from oracle import nedrt_oracle as N
+    NE, NF = N.counts(m)
+    U = np.zeros(NE + NF)
+    it = ctypes.c_int(0)
+    dp = ctypes.POINTER(ctypes.c_double)
+    KH = np.ascontiguousarray(KH, dtype=np.float64)
+    FH = np.ascontiguousarray(FH, dtype=np.float64)
+    st = L.msfec_host_nedrt_coarse_solve(m, KH.ctypes.data_as(dp), FH.ctypes.data_as(dp), U.ctypes.data_as(dp),
+                                         rtol, 50000, ctypes.byref(it))
+    assert st == 0, (st, it.value)
+    return U
+
+
+def scipy_nedrt_coarse(m, KH, FH):
+    """Independent assembly (global maps of the oracle) and sparse direct solve."""
+    from oracle import nedrt_adjoint as NA
+    g, bnd = NA.coarse_maps(m)
+    n = bnd.size
+    K = sp.coo_matrix((np.asarray(KH).ravel(), (np.repeat(g, 18, axis=1).ravel(), np.tile(g, (1, 18)).ravel())),
+                      shape=(n, n)).tocsr()
+    F = np.zeros(n)
+    np.add.at(F, g.ravel(), np.asarray(FH).ravel())
+    I = np.where(~bnd)[0]
+    U = np.zeros(n)
+    U[I] = spla.spsolve(K[I][:, I].tocsc(), F[I])
+    return U
+
+
+@pytest.mark.parametrize("m", [2, 3])
+def test_nedrt_coarse_solver_matches_scipy(m):
+    from oracle import nedrt_oracle as N
+    cells, ainv6, bdiv, load = workloads.nedrt_tensor(m=m, depth=1, seed=8)
+    res = N.build(cells, N.sym6_to_ainv(ainv6), bdiv, load.kind, list(load.params), want_phi=False)
+    rng = np.random.default_rng(m)
+    # a generic face load as well as the (divergence-free) trig load of the workload
+    for FH in (res["FH"], res["FH"] + np.concatenate([np.zeros((m ** 3, 12)), rng.standard_normal((m ** 3, 6))], 1)):
+        U = nedrt_coarse_solve(m, res["KH"], FH)
+        Us = scipy_nedrt_coarse(m, res["KH"], FH)
+        assert np.abs(U - Us).max() <= 1e-10 * np.abs(Us).max()

@@ -1,7 +1,8 @@
-"""Global multiscale Q1 solution from GPU-built K_H/F_H vs the FP64 oracle's
-(coarse assembly + solve on the host, the reference's QMultiscale flow), and
-the C++ QBasis-compatible shim driver on the GPU.
-Tolerance (stated): coarse solution relative L2 difference <= 1e-9."""
+"""Global multiscale Q1 and Ned_RT solutions from GPU-built K_H/F_H vs the
+FP64 oracle's (coarse assembly + solve on the host, the reference's
+QMultiscale / NedRTMultiscale flow), and the C++ QBasis-compatible shim driver
+on the GPU. Tolerance (stated): relative L2 difference <= 1e-9 of the coarse
+solution, and for Ned_RT also of the fine reconstruction sigma_h, u_h."""
 import json
 import os
 import subprocess
@@ -10,7 +11,7 @@ import numpy as np
 import pytest
 
 import workloads
-from test_coarse_solve import coarse_solve
+from test_coarse_solve import coarse_solve, nedrt_coarse_solve
 
 pytestmark = pytest.mark.gpu
 
@@ -27,6 +28,38 @@ def test_global_multiscale_solution_matches_oracle(gpu, oracle_lib, precision):
     Ur = coarse_solve(m, ref["KH"], ref["FH"])
     rel = np.linalg.norm(U - Ur) / np.linalg.norm(Ur)
     assert rel <= 1e-9, rel
+
+
+@pytest.mark.parametrize("precision", ("mixed", "fp64"))
+def test_global_nedrt_solution_matches_oracle(gpu, precision):
+    from oracle import nedrt_adjoint as NA
+    from oracle import nedrt_oracle as N
+    m, depth = 3, 2
+    cells, ainv6, bdiv, load = workloads.nedrt_tensor(m=m, depth=depth, seed=12)
+    h = gpu.Handle(precision=gpu.PRECISION_MIXED if precision == "mixed" else gpu.PRECISION_FP64)
+    KH, FH, rep, st = h.nedrt_build(cells, ainv6, bdiv, load)
+    assert st == gpu.SUCCESS and rep["converged"].all()
+    ref = N.build(cells, N.sym6_to_ainv(ainv6), bdiv, load.kind, list(load.params))
+    rng = np.random.default_rng(5)
+    # the trig load is divergence-free (its coarse solution has no edge part);
+    # a generic face load exercises the edge/face coupling as well
+    extra = np.concatenate([np.zeros((m ** 3, 12)), rng.standard_normal((m ** 3, 6))], 1)
+    g, _ = NA.coarse_maps(m)
+    n = 1 << depth
+    NE, NF = N.counts(n)
+    phi = h.nedrt_basis().reshape(m ** 3, 18, NE + NF)
+    for F_add in (0.0, extra):
+        U = nedrt_coarse_solve(m, KH, FH + F_add)
+        Ur = nedrt_coarse_solve(m, ref["KH"], ref["FH"] + F_add)
+        assert np.linalg.norm(U - Ur) <= 1e-9 * np.linalg.norm(Ur)
+        # fine reconstruction (set_global_weights): sigma from edge bases, u from face bases
+        sig = np.einsum("ce,ced->cd", U[g[:, :12]], phi[:, :12, :NE])
+        sig_r = np.einsum("ce,ced->cd", Ur[g[:, :12]], np.array(ref["Phi"])[:, :12, :NE])
+        u = np.einsum("cf,cfd->cd", U[g[:, 12:]], phi[:, 12:, NE:])
+        u_r = np.einsum("cf,cfd->cd", Ur[g[:, 12:]], np.array(ref["Phi"])[:, 12:, NE:])
+        assert np.linalg.norm(u - u_r) <= 1e-9 * np.linalg.norm(u_r)
+        if np.linalg.norm(sig_r) > 1e-12 * np.linalg.norm(u_r):
+            assert np.linalg.norm(sig - sig_r) <= 1e-9 * np.linalg.norm(sig_r)
 
 
 def test_qbasis_shim_example_driver(gpu):
