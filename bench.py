@@ -69,6 +69,10 @@ class Workload:
             self.cells, self.ainv6, self.bdiv, self.load = workloads.nedrt_tensor(m=8, depth=3, seed=2)
             self.cfg = {"workload": "nedrt_tensor_coarse8^3_L3_18rhs", "coarse_cells": 512, "depth": 3,
                         "seed": 2, "B": "1-0.9 sin(2 pi 14 x)", "load": "vec trig"}
+        elif name == "nedrt_l4":
+            self.kind = "nedrt"
+            self.cells, self.ainv6, self.bdiv, self.load = workloads.nedrt_tensor(m=8, depth=4, seed=5)
+            self.cfg = {"workload": "nedrt_tensor_coarse8^3_L4_18rhs", "coarse_cells": 512, "depth": 4, "seed": 5}
         elif name == "nedrt_large":
             self.kind = "nedrt"
             self.cells, self.ainv6, self.bdiv, self.load = workloads.nedrt_tensor(m=16, depth=4, seed=5)
@@ -551,7 +555,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="nedrt_small",
-                    choices=["nedrt_small", "nedrt_large", "q1_uneven", "q1_small", "q1_adjoint_fwd"])
+                    choices=["nedrt_small", "nedrt_l4", "nedrt_large", "q1_uneven", "q1_small", "q1_adjoint_fwd"])
     ap.add_argument("--extra", default="q1_uneven", help="comma-separated workloads reported beside the headline")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--skip-fp64", action="store_true")

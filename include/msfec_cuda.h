@@ -240,6 +240,22 @@ msfec_status msfec_q1_eval_fine(msfec_handle *handle, const double *weights,
                                 const double *points, double *values);
 
 /*
+ * Standard fine-scale Q1 solve (the reference's QReferenceSolution path,
+ * source/Q/q_ref.cc:139-363, as an independent accuracy reference for the
+ * multiscale solution): -div(a grad u) + r u = f on the box `domain`
+ * (uniformly refined depth times, depth 1..5, e.g. the unit cube with depth
+ * 5 = the 32^3 fine grid of a coarse 4^3 x depth-3 multiscale run) with
+ * homogeneous Dirichlet data. The same persistent solver runs one
+ * source-mode item (FP32 PCG + FP64 refinement in MIXED). Host buffers,
+ * synchronous. a, reaction: n^3 per fine cell; u: (n+1)^3 nodal values
+ * (node = i + (n+1)(j + (n+1)k)). report may be NULL.
+ */
+msfec_status msfec_q1_fine_solve(msfec_handle *handle, const msfec_cell *domain,
+                                 const double *a, const double *reaction,
+                                 const msfec_load *load, double *u,
+                                 msfec_cell_report *report);
+
+/*
  * Ned_RT (lowest-order Nedelec sigma x Raviart-Thomas u) basis build from
  * host buffers (synchronous). Replaces NedRTBasis::run
  * (source/Ned_RT/ned_rt_basis.cc:1279-1428) for every cell of the batch,

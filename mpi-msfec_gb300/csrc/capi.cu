@@ -145,6 +145,7 @@ struct msfec_handle {
   DevBuf<double> adj_rhs, adj_sol, adj_U, adj_lam, adj_gk, adj_grad, adj_KH, adj_FH;
   DevBuf<Q1Item> adj_items;
   DevBuf<Q1Unit> adj_units;
+  DevBuf<Q1Cell> fs_cell;  // standard fine solve: the domain as one lattice
   // Ned_RT state of the last build
   DevBuf<NRCell> nr_cells;
   DevBuf<NRItem> nr_items;
@@ -841,6 +842,7 @@ void msfec_destroy(msfec_handle *h) {
     h->adj_FH.release();
     h->adj_items.release();
     h->adj_units.release();
+    h->fs_cell.release();
     h->nr_cells.release();
     h->nr_items.release();
     h->nr_phi.release();
@@ -1084,6 +1086,109 @@ msfec_status msfec_q1_backward(msfec_handle *h, int32_t ncells, const msfec_cell
     for (int v = 0; v < 2; ++v)
       if (!stats[(size_t)c * 8 + v].converged)
         return fail(h, MSFEC_ERROR_NOT_CONVERGED, "adjoint local solve missed rtol");
+  return MSFEC_SUCCESS;
+}
+
+msfec_status msfec_q1_fine_solve(msfec_handle *h, const msfec_cell *domain, const double *a, const double *reaction,
+                                 const msfec_load *load, double *u, msfec_cell_report *report) {
+  if (!h) return MSFEC_ERROR_INVALID_ARGUMENT;
+  if (!domain || !a || !u) return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "null pointer");
+  if (!cell_ok(*domain)) return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "domain box invalid (depth 1..5)");
+  if (!load_ok(load) || (load && load->kind == MSFEC_LOAD_VEC_TRIG))
+    return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "invalid Q1 load");
+  const int n = 1 << domain->depth;
+  const int64_t nfine = (int64_t)n * n * n, nodes = (int64_t)(n + 1) * (n + 1) * (n + 1);
+  for (int64_t e = 0; e < nfine; ++e) {
+    if (!(a[e] > 0.0) || !std::isfinite(a[e])) return fail(h, MSFEC_ERROR_NUMERICAL, "coefficient a not positive/finite");
+    if (reaction && (!(reaction[e] >= 0.0) || !std::isfinite(reaction[e])))
+      return fail(h, MSFEC_ERROR_NUMERICAL, "reaction coefficient negative or non-finite");
+  }
+  const bool fp64 = h->cfg.precision == MSFEC_PRECISION_FP64;
+  const bool has_r = reaction != nullptr;
+  DeviceGuard g(h->device);
+  cudaStream_t st = h->stream;
+  // one source item for plane 0 (the load vector), zero Dirichlet data
+  Q1Plan plan = make_q1_plan(1, domain, fp64, has_r);
+  std::vector<Q1Item> items;
+  std::vector<Q1Unit> units;
+  for (const Q1Item &it : plan.items)
+    if (it.rhs0 == 0) {
+      Q1Item s = it;
+      s.mode = 1;
+      items.push_back(s);
+      units.push_back(Q1Unit{(int)items.size() - 1, 1, s.slab, 0});
+    }
+  const size_t planes = (size_t)nodes * 8;
+  MSFEC_CUDA_TRY(h, h->a.reserve(nfine));
+  if (has_r) MSFEC_CUDA_TRY(h, h->react.reserve(nfine));
+  MSFEC_CUDA_TRY(h, h->fs_cell.reserve(1));
+  MSFEC_CUDA_TRY(h, h->adj_rhs.reserve(planes));
+  MSFEC_CUDA_TRY(h, h->adj_sol.reserve(planes));
+  MSFEC_CUDA_TRY(h, h->adj_items.reserve(items.size()));
+  MSFEC_CUDA_TRY(h, h->adj_units.reserve(units.size()));
+  MSFEC_CUDA_TRY(h, h->queue.reserve(2));
+  MSFEC_CUDA_TRY(h, h->stats.reserve(8));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->a.ptr, a, nfine * sizeof(double), cudaMemcpyHostToDevice, st));
+  if (has_r) MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->react.ptr, reaction, nfine * sizeof(double), cudaMemcpyHostToDevice, st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->fs_cell.ptr, plan.cells.data(), sizeof(Q1Cell), cudaMemcpyHostToDevice, st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->adj_items.ptr, items.data(), items.size() * sizeof(Q1Item),
+                                    cudaMemcpyHostToDevice, st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->adj_units.ptr, units.data(), units.size() * sizeof(Q1Unit),
+                                    cudaMemcpyHostToDevice, st));
+  MSFEC_CUDA_TRY(h, cudaMemsetAsync(h->adj_rhs.ptr, 0, planes * sizeof(double), st));
+  MSFEC_CUDA_TRY(h, cudaMemsetAsync(h->stats.ptr, 0, 8 * sizeof(Q1Stat), st));
+  MSFEC_CUDA_TRY(h, cudaMemsetAsync(h->queue.ptr, 0, 2 * sizeof(int), st));
+  msfec_load ld;
+  if (load) {
+    ld = *load;
+  } else {
+    std::memset(&ld, 0, sizeof(ld));
+  }
+  MSFEC_CUDA_TRY(h, q1_adjoint_rhs_launch(h->fs_cell.ptr, 1, ld, 0, nullptr, nullptr, nullptr, h->adj_rhs.ptr, st));
+  Q1Params prm;
+  prm.cells = h->fs_cell.ptr;
+  prm.items = h->adj_items.ptr;
+  prm.units = h->adj_units.ptr;
+  prm.n_units = (int)units.size();
+  prm.queue = h->queue.ptr;
+  prm.a = h->a.ptr;
+  prm.react = has_r ? h->react.ptr : nullptr;
+  prm.phi = h->adj_sol.ptr;
+  prm.y = h->adj_sol.ptr;  // not written by source items
+  prm.src_rhs = h->adj_rhs.ptr;
+  prm.src_out = h->adj_sol.ptr;
+  prm.stats = h->stats.ptr;
+  prm.rtol = h->cfg.rtol;
+  prm.inner_rtol = h->cfg.inner_rtol;
+  prm.max_iter = h->cfg.max_iter;
+  prm.max_refine = h->cfg.max_refine;
+  int occ = 0;
+  MSFEC_CUDA_TRY(h, q1_solve_occupancy(fp64, plan.cluster, has_r, plan.smem, &occ));
+  if (occ <= 0) return fail(h, MSFEC_ERROR_NOT_SUPPORTED, "local solver kernel cannot be resident");
+  const int grid = plan.cluster;  // one item: one CTA, or one cluster for a slab item
+  if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[0], st));
+  MSFEC_CUDA_TRY(h, q1_solve_launch(fp64, plan.cluster, has_r, prm, plan.smem, grid, st));
+  if (h->timing) {
+    MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[1], st));
+    MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[2], st));
+    MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[3], st));
+  }
+  h->ev_recorded = h->timing;
+  h->last_launches = 2;
+  h->last_graph = 0;
+  Q1Stat stat;
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(u, h->adj_sol.ptr, nodes * sizeof(double), cudaMemcpyDeviceToHost, st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(&stat, h->stats.ptr, sizeof(Q1Stat), cudaMemcpyDeviceToHost, st));
+  MSFEC_CUDA_TRY(h, cudaStreamSynchronize(st));
+  const bool ok = stat.converged && !(stat.flags & 1);
+  if (report) {
+    report->iterations = stat.iters;
+    report->refinements = stat.refinements;
+    report->converged = ok ? 1 : 0;
+    report->reserved = 0;
+    report->residual = stat.rel_residual;
+  }
+  if (!ok) return fail(h, MSFEC_ERROR_NOT_CONVERGED, "fine-scale solve missed rtol");
   return MSFEC_SUCCESS;
 }
 

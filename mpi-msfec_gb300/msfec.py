@@ -38,7 +38,7 @@ EXPORTED = [
     "msfec_q1_basis_device", "msfec_q1_eval_fine", "msfec_set_timing", "msfec_get_timings",
     "msfec_nedrt_build", "msfec_nedrt_build_device", "msfec_nedrt_basis_size",
     "msfec_nedrt_get_basis", "msfec_q1_backward", "msfec_nedrt_build_noalloc",
-    "msfec_set_graph", "msfec_autotune",
+    "msfec_set_graph", "msfec_autotune", "msfec_q1_fine_solve",
 ]
 
 
@@ -138,6 +138,8 @@ def load_library(path: str = LIB_PATH):
     L.msfec_autotune.argtypes = [_vp, ctypes.c_int32, ctypes.c_int32, _vp, _vp, _vp, ctypes.POINTER(Load),
                                  ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_float)]
     L.msfec_autotune.restype = ctypes.c_int
+    L.msfec_q1_fine_solve.argtypes = [_vp, _vp, _dp, _dp, ctypes.POINTER(Load), _dp, _vp]
+    L.msfec_q1_fine_solve.restype = ctypes.c_int
     L.msfec_set_graph.argtypes = [_vp, ctypes.c_int32]
     L.msfec_set_graph.restype = ctypes.c_int
     _lib = L
@@ -257,6 +259,20 @@ class Handle:
 
     def set_timing(self, enable=True):
         return self.check(self._lib.msfec_set_timing(self._h, 1 if enable else 0))
+
+    def q1_fine_solve(self, domain, a, reaction, load):
+        """msfec_q1_fine_solve: standard fine-scale solve on one box; returns (u, report, status)."""
+        domain = np.ascontiguousarray(domain, dtype=CELL_DTYPE).reshape(1)
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        reaction = None if reaction is None else np.ascontiguousarray(reaction, dtype=np.float64)
+        n = 1 << int(domain["depth"][0])
+        u = np.zeros((n + 1) ** 3)
+        rep = np.zeros(1, dtype=REPORT_DTYPE)
+        st = self._lib.msfec_q1_fine_solve(self._h, domain.ctypes.data_as(_vp), _d(a),
+                                           None if reaction is None else _d(reaction), ctypes.byref(load),
+                                           _d(u), rep.ctypes.data_as(_vp))
+        self.check(st, allow=(ERROR_NOT_CONVERGED,))
+        return u, rep[0], st
 
     def autotune(self, kind, cells, coef0, coef1, load):
         """msfec_autotune on a sample batch; returns (choice, n_candidates, times_ms)."""
