@@ -345,6 +345,32 @@ msfec_status msfec_autotune(msfec_handle *handle, int32_t kind, int32_t ncells,
                             const double *coef1, const msfec_load *load,
                             int32_t *choice, float *times_ms);
 
+/*
+ * Adjoint of the Ned_RT build: dJ/d(log A) and dJ/d(log B) per fine cell
+ * (A_e scaled by exp(ta_e), B_e by exp(tb_e)) for a misfit J of the coarse
+ * multiscale u field (face bases' u-blocks weighted by the coarse solution,
+ * NedRTBasis::set_global_weights, ned_rt_basis.cc:1155-1181) at points. Host
+ * buffers, synchronous; the caller owns the coarse problem:
+ *   U, lambda  [ncells][18] coarse solution and coarse adjoint
+ *              (K_H^-T dJ/dU, K_H nonsymmetric) restricted to each cell
+ *   points     [npoints][3] in cell cell_of[p]; dJ_du[p][3] = dJ / d u_h(points[p])
+ *   grad_a, grad_b  [fine cells] outputs
+ * Four adjoint local problems per cell (edge / face bases x lambda / U
+ * weights) run as source items of the batched MINRES solver (A^T = S A S, S
+ * = -1 on face rows); the basis is rebuilt unless reuse_basis != 0 and the
+ * last Ned_RT build on this handle is the same batch. For the divergence-free
+ * MSFEC_LOAD_VEC_TRIG load the coarse solution has no edge part and grad_a
+ * vanishes to rounding; B carries the sensitivity.
+ */
+msfec_status msfec_nedrt_backward(msfec_handle *handle, int32_t ncells,
+                                  const msfec_cell *cells, const double *ainv6,
+                                  const double *bdiv, const msfec_load *load,
+                                  int32_t reuse_basis, const double *U,
+                                  const double *lambda, int32_t npoints,
+                                  const int32_t *cell_of, const double *points,
+                                  const double *dJ_du, double *grad_a,
+                                  double *grad_b);
+
 /* Basis of the last Ned_RT build: per cell 18 rows (coarse basis order) of
    NE + NF fine DoFs (edges x|y|z then faces x|y|z, lexicographic), sigma and u
    of every basis function. Size in doubles, and copy to host. */

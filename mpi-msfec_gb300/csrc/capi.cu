@@ -52,6 +52,14 @@ cudaError_t q1_adjoint_rhs_launch(const Q1Cell *cells, int ncells, const msfec_l
 cudaError_t q1_gradient_launch(const Q1Cell *cells, int ncells, const double *a, const double *phi, const double *sol,
                                const double *U, const double *lam, double *grad, cudaStream_t st);
 cudaError_t nedrt_solve_launch(bool fp64, const NRParams &prm, size_t smem, int grid, cudaStream_t st);
+cudaError_t nedrt_adjoint_prepare_launch(const NRCell *cells, int ncells, const double *phi, const double *U,
+                                         const double *lam, const msfec_load &load, int npoints, const int *cell_of,
+                                         const double *pts, const double *dJdu, const double *ainv6,
+                                         const double *bdiv, double *comb, double *bload, double *e, double *work,
+                                         double *rhs, cudaStream_t st);
+cudaError_t nedrt_adjoint_gradient_launch(const NRCell *cells, int ncells, const double *ainv6, const double *bdiv,
+                                          const double *comb, const double *work, const double *xsol, double *ga,
+                                          double *gb, cudaStream_t st);
 cudaError_t nedrt_galerkin_launch(const NRCell *cells, int ncells, const double *phi, const double *y,
                                   const msfec_load &load, double *KH, double *FH, msfec_cell_report *rep,
                                   const NRStat *stats, cudaStream_t st);
@@ -154,6 +162,11 @@ struct msfec_handle {
   DevBuf<float> nr_scratch;
   DevBuf<double> nr_ainv, nr_bdiv, nr_KH, nr_FH;
   int64_t nr_basis_doubles = 0;
+  std::vector<msfec_cell> nr_h_cells;  // batch of the Ned_RT basis held in nr_phi
+  // Ned_RT adjoint buffers
+  DevBuf<double> nra_U, nra_lam, nra_comb, nra_b, nra_e, nra_work, nra_rhs, nra_x, nra_pts, nra_dJ, nra_ga, nra_gb;
+  DevBuf<int> nra_cell;
+  DevBuf<NRItem> nra_items;
   int q1_ncells = 0;
   int64_t q1_basis_doubles = 0;
   std::vector<Q1Cell> h_cells;
@@ -677,7 +690,7 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
   std::vector<NRItem> items;
   items.reserve((size_t)ncells * 18);
   for (int c : order)
-    for (int b = 0; b < 18; ++b) items.push_back(NRItem{c, b});
+    for (int b = 0; b < 18; ++b) items.push_back(NRItem{c, b, 0});
   const size_t ws_floats = nr_workspace_floats(nmax, fp64 ? 8 : 4);
   const bool use_smem = ws_floats * 4 <= kNRSmemLimit;
   const size_t smem = use_smem ? ws_floats * 4 : 0;
@@ -699,7 +712,7 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
   MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->nr_cells.ptr, hc.data(), hc.size() * sizeof(NRCell), cudaMemcpyHostToDevice, st));
   MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->nr_items.ptr, items.data(), items.size() * sizeof(NRItem),
                                     cudaMemcpyHostToDevice, st));
-  NRParams prm;
+  NRParams prm{};
   prm.cells = h->nr_cells.ptr;
   prm.items = h->nr_items.ptr;
   prm.n_items = (int)items.size();
@@ -740,6 +753,7 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
   const msfec_status s = run_sequence(h, h->nr_graph, std::move(key), d_rep ? 3 : 2, seq);
   if (s != MSFEC_SUCCESS) return s;
   h->nr_graph_basis = dofs * 18;
+  h->nr_h_cells.assign(cells, cells + ncells);
   h->nr_basis_doubles = dofs * 18;
   return MSFEC_SUCCESS;
 }
@@ -853,6 +867,11 @@ void msfec_destroy(msfec_handle *h) {
     h->nr_bdiv.release();
     h->nr_KH.release();
     h->nr_FH.release();
+    for (DevBuf<double> *b : {&h->nra_U, &h->nra_lam, &h->nra_comb, &h->nra_b, &h->nra_e, &h->nra_work, &h->nra_rhs,
+                              &h->nra_x, &h->nra_pts, &h->nra_dJ, &h->nra_ga, &h->nra_gb})
+      b->release();
+    h->nra_cell.release();
+    h->nra_items.release();
     h->q1_graph.reset();
     h->nr_graph.reset();
     if (h->aux_stream) cudaStreamSynchronize(h->aux_stream);
@@ -1324,6 +1343,166 @@ msfec_status msfec_autotune(msfec_handle *h, int32_t kind, int32_t ncells, const
   return MSFEC_SUCCESS;
 }
 
+static bool nr_same_batch(const msfec_handle *h, int ncells, const msfec_cell *cells) {
+  if (h->nr_basis_doubles <= 0 || (int)h->nr_h_cells.size() != ncells) return false;
+  for (int c = 0; c < ncells; ++c) {
+    const msfec_cell &a = h->nr_h_cells[c], &b = cells[c];
+    if (a.depth != b.depth) return false;
+    for (int d = 0; d < 3; ++d)
+      if (a.origin[d] != b.origin[d] || a.size[d] != b.size[d]) return false;
+  }
+  return true;
+}
+
+msfec_status msfec_nedrt_backward(msfec_handle *h, int32_t ncells, const msfec_cell *cells, const double *ainv6,
+                                  const double *bdiv, const msfec_load *load, int32_t reuse_basis, const double *U,
+                                  const double *lambda, int32_t npoints, const int32_t *cell_of, const double *points,
+                                  const double *dJ_du, double *grad_a, double *grad_b) {
+  if (!h) return MSFEC_ERROR_INVALID_ARGUMENT;
+  if (ncells <= 0 || !cells || !ainv6 || !bdiv || !U || !lambda || !grad_a || !grad_b || npoints < 0 ||
+      (npoints > 0 && (!cell_of || !points || !dJ_du)))
+    return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "null pointer or invalid count");
+  int64_t nfine = 0, dofs = 0;
+  int nmax = 0;
+  for (int c = 0; c < ncells; ++c) {
+    if (!cell_ok(cells[c]) || cells[c].depth > kNRMaxDepth)
+      return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "cell " + std::to_string(c) + " invalid (Ned_RT depth 1..4)");
+    const int n = 1 << cells[c].depth;
+    int NEx, NFx, NE, NF;
+    nr_counts(n, NEx, NFx, NE, NF);
+    nfine += (int64_t)n * n * n;
+    dofs += NE + NF;
+    nmax = std::max(nmax, n);
+  }
+  for (int p = 0; p < npoints; ++p) {
+    if (cell_of[p] < 0 || cell_of[p] >= ncells) return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "cell_of out of range");
+    for (int d = 0; d < 3; ++d)
+      if (!std::isfinite(points[3 * p + d]) || !std::isfinite(dJ_du[3 * p + d]))
+        return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "non-finite point or dJ/du");
+  }
+  if (!load_ok(load) || !nr_load_ok(load)) return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "invalid Ned_RT load");
+  const bool fp64 = h->cfg.precision == MSFEC_PRECISION_FP64;
+  DeviceGuard g(h->device);
+  cudaStream_t st = h->stream;
+  MSFEC_CUDA_TRY(h, h->nr_ainv.reserve(nfine * 6));
+  MSFEC_CUDA_TRY(h, h->nr_bdiv.reserve(nfine));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->nr_ainv.ptr, ainv6, nfine * 6 * sizeof(double), cudaMemcpyHostToDevice, st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->nr_bdiv.ptr, bdiv, nfine * sizeof(double), cudaMemcpyHostToDevice, st));
+  if (!(reuse_basis && nr_same_batch(h, ncells, cells))) {
+    MSFEC_CUDA_TRY(h, h->nr_KH.reserve((size_t)ncells * 324));
+    MSFEC_CUDA_TRY(h, h->nr_FH.reserve((size_t)ncells * 18));
+    const msfec_status s = nedrt_build_impl(h, ncells, cells, h->nr_ainv.ptr, h->nr_bdiv.ptr, load, h->nr_KH.ptr,
+                                            h->nr_FH.ptr, nullptr);
+    if (s != MSFEC_SUCCESS) return s;
+  }
+  // per-cell combinations, face load, dJ/du, adjoint right-hand sides
+  const size_t nd = (size_t)dofs;
+  MSFEC_CUDA_TRY(h, h->nra_U.reserve((size_t)ncells * 18));
+  MSFEC_CUDA_TRY(h, h->nra_lam.reserve((size_t)ncells * 18));
+  MSFEC_CUDA_TRY(h, h->nra_comb.reserve(kNRSrcRhs * nd));
+  MSFEC_CUDA_TRY(h, h->nra_b.reserve(nd));
+  MSFEC_CUDA_TRY(h, h->nra_e.reserve(nd));
+  MSFEC_CUDA_TRY(h, h->nra_work.reserve(kNRSrcRhs * nd));
+  MSFEC_CUDA_TRY(h, h->nra_rhs.reserve(kNRSrcRhs * nd));
+  MSFEC_CUDA_TRY(h, h->nra_x.reserve(kNRSrcRhs * nd));
+  MSFEC_CUDA_TRY(h, h->nra_pts.reserve((size_t)std::max(npoints, 1) * 3));
+  MSFEC_CUDA_TRY(h, h->nra_dJ.reserve((size_t)std::max(npoints, 1) * 3));
+  MSFEC_CUDA_TRY(h, h->nra_cell.reserve(std::max(npoints, 1)));
+  MSFEC_CUDA_TRY(h, h->nra_ga.reserve(nfine));
+  MSFEC_CUDA_TRY(h, h->nra_gb.reserve(nfine));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->nra_U.ptr, U, (size_t)ncells * 18 * sizeof(double), cudaMemcpyHostToDevice, st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->nra_lam.ptr, lambda, (size_t)ncells * 18 * sizeof(double),
+                                    cudaMemcpyHostToDevice, st));
+  if (npoints > 0) {
+    MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->nra_pts.ptr, points, (size_t)npoints * 3 * sizeof(double),
+                                      cudaMemcpyHostToDevice, st));
+    MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->nra_dJ.ptr, dJ_du, (size_t)npoints * 3 * sizeof(double),
+                                      cudaMemcpyHostToDevice, st));
+    MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->nra_cell.ptr, cell_of, (size_t)npoints * sizeof(int), cudaMemcpyHostToDevice,
+                                      st));
+  }
+  MSFEC_CUDA_TRY(h, cudaMemsetAsync(h->nra_b.ptr, 0, nd * sizeof(double), st));
+  MSFEC_CUDA_TRY(h, cudaMemsetAsync(h->nra_e.ptr, 0, nd * sizeof(double), st));
+  msfec_load ld;
+  if (load) {
+    ld = *load;
+  } else {
+    std::memset(&ld, 0, sizeof(ld));
+  }
+  if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[0], st));
+  MSFEC_CUDA_TRY(h, nedrt_adjoint_prepare_launch(h->nr_cells.ptr, ncells, h->nr_phi.ptr, h->nra_U.ptr, h->nra_lam.ptr,
+                                                 ld, npoints, h->nra_cell.ptr, h->nra_pts.ptr, h->nra_dJ.ptr,
+                                                 h->nr_ainv.ptr, h->nr_bdiv.ptr, h->nra_comb.ptr, h->nra_b.ptr,
+                                                 h->nra_e.ptr, h->nra_work.ptr, h->nra_rhs.ptr, st));
+  // four source-mode solves per cell on the batched solver, deepest cells first
+  std::vector<int> order(ncells);
+  for (int c = 0; c < ncells; ++c) order[c] = c;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cells[x].depth > cells[y].depth; });
+  std::vector<NRItem> items;
+  for (int c : order)
+    for (int k = 0; k < kNRSrcRhs; ++k) items.push_back(NRItem{c, k, 1});
+  const size_t ws_floats = nr_workspace_floats(nmax, fp64 ? 8 : 4);
+  const bool use_smem = ws_floats * 4 <= kNRSmemLimit;
+  const size_t smem = use_smem ? ws_floats * 4 : 0;
+  int grid = std::min<int>((int)items.size(), h->num_sms);
+  if (!use_smem) {
+    int deepest = 0;
+    while ((1 << deepest) < nmax) ++deepest;
+    const int cap = h->nr_ctas[fp64 ? 0 : 1][std::min(deepest, kNRMaxDepthCfg)];
+    if (cap > 0) grid = std::min(grid, cap);
+    if (h->nr_scratch.cap < ws_floats * grid) h->nr_graph.reset();  // a captured build holds the old slots
+    MSFEC_CUDA_TRY(h, h->nr_scratch.reserve(ws_floats * grid));
+  }
+  MSFEC_CUDA_TRY(h, h->nra_items.reserve(items.size()));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->nra_items.ptr, items.data(), items.size() * sizeof(NRItem),
+                                    cudaMemcpyHostToDevice, st));
+  MSFEC_CUDA_TRY(h, cudaMemsetAsync(h->queue.ptr, 0, sizeof(int), st));
+  NRParams prm{};
+  prm.cells = h->nr_cells.ptr;
+  prm.items = h->nra_items.ptr;
+  prm.n_items = (int)items.size();
+  prm.queue = h->queue.ptr;
+  prm.ainv6 = h->nr_ainv.ptr;
+  prm.bdiv = h->nr_bdiv.ptr;
+  prm.phi = h->nr_phi.ptr;
+  prm.y = h->nr_y.ptr;
+  prm.stats = h->nr_stats.ptr;
+  prm.src_rhs = h->nra_rhs.ptr;
+  prm.src_out = h->nra_x.ptr;
+  prm.scratch = use_smem ? nullptr : h->nr_scratch.ptr;
+  prm.scratch_floats = ws_floats;
+  prm.use_smem = use_smem ? 1 : 0;
+  prm.rtol = h->cfg.nedrt_rtol;
+  prm.inner_rtol = h->cfg.inner_rtol;
+  prm.max_iter = std::max(h->cfg.max_iter, 8000);
+  prm.max_refine = h->cfg.max_refine;
+  MSFEC_CUDA_TRY(h, nedrt_solve_launch(fp64, prm, smem, grid, st));
+  if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[1], st));
+  MSFEC_CUDA_TRY(h, nedrt_adjoint_gradient_launch(h->nr_cells.ptr, ncells, h->nr_ainv.ptr, h->nr_bdiv.ptr,
+                                                  h->nra_comb.ptr, h->nra_work.ptr, h->nra_x.ptr, h->nra_ga.ptr,
+                                                  h->nra_gb.ptr, st));
+  if (h->timing) {
+    MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[2], st));
+    MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[3], st));
+  }
+  h->ev_recorded = h->timing;
+  h->last_launches = (npoints > 0 ? 4 : 3) + 2;
+  h->last_graph = 0;
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(grad_a, h->nra_ga.ptr, nfine * sizeof(double), cudaMemcpyDeviceToHost, st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(grad_b, h->nra_gb.ptr, nfine * sizeof(double), cudaMemcpyDeviceToHost, st));
+  std::vector<NRStat> stats((size_t)ncells * 18);
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(stats.data(), h->nr_stats.ptr, stats.size() * sizeof(NRStat),
+                                    cudaMemcpyDeviceToHost, st));
+  MSFEC_CUDA_TRY(h, cudaStreamSynchronize(st));
+  for (int c = 0; c < ncells; ++c)
+    for (int k = 0; k < kNRSrcRhs; ++k) {
+      const NRStat &q = stats[(size_t)c * 18 + k];
+      if (!q.converged || (q.flags & 1))
+        return fail(h, MSFEC_ERROR_NOT_CONVERGED, "Ned_RT adjoint local solve missed nedrt_rtol");
+    }
+  return MSFEC_SUCCESS;
+}
+
 int64_t msfec_nedrt_basis_size(const msfec_handle *h) { return h ? h->nr_basis_doubles : 0; }
 
 msfec_status msfec_nedrt_get_basis(msfec_handle *h, double *Phi, int64_t capacity) {
@@ -1446,7 +1625,7 @@ __global__ void __launch_bounds__(kNRPlanThreads)
     q.dof_off = pd;
     cells[c] = q;
     const long long slot = first[dep] + ((pk >> (16 * (dep - 1))) & 0xFFFF);
-    for (int b = 0; b < 18; ++b) items[slot * 18 + b] = NRItem{c, b};
+    for (int b = 0; b < 18; ++b) items[slot * 18 + b] = NRItem{c, b, 0};
     int NEx, NFx, NE, NF;
     nr_counts(n, NEx, NFx, NE, NF);
     pf += (long long)n * n * n;
@@ -1532,7 +1711,7 @@ msfec_status msfec_nedrt_build_noalloc(msfec_handle *h, int32_t ncells, const ms
   MSFEC_CUDA_TRY(h, cudaMemcpyAsync(d_in, cells, (size_t)ncells * sizeof(msfec_cell), cudaMemcpyHostToDevice, st));
   nr_static_plan_kernel<<<1, kNRPlanThreads, 0, st>>>(d_in, ncells, d_cells, d_items, queue);
   MSFEC_CUDA_TRY(h, cudaGetLastError());
-  NRParams prm;
+  NRParams prm{};
   prm.cells = d_cells;
   prm.items = d_items;
   prm.n_items = (int)nitems;

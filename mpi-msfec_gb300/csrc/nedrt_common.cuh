@@ -29,8 +29,11 @@ struct NRCell {
 
 struct NRItem {
   int cell;
-  int basis;  // 0..17
+  int basis;  // 0..17 (basis mode); right-hand side 0..3 of the cell (source mode)
+  int mode;   // 0 basis function, 1 source: zero Dirichlet data, load from src_rhs
 };
+
+constexpr int kNRSrcRhs = 4;  // source-mode right-hand sides per cell (adjoint)
 
 struct NRStat {
   int iters;
@@ -50,6 +53,8 @@ struct NRParams {
   double *phi;          // [18][ndof] per cell
   double *y;            // [18][ndof] per cell: A P_b (primary block of basis b)
   NRStat *stats;        // [cell][18]
+  const double *src_rhs;  // source mode: [cell][kNRSrcRhs][ndof] at kNRSrcRhs * dof_off
+  double *src_out;        // source mode: solutions, same layout
   float *scratch;       // global workspace when the item does not fit shared memory
   size_t scratch_floats;  // per CTA
   int use_smem;

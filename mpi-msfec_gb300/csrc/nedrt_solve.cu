@@ -416,6 +416,7 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
   const int n = g.n, N = g.N;
   const int nc = n * n * n;
   const int bb = it.basis;
+  const bool src = it.mode == 1;
   const int tid = threadIdx.x;
   constexpr bool kMixed = sizeof(T) == 4;
   const double invV = 1.0 / (Cc.h[0] * Cc.h[1] * Cc.h[2]);
@@ -440,7 +441,9 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
   float *facc = ws + Np;
   const double *ag = prm.ainv6 + 6 * Cc.coef_off;
   const double *bg = prm.bdiv + Cc.coef_off;
-  double *phi = prm.phi + 18 * Cc.dof_off + (size_t)bb * N;
+  double *phi = src ? prm.src_out + kNRSrcRhs * Cc.dof_off + (size_t)bb * N
+                    : prm.phi + 18 * Cc.dof_off + (size_t)bb * N;
+  const double *fsrc = src ? prm.src_rhs + kNRSrcRhs * Cc.dof_off + (size_t)bb * N : nullptr;
   double *yout = prm.y + 18 * Cc.dof_off + (size_t)bb * N;
 
   // tables
@@ -510,17 +513,18 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
       for (int d = tid; d < N; d += kNRThreads) {
         int dir, i, j, k;
         dof_geometry(g, d, dir, i, j, k);
-        phi[d] = coarse_dof(bb, dir, i, j, k, n);
+        phi[d] = src ? 0.0 : coarse_dof(bb, dir, i, j, k, n);
       }
       __syncthreads();
     }
     double part[2] = {0.0, 0.0};
     for (int pass = (ir == 0 ? 0 : 1); pass < 2; ++pass) {
       // pass 0: lift of the boundary data only (scale of the stopping test)
+      // accumulator starts at -f for a source item (r = f - A phi)
       if (fp32_res) {
-        for (int d = tid; d < N; d += kNRThreads) facc[d] = 0.0f;
+        for (int d = tid; d < N; d += kNRThreads) facc[d] = src ? (float)-fsrc[d] : 0.0f;
       } else {
-        for (int d = tid; d < N; d += kNRThreads) dacc[d] = 0.0;
+        for (int d = tid; d < N; d += kNRThreads) dacc[d] = src ? -fsrc[d] : 0.0;
       }
       __syncthreads();
       for (int c = tid; c < nc; c += kNRThreads) {
@@ -538,7 +542,8 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
           fb[t] = dof_geometry(g, f[t], dir, i, j, k);
         }
         double rc[6];
-        if (bb < 12) {
+        const bool curl_rhs = !src && bb < 12;
+        if (curl_rhs) {
           curl_rhs_cell(bb, c % n, (c / n) % n, c / (n * n), n, Cc.h, rc);
         }
         if (fp32_res) {
@@ -548,7 +553,7 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
             cell_apply_s<float, double, float, 1, false>(phi, facc, Ff, ai, a[6] * (float)invV, e, f, eb, fb);
           else
             cell_apply_s<float, double, float, 0, false>(phi, facc, Ff, ai, a[6] * (float)invV, e, f, eb, fb);
-          if (bb < 12)
+          if (curl_rhs)
 #pragma unroll
             for (int t = 0; t < 6; ++t) atomicAdd(facc + f[t], (float)-rc[t]);
         } else {
@@ -558,7 +563,7 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
             cell_apply_s<double, double, double, 1, false>(phi, dacc, Fd, ai, bg[c] * invV, e, f, eb, fb);
           else
             cell_apply_s<double, double, double, 0, false>(phi, dacc, Fd, ai, bg[c] * invV, e, f, eb, fb);
-          if (bb < 12)
+          if (curl_rhs)
 #pragma unroll
             for (int t = 0; t < 6; ++t) atomicAdd(dacc + f[t], -rc[t]);
         }
@@ -726,21 +731,23 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
   }
 
   // ---------------- y_b = A P_b (FP64), P_b = primary block of basis b ----------------
-  for (int d = tid; d < N; d += kNRThreads) dacc[d] = 0.0;
-  __syncthreads();
-  for (int c = tid; c < nc; c += kNRThreads) {
-    int e[12], f[6];
-    cell_dofs(g, c, e, f);
-    const bool eb[12] = {}, fb[6] = {};
-    const double *a = ag + 6 * (size_t)c;
-    const double ai[6] = {a[0], a[1], a[2], a[3], a[4], a[5]};
-    if (bb < 12)
-      cell_apply_s<double, double, double, 2, false>(phi, dacc, Fd, ai, bg[c] * invV, e, f, eb, fb);
-    else
-      cell_apply_s<double, double, double, 3, false>(phi, dacc, Fd, ai, bg[c] * invV, e, f, eb, fb);
+  if (!src) {  // block-uniform
+    for (int d = tid; d < N; d += kNRThreads) dacc[d] = 0.0;
+    __syncthreads();
+    for (int c = tid; c < nc; c += kNRThreads) {
+      int e[12], f[6];
+      cell_dofs(g, c, e, f);
+      const bool eb[12] = {}, fb[6] = {};
+      const double *a = ag + 6 * (size_t)c;
+      const double ai[6] = {a[0], a[1], a[2], a[3], a[4], a[5]};
+      if (bb < 12)
+        cell_apply_s<double, double, double, 2, false>(phi, dacc, Fd, ai, bg[c] * invV, e, f, eb, fb);
+      else
+        cell_apply_s<double, double, double, 3, false>(phi, dacc, Fd, ai, bg[c] * invV, e, f, eb, fb);
+    }
+    __syncthreads();
+    for (int d = tid; d < N; d += kNRThreads) yout[d] = dacc[d];
   }
-  __syncthreads();
-  for (int d = tid; d < N; d += kNRThreads) yout[d] = dacc[d];
   if (tid == 0) {
     NRStat st;
     st.iters = its;
@@ -910,6 +917,302 @@ __global__ void nedrt_report_kernel(const NRStat *__restrict__ stats, int ncells
   rep[c] = r;
 }
 
+
+// ---------------------------------------------------------------------------
+// Adjoint of the Ned_RT build (parameters: log-scales of A and B per fine
+// cell). With s = P U, t = P lambda (P: primary blocks of the basis), the four
+// combinations Phi_E lambda, Phi_E U, Phi_F lambda, Phi_F U (E: the 12 edge
+// bases, F: the 6 face bases), e = dJ/du_h and the face load b:
+//   rhs_k = S Pi_k w_k on interior DoFs, solved with A_II (source items),
+//   eta_k = S x_k (A_II^T = S A_II S), and per fine cell
+//   dJ/dta = t_s^T M s_s + sum_k eta_k,s^T M c_k,s,  dJ/dtb = -(same with D),
+// c_k the k-th combination; w_0 = -A s, w_1 = -A^T t (sigma block),
+// w_2 = b - A s, w_3 = e - A^T t (u block).
+constexpr int kAdjThreads = 256;
+
+// comb[4][N] per cell (at 4 dof_off): Phi_E lambda, Phi_E U, Phi_F lambda, Phi_F U.
+__global__ void __launch_bounds__(kAdjThreads) nr_adj_combine_kernel(const NRCell *__restrict__ cells,
+                                                                     const double *__restrict__ phi,
+                                                                     const double *__restrict__ U,
+                                                                     const double *__restrict__ lam,
+                                                                     double *__restrict__ comb) {
+  __shared__ double w[2][18];
+  const int c = blockIdx.x;
+  const NRCell C = cells[c];
+  int NEx, NFx, NE, NF;
+  nr_counts(C.n, NEx, NFx, NE, NF);
+  const int N = NE + NF;
+  if (threadIdx.x < 18) {
+    w[0][threadIdx.x] = lam[18 * (size_t)c + threadIdx.x];
+    w[1][threadIdx.x] = U[18 * (size_t)c + threadIdx.x];
+  }
+  __syncthreads();
+  const double *P = phi + 18 * C.dof_off;
+  double *out = comb + kNRSrcRhs * C.dof_off;
+  for (int d = threadIdx.x; d < N; d += kAdjThreads) {
+    double el = 0.0, eu = 0.0, fl = 0.0, fu = 0.0;
+#pragma unroll
+    for (int b = 0; b < 12; ++b) {
+      const double v = P[(size_t)b * N + d];
+      el = fma(w[0][b], v, el);
+      eu = fma(w[1][b], v, eu);
+    }
+#pragma unroll
+    for (int b = 12; b < 18; ++b) {
+      const double v = P[(size_t)b * N + d];
+      fl = fma(w[0][b], v, fl);
+      fu = fma(w[1][b], v, fu);
+    }
+    out[d] = el;
+    out[(size_t)N + d] = eu;
+    out[2 * (size_t)N + d] = fl;
+    out[3 * (size_t)N + d] = fu;
+  }
+}
+
+// e = dJ/du_h: point k in coarse cell cell_of[k] spreads dJ_du[k][d] onto the
+// two faces of normal d of its fine cell with the RT0 weights.
+__global__ void nr_adj_point_kernel(const NRCell *__restrict__ cells, int npoints, const int *__restrict__ cell_of,
+                                    const double *__restrict__ pts, const double *__restrict__ dJdu,
+                                    double *__restrict__ e) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= npoints) return;
+  const NRCell C = cells[cell_of[k]];
+  NRGeom g;
+  g.n = C.n;
+  g.L = C.depth;
+  nr_counts(g.n, g.NEx, g.NFx, g.NE, g.NF);
+  g.N = g.NE + g.NF;
+  int fi[3];
+  double tau[3];
+  for (int d = 0; d < 3; ++d) {
+    const double s = (pts[3 * (size_t)k + d] - C.origin[d]) / C.h[d];
+    fi[d] = min(max((int)floor(s), 0), C.n - 1);
+    tau[d] = s - fi[d];
+  }
+  const int cell = fi[0] + C.n * (fi[1] + C.n * fi[2]);
+  int ed[12], f[6];
+  cell_dofs(g, cell, ed, f);
+  for (int d = 0; d < 3; ++d) {
+    int o1, o2;
+    other_axes(d, o1, o2);
+    const double area = C.h[o1] * C.h[o2];
+    const double gk = dJdu[3 * (size_t)k + d];
+    atomicAdd(e + C.dof_off + f[2 * d], gk * (1.0 - tau[d]) / area);
+    atomicAdd(e + C.dof_off + f[2 * d + 1], gk * tau[d] / area);
+  }
+}
+
+// Face load b_f = (v_f, f) of every fine face (2x2x2 Gauss, the vector trig load).
+__global__ void __launch_bounds__(kAdjThreads) nr_adj_face_load_kernel(const NRCell *__restrict__ cells,
+                                                                       msfec_load load, double *__restrict__ b) {
+  const int c = blockIdx.x;
+  const NRCell C = cells[c];
+  NRGeom g;
+  g.n = C.n;
+  g.L = C.depth;
+  nr_counts(g.n, g.NEx, g.NFx, g.NE, g.NF);
+  g.N = g.NE + g.NF;
+  if (load.kind != MSFEC_LOAD_VEC_TRIG) return;
+  const int n = g.n, nc = n * n * n;
+  const double w = load.params[1] * M_PI, p0 = load.params[0];
+  const double gq = 0.5 / sqrt(3.0);
+  const double qp[2] = {0.5 - gq, 0.5 + gq};
+  const double jxw = 0.125 * C.h[0] * C.h[1] * C.h[2];
+  for (int cell = threadIdx.x; cell < nc; cell += kAdjThreads) {
+    const int i = cell & (n - 1), j = (cell >> g.L) & (n - 1), k = cell >> (2 * g.L);
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    for (int q = 0; q < 8; ++q) {
+      const double xl[3] = {qp[q & 1], qp[(q >> 1) & 1], qp[q >> 2]};
+      const double X = C.origin[0] + (i + xl[0]) * C.h[0], Y = C.origin[1] + (j + xl[1]) * C.h[1],
+                   Z = C.origin[2] + (k + xl[2]) * C.h[2];
+      const double sx = sin(w * X), sy = sin(w * Y), sz = sin(w * Z);
+      const double fv[3] = {p0 * sy * sz, p0 * sz * sx, p0 * sx * sy};
+      for (int d = 0; d < 3; ++d) {
+        int o1, o2;
+        other_axes(d, o1, o2);
+        const double sc = jxw * fv[d] / (C.h[o1] * C.h[o2]);
+        acc[2 * d] += sc * (1.0 - xl[d]);
+        acc[2 * d + 1] += sc * xl[d];
+      }
+    }
+    int ed[12], f[6];
+    cell_dofs(g, cell, ed, f);
+    for (int t = 0; t < 6; ++t) atomicAdd(b + C.dof_off + f[t], acc[t]);
+  }
+}
+
+// Right-hand sides of the four adjoint solves (see above). work[4][N] per cell
+// (at 4 dof_off): s, S t, A s, A S t.
+__global__ void __launch_bounds__(kAdjThreads) nr_adj_rhs_kernel(const NRCell *__restrict__ cells,
+                                                                 const double *__restrict__ ainv6,
+                                                                 const double *__restrict__ bdiv,
+                                                                 const double *__restrict__ comb,
+                                                                 const double *__restrict__ bload,
+                                                                 const double *__restrict__ e,
+                                                                 double *__restrict__ work, double *__restrict__ rhs) {
+  __shared__ NRFactors<double> F;
+  const int c = blockIdx.x;
+  const NRCell C = cells[c];
+  NRGeom g;
+  g.n = C.n;
+  g.L = C.depth;
+  nr_counts(g.n, g.NEx, g.NFx, g.NE, g.NF);
+  g.N = g.NE + g.NF;
+  const int N = g.N, n = g.n, nc = n * n * n;
+  if (threadIdx.x == 0) make_factors(C.h, F);
+  const double *cb = comb + kNRSrcRhs * C.dof_off;
+  double *s = work + kNRSrcRhs * C.dof_off, *st = s + N, *as = st + N, *ast = as + N;
+  for (int d = threadIdx.x; d < N; d += kAdjThreads) {
+    const bool edge = d < g.NE;
+    s[d] = edge ? cb[(size_t)N + d] : cb[3 * (size_t)N + d];  // sigma of Phi_E U, u of Phi_F U
+    st[d] = edge ? cb[d] : -cb[2 * (size_t)N + d];           // S (sigma of Phi_E lambda, u of Phi_F lambda)
+    as[d] = 0.0;
+    ast[d] = 0.0;
+  }
+  __syncthreads();
+  const double invV = 1.0 / (C.h[0] * C.h[1] * C.h[2]);
+  const double *ag = ainv6 + 6 * C.coef_off;
+  const double *bg = bdiv + C.coef_off;
+  for (int cell = threadIdx.x; cell < nc; cell += kAdjThreads) {
+    int ed[12], f[6];
+    cell_dofs(g, cell, ed, f);
+    const bool eb[12] = {}, fb[6] = {};
+    const double ai[6] = {ag[6 * cell], ag[6 * cell + 1], ag[6 * cell + 2], ag[6 * cell + 3], ag[6 * cell + 4],
+                          ag[6 * cell + 5]};
+    cell_apply_s<double, double, double, 0, false>(s, as, F, ai, bg[cell] * invV, ed, f, eb, fb);
+    cell_apply_s<double, double, double, 0, false>(st, ast, F, ai, bg[cell] * invV, ed, f, eb, fb);
+  }
+  __syncthreads();
+  double *r = rhs + kNRSrcRhs * C.dof_off;
+  const double *bl = bload + C.dof_off, *ee = e + C.dof_off;
+  for (int d = threadIdx.x; d < N; d += kAdjThreads) {
+    int dir, i, j, k;
+    const bool bnd = dof_geometry(g, d, dir, i, j, k);
+    const bool edge = d < g.NE;
+    const double at = edge ? ast[d] : -ast[d];  // (A^T t)_d = S_d (A S t)_d
+    double r0 = 0.0, r1 = 0.0, r2 = 0.0, r3 = 0.0;
+    if (!bnd) {
+      if (edge) {
+        r0 = -as[d];
+        r1 = -at;
+      } else {
+        r2 = -(bl[d] - as[d]);
+        r3 = -(ee[d] - at);
+      }
+    }
+    r[d] = r0;
+    r[(size_t)N + d] = r1;
+    r[2 * (size_t)N + d] = r2;
+    r[3 * (size_t)N + d] = r3;
+  }
+}
+
+// x^T M_e y over the 12 edges of one fine cell (edge-mass part of cell_apply_s).
+__device__ __forceinline__ double edge_mass_form(const NRFactors<double> &F, const double (&ai)[6],
+                                                 const double (&x)[12], const double (&y)[12]) {
+  const double A[3][3] = {{ai[0], ai[3], ai[4]}, {ai[3], ai[1], ai[5]}, {ai[4], ai[5], ai[2]}};
+  double my[12];
+#pragma unroll
+  for (int p = 0; p < 3; ++p) {
+    const double k = A[p][p] * F.hd[p];
+    double t[4];
+#pragma unroll
+    for (int l = 0; l < 4; ++l) t[l] = 2.0 * y[4 * p + l] + y[4 * p + (l ^ 1)];
+#pragma unroll
+    for (int l = 0; l < 4; ++l) my[4 * p + l] = k * (2.0 * t[l] + t[l ^ 2]);
+  }
+#pragma unroll
+  for (int p = 0; p < 3; ++p)
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      if (q == p) continue;
+      const int r = 3 - p - q;
+      double s0 = 0.0, s1 = 0.0;
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        if (edge_pos(q, m, r))
+          s1 += y[4 * q + m];
+        else
+          s0 += y[4 * q + m];
+      }
+      const double k = A[p][q] * F.hq[r];
+#pragma unroll
+      for (int l = 0; l < 4; ++l) my[4 * p + l] += k * (edge_pos(p, l, r) ? s0 + 2.0 * s1 : 2.0 * s0 + s1);
+    }
+  double out = 0.0;
+#pragma unroll
+  for (int l = 0; l < 12; ++l) out = fma(x[l], my[l], out);
+  return out;
+}
+
+// Per fine cell: dJ/dta (edge-mass forms) and dJ/dtb (div-div forms).
+__global__ void __launch_bounds__(kAdjThreads) nr_adj_gradient_kernel(const NRCell *__restrict__ cells,
+                                                                      const double *__restrict__ ainv6,
+                                                                      const double *__restrict__ bdiv,
+                                                                      const double *__restrict__ comb,
+                                                                      const double *__restrict__ work,
+                                                                      const double *__restrict__ xsol,
+                                                                      double *__restrict__ ga, double *__restrict__ gb) {
+  __shared__ NRFactors<double> F;
+  const int c = blockIdx.x;
+  const NRCell C = cells[c];
+  NRGeom g;
+  g.n = C.n;
+  g.L = C.depth;
+  nr_counts(g.n, g.NEx, g.NFx, g.NE, g.NF);
+  g.N = g.NE + g.NF;
+  const int N = g.N, n = g.n, nc = n * n * n;
+  if (threadIdx.x == 0) make_factors(C.h, F);
+  __syncthreads();
+  const double *cb = comb + kNRSrcRhs * C.dof_off;
+  const double *s = work + kNRSrcRhs * C.dof_off, *st = s + N;
+  const double *xs = xsol + kNRSrcRhs * C.dof_off;
+  const double invV = 1.0 / (C.h[0] * C.h[1] * C.h[2]);
+  for (int cell = threadIdx.x; cell < nc; cell += kAdjThreads) {
+    int ed[12], f[6];
+    cell_dofs(g, cell, ed, f);
+    const double *a = ainv6 + 6 * (C.coef_off + cell);
+    const double ai[6] = {a[0], a[1], a[2], a[3], a[4], a[5]};
+    double xe[12], ye[12];
+    // t^T M s and t^T D s (t = S (S t): sigma part of st as is, u part negated)
+#pragma unroll
+    for (int l = 0; l < 12; ++l) {
+      xe[l] = st[ed[l]];
+      ye[l] = s[ed[l]];
+    }
+    double qa = edge_mass_form(F, ai, xe, ye);
+    double dt = 0.0, ds = 0.0;
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      const double sg = (t & 1) ? 1.0 : -1.0;
+      dt += sg * -st[f[t]];
+      ds += sg * s[f[t]];
+    }
+    double qd = dt * ds;
+#pragma unroll
+    for (int k = 0; k < kNRSrcRhs; ++k) {
+      const double *xk = xs + (size_t)k * N, *ck = cb + (size_t)k * N;
+#pragma unroll
+      for (int l = 0; l < 12; ++l) {
+        xe[l] = xk[ed[l]];  // eta_k = S x_k: sigma part unchanged
+        ye[l] = ck[ed[l]];
+      }
+      qa += edge_mass_form(F, ai, xe, ye);
+      double dx = 0.0, dy = 0.0;
+#pragma unroll
+      for (int t = 0; t < 6; ++t) {
+        const double sg = (t & 1) ? 1.0 : -1.0;
+        dx += sg * -xk[f[t]];  // u part of eta_k = -x_k
+        dy += sg * ck[f[t]];
+      }
+      qd += dx * dy;
+    }
+    ga[C.coef_off + cell] = qa;
+    gb[C.coef_off + cell] = -bdiv[C.coef_off + cell] * invV * qd;
+  }
+}
+
 }  // namespace nrimpl
 
 cudaError_t nedrt_solve_launch(bool fp64, const NRParams &prm, size_t smem, int grid, cudaStream_t st) {
@@ -938,4 +1241,27 @@ cudaError_t nedrt_galerkin_launch(const NRCell *cells, int ncells, const double 
   return cudaGetLastError();
 }
 
+
+cudaError_t nedrt_adjoint_prepare_launch(const NRCell *cells, int ncells, const double *phi, const double *U,
+                                         const double *lam, const msfec_load &load, int npoints, const int *cell_of,
+                                         const double *pts, const double *dJdu, const double *ainv6,
+                                         const double *bdiv, double *comb, double *bload, double *e, double *work,
+                                         double *rhs, cudaStream_t st) {
+  if (ncells <= 0) return cudaSuccess;
+  nrimpl::nr_adj_combine_kernel<<<ncells, nrimpl::kAdjThreads, 0, st>>>(cells, phi, U, lam, comb);
+  nrimpl::nr_adj_face_load_kernel<<<ncells, nrimpl::kAdjThreads, 0, st>>>(cells, load, bload);
+  if (npoints > 0)
+    nrimpl::nr_adj_point_kernel<<<(npoints + 127) / 128, 128, 0, st>>>(cells, npoints, cell_of, pts, dJdu, e);
+  nrimpl::nr_adj_rhs_kernel<<<ncells, nrimpl::kAdjThreads, 0, st>>>(cells, ainv6, bdiv, comb, bload, e, work, rhs);
+  return cudaGetLastError();
+}
+
+cudaError_t nedrt_adjoint_gradient_launch(const NRCell *cells, int ncells, const double *ainv6, const double *bdiv,
+                                          const double *comb, const double *work, const double *xsol, double *ga,
+                                          double *gb, cudaStream_t st) {
+  if (ncells <= 0) return cudaSuccess;
+  nrimpl::nr_adj_gradient_kernel<<<ncells, nrimpl::kAdjThreads, 0, st>>>(cells, ainv6, bdiv, comb, work, xsol, ga,
+                                                                          gb);
+  return cudaGetLastError();
+}
 }  // namespace msfec

@@ -38,7 +38,7 @@ EXPORTED = [
     "msfec_q1_basis_device", "msfec_q1_eval_fine", "msfec_set_timing", "msfec_get_timings",
     "msfec_nedrt_build", "msfec_nedrt_build_device", "msfec_nedrt_basis_size",
     "msfec_nedrt_get_basis", "msfec_q1_backward", "msfec_nedrt_build_noalloc",
-    "msfec_set_graph", "msfec_autotune", "msfec_q1_fine_solve",
+    "msfec_set_graph", "msfec_autotune", "msfec_q1_fine_solve", "msfec_nedrt_backward",
 ]
 
 
@@ -140,6 +140,9 @@ def load_library(path: str = LIB_PATH):
     L.msfec_autotune.restype = ctypes.c_int
     L.msfec_q1_fine_solve.argtypes = [_vp, _vp, _dp, _dp, ctypes.POINTER(Load), _dp, _vp]
     L.msfec_q1_fine_solve.restype = ctypes.c_int
+    L.msfec_nedrt_backward.argtypes = [_vp, ctypes.c_int32, _vp, _dp, _dp, ctypes.POINTER(Load), ctypes.c_int32,
+                                       _dp, _dp, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32), _dp, _dp, _dp, _dp]
+    L.msfec_nedrt_backward.restype = ctypes.c_int
     L.msfec_set_graph.argtypes = [_vp, ctypes.c_int32]
     L.msfec_set_graph.restype = ctypes.c_int
     _lib = L
@@ -259,6 +262,25 @@ class Handle:
 
     def set_timing(self, enable=True):
         return self.check(self._lib.msfec_set_timing(self._h, 1 if enable else 0))
+
+    def nedrt_backward(self, cells, ainv6, bdiv, load, U, lam, cell_of, points, dJ_du, reuse_basis=True):
+        """(dJ/d log A, dJ/d log B) per fine cell (msfec_nedrt_backward)."""
+        cells = np.ascontiguousarray(cells, dtype=CELL_DTYPE)
+        ainv6 = np.ascontiguousarray(ainv6, dtype=np.float64)
+        bdiv = np.ascontiguousarray(bdiv, dtype=np.float64)
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        lam = np.ascontiguousarray(lam, dtype=np.float64)
+        cell_of = np.ascontiguousarray(cell_of, dtype=np.int32)
+        points = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+        dJ_du = np.ascontiguousarray(dJ_du, dtype=np.float64).reshape(-1, 3)
+        ga = np.zeros(bdiv.size)
+        gb = np.zeros(bdiv.size)
+        st = self._lib.msfec_nedrt_backward(self._h, cells.shape[0], cells.ctypes.data_as(_vp), _d(ainv6), _d(bdiv),
+                                            ctypes.byref(load), 1 if reuse_basis else 0, _d(U), _d(lam),
+                                            points.shape[0], cell_of.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                            _d(points), _d(dJ_du), _d(ga), _d(gb))
+        self.check(st)
+        return ga, gb
 
     def q1_fine_solve(self, domain, a, reaction, load):
         """msfec_q1_fine_solve: standard fine-scale solve on one box; returns (u, report, status)."""

@@ -2,8 +2,9 @@
 
 Multiscale Nedelec x Raviart-Thomas solution on a structured m^3 coarse grid
 of the unit cube with essential conditions (coarse tangential edges and normal
-faces on the boundary are zero). Parameter: one log-scale per fine cell,
-A_e = exp(theta_e) Ahat_e (A^-1 scaled by exp(-theta_e)). Misfit of the coarse
+faces on the boundary are zero). Parameters: two log-scales per fine cell,
+A_e = exp(ta_e) Ahat_e (A^-1 scaled by exp(-ta_e)) and B_e = exp(tb_e) Bhat_e.
+Misfit of the coarse
 multiscale u field (face bases' u-blocks weighted by the coarse solution, as
 NedRTBasis::set_global_weights forms it, source/Ned_RT/ned_rt_basis.cc:
 1155-1181) at points: J = 1/2 sum_k |u_h(x_k) - d_k|^2.
@@ -11,9 +12,10 @@ NedRTBasis::set_global_weights forms it, source/Ned_RT/ned_rt_basis.cc:
 With K_H = P^T A P (primary blocks P of the basis, the reference's
 assemble_global_element_matrix, ned_rt_basis.cc:849-948), F_H = P_u^T b,
 s = P U, t = P lambda (lambda = K^-T dJ/dU), e = dJ/du_h (fine face vector),
-dA/dtheta_e = -M_e (edge mass of cell e), the gradient is
+dA/dta_e = -M_e (edge mass of cell e), dA/dtb_e = +D_e (div-div of cell e):
 
-  dJ/dtheta_e = t_s^T M_e s_s + sum_j eta_j,s^T M_e phi_j,s       (s: sigma block)
+  dJ/dta_e = + t_s^T M_e s_s + sum_j eta_j,s^T M_e phi_j,s    (s: sigma block)
+  dJ/dtb_e = - t_u^T D_e s_u - sum_j eta_j,u^T D_e phi_j,u    (u: u block)
   eta_j = A_II^-T (Pi_j w_j)_I,
   w_j = -lambda_j A s - U_j A^T t + [j face] (lambda_j b + U_j e),
 
@@ -21,7 +23,9 @@ Pi_j the primary block of basis j. eta_j is linear in (lambda_j, U_j) with
 four distinct right-hand sides per cell (edge / face bases x lambda / U), so
 four transposed local solves per cell (A^T = S A S, S = +1 on edges, -1 on
 faces). The reference has no adjoint; this is the derivative of its Ned_RT
-path restated here.
+path restated here. For the divergence-free trig load the coarse solution has
+no edge part and does not depend on A (dJ/dta vanishes); B carries the
+sensitivity.
 """
 import numpy as np
 import scipy.sparse as sp
@@ -84,13 +88,15 @@ def eval_u(cells, Phi, U, g, m, cell_of, points, with_jac=False):
     return (out, jac) if with_jac else out
 
 
-def misfit(cells, m, ainv_hat, theta, bdiv, load_kind, load_params, cell_of, points, data, gradient=True):
-    """(J, dJ/dtheta or None) for a uniform-depth batch on the m^3 coarse grid."""
+def misfit(cells, m, ainv_hat, bdiv_hat, ta, tb, load_kind, load_params, cell_of, points, data, gradient=True):
+    """(J, dJ/dta, dJ/dtb) (gradients None without `gradient`) for a
+    uniform-depth batch on the m^3 coarse grid."""
     depth = int(cells["depth"][0])
     n = 1 << depth
     NE, NF = N.counts(n)
     nf = n ** 3
-    ainv = ainv_hat * np.exp(-theta)[:, None, None]
+    ainv = ainv_hat * np.exp(-ta)[:, None, None]
+    bdiv = bdiv_hat * np.exp(tb)
     g, cb = coarse_maps(m)
     Ncoarse = cb.size
     Phi, KH, FH, Amat = [], [], [], []
@@ -115,7 +121,7 @@ def misfit(cells, m, ainv_hat, theta, bdiv, load_kind, load_params, cell_of, poi
     r = u - data
     J = 0.5 * float(np.sum(r ** 2))
     if not gradient:
-        return J, None
+        return J, None, None
     # e = dJ/du_h per coarse cell (fine face vector), dJ/dU (face bases only)
     e_cell = [np.zeros(NF) for _ in range(m ** 3)]
     for p in range(len(points)):
@@ -132,7 +138,10 @@ def misfit(cells, m, ainv_hat, theta, bdiv, load_kind, load_params, cell_of, poi
     S = np.r_[np.ones(NE), -np.ones(NF)]
     h = np.asarray(cells["size"][0]) / n
     eidx, _ = N.cell_dofs(n)
-    grad = np.zeros_like(theta)
+    ga = np.zeros_like(ta)
+    gb = np.zeros_like(tb)
+    _, fidx = N.cell_dofs(n)
+    fsgn = np.array([-1.0, 1.0, -1.0, 1.0, -1.0, 1.0])
     for c in range(m ** 3):
         sl = slice(c * nf, (c + 1) * nf)
         A = Amat[c]
@@ -169,5 +178,11 @@ def misfit(cells, m, ainv_hat, theta, bdiv, load_kind, load_params, cell_of, poi
         def q(x, y):
             return np.einsum("ea,eab,eb->e", x[eidx], Me, y[eidx])
 
-        grad[sl] = q(t, s) + q(eEl, PhEl) + q(eEU, PhEU) + q(eFl, PhFl) + q(eFU, PhFU)
-    return J, grad
+        def qd(x, y):  # x_u^T D_e y_u = B_e / |K| div_e(x) div_e(y)
+            dx = (x[NE:][fidx] * fsgn).sum(1)
+            dy = (y[NE:][fidx] * fsgn).sum(1)
+            return bdiv[sl] / np.prod(h) * dx * dy
+
+        ga[sl] = q(t, s) + q(eEl, PhEl) + q(eEU, PhEU) + q(eFl, PhFl) + q(eFU, PhFU)
+        gb[sl] = -(qd(t, s) + qd(eEl, PhEl) + qd(eEU, PhEU) + qd(eFl, PhFl) + qd(eFU, PhFU))
+    return J, ga, gb
