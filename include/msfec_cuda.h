@@ -357,7 +357,10 @@ msfec_status msfec_autotune(msfec_handle *handle, int32_t kind, int32_t ncells,
  *   grad_a, grad_b  [fine cells] outputs
  * Four adjoint local problems per cell (edge / face bases x lambda / U
  * weights) run as source items of the batched MINRES solver (A^T = S A S, S
- * = -1 on face rows); the basis is rebuilt unless reuse_basis != 0 and the
+ * = -1 on face rows), to max(nedrt_rtol, 1e-11) relative residual, taken
+ * relative to max(||f||, 1e-3 of the cell's adjoint source scale) (the
+ * right-hand sides are projections and differences that can cancel to
+ * rounding); the basis is rebuilt unless reuse_basis != 0 and the
  * last Ned_RT build on this handle is the same batch. For the divergence-free
  * MSFEC_LOAD_VEC_TRIG load the coarse solution has no edge part and grad_a
  * vanishes to rounding; B carries the sensitivity.

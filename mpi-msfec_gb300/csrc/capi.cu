@@ -56,7 +56,7 @@ cudaError_t nedrt_adjoint_prepare_launch(const NRCell *cells, int ncells, const 
                                          const double *lam, const msfec_load &load, int npoints, const int *cell_of,
                                          const double *pts, const double *dJdu, const double *ainv6,
                                          const double *bdiv, double *comb, double *bload, double *e, double *work,
-                                         double *rhs, cudaStream_t st);
+                                         double *rhs, double *floor_out, cudaStream_t st);
 cudaError_t nedrt_adjoint_gradient_launch(const NRCell *cells, int ncells, const double *ainv6, const double *bdiv,
                                           const double *comb, const double *work, const double *xsol, double *ga,
                                           double *gb, cudaStream_t st);
@@ -164,7 +164,8 @@ struct msfec_handle {
   int64_t nr_basis_doubles = 0;
   std::vector<msfec_cell> nr_h_cells;  // batch of the Ned_RT basis held in nr_phi
   // Ned_RT adjoint buffers
-  DevBuf<double> nra_U, nra_lam, nra_comb, nra_b, nra_e, nra_work, nra_rhs, nra_x, nra_pts, nra_dJ, nra_ga, nra_gb;
+  DevBuf<double> nra_U, nra_lam, nra_comb, nra_b, nra_e, nra_work, nra_rhs, nra_x, nra_pts, nra_dJ, nra_ga, nra_gb,
+      nra_floor;
   DevBuf<int> nra_cell;
   DevBuf<NRItem> nra_items;
   int q1_ncells = 0;
@@ -868,7 +869,7 @@ void msfec_destroy(msfec_handle *h) {
     h->nr_KH.release();
     h->nr_FH.release();
     for (DevBuf<double> *b : {&h->nra_U, &h->nra_lam, &h->nra_comb, &h->nra_b, &h->nra_e, &h->nra_work, &h->nra_rhs,
-                              &h->nra_x, &h->nra_pts, &h->nra_dJ, &h->nra_ga, &h->nra_gb})
+                              &h->nra_x, &h->nra_pts, &h->nra_dJ, &h->nra_ga, &h->nra_gb, &h->nra_floor})
       b->release();
     h->nra_cell.release();
     h->nra_items.release();
@@ -1408,6 +1409,7 @@ msfec_status msfec_nedrt_backward(msfec_handle *h, int32_t ncells, const msfec_c
   MSFEC_CUDA_TRY(h, h->nra_pts.reserve((size_t)std::max(npoints, 1) * 3));
   MSFEC_CUDA_TRY(h, h->nra_dJ.reserve((size_t)std::max(npoints, 1) * 3));
   MSFEC_CUDA_TRY(h, h->nra_cell.reserve(std::max(npoints, 1)));
+  MSFEC_CUDA_TRY(h, h->nra_floor.reserve(ncells));
   MSFEC_CUDA_TRY(h, h->nra_ga.reserve(nfine));
   MSFEC_CUDA_TRY(h, h->nra_gb.reserve(nfine));
   MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->nra_U.ptr, U, (size_t)ncells * 18 * sizeof(double), cudaMemcpyHostToDevice, st));
@@ -1433,7 +1435,7 @@ msfec_status msfec_nedrt_backward(msfec_handle *h, int32_t ncells, const msfec_c
   MSFEC_CUDA_TRY(h, nedrt_adjoint_prepare_launch(h->nr_cells.ptr, ncells, h->nr_phi.ptr, h->nra_U.ptr, h->nra_lam.ptr,
                                                  ld, npoints, h->nra_cell.ptr, h->nra_pts.ptr, h->nra_dJ.ptr,
                                                  h->nr_ainv.ptr, h->nr_bdiv.ptr, h->nra_comb.ptr, h->nra_b.ptr,
-                                                 h->nra_e.ptr, h->nra_work.ptr, h->nra_rhs.ptr, st));
+                                                 h->nra_e.ptr, h->nra_work.ptr, h->nra_rhs.ptr, h->nra_floor.ptr, st));
   // four source-mode solves per cell on the batched solver, deepest cells first
   std::vector<int> order(ncells);
   for (int c = 0; c < ncells; ++c) order[c] = c;
@@ -1469,10 +1471,15 @@ msfec_status msfec_nedrt_backward(msfec_handle *h, int32_t ncells, const msfec_c
   prm.stats = h->nr_stats.ptr;
   prm.src_rhs = h->nra_rhs.ptr;
   prm.src_out = h->nra_x.ptr;
+  prm.src_floor = h->nra_floor.ptr;
   prm.scratch = use_smem ? nullptr : h->nr_scratch.ptr;
   prm.scratch_floats = ws_floats;
   prm.use_smem = use_smem ? 1 : 0;
-  prm.rtol = h->cfg.nedrt_rtol;
+  // The adjoint right-hand sides are projections and differences (-A s on the
+  // edge rows, b - A s, e - A^T t) that can be small against A x or cancel to
+  // rounding: they stop at max(nedrt_rtol, 1e-11) relative to max(||f||, the
+  // cell's floor from nr_adj_rhs_kernel) (the basis solves keep nedrt_rtol).
+  prm.rtol = std::max(h->cfg.nedrt_rtol, 1e-11);
   prm.inner_rtol = h->cfg.inner_rtol;
   prm.max_iter = std::max(h->cfg.max_iter, 8000);
   prm.max_refine = h->cfg.max_refine;
@@ -1498,7 +1505,11 @@ msfec_status msfec_nedrt_backward(msfec_handle *h, int32_t ncells, const msfec_c
     for (int k = 0; k < kNRSrcRhs; ++k) {
       const NRStat &q = stats[(size_t)c * 18 + k];
       if (!q.converged || (q.flags & 1))
-        return fail(h, MSFEC_ERROR_NOT_CONVERGED, "Ned_RT adjoint local solve missed nedrt_rtol");
+        return fail(h, MSFEC_ERROR_NOT_CONVERGED,
+                    "Ned_RT adjoint local solve missed its tolerance (cell " + std::to_string(c) + ", rhs " +
+                        std::to_string(k) + ", relative residual " + std::to_string(q.rel_residual) + ", " +
+                        std::to_string(q.iters) + " iterations, " + std::to_string(q.refinements) +
+                        " refinements)");
     }
   return MSFEC_SUCCESS;
 }

@@ -55,6 +55,7 @@ struct NRParams {
   NRStat *stats;        // [cell][18]
   const double *src_rhs;  // source mode: [cell][kNRSrcRhs][ndof] at kNRSrcRhs * dof_off
   double *src_out;        // source mode: solutions, same layout
+  const double *src_floor;  // source mode: [cell] lower bound of the ||f|| the stopping test scales
   float *scratch;       // global workspace when the item does not fit shared memory
   size_t scratch_floats;  // per CTA
   int use_smem;

@@ -584,6 +584,9 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
       double tot[2];
       block_sum<double, 2>(sh, part, tot);
       if (ir == 0) bnorm2 = tot[0];
+      // a source right-hand side that cancelled to rounding is solved to rtol of
+      // its cell's adjoint scale, not of its own (noise-level) norm
+      if (ir == 0 && src) bnorm2 = fmax(bnorm2, prm.src_floor[it.cell] * prm.src_floor[it.cell]);
       rnorm2 = tot[1];
     }
     ++nref;
@@ -1050,7 +1053,8 @@ __global__ void __launch_bounds__(kAdjThreads) nr_adj_rhs_kernel(const NRCell *_
                                                                  const double *__restrict__ comb,
                                                                  const double *__restrict__ bload,
                                                                  const double *__restrict__ e,
-                                                                 double *__restrict__ work, double *__restrict__ rhs) {
+                                                                 double *__restrict__ work, double *__restrict__ rhs,
+                                                                 double *__restrict__ floor_out) {
   __shared__ NRFactors<double> F;
   const int c = blockIdx.x;
   const NRCell C = cells[c];
@@ -1086,6 +1090,7 @@ __global__ void __launch_bounds__(kAdjThreads) nr_adj_rhs_kernel(const NRCell *_
   __syncthreads();
   double *r = rhs + kNRSrcRhs * C.dof_off;
   const double *bl = bload + C.dof_off, *ee = e + C.dof_off;
+  double scale2 = 0.0;
   for (int d = threadIdx.x; d < N; d += kAdjThreads) {
     int dir, i, j, k;
     const bool bnd = dof_geometry(g, d, dir, i, j, k);
@@ -1105,6 +1110,17 @@ __global__ void __launch_bounds__(kAdjThreads) nr_adj_rhs_kernel(const NRCell *_
     r[(size_t)N + d] = r1;
     r[2 * (size_t)N + d] = r2;
     r[3 * (size_t)N + d] = r3;
+    if (!bnd) scale2 += as[d] * as[d] + at * at + bl[d] * bl[d] + ee[d] * ee[d];
+  }
+  // floor of the stopping scale: 1e-3 of the cell's adjoint source scale
+  __shared__ double red[kAdjThreads / 32];
+  for (int off = 16; off >= 1; off >>= 1) scale2 += __shfl_xor_sync(0xffffffffu, scale2, off);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = scale2;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < kAdjThreads / 32; ++w) t += red[w];
+    floor_out[c] = 1e-3 * sqrt(t);
   }
 }
 
@@ -1246,13 +1262,14 @@ cudaError_t nedrt_adjoint_prepare_launch(const NRCell *cells, int ncells, const 
                                          const double *lam, const msfec_load &load, int npoints, const int *cell_of,
                                          const double *pts, const double *dJdu, const double *ainv6,
                                          const double *bdiv, double *comb, double *bload, double *e, double *work,
-                                         double *rhs, cudaStream_t st) {
+                                         double *rhs, double *floor_out, cudaStream_t st) {
   if (ncells <= 0) return cudaSuccess;
   nrimpl::nr_adj_combine_kernel<<<ncells, nrimpl::kAdjThreads, 0, st>>>(cells, phi, U, lam, comb);
   nrimpl::nr_adj_face_load_kernel<<<ncells, nrimpl::kAdjThreads, 0, st>>>(cells, load, bload);
   if (npoints > 0)
     nrimpl::nr_adj_point_kernel<<<(npoints + 127) / 128, 128, 0, st>>>(cells, npoints, cell_of, pts, dJdu, e);
-  nrimpl::nr_adj_rhs_kernel<<<ncells, nrimpl::kAdjThreads, 0, st>>>(cells, ainv6, bdiv, comb, bload, e, work, rhs);
+  nrimpl::nr_adj_rhs_kernel<<<ncells, nrimpl::kAdjThreads, 0, st>>>(cells, ainv6, bdiv, comb, bload, e, work, rhs,
+                                                                     floor_out);
   return cudaGetLastError();
 }
 
