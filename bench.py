@@ -414,6 +414,41 @@ def adjoint_timing(local, stream, steps=3):
             "note": "host-buffer C ABI for both; backward = 2 adjoint local problems per cell + gradient kernel"}
 
 
+def adjoint_timing_nedrt(local, stream, steps=3):
+    """Backward / forward time of the Ned_RT adjoint on coarse 8^3 x depth 3 (the
+    headline batch, 512 observation points): forward = msfec_nedrt_build, backward
+    = msfec_nedrt_backward reusing the stored basis (host buffers for both)."""
+    import msfec
+    import workloads
+    cells, ainv6, bdiv, load = workloads.nedrt_tensor(m=8, depth=3, seed=2)
+    rng = np.random.default_rng(7)
+    npts = 512
+    cell_of = rng.integers(0, len(cells), npts).astype(np.int32)
+    pts = cells["origin"][cell_of] + rng.random((npts, 3)) * cells["size"][cell_of]
+    U = rng.standard_normal((len(cells), 18))
+    lam = rng.standard_normal((len(cells), 18))
+    g = rng.standard_normal((npts, 3))
+    h = msfec.Handle(precision=msfec.PRECISION_MIXED, device=local)
+    h.set_stream(stream.cuda_stream)
+    h.nedrt_build(cells, ainv6, bdiv, load)
+    h.nedrt_backward(cells, ainv6, bdiv, load, U, lam, cell_of, pts, g)
+    fw, bw = [], []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        h.nedrt_build(cells, ainv6, bdiv, load)
+        t1 = time.perf_counter()
+        h.nedrt_backward(cells, ainv6, bdiv, load, U, lam, cell_of, pts, g, reuse_basis=True)
+        t2 = time.perf_counter()
+        fw.append(t1 - t0)
+        bw.append(t2 - t1)
+    h.close()
+    f, b = float(np.median(fw)), float(np.median(bw))
+    return {"workload": "nedrt_tensor_coarse8^3_L3, 512 observation points", "forward_ms": f * 1e3,
+            "backward_ms": b * 1e3, "bwd_over_fwd": b / f,
+            "note": "host-buffer C ABI for both; backward = 4 adjoint local problems per cell (vs 18 basis "
+                    "problems forward) + gradient kernel, d/dlog A and d/dlog B"}
+
+
 def run_ours(args):
     import torch
     import msfec
@@ -478,6 +513,7 @@ def run_ours(args):
             extras[name]["config"] = ex["wl"].cfg
     if not args.skip_extra and not args.skip_adjoint:
         extras["adjoint_q1"] = adjoint_timing(local, stream)
+        extras["adjoint_nedrt"] = adjoint_timing_nedrt(local, stream)
     if rank != 0:
         if dist is not None:
             dist.destroy_process_group()
