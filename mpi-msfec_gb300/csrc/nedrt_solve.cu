@@ -465,7 +465,7 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
     for (int q = 0; q < 6; ++q) cf[7 * c + q] = (float)ag[6 * (size_t)c + q];
     cf[7 * c + 6] = (float)bg[c];
   }
-  for (int d = tid; d < N; d += kNRThreads) pd[d] = 0.0f;
+  for (int d = tid; d < (int)Np; d += kNRThreads) pd[d] = 0.0f;  // pad [N, Np) stays 0
   __syncthreads();
 
   // ---- block-Jacobi preconditioner: diag(M) on edges, then the lumped Schur
@@ -570,8 +570,8 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
       }
       __syncthreads();
       // r = -(A phi - f) on interior DoFs (boundary: 0), kept in vA
-      for (int d = tid; d < N; d += kNRThreads) {
-        const bool interior = pd[d] > 0.0f;
+      for (int d = tid; d < (int)Np; d += kNRThreads) {
+        const bool interior = pd[d] > 0.0f;  // false on the pad [N, Np)
         const double r = interior ? -(fp32_res ? (double)facc[d] : dacc[d]) : 0.0;
         part[pass] += r * r;
         // MINRES runs on the symmetric form S A (S = +1 on edges, -1 on faces):
@@ -605,7 +605,7 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
     // The Lanczos vectors are kept unnormalised (v_j = v~_j / g_j, g_j =
     // gamma_j), so there is no normalisation pass; each phase's reduction is
     // published per warp and summed by every thread after the barrier.
-    for (int d = tid; d < N; d += kNRThreads) {
+    for (int d = tid; d < (int)Np; d += kNRThreads) {  // pads included: the float4 passes cover [0, Np)
       vB[d] = T(0);
       wA[d] = T(0);
       wB[d] = T(0);
@@ -617,7 +617,7 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
     T gam;                 // gamma_j
     {
       T p1[1] = {T(0)};
-      for (int d = tid; d < N; d += kNRThreads) {
+      for (int d = tid; d < (int)Np; d += kNRThreads) {
         const T z = (T)pd[d] * vc[d];
         zt[d] = z;
         p1[0] += z * vc[d];
@@ -658,11 +658,33 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
         }
       }
       if (pending) {  // w_j = (z_{j-1} - a3 w_{j-2} - a2 w_{j-1}) / a1, x += c eta w_j
-        for (int d = tid; d < N; d += kNRThreads) {
-          const T z = (T)pd[d] * vp[d] * gi_p;
-          const T wn = (z - p_a3 * wo[d] - p_a2 * wc[d]) * p_ia1;
-          wo[d] = wn;
-          xk[d] += p_step * wn;
+        if constexpr (kMixed) {  // 4 DoFs per thread and vector access (pads are 0)
+          const float4 *pd4 = reinterpret_cast<const float4 *>(pd);
+          const float4 *vp4 = reinterpret_cast<const float4 *>(vp);
+          float4 *wo4 = reinterpret_cast<float4 *>(wo);
+          const float4 *wc4 = reinterpret_cast<const float4 *>(wc);
+          float4 *xk4 = reinterpret_cast<float4 *>(xk);
+          for (int q = tid; q < (int)(Np / 4); q += kNRThreads) {
+            const float4 pv = pd4[q], v = vp4[q], a = wo4[q], b = wc4[q];
+            float4 x = xk4[q], wn;
+            wn.x = (pv.x * v.x * gi_p - p_a3 * a.x - p_a2 * b.x) * p_ia1;
+            wn.y = (pv.y * v.y * gi_p - p_a3 * a.y - p_a2 * b.y) * p_ia1;
+            wn.z = (pv.z * v.z * gi_p - p_a3 * a.z - p_a2 * b.z) * p_ia1;
+            wn.w = (pv.w * v.w * gi_p - p_a3 * a.w - p_a2 * b.w) * p_ia1;
+            x.x += p_step * wn.x;
+            x.y += p_step * wn.y;
+            x.z += p_step * wn.z;
+            x.w += p_step * wn.w;
+            wo4[q] = wn;
+            xk4[q] = x;
+          }
+        } else {
+          for (int d = tid; d < N; d += kNRThreads) {
+            const T z = (T)pd[d] * vp[d] * gi_p;
+            const T wn = (z - p_a3 * wo[d] - p_a2 * wc[d]) * p_ia1;
+            wo[d] = wn;
+            xk[d] += p_step * wn;
+          }
         }
         T *t = wo;
         wo = wc;
@@ -674,18 +696,47 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
       // ---- phase 2
       T gpart = T(0);
       const T gg = gam * gi_p;
-      for (int d = tid; d < N; d += kNRThreads) {
-        const float pdd = pd[d];
-        T vn = T(0);
-        if (pdd > 0.0f) {
-          const T a = d < g.NE ? az[d] : -az[d];
-          vn = (a - delta * vc[d]) * gi_c - gg * vp[d];
+      if constexpr (kMixed) {  // 4 DoFs per thread and vector access (pads are 0)
+        const float4 *pd4 = reinterpret_cast<const float4 *>(pd);
+        const float4 *vc4 = reinterpret_cast<const float4 *>(vc);
+        float4 *vp4 = reinterpret_cast<float4 *>(vp);
+        float4 *az4 = reinterpret_cast<float4 *>(az);
+        float4 *zt4 = reinterpret_cast<float4 *>(zt);
+        for (int q = tid; q < (int)(Np / 4); q += kNRThreads) {
+          const float4 pv = pd4[q], a = az4[q], c = vc4[q], v = vp4[q];
+          const int d0 = 4 * q;
+          auto lane = [&](float pdd, float ad, float cd, float vd, int d) {
+            const float sa = d < g.NE ? ad : -ad;
+            return pdd > 0.0f ? (sa - delta * cd) * gi_c - gg * vd : 0.0f;
+          };
+          float4 vn, z;
+          vn.x = lane(pv.x, a.x, c.x, v.x, d0);
+          vn.y = lane(pv.y, a.y, c.y, v.y, d0 + 1);
+          vn.z = lane(pv.z, a.z, c.z, v.z, d0 + 2);
+          vn.w = lane(pv.w, a.w, c.w, v.w, d0 + 3);
+          z.x = pv.x * vn.x;
+          z.y = pv.y * vn.y;
+          z.z = pv.z * vn.z;
+          z.w = pv.w * vn.w;
+          vp4[q] = vn;
+          az4[q] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+          zt4[q] = z;
+          gpart += z.x * vn.x + z.y * vn.y + z.z * vn.z + z.w * vn.w;
         }
-        vp[d] = vn;
-        az[d] = T(0);
-        const T z = (T)pdd * vn;
-        zt[d] = z;
-        gpart += z * vn;
+      } else {
+        for (int d = tid; d < N; d += kNRThreads) {
+          const float pdd = pd[d];
+          T vn = T(0);
+          if (pdd > 0.0f) {
+            const T a = d < g.NE ? az[d] : -az[d];
+            vn = (a - delta * vc[d]) * gi_c - gg * vp[d];
+          }
+          vp[d] = vn;
+          az[d] = T(0);
+          const T z = (T)pdd * vn;
+          zt[d] = z;
+          gpart += z * vn;
+        }
       }
       warp_publish<T>(sh, 1, gpart);
       __syncthreads();
