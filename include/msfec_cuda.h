@@ -301,7 +301,7 @@ msfec_status msfec_nedrt_build_device(msfec_handle *handle, int32_t ncells,
  * and status (about 1.06 MB per depth-3 cell, 7.76 MB per depth-4 cell) do not
  * fit, or that holds more than 4096 cells, is rejected with
  * MSFEC_ERROR_INVALID_ARGUMENT and a message naming the bytes needed; split
- * it. Depth-4 cells also take 0.98 MB (mixed) / 1.73 MB (FP64) of MINRES
+ * it. Depth-4 cells also take 0.99 MB (mixed) / 1.75 MB (FP64) of MINRES
  * workspace per concurrent CTA from the pool, so fewer CTAs run when space is
  * short. The first call on each device looks up the pool's address (and may
  * load the library's module for it): make that first call before any stream

@@ -74,7 +74,7 @@ __host__ __device__ inline void nr_counts(int n, int &NEx, int &NFx, int &NE, in
 
 // Workspace (floats) of one item: preconditioner (float) + 7 Krylov vectors
 // of precision T (tsize bytes), all over the full DoF set, plus float copies of
-// the coefficients (7 per fine cell).
+// the coefficients (8 per fine cell: A^-1 (6), B/|K|, pad; 16-byte aligned).
 __host__ __device__ inline size_t nr_workspace_floats(int n, int tsize) {
   int NEx, NFx, NE, NF;
   nr_counts(n, NEx, NFx, NE, NF);
@@ -82,7 +82,7 @@ __host__ __device__ inline size_t nr_workspace_floats(int n, int tsize) {
   const size_t al = 64;
   const size_t Np = (N + al - 1) / al * al;
   const size_t nc = (size_t)n * n * n;
-  return Np + 7 * Np * (size_t)(tsize / 4) + (7 * nc + al - 1) / al * al;
+  return Np + 7 * Np * (size_t)(tsize / 4) + (8 * nc + al - 1) / al * al;
 }
 
 }  // namespace msfec

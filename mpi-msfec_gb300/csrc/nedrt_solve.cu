@@ -41,7 +41,7 @@ struct NRShared {
   float Cf[12][6];
   NRFactors<float> Ff;  // tensor-product factors of the current item's cell
   NRFactors<double> Fd;
-  float fslot[2][kNRWarps];  // per-warp partials of the two fused MINRES reductions
+  alignas(16) float fslot[2][kNRWarps];  // per-warp partials of the two fused MINRES reductions
   double dslot[2][kNRWarps];
   int item;
 };
@@ -355,15 +355,18 @@ __device__ __forceinline__ void warp_publish(NRShared &sh, int slot, VT v) {
 // Same summation order in every thread: identical decisions block-wide.
 template <typename VT>
 __device__ __forceinline__ VT slot_total(const NRShared &sh, int slot) {
-  VT s = VT(0);
+  if constexpr (sizeof(VT) == 4) {  // 16 partials: four 16-byte loads, pairwise sums
+    static_assert(kNRWarps == 16, "slot_total reads 16 float partials");
+    const float4 *p = reinterpret_cast<const float4 *>(sh.fslot[slot]);
+    const float4 a = p[0], b = p[1], c = p[2], d = p[3];
+    return ((a.x + a.y) + (a.z + a.w)) + ((b.x + b.y) + (b.z + b.w)) + (((c.x + c.y) + (c.z + c.w)) +
+                                                                       ((d.x + d.y) + (d.z + d.w)));
+  } else {
+    VT s = VT(0);
 #pragma unroll
-  for (int w = 0; w < kNRWarps; ++w) {
-    if constexpr (sizeof(VT) == 4)
-      s += sh.fslot[slot][w];
-    else
-      s += sh.dslot[slot][w];
+    for (int w = 0; w < kNRWarps; ++w) s += sh.dslot[slot][w];
+    return s;
   }
-  return s;
 }
 
 template <typename VT, int NV>
@@ -462,8 +465,9 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
   }
   for (int c = tid; c < nc; c += kNRThreads) {
 #pragma unroll
-    for (int q = 0; q < 6; ++q) cf[7 * c + q] = (float)ag[6 * (size_t)c + q];
-    cf[7 * c + 6] = (float)bg[c];
+    for (int q = 0; q < 6; ++q) cf[8 * c + q] = (float)ag[6 * (size_t)c + q];
+    cf[8 * c + 6] = (float)(bg[c] * invV);  // B / |K|
+    cf[8 * c + 7] = 0.0f;
   }
   for (int d = tid; d < (int)Np; d += kNRThreads) pd[d] = 0.0f;  // pad [N, Np) stays 0
   __syncthreads();
@@ -473,7 +477,7 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
   for (int c = tid; c < nc; c += kNRThreads) {
     int e[12], f[6];
     cell_dofs(g, c, e, f);
-    const float *a = cf + 7 * c;
+    const float *a = cf + 8 * c;
     const float Ad[3] = {a[0], a[1], a[2]};
 #pragma unroll
     for (int l = 0; l < 12; ++l) atomicAdd(pd + e[l], Ad[l >> 2] * sh.Gf[l >> 2][l >> 2][l & 3][l & 3]);
@@ -482,13 +486,13 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
   for (int c = tid; c < nc; c += kNRThreads) {
     int e[12], f[6];
     cell_dofs(g, c, e, f);
-    const float bdv = cf[7 * c + 6];
+    const float bdv = cf[8 * c + 6];
     float me[12];
 #pragma unroll
     for (int l = 0; l < 12; ++l) me[l] = pd[e[l]];
 #pragma unroll
     for (int t = 0; t < 6; ++t) {
-      float s = bdv * (float)invV;
+      float s = bdv;
 #pragma unroll
       for (int l = 0; l < 12; ++l) s += sh.Cf[l][t] * sh.Cf[l][t] / me[l];
       atomicAdd(pd + f[t], s);
@@ -547,12 +551,12 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
           curl_rhs_cell(bb, c % n, (c / n) % n, c / (n * n), n, Cc.h, rc);
         }
         if (fp32_res) {
-          const float *a = cf + 7 * c;
+          const float *a = cf + 8 * c;
           const float ai[6] = {a[0], a[1], a[2], a[3], a[4], a[5]};
           if (pass == 0)
-            cell_apply_s<float, double, float, 1, false>(phi, facc, Ff, ai, a[6] * (float)invV, e, f, eb, fb);
+            cell_apply_s<float, double, float, 1, false>(phi, facc, Ff, ai, a[6], e, f, eb, fb);
           else
-            cell_apply_s<float, double, float, 0, false>(phi, facc, Ff, ai, a[6] * (float)invV, e, f, eb, fb);
+            cell_apply_s<float, double, float, 0, false>(phi, facc, Ff, ai, a[6], e, f, eb, fb);
           if (curl_rhs)
 #pragma unroll
             for (int t = 0; t < 6; ++t) atomicAdd(facc + f[t], (float)-rc[t]);
@@ -648,9 +652,10 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
         cell_dofs(g, c, e, f);
         const bool eb[12] = {}, fb[6] = {};
         if constexpr (kMixed) {
-          const float *a = cf + 7 * c;
-          const float ai[6] = {a[0], a[1], a[2], a[3], a[4], a[5]};
-          dpart += cell_apply_s<float, float, float, 0, true>(zt, az, Ff, ai, a[6] * (float)invV, e, f, eb, fb);
+          const float4 c0 = reinterpret_cast<const float4 *>(cf)[2 * c];
+          const float4 c1 = reinterpret_cast<const float4 *>(cf)[2 * c + 1];
+          const float ai[6] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y};
+          dpart += cell_apply_s<float, float, float, 0, true>(zt, az, Ff, ai, c1.z, e, f, eb, fb);
         } else {
           const double *a = ag + 6 * (size_t)c;
           const double ai[6] = {a[0], a[1], a[2], a[3], a[4], a[5]};
