@@ -52,6 +52,8 @@ cudaError_t q1_adjoint_rhs_launch(const Q1Cell *cells, int ncells, const msfec_l
 cudaError_t q1_gradient_launch(const Q1Cell *cells, int ncells, const double *a, const double *phi, const double *sol,
                                const double *U, const double *lam, double *grad, cudaStream_t st);
 cudaError_t nedrt_solve_launch(bool fp64, const NRParams &prm, size_t smem, int grid, cudaStream_t st);
+cudaError_t nedrt_solve_launch_split(const NRParams &prm, size_t smem, int grid, cudaStream_t st);
+cudaError_t nedrt_split_occupancy(size_t smem, int *blocks_per_sm);
 cudaError_t nedrt_adjoint_prepare_launch(const NRCell *cells, int ncells, const double *phi, const double *U,
                                          const double *lam, const msfec_load &load, int npoints, const int *cell_of,
                                          const double *pts, const double *dJdu, const double *ainv6,
@@ -183,7 +185,8 @@ struct msfec_handle {
   // launch shapes picked by msfec_autotune ([precision][...]; -1 / 0 = default)
   int q1_split[2][2] = {{-1, -1}, {-1, -1}};  // [precision][has reaction]: 1 = split launches
   int nr_ctas[2][kNRMaxDepthCfg + 1] = {};    // [precision][deepest depth]: resident CTAs
-  int force_split = -1, force_ctas = 0;       // candidate under trial
+  int nr_split[kNRMaxDepthCfg + 1] = {-1, -1, -1, -1, -1};  // [deepest depth] mixed: 1 = two 256-thread CTAs/SM
+  int force_split = -1, force_ctas = 0, force_nr_split = -1;  // candidate under trial
   cudaStream_t aux_stream = nullptr;          // second stream of the split Q1 launch
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int last_graph = 0;  // 0 direct launches, 1 captured a new graph, 2 replayed
@@ -650,6 +653,7 @@ msfec_status q1_backward_impl(msfec_handle *h, int ncells, const msfec_cell *cel
 
 constexpr int kNRMaxDepth = 4;
 constexpr size_t kNRSmemLimit = 200 * 1024;
+constexpr size_t kNRSplitSmemLimit = 108 * 1024;  // two CTAs per SM (228 KB, minus static shared memory)
 
 msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cells, const double *d_ainv,
                               const double *d_bdiv, const msfec_load *load, double *d_KH, double *d_FH,
@@ -692,15 +696,28 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
   items.reserve((size_t)ncells * 18);
   for (int c : order)
     for (int b = 0; b < 18; ++b) items.push_back(NRItem{c, b, 0});
-  const size_t ws_floats = nr_workspace_floats(nmax, fp64 ? 8 : 4);
-  const bool use_smem = ws_floats * 4 <= kNRSmemLimit;
-  const size_t smem = use_smem ? ws_floats * 4 : 0;
+  int deepest = 0;
+  while ((1 << deepest) < nmax) ++deepest;
+  deepest = std::min(deepest, kNRMaxDepthCfg);
+  // mixed precision with a small enough item: two 256-thread CTAs per SM
+  // (split workspace) unless the autotuner chose the 512-thread CTA
+  const int split_sel = h->force_nr_split >= 0 ? h->force_nr_split : h->nr_split[deepest];
+  const bool split = !fp64 && nr_split_smem_floats(nmax) * 4 <= kNRSplitSmemLimit && split_sel != 0;
+  size_t ws_floats = nr_workspace_floats(nmax, fp64 ? 8 : 4);
+  bool use_smem = ws_floats * 4 <= kNRSmemLimit;
+  size_t smem = use_smem ? ws_floats * 4 : 0;
   cudaStream_t st = h->stream;
   int grid = std::min<int>((int)items.size(), h->num_sms);
-  if (!use_smem) {  // resident CTAs = workspace slots (L2 footprint), possibly autotuned
-    int deepest = 0;
-    while ((1 << deepest) < nmax) ++deepest;
-    const int cap = h->force_ctas > 0 ? h->force_ctas : h->nr_ctas[fp64 ? 0 : 1][std::min(deepest, kNRMaxDepthCfg)];
+  if (split) {
+    smem = nr_split_smem_floats(nmax) * 4;
+    ws_floats = nr_split_global_floats(nmax);  // global slot per CTA
+    use_smem = true;
+    int occ = 0;
+    MSFEC_CUDA_TRY(h, nedrt_split_occupancy(smem, &occ));
+    if (occ <= 0) return fail(h, MSFEC_ERROR_NOT_SUPPORTED, "split Ned_RT solver cannot be resident");
+    grid = std::min<int>((int)items.size(), occ * h->num_sms);
+  } else if (!use_smem) {  // resident CTAs = workspace slots (L2 footprint), possibly autotuned
+    const int cap = h->force_ctas > 0 ? h->force_ctas : h->nr_ctas[fp64 ? 0 : 1][deepest];
     if (cap > 0) grid = std::min(grid, cap);
   }
   MSFEC_CUDA_TRY(h, h->nr_cells.reserve(ncells));
@@ -709,7 +726,7 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
   MSFEC_CUDA_TRY(h, h->nr_phi.reserve((size_t)dofs * 18));
   MSFEC_CUDA_TRY(h, h->nr_y.reserve((size_t)dofs * 18));
   MSFEC_CUDA_TRY(h, h->nr_stats.reserve((size_t)ncells * 18));
-  if (!use_smem) MSFEC_CUDA_TRY(h, h->nr_scratch.reserve(ws_floats * grid));
+  if (!use_smem || split) MSFEC_CUDA_TRY(h, h->nr_scratch.reserve(ws_floats * grid));
   MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->nr_cells.ptr, hc.data(), hc.size() * sizeof(NRCell), cudaMemcpyHostToDevice, st));
   MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->nr_items.ptr, items.data(), items.size() * sizeof(NRItem),
                                     cudaMemcpyHostToDevice, st));
@@ -723,7 +740,7 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
   prm.phi = h->nr_phi.ptr;
   prm.y = h->nr_y.ptr;
   prm.stats = h->nr_stats.ptr;
-  prm.scratch = use_smem ? nullptr : h->nr_scratch.ptr;
+  prm.scratch = (use_smem && !split) ? nullptr : h->nr_scratch.ptr;
   prm.scratch_floats = ws_floats;
   prm.use_smem = use_smem ? 1 : 0;
   prm.rtol = h->cfg.nedrt_rtol;
@@ -732,7 +749,8 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
   prm.max_refine = h->cfg.max_refine;
   if (h->cfg.verbose)
     fprintf(stderr, "[msfec] nedrt plan: %d cells, %zu items, workspace %zu floats (%s), grid %d, %s\n", ncells,
-            items.size(), ws_floats, use_smem ? "shared" : "global", grid, fp64 ? "fp64" : "mixed");
+            items.size(), ws_floats, split ? "split, 2 CTAs/SM" : (use_smem ? "shared" : "global"), grid,
+            fp64 ? "fp64" : "mixed");
   msfec_load ld;
   if (load) {
     ld = *load;
@@ -742,7 +760,8 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
   auto seq = [&](bool timed) -> cudaError_t {
     cudaError_t e = cudaMemsetAsync(h->queue.ptr, 0, sizeof(int), st);
     if (e == cudaSuccess && timed) e = cudaEventRecord(h->ev[0], st);
-    if (e == cudaSuccess) e = nedrt_solve_launch(fp64, prm, smem, grid, st);
+    if (e == cudaSuccess)
+      e = split ? nedrt_solve_launch_split(prm, smem, grid, st) : nedrt_solve_launch(fp64, prm, smem, grid, st);
     if (e == cudaSuccess && timed) e = cudaEventRecord(h->ev[1], st);
     if (e == cudaSuccess)
       e = nedrt_galerkin_launch(h->nr_cells.ptr, ncells, h->nr_phi.ptr, h->nr_y.ptr, ld, d_KH, d_FH, d_rep,
@@ -1291,15 +1310,21 @@ msfec_status msfec_autotune(msfec_handle *h, int32_t kind, int32_t ncells, const
   for (int c = 0; c < ncells; ++c) deepest = std::max(deepest, (int)cells[c].depth);
   // candidates
   std::vector<int> cand;
+  bool nr_split_tune = false;
   if (kind == MSFEC_KIND_Q1) {
     const Q1Plan p = make_q1_plan(ncells, cells, fp64, coef1 != nullptr, true);
     cand = p.split ? std::vector<int>{0, 1} : std::vector<int>{0};
   } else {
     const int nmax = 1 << std::min(deepest, kNRMaxDepthCfg);
     const bool smem_ws = nr_workspace_floats(nmax, fp64 ? 8 : 4) * 4 <= kNRSmemLimit;
-    cand.push_back(h->num_sms);
-    if (!smem_ws)
-      for (int k : {7, 6, 5, 4}) cand.push_back(std::max(1, h->num_sms * k / 8));
+    nr_split_tune = !fp64 && nr_split_smem_floats(nmax) * 4 <= kNRSplitSmemLimit;
+    if (nr_split_tune) {
+      cand = {0, 1};  // one 512-thread CTA per SM, two 256-thread CTAs per SM
+    } else {
+      cand.push_back(h->num_sms);
+      if (!smem_ws)
+        for (int k : {7, 6, 5, 4}) cand.push_back(std::max(1, h->num_sms * k / 8));
+    }
   }
   choice[0] = 0;
   choice[1] = (int32_t)cand.size();
@@ -1313,6 +1338,8 @@ msfec_status msfec_autotune(msfec_handle *h, int32_t kind, int32_t ncells, const
   for (size_t k = 0; k < cand.size() && s == MSFEC_SUCCESS; ++k) {
     if (kind == MSFEC_KIND_Q1)
       h->force_split = cand[k];
+    else if (nr_split_tune)
+      h->force_nr_split = cand[k];
     else
       h->force_ctas = cand[k];
     msfec_timings t{};
@@ -1331,11 +1358,14 @@ msfec_status msfec_autotune(msfec_handle *h, int32_t kind, int32_t ncells, const
   }
   h->force_split = -1;
   h->force_ctas = 0;
+  h->force_nr_split = -1;
   h->graph_mode = graph0;
   msfec_set_timing(h, timing0 ? 1 : 0);
   if (s != MSFEC_SUCCESS) return s;
   if (kind == MSFEC_KIND_Q1)
     h->q1_split[fp64 ? 0 : 1][coef1 ? 1 : 0] = cand[choice[0]];
+  else if (nr_split_tune)
+    h->nr_split[std::min(deepest, kNRMaxDepthCfg)] = cand[choice[0]];
   else
     h->nr_ctas[fp64 ? 0 : 1][std::min(deepest, kNRMaxDepthCfg)] = cand[choice[0]] == h->num_sms ? 0 : cand[choice[0]];
   if (h->cfg.verbose)

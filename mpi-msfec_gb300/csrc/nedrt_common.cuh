@@ -85,4 +85,20 @@ __host__ __device__ inline size_t nr_workspace_floats(int n, int tsize) {
   return Np + 7 * Np * (size_t)(tsize / 4) + (8 * nc + al - 1) / al * al;
 }
 
+// Split workspace of the two-CTAs-per-SM mixed variant (256 threads): the
+// shared part holds the preconditioner and 6 FP32 Krylov vectors, the
+// per-CTA global slot the correction x and the 8 float coefficients per cell.
+__host__ __device__ inline size_t nr_split_smem_floats(int n) {
+  int NEx, NFx, NE, NF;
+  nr_counts(n, NEx, NFx, NE, NF);
+  const size_t Np = ((size_t)NE + NF + 63) / 64 * 64;
+  return 7 * Np;
+}
+__host__ __device__ inline size_t nr_split_global_floats(int n) {
+  int NEx, NFx, NE, NF;
+  nr_counts(n, NEx, NFx, NE, NF);
+  const size_t Np = ((size_t)NE + NF + 63) / 64 * 64;
+  return Np + (8 * (size_t)n * n * n + 63) / 64 * 64;
+}
+
 }  // namespace msfec

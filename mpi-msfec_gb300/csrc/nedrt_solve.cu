@@ -353,23 +353,28 @@ __device__ __forceinline__ void warp_publish(NRShared &sh, int slot, VT v) {
 }
 
 // Same summation order in every thread: identical decisions block-wide.
-template <typename VT>
+template <typename VT, int NW>
 __device__ __forceinline__ VT slot_total(const NRShared &sh, int slot) {
-  if constexpr (sizeof(VT) == 4) {  // 16 partials: four 16-byte loads, pairwise sums
-    static_assert(kNRWarps == 16, "slot_total reads 16 float partials");
+  if constexpr (sizeof(VT) == 4) {  // NW partials: 16-byte loads, pairwise sums
+    static_assert(NW == 16 || NW == 8, "slot_total reads 8 or 16 float partials");
     const float4 *p = reinterpret_cast<const float4 *>(sh.fslot[slot]);
-    const float4 a = p[0], b = p[1], c = p[2], d = p[3];
-    return ((a.x + a.y) + (a.z + a.w)) + ((b.x + b.y) + (b.z + b.w)) + (((c.x + c.y) + (c.z + c.w)) +
-                                                                       ((d.x + d.y) + (d.z + d.w)));
+    const float4 a = p[0], b = p[1];
+    const float s8 = ((a.x + a.y) + (a.z + a.w)) + ((b.x + b.y) + (b.z + b.w));
+    if constexpr (NW == 8) {
+      return s8;
+    } else {
+      const float4 c = p[2], d = p[3];
+      return s8 + (((c.x + c.y) + (c.z + c.w)) + ((d.x + d.y) + (d.z + d.w)));
+    }
   } else {
     VT s = VT(0);
 #pragma unroll
-    for (int w = 0; w < kNRWarps; ++w) s += sh.dslot[slot][w];
+    for (int w = 0; w < NW; ++w) s += sh.dslot[slot][w];
     return s;
   }
 }
 
-template <typename VT, int NV>
+template <typename VT, int NV, int NW>
 __device__ __forceinline__ void block_sum(NRShared &sh, VT (&v)[NV], VT (&out)[NV]) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -391,7 +396,7 @@ __device__ __forceinline__ void block_sum(NRShared &sh, VT (&v)[NV], VT (&out)[N
   for (int t = 0; t < NV; ++t) {
     VT s = VT(0);
 #pragma unroll
-    for (int w = 0; w < kNRWarps; ++w) {
+    for (int w = 0; w < NW; ++w) {
       if constexpr (sizeof(VT) == 4)
         s += sh.fred[w][t];
       else
@@ -406,8 +411,13 @@ extern __shared__ __align__(256) unsigned char nr_dyn_smem[];
 // One (cell, basis) item. SMEM: the workspace is the dynamic shared memory
 // (known at compile time, so every vector access is a shared-memory access),
 // otherwise this CTA's slot of the global scratch.
-template <typename T, bool SMEM>
+template <typename T, bool SMEM, int NT>
 __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
+  // NT = 256 (two CTAs per SM, mixed precision, shared workspace): the
+  // correction x and the float coefficients live in this CTA's global slot so
+  // that the shared part (preconditioner + 6 vectors) fits twice per SM.
+  constexpr bool kSplitWs = NT == 256;
+  constexpr int NW = NT / 32;
   float *ws = SMEM ? reinterpret_cast<float *>(nr_dyn_smem) : prm.scratch + (size_t)blockIdx.x * prm.scratch_floats;
   const NRItem it = prm.items[item_id];
   const NRCell Cc = prm.cells[it.cell];
@@ -432,8 +442,9 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
   T *vB = vA + Np;
   T *wA = vB + Np;  // MINRES directions w_{j-1}, w_j (roles swap)
   T *wB = wA + Np;
-  T *xk = wB + Np;
-  float *cf = ws + Np + 7 * Np * (sizeof(T) / 4);
+  float *gws = prm.scratch + (size_t)blockIdx.x * prm.scratch_floats;  // split workspace only
+  T *xk = kSplitWs ? reinterpret_cast<T *>(gws) : wB + Np;
+  float *cf = kSplitWs ? gws + Np * (sizeof(T) / 4) : ws + Np + 7 * Np * (sizeof(T) / 4);
   double *dacc = reinterpret_cast<double *>(ws + Np);  // FP64 residual accumulator, aliases zt..
   const NRFactors<float> &Ff = sh.Ff;
   const NRFactors<double> &Fd = sh.Fd;
@@ -450,7 +461,7 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
   double *yout = prm.y + 18 * Cc.dof_off + (size_t)bb * N;
 
   // tables
-  for (int t = tid; t < 144 + 72; t += kNRThreads) {
+  for (int t = tid; t < 144 + 72; t += NT) {
     if (t < 144) {
       const int p = t / 48, q = (t / 16) % 3, l4 = (t / 4) % 4, m4 = t % 4;
       const double v = table_G(Cc.h, p, q, l4, m4);
@@ -463,18 +474,18 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
       sh.Cf[l][f] = (float)v;
     }
   }
-  for (int c = tid; c < nc; c += kNRThreads) {
+  for (int c = tid; c < nc; c += NT) {
 #pragma unroll
     for (int q = 0; q < 6; ++q) cf[8 * c + q] = (float)ag[6 * (size_t)c + q];
     cf[8 * c + 6] = (float)(bg[c] * invV);  // B / |K|
     cf[8 * c + 7] = 0.0f;
   }
-  for (int d = tid; d < (int)Np; d += kNRThreads) pd[d] = 0.0f;  // pad [N, Np) stays 0
+  for (int d = tid; d < (int)Np; d += NT) pd[d] = 0.0f;  // pad [N, Np) stays 0
   __syncthreads();
 
   // ---- block-Jacobi preconditioner: diag(M) on edges, then the lumped Schur
   // diagonal D_ff + sum_l C_lf^2 / M_ll on faces (cell-local approximation).
-  for (int c = tid; c < nc; c += kNRThreads) {
+  for (int c = tid; c < nc; c += NT) {
     int e[12], f[6];
     cell_dofs(g, c, e, f);
     const float *a = cf + 8 * c;
@@ -483,7 +494,7 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
     for (int l = 0; l < 12; ++l) atomicAdd(pd + e[l], Ad[l >> 2] * sh.Gf[l >> 2][l >> 2][l & 3][l & 3]);
   }
   __syncthreads();
-  for (int c = tid; c < nc; c += kNRThreads) {
+  for (int c = tid; c < nc; c += NT) {
     int e[12], f[6];
     cell_dofs(g, c, e, f);
     const float bdv = cf[8 * c + 6];
@@ -499,7 +510,7 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
     }
   }
   __syncthreads();
-  for (int d = tid; d < N; d += kNRThreads) {
+  for (int d = tid; d < N; d += NT) {
     int dir, i, j, k;
     const bool bnd = dof_geometry(g, d, dir, i, j, k);
     pd[d] = bnd ? 0.0f : 1.0f / pd[d];
@@ -514,7 +525,7 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
     // ---------------- residual r = f - A phi on the interior ----------------
     if (ir == 0) {
       // phi0 = coarse function on every DoF (satisfies the boundary data)
-      for (int d = tid; d < N; d += kNRThreads) {
+      for (int d = tid; d < N; d += NT) {
         int dir, i, j, k;
         dof_geometry(g, d, dir, i, j, k);
         phi[d] = src ? 0.0 : coarse_dof(bb, dir, i, j, k, n);
@@ -526,12 +537,12 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
       // pass 0: lift of the boundary data only (scale of the stopping test)
       // accumulator starts at -f for a source item (r = f - A phi)
       if (fp32_res) {
-        for (int d = tid; d < N; d += kNRThreads) facc[d] = src ? (float)-fsrc[d] : 0.0f;
+        for (int d = tid; d < N; d += NT) facc[d] = src ? (float)-fsrc[d] : 0.0f;
       } else {
-        for (int d = tid; d < N; d += kNRThreads) dacc[d] = src ? -fsrc[d] : 0.0;
+        for (int d = tid; d < N; d += NT) dacc[d] = src ? -fsrc[d] : 0.0;
       }
       __syncthreads();
-      for (int c = tid; c < nc; c += kNRThreads) {
+      for (int c = tid; c < nc; c += NT) {
         int e[12], f[6];
         cell_dofs(g, c, e, f);
         bool eb[12], fb[6];
@@ -574,7 +585,7 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
       }
       __syncthreads();
       // r = -(A phi - f) on interior DoFs (boundary: 0), kept in vA
-      for (int d = tid; d < (int)Np; d += kNRThreads) {
+      for (int d = tid; d < (int)Np; d += NT) {
         const bool interior = pd[d] > 0.0f;  // false on the pad [N, Np)
         const double r = interior ? -(fp32_res ? (double)facc[d] : dacc[d]) : 0.0;
         part[pass] += r * r;
@@ -586,7 +597,7 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
     }
     {
       double tot[2];
-      block_sum<double, 2>(sh, part, tot);
+      block_sum<double, 2, NW>(sh, part, tot);
       if (ir == 0) bnorm2 = tot[0];
       // a source right-hand side that cancelled to rounding is solved to rtol of
       // its cell's adjoint scale, not of its own (noise-level) norm
@@ -609,7 +620,7 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
     // The Lanczos vectors are kept unnormalised (v_j = v~_j / g_j, g_j =
     // gamma_j), so there is no normalisation pass; each phase's reduction is
     // published per warp and summed by every thread after the barrier.
-    for (int d = tid; d < (int)Np; d += kNRThreads) {  // pads included: the float4 passes cover [0, Np)
+    for (int d = tid; d < (int)Np; d += NT) {  // pads included: the float4 passes cover [0, Np)
       vB[d] = T(0);
       wA[d] = T(0);
       wB[d] = T(0);
@@ -621,13 +632,13 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
     T gam;                 // gamma_j
     {
       T p1[1] = {T(0)};
-      for (int d = tid; d < (int)Np; d += kNRThreads) {
+      for (int d = tid; d < (int)Np; d += NT) {
         const T z = (T)pd[d] * vc[d];
         zt[d] = z;
         p1[0] += z * vc[d];
       }
       T t1[1];
-      block_sum<T, 1>(sh, p1, t1);
+      block_sum<T, 1, NW>(sh, p1, t1);
       gam = sqrt(t1[0]);
     }
     const T eta0 = gam;
@@ -647,7 +658,7 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
     for (int iter = 0; active && iter < prm.max_iter; ++iter) {
       // ---- phase 1
       T dpart = T(0);
-      for (int c = tid; c < nc; c += kNRThreads) {
+      for (int c = tid; c < nc; c += NT) {
         int e[12], f[6];
         cell_dofs(g, c, e, f);
         const bool eb[12] = {}, fb[6] = {};
@@ -669,7 +680,7 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
           float4 *wo4 = reinterpret_cast<float4 *>(wo);
           const float4 *wc4 = reinterpret_cast<const float4 *>(wc);
           float4 *xk4 = reinterpret_cast<float4 *>(xk);
-          for (int q = tid; q < (int)(Np / 4); q += kNRThreads) {
+          for (int q = tid; q < (int)(Np / 4); q += NT) {
             const float4 pv = pd4[q], v = vp4[q], a = wo4[q], b = wc4[q];
             float4 x = xk4[q], wn;
             wn.x = (pv.x * v.x * gi_p - p_a3 * a.x - p_a2 * b.x) * p_ia1;
@@ -684,7 +695,7 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
             xk4[q] = x;
           }
         } else {
-          for (int d = tid; d < N; d += kNRThreads) {
+          for (int d = tid; d < N; d += NT) {
             const T z = (T)pd[d] * vp[d] * gi_p;
             const T wn = (z - p_a3 * wo[d] - p_a2 * wc[d]) * p_ia1;
             wo[d] = wn;
@@ -697,7 +708,7 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
       }
       warp_publish<T>(sh, 0, dpart);
       __syncthreads();
-      const T delta = slot_total<T>(sh, 0) * gi_c * gi_c;
+      const T delta = slot_total<T, NW>(sh, 0) * gi_c * gi_c;
       // ---- phase 2
       T gpart = T(0);
       const T gg = gam * gi_p;
@@ -707,7 +718,7 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
         float4 *vp4 = reinterpret_cast<float4 *>(vp);
         float4 *az4 = reinterpret_cast<float4 *>(az);
         float4 *zt4 = reinterpret_cast<float4 *>(zt);
-        for (int q = tid; q < (int)(Np / 4); q += kNRThreads) {
+        for (int q = tid; q < (int)(Np / 4); q += NT) {
           const float4 pv = pd4[q], a = az4[q], c = vc4[q], v = vp4[q];
           const int d0 = 4 * q;
           auto lane = [&](float pdd, float ad, float cd, float vd, int d) {
@@ -729,7 +740,7 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
           gpart += z.x * vn.x + z.y * vn.y + z.z * vn.z + z.w * vn.w;
         }
       } else {
-        for (int d = tid; d < N; d += kNRThreads) {
+        for (int d = tid; d < N; d += NT) {
           const float pdd = pd[d];
           T vn = T(0);
           if (pdd > 0.0f) {
@@ -745,7 +756,7 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
       }
       warp_publish<T>(sh, 1, gpart);
       __syncthreads();
-      const T gnew = sqrt(fmax(slot_total<T>(sh, 1), T(0)));
+      const T gnew = sqrt(fmax(slot_total<T, NW>(sh, 1), T(0)));
       const T a0 = cc * delta - c_prev * ss * gam;
       const T a1 = sqrt(a0 * a0 + gnew * gnew);
       const T a2 = ss * delta + c_prev * cc * gam;
@@ -777,23 +788,23 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
       if (fabs(eta) <= target || gnew == T(0)) active = false;
     }
     if (pending)
-      for (int d = tid; d < N; d += kNRThreads) {
+      for (int d = tid; d < N; d += NT) {
         const T z = (T)pd[d] * vp[d] * gi_p;
         const T wn = (z - p_a3 * wo[d] - p_a2 * wc[d]) * p_ia1;
         xk[d] += p_step * wn;
       }
     __syncthreads();
     // ---------------- phi_I += x (FP64, HBM) ----------------
-    for (int d = tid; d < N; d += kNRThreads)
+    for (int d = tid; d < N; d += NT)
       if (pd[d] > 0.0f) phi[d] += (double)xk[d];
     __syncthreads();
   }
 
   // ---------------- y_b = A P_b (FP64), P_b = primary block of basis b ----------------
   if (!src) {  // block-uniform
-    for (int d = tid; d < N; d += kNRThreads) dacc[d] = 0.0;
+    for (int d = tid; d < N; d += NT) dacc[d] = 0.0;
     __syncthreads();
-    for (int c = tid; c < nc; c += kNRThreads) {
+    for (int c = tid; c < nc; c += NT) {
       int e[12], f[6];
       cell_dofs(g, c, e, f);
       const bool eb[12] = {}, fb[6] = {};
@@ -805,7 +816,7 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
         cell_apply_s<double, double, double, 3, false>(phi, dacc, Fd, ai, bg[c] * invV, e, f, eb, fb);
     }
     __syncthreads();
-    for (int d = tid; d < N; d += kNRThreads) yout[d] = dacc[d];
+    for (int d = tid; d < N; d += NT) yout[d] = dacc[d];
   }
   if (tid == 0) {
     NRStat st;
@@ -819,18 +830,22 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
   __syncthreads();
 }
 
-template <typename T>
-__global__ void __launch_bounds__(kNRThreads, 1) nedrt_solve_kernel(NRParams prm) {
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT, 512 / NT) nedrt_solve_kernel(NRParams prm) {
   __shared__ NRShared sh;
   for (;;) {
     if (threadIdx.x == 0) sh.item = atomicAdd(prm.queue, 1);
     __syncthreads();
     const int item = sh.item;
     if (item >= prm.n_items) break;
-    if (prm.use_smem)
-      solve_item<T, true>(prm, sh, item);
-    else
-      solve_item<T, false>(prm, sh, item);
+    if constexpr (NT == 256) {
+      solve_item<T, true, 256>(prm, sh, item);  // split workspace: shared vectors + global x / coefficients
+    } else {
+      if (prm.use_smem)
+        solve_item<T, true, NT>(prm, sh, item);
+      else
+        solve_item<T, false, NT>(prm, sh, item);
+    }
   }
 }
 
@@ -1289,17 +1304,38 @@ __global__ void __launch_bounds__(kAdjThreads) nr_adj_gradient_kernel(const NRCe
 
 cudaError_t nedrt_solve_launch(bool fp64, const NRParams &prm, size_t smem, int grid, cudaStream_t st) {
   if (fp64) {
-    auto k = nrimpl::nedrt_solve_kernel<double>;
+    auto k = nrimpl::nedrt_solve_kernel<double, kNRThreads>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     k<<<grid, kNRThreads, smem, st>>>(prm);
   } else {
-    auto k = nrimpl::nedrt_solve_kernel<float>;
+    auto k = nrimpl::nedrt_solve_kernel<float, kNRThreads>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     k<<<grid, kNRThreads, smem, st>>>(prm);
   }
   return cudaGetLastError();
+}
+
+// Mixed precision, two 256-thread CTAs per SM with the split workspace
+// (shared: preconditioner + 6 FP32 vectors; global slot: x + coefficients).
+cudaError_t nedrt_solve_launch_split(const NRParams &prm, size_t smem, int grid, cudaStream_t st) {
+  auto k = nrimpl::nedrt_solve_kernel<float, 256>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  if (e != cudaSuccess) return e;
+  k<<<grid, 256, smem, st>>>(prm);
+  return cudaGetLastError();
+}
+
+cudaError_t nedrt_split_occupancy(size_t smem, int *blocks_per_sm) {
+  auto k = nrimpl::nedrt_solve_kernel<float, 256>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k, 256, smem);
 }
 
 cudaError_t nedrt_galerkin_launch(const NRCell *cells, int ncells, const double *phi, const double *y,

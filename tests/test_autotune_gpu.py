@@ -59,6 +59,13 @@ def test_nedrt_autotune_global_workspace(gpu):
     KH0, _, _, _ = gpu.Handle(precision=gpu.PRECISION_FP64).nedrt_build(cells, ainv6, bdiv, load)
     for c in range(len(cells)):
         assert _rel(KH[c], KH0[c]) <= 1e-11
-    # shared-memory workspace (mixed, depth 3): a single candidate, no trial builds
+    # mixed depth 3 (shared workspace): one 512-thread CTA or two 256-thread CTAs per SM
     h2 = gpu.Handle()
-    assert h2.autotune(gpu.KIND_NEDRT, cells, ainv6, bdiv, load)[:2] == (0, 1)
+    choice, ncand, times = h2.autotune(gpu.KIND_NEDRT, cells, ainv6, bdiv, load)
+    assert ncand == 2 and choice in (0, 1) and all(t > 0 for t in times), (choice, times)
+    print("nedrt autotune (mixed, depth 3): 512x1 %.1f ms, 256x2 %.1f ms -> %d" % (times[0], times[1], choice))
+    KH2, _, rep2, st2 = h2.nedrt_build(cells, ainv6, bdiv, load)
+    KH20, _, _, _ = gpu.Handle().nedrt_build(cells, ainv6, bdiv, load)
+    assert st2 == gpu.SUCCESS and rep2["converged"].all()
+    for c in range(len(cells)):
+        assert _rel(KH2[c], KH20[c]) <= 1e-11
