@@ -74,6 +74,16 @@ std::vector<char> boundary(int m) {
 
 }  // namespace
 
+// Global coarse DoF indices of cell (i, j, k) of the m^3 grid, for the
+// assembly and for set_global_weights (18 weights per cell).
+extern "C" int msfec_host_nedrt_cell_dofs(int m, int cell, int *g18) {
+  if (m < 1 || cell < 0 || cell >= m * m * m || !g18) return 1;
+  int g[18];
+  cell_map(m, cell % m, (cell / m) % m, cell / (m * m), g);
+  for (int t = 0; t < 18; ++t) g18[t] = g[t];
+  return 0;
+}
+
 extern "C" int msfec_host_nedrt_coarse_solve(int m, const double *KH, const double *FH, double *U, double rtol,
                                              int max_iter, int *iters) {
   if (m < 1 || !KH || !FH || !U) return 1;

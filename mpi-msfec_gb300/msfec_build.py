@@ -19,6 +19,7 @@ LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libmsfec_cuda.so")
 HOSTLIB = os.path.join(LIBDIR, "libmsfec_host.so")
 EXAMPLE = os.path.join(LIBDIR, "example_q1")
+EXAMPLE_NR = os.path.join(LIBDIR, "example_nedrt")
 HOST = os.path.join(HERE, "host")
 CXX = os.environ.get("CXX", "g++")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
@@ -82,14 +83,15 @@ def build_host(objs=()):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("host shim build failed:\n" + r.stderr)
-    ex = os.path.join(HOST, "example_q1.cpp")
-    if not os.path.exists(EXAMPLE) or os.path.getmtime(ex) > os.path.getmtime(EXAMPLE) or \
-            os.path.getmtime(HOSTLIB) > os.path.getmtime(EXAMPLE):
-        cmd = [CXX, "-O2", "-std=c++17", "-I", INCLUDE, "-o", EXAMPLE, ex, "-L", LIBDIR, "-lmsfec_host",
-               "-lmsfec_cuda", "-Wl,-rpath,$ORIGIN"]
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError("example build failed:\n" + r.stderr)
+    for src_name, out in (("example_q1.cpp", EXAMPLE), ("example_nedrt.cpp", EXAMPLE_NR)):
+        ex = os.path.join(HOST, src_name)
+        if not os.path.exists(out) or os.path.getmtime(ex) > os.path.getmtime(out) or \
+                os.path.getmtime(HOSTLIB) > os.path.getmtime(out):
+            cmd = [CXX, "-O2", "-std=c++17", "-I", INCLUDE, "-o", out, ex, "-L", LIBDIR, "-lmsfec_host",
+                   "-lmsfec_cuda", "-Wl,-rpath,$ORIGIN"]
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError("example build failed:\n" + r.stderr)
 
 
 if __name__ == "__main__":

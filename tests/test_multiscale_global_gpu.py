@@ -75,3 +75,26 @@ def test_qbasis_shim_example_driver(gpu):
     KH, FH, rep, st = h.q1_build(cells, acoef, None, gpu.make_load(gpu.LOAD_SIN_PRODUCT, (1, 1, 0, 0)))
     assert abs(res["KH0_00"] - KH[0, 0, 0]) <= 1e-12 * abs(KH[0, 0, 0])
     assert res["coarse_cg_iterations"] > 0 and np.isfinite(res["u_centre"])
+
+
+def test_nedrtbasis_shim_example_driver(gpu):
+    """The C++ NedRTBasis-compatible shim driver (run, getters, host coarse
+    solve, set_global_weights, fine sigma/u) against the same build through the
+    Python view of the ABI and the host coarse solver."""
+    import msfec_build
+    m, depth = 2, 2
+    out = subprocess.run([msfec_build.EXAMPLE_NR, str(m), str(depth)], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    res = json.loads(out.stdout.strip().splitlines()[-1])
+    cells = workloads.coarse_grid(m, depth)
+    cen = workloads.fine_centres(cells)
+    a = 1.0 / (1.0 + 0.5 * np.sin(20.0 * cen[:, 0]) * np.sin(17.0 * cen[:, 1]))
+    ainv6 = np.stack([a, a, a, 0 * a, 0 * a, 0 * a], 1)
+    bdiv = 1.0 - 0.9 * np.sin(2 * np.pi * 14.0 * cen[:, 0])
+    load = gpu.make_load(gpu.LOAD_VEC_TRIG, (1, 1, 0, 0))
+    KH, FH, rep, st = gpu.Handle().nedrt_build(cells, ainv6, bdiv, load)
+    assert st == gpu.SUCCESS and rep["converged"].all()
+    assert abs(res["KH0_1212"] - KH[0, 12, 12]) <= 1e-12 * abs(KH[0, 12, 12])
+    U = nedrt_coarse_solve(m, KH, FH, rtol=1e-12)
+    assert abs(res["U_norm"] - np.linalg.norm(U)) <= 1e-9 * np.linalg.norm(U)
+    assert res["coarse_minres_iterations"] > 0 and res["fine_u_norm"] > 0
