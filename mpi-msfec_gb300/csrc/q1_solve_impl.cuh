@@ -514,6 +514,31 @@ __device__ void solve_item(const Q1Params &prm, Q1Shared &sh, unsigned char *sme
       double part[2][R];
 #pragma unroll
       for (int t = 0; t < R; ++t) part[0][t] = part[1][t] = 0.0;
+      if (!fp32_res && ir > 0) {
+        // Refinement residual in FP64: the Krylov thread -> (column, rhs) map
+        // and a z-column sweep whose coefficient layer sums slide from one
+        // plane to the next (half the FP64 layer-sum work of a per-node
+        // apply, entries grouped by the 8 stiffness patterns). Writes y = K phi.
+        double acc = 0.0;
+#pragma unroll
+        for (int s = 0; s < UMAX; ++s) {
+          if (!cval[s]) continue;
+          double q[PMAX], ctr[PMAX];
+          column_apply_f64<R, PMAX, HAS_R>(slab_d, ag, rg, n, rho, ci[s], cj[s], P, cd, mmd, q, ctr);
+#pragma unroll
+          for (int pk = 0; pk < PMAX; ++pk)
+            if (pk < P) {
+              const size_t gnode = ((size_t)(k0 + pk) * N1 + cj[s]) * N1 + ci[s];
+              const double f = src ? __ldg(f_c + (size_t)(it.rhs0 + rho) * nn + gnode) : 0.0;
+              const double rr = f - q[pk];
+              xs[own_idx(s, pk) * R + rho] = (T)rr;
+              acc += rr * rr;
+              if (!src) y_c[(size_t)(it.rhs0 + rho) * nn + gnode] = q[pk];
+            }
+        }
+#pragma unroll
+        for (int t = 0; t < R; ++t) part[1][t] = t == rho ? acc : 0.0;
+      } else
       for (size_t e = tid; e < own_nodes; e += kQ1Threads) {
         const int pk = (int)(e / ncol), col = (int)(e % ncol);
         const int i = col % m + 1, j = col / m + 1, k = k0 + pk;
