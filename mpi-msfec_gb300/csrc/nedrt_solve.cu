@@ -35,10 +35,9 @@ struct NRFactors {
 struct NRShared {
   double wred[kNRWarps][3];
   float fred[kNRWarps][3];  // float slots: no FP64 instruction in the FP32 Krylov loop
-  double G[3][3][4][4];  // edge-mass geometry: M_e = sum_pq A^-1_pq G[p][q]
-  double C[12][6];       // (curl tau_l, v_f) on the fine cell
-  float Gf[3][3][4][4];
-  float Cf[12][6];
+  // closed-form element tables of the current item's cell (preconditioner setup):
+  float Gf[3][3][4][4];  // edge-mass geometry: M_e = sum_pq A^-1_pq Gf[p][q]
+  float Cf[12][6];       // (curl tau_l, v_f) on the fine cell
   NRFactors<float> Ff;  // tensor-product factors of the current item's cell
   NRFactors<double> Fd;
   alignas(16) float fslot[2][kNRWarps];  // per-warp partials of the two fused MINRES reductions
@@ -465,12 +464,10 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
     if (t < 144) {
       const int p = t / 48, q = (t / 16) % 3, l4 = (t / 4) % 4, m4 = t % 4;
       const double v = table_G(Cc.h, p, q, l4, m4);
-      sh.G[p][q][l4][m4] = v;
       sh.Gf[p][q][l4][m4] = (float)v;
     } else {
       const int u = t - 144, l = u / 6, f = u % 6;
       const double v = table_C(Cc.h, l, f);
-      sh.C[l][f] = v;
       sh.Cf[l][f] = (float)v;
     }
   }
