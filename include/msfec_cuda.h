@@ -374,6 +374,39 @@ msfec_status msfec_nedrt_backward(msfec_handle *handle, int32_t ncells,
                                   const double *dJ_du, double *grad_a,
                                   double *grad_b);
 
+/*
+ * Q1 x Nedelec (Q_Ned) basis build from host buffers (synchronous). Replaces
+ * QNedBasis::run (source/Q_Ned/q_ned_basis.cc) for every cell of the batch,
+ * followed by get_global_element_matrix / get_global_element_rhs.
+ *   a6     A per fine cell, 6 doubles (a00 a11 a22 a01 a02 a12), SPD: the
+ *          curl-curl weight (the reference's Diffusion_A)
+ *   binv   B^-1 per fine cell (> 0): the sigma mass weight (DiffusionInverse_B)
+ *   load   MSFEC_LOAD_ZERO or MSFEC_LOAD_VEC_TRIG (global load (v, f), F_H only)
+ *   KH     [ncells][20][20]: rows/cols 0..7 coarse vertices (H1 bases,
+ *          GeometryInfo<3>), 8..19 coarse lines (curl bases); FH [ncells][20]
+ *          (vertex rows 0)
+ * Depth 1..4. Tolerance nedrt_rtol (the same mixed-form solver).
+ */
+msfec_status msfec_qned_build(msfec_handle *handle, int32_t ncells,
+                              const msfec_cell *cells, const double *a6,
+                              const double *binv, const msfec_load *load,
+                              double *KH, double *FH,
+                              msfec_cell_report *reports);
+
+/* Device-pointer variant (asynchronous on the handle's stream); cells on the host. */
+msfec_status msfec_qned_build_device(msfec_handle *handle, int32_t ncells,
+                                     const msfec_cell *cells, const double *d_a6,
+                                     const double *d_binv,
+                                     const msfec_load *load, double *d_KH,
+                                     double *d_FH,
+                                     msfec_cell_report *d_reports);
+
+/* Basis of the last Q_Ned build: per cell 20 rows of NV + NE fine DoFs
+   (vertices i + (n+1)(j + (n+1)k), then edges x|y|z). */
+int64_t msfec_qned_basis_size(const msfec_handle *handle);
+msfec_status msfec_qned_get_basis(msfec_handle *handle, double *Phi,
+                                  int64_t capacity);
+
 /* Basis of the last Ned_RT build: per cell 18 rows (coarse basis order) of
    NE + NF fine DoFs (edges x|y|z then faces x|y|z, lexicographic), sigma and u
    of every basis function. Size in doubles, and copy to host. */

@@ -17,6 +17,7 @@
 #include "../../include/msfec_cuda.h"
 #include "nedrt_common.cuh"
 #include "q1_common.cuh"
+#include "qned_common.cuh"
 
 namespace msfec {
 cudaError_t q1_solve_launch_f32_c1(bool has_r, const Q1Params &prm, size_t smem, int grid, cudaStream_t st);
@@ -53,6 +54,10 @@ cudaError_t q1_gradient_launch(const Q1Cell *cells, int ncells, const double *a,
                                const double *U, const double *lam, double *grad, cudaStream_t st);
 cudaError_t nedrt_solve_launch(bool fp64, const NRParams &prm, size_t smem, int grid, cudaStream_t st);
 cudaError_t nedrt_solve_launch_split(const NRParams &prm, size_t smem, int grid, cudaStream_t st);
+cudaError_t qned_solve_launch(bool fp64, const QNParams &prm, size_t smem, int grid, cudaStream_t st);
+cudaError_t qned_galerkin_launch(const NRCell *cells, int ncells, const double *phi, const double *y,
+                                 const msfec_load &load, double *eload, double *KH, double *FH,
+                                 msfec_cell_report *rep, const NRStat *stats, cudaStream_t st);
 cudaError_t nedrt_split_occupancy(size_t smem, int *blocks_per_sm);
 cudaError_t nedrt_adjoint_prepare_launch(const NRCell *cells, int ncells, const double *phi, const double *U,
                                          const double *lam, const msfec_load &load, int npoints, const int *cell_of,
@@ -170,6 +175,13 @@ struct msfec_handle {
       nra_floor;
   DevBuf<int> nra_cell;
   DevBuf<NRItem> nra_items;
+  // Q_Ned state of the last build
+  DevBuf<NRCell> qn_cells;
+  DevBuf<NRItem> qn_items;
+  DevBuf<double> qn_phi, qn_y, qn_eload, qn_a6, qn_binv, qn_KH, qn_FH;
+  DevBuf<NRStat> qn_stats;
+  DevBuf<float> qn_scratch;
+  int64_t qn_basis_doubles = 0;
   int q1_ncells = 0;
   int64_t q1_basis_doubles = 0;
   std::vector<Q1Cell> h_cells;
@@ -778,6 +790,99 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
   return MSFEC_SUCCESS;
 }
 
+
+// Q_Ned batch: plan (cells deepest first, 20 items per cell), launches.
+msfec_status qned_build_impl(msfec_handle *h, int ncells, const msfec_cell *cells, const double *d_a6,
+                             const double *d_binv, const msfec_load *load, double *d_KH, double *d_FH,
+                             msfec_cell_report *d_rep) {
+  const bool fp64 = h->cfg.precision == MSFEC_PRECISION_FP64;
+  std::vector<NRCell> hc(ncells);
+  int64_t fine = 0, dofs = 0;
+  int nmax = 0;
+  for (int c = 0; c < ncells; ++c) {
+    NRCell &q = hc[c];
+    const int n = 1 << cells[c].depth;
+    for (int d = 0; d < 3; ++d) {
+      q.origin[d] = cells[c].origin[d];
+      q.h[d] = cells[c].size[d] / n;
+    }
+    q.depth = cells[c].depth;
+    q.n = n;
+    q.coef_off = fine;
+    q.dof_off = dofs;
+    int NV, NEx, NE;
+    qn_counts(n, NV, NEx, NE);
+    fine += (int64_t)n * n * n;
+    dofs += NV + NE;
+    nmax = std::max(nmax, n);
+  }
+  std::vector<int> order(ncells);
+  for (int c = 0; c < ncells; ++c) order[c] = c;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cells[x].depth > cells[y].depth; });
+  std::vector<NRItem> items;
+  items.reserve((size_t)ncells * kQNBases);
+  for (int c : order)
+    for (int b = 0; b < kQNBases; ++b) items.push_back(NRItem{c, b, 0});
+  const size_t ws_floats = qn_workspace_floats(nmax, fp64 ? 8 : 4);
+  const bool use_smem = ws_floats * 4 <= kNRSmemLimit;
+  const size_t smem = use_smem ? ws_floats * 4 : 0;
+  const int grid = std::min<int>((int)items.size(), h->num_sms);
+  cudaStream_t st = h->stream;
+  MSFEC_CUDA_TRY(h, h->qn_cells.reserve(ncells));
+  MSFEC_CUDA_TRY(h, h->qn_items.reserve(items.size()));
+  MSFEC_CUDA_TRY(h, h->queue.reserve(2));
+  MSFEC_CUDA_TRY(h, h->qn_phi.reserve((size_t)dofs * kQNBases));
+  MSFEC_CUDA_TRY(h, h->qn_y.reserve((size_t)dofs * kQNBases));
+  MSFEC_CUDA_TRY(h, h->qn_eload.reserve((size_t)dofs));
+  MSFEC_CUDA_TRY(h, h->qn_stats.reserve((size_t)ncells * kQNBases));
+  if (!use_smem) MSFEC_CUDA_TRY(h, h->qn_scratch.reserve(ws_floats * grid));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->qn_cells.ptr, hc.data(), hc.size() * sizeof(NRCell), cudaMemcpyHostToDevice, st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->qn_items.ptr, items.data(), items.size() * sizeof(NRItem),
+                                    cudaMemcpyHostToDevice, st));
+  MSFEC_CUDA_TRY(h, cudaMemsetAsync(h->queue.ptr, 0, sizeof(int), st));
+  MSFEC_CUDA_TRY(h, cudaMemsetAsync(h->qn_eload.ptr, 0, (size_t)dofs * sizeof(double), st));
+  QNParams prm{};
+  prm.cells = h->qn_cells.ptr;
+  prm.items = h->qn_items.ptr;
+  prm.n_items = (int)items.size();
+  prm.queue = h->queue.ptr;
+  prm.a6 = d_a6;
+  prm.binv = d_binv;
+  prm.phi = h->qn_phi.ptr;
+  prm.y = h->qn_y.ptr;
+  prm.stats = h->qn_stats.ptr;
+  prm.scratch = use_smem ? nullptr : h->qn_scratch.ptr;
+  prm.scratch_floats = ws_floats;
+  prm.use_smem = use_smem ? 1 : 0;
+  prm.rtol = h->cfg.nedrt_rtol;
+  prm.inner_rtol = h->cfg.inner_rtol;
+  prm.max_iter = std::max(h->cfg.max_iter, 8000);
+  prm.max_refine = h->cfg.max_refine;
+  if (h->cfg.verbose)
+    fprintf(stderr, "[msfec] qned plan: %d cells, %zu items, workspace %zu floats (%s), grid %d, %s\n", ncells,
+            items.size(), ws_floats, use_smem ? "shared" : "global", grid, fp64 ? "fp64" : "mixed");
+  msfec_load ld;
+  if (load) {
+    ld = *load;
+  } else {
+    std::memset(&ld, 0, sizeof(ld));
+  }
+  if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[0], st));
+  MSFEC_CUDA_TRY(h, qned_solve_launch(fp64, prm, smem, grid, st));
+  if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[1], st));
+  MSFEC_CUDA_TRY(h, qned_galerkin_launch(h->qn_cells.ptr, ncells, h->qn_phi.ptr, h->qn_y.ptr, ld, h->qn_eload.ptr,
+                                         d_KH, d_FH, d_rep, h->qn_stats.ptr, st));
+  if (h->timing) {
+    MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[2], st));
+    MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[3], st));
+  }
+  h->ev_recorded = h->timing;
+  h->last_launches = d_rep ? 4 : 3;
+  h->last_graph = 0;
+  h->qn_basis_doubles = dofs * kQNBases;
+  return MSFEC_SUCCESS;
+}
+
 bool nr_load_ok(const msfec_load *l) {
   return !l || l->kind == MSFEC_LOAD_ZERO || l->kind == MSFEC_LOAD_VEC_TRIG;
 }
@@ -892,6 +997,12 @@ void msfec_destroy(msfec_handle *h) {
       b->release();
     h->nra_cell.release();
     h->nra_items.release();
+    h->qn_cells.release();
+    h->qn_items.release();
+    for (DevBuf<double> *b : {&h->qn_phi, &h->qn_y, &h->qn_eload, &h->qn_a6, &h->qn_binv, &h->qn_KH, &h->qn_FH})
+      b->release();
+    h->qn_stats.release();
+    h->qn_scratch.release();
     h->q1_graph.reset();
     h->nr_graph.reset();
     if (h->aux_stream) cudaStreamSynchronize(h->aux_stream);
@@ -1541,6 +1652,87 @@ msfec_status msfec_nedrt_backward(msfec_handle *h, int32_t ncells, const msfec_c
                         std::to_string(q.iters) + " iterations, " + std::to_string(q.refinements) +
                         " refinements)");
     }
+  return MSFEC_SUCCESS;
+}
+
+msfec_status msfec_qned_build_device(msfec_handle *h, int32_t ncells, const msfec_cell *cells, const double *d_a6,
+                                     const double *d_binv, const msfec_load *load, double *d_KH, double *d_FH,
+                                     msfec_cell_report *d_reports) {
+  if (!h) return MSFEC_ERROR_INVALID_ARGUMENT;
+  if (ncells < 0 || (ncells > 0 && (!cells || !d_a6 || !d_binv || !d_KH || !d_FH)))
+    return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "null pointer or negative cell count");
+  for (int c = 0; c < ncells; ++c)
+    if (!cell_ok(cells[c]) || cells[c].depth > kNRMaxDepth)
+      return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "cell " + std::to_string(c) + " invalid (Q_Ned depth 1..4)");
+  if (!load_ok(load) || !nr_load_ok(load)) return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "invalid Q_Ned load");
+  if (ncells == 0) {
+    h->qn_basis_doubles = 0;
+    return MSFEC_SUCCESS;
+  }
+  DeviceGuard g(h->device);
+  return qned_build_impl(h, ncells, cells, d_a6, d_binv, load, d_KH, d_FH, d_reports);
+}
+
+msfec_status msfec_qned_build(msfec_handle *h, int32_t ncells, const msfec_cell *cells, const double *a6,
+                              const double *binv, const msfec_load *load, double *KH, double *FH,
+                              msfec_cell_report *reports) {
+  if (!h) return MSFEC_ERROR_INVALID_ARGUMENT;
+  if (ncells < 0 || (ncells > 0 && (!cells || !a6 || !binv || !KH || !FH)))
+    return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "null pointer or negative cell count");
+  int64_t nfine = 0;
+  for (int c = 0; c < ncells; ++c) {
+    if (!cell_ok(cells[c]) || cells[c].depth > kNRMaxDepth)
+      return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "cell " + std::to_string(c) + " invalid (Q_Ned depth 1..4)");
+    const int64_t n = 1LL << cells[c].depth;
+    nfine += n * n * n;
+  }
+  if (!load_ok(load) || !nr_load_ok(load)) return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "invalid Q_Ned load");
+  for (int64_t e = 0; e < nfine; ++e) {
+    const double *a = a6 + 6 * e;
+    const double m1 = a[0], m2 = a[0] * a[1] - a[3] * a[3];
+    const double m3 = a[0] * (a[1] * a[2] - a[5] * a[5]) - a[3] * (a[3] * a[2] - a[5] * a[4]) +
+                      a[4] * (a[3] * a[5] - a[1] * a[4]);
+    bool ok = m1 > 0.0 && m2 > 0.0 && m3 > 0.0 && binv[e] > 0.0 && std::isfinite(binv[e]);
+    for (int q = 0; q < 6; ++q) ok = ok && std::isfinite(a[q]);
+    if (!ok) return fail(h, MSFEC_ERROR_NUMERICAL, "A not SPD / finite or B^-1 not positive at fine cell " + std::to_string(e));
+  }
+  if (ncells == 0) return msfec_qned_build_device(h, 0, cells, nullptr, nullptr, load, nullptr, nullptr, nullptr);
+  DeviceGuard g(h->device);
+  cudaStream_t st = h->stream;
+  MSFEC_CUDA_TRY(h, h->qn_a6.reserve(nfine * 6));
+  MSFEC_CUDA_TRY(h, h->qn_binv.reserve(nfine));
+  MSFEC_CUDA_TRY(h, h->qn_KH.reserve((size_t)ncells * kQNBases * kQNBases));
+  MSFEC_CUDA_TRY(h, h->qn_FH.reserve((size_t)ncells * kQNBases));
+  MSFEC_CUDA_TRY(h, h->rep.reserve(ncells));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->qn_a6.ptr, a6, nfine * 6 * sizeof(double), cudaMemcpyHostToDevice, st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->qn_binv.ptr, binv, nfine * sizeof(double), cudaMemcpyHostToDevice, st));
+  msfec_status s = qned_build_impl(h, ncells, cells, h->qn_a6.ptr, h->qn_binv.ptr, load, h->qn_KH.ptr, h->qn_FH.ptr,
+                                   h->rep.ptr);
+  if (s != MSFEC_SUCCESS) return s;
+  std::vector<msfec_cell_report> rep(ncells);
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(KH, h->qn_KH.ptr, (size_t)ncells * kQNBases * kQNBases * sizeof(double),
+                                    cudaMemcpyDeviceToHost, st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(FH, h->qn_FH.ptr, (size_t)ncells * kQNBases * sizeof(double),
+                                    cudaMemcpyDeviceToHost, st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(rep.data(), h->rep.ptr, (size_t)ncells * sizeof(msfec_cell_report),
+                                    cudaMemcpyDeviceToHost, st));
+  MSFEC_CUDA_TRY(h, cudaStreamSynchronize(st));
+  if (reports) std::memcpy(reports, rep.data(), rep.size() * sizeof(msfec_cell_report));
+  for (const auto &r : rep)
+    if (!r.converged) return fail(h, MSFEC_ERROR_NOT_CONVERGED, "at least one Q_Ned local solve missed nedrt_rtol");
+  return MSFEC_SUCCESS;
+}
+
+int64_t msfec_qned_basis_size(const msfec_handle *h) { return h ? h->qn_basis_doubles : 0; }
+
+msfec_status msfec_qned_get_basis(msfec_handle *h, double *Phi, int64_t capacity) {
+  if (!h || !Phi) return MSFEC_ERROR_INVALID_ARGUMENT;
+  if (h->qn_basis_doubles <= 0) return fail(h, MSFEC_ERROR_INVALID_STATE, "no Q_Ned basis built yet");
+  if (capacity < h->qn_basis_doubles) return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "capacity too small");
+  DeviceGuard g(h->device);
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(Phi, h->qn_phi.ptr, h->qn_basis_doubles * sizeof(double), cudaMemcpyDeviceToHost,
+                                    h->stream));
+  MSFEC_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
   return MSFEC_SUCCESS;
 }
 

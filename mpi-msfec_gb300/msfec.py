@@ -39,6 +39,7 @@ EXPORTED = [
     "msfec_nedrt_build", "msfec_nedrt_build_device", "msfec_nedrt_basis_size",
     "msfec_nedrt_get_basis", "msfec_q1_backward", "msfec_nedrt_build_noalloc",
     "msfec_set_graph", "msfec_autotune", "msfec_q1_fine_solve", "msfec_nedrt_backward",
+    "msfec_qned_build", "msfec_qned_build_device", "msfec_qned_basis_size", "msfec_qned_get_basis",
 ]
 
 
@@ -143,6 +144,12 @@ def load_library(path: str = LIB_PATH):
     L.msfec_nedrt_backward.argtypes = [_vp, ctypes.c_int32, _vp, _dp, _dp, ctypes.POINTER(Load), ctypes.c_int32,
                                        _dp, _dp, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32), _dp, _dp, _dp, _dp]
     L.msfec_nedrt_backward.restype = ctypes.c_int
+    L.msfec_qned_build.argtypes = [_vp, ctypes.c_int32, _vp, _dp, _dp, ctypes.POINTER(Load), _dp, _dp, _vp]
+    L.msfec_qned_build.restype = ctypes.c_int
+    L.msfec_qned_basis_size.argtypes = [_vp]
+    L.msfec_qned_basis_size.restype = ctypes.c_int64
+    L.msfec_qned_get_basis.argtypes = [_vp, _dp, ctypes.c_int64]
+    L.msfec_qned_get_basis.restype = ctypes.c_int
     L.msfec_set_graph.argtypes = [_vp, ctypes.c_int32]
     L.msfec_set_graph.restype = ctypes.c_int
     _lib = L
@@ -368,6 +375,26 @@ class Handle:
                                                  _vp(d_ainv6), _vp(d_bdiv), ctypes.byref(load),
                                                  _vp(d_KH), _vp(d_FH), _vp(d_reports or 0))
         return self.check(st)
+
+    def qned_build(self, cells, a6, binv, load):
+        """Q_Ned basis build from host arrays; returns (KH [c,20,20], FH [c,20], reports, status)."""
+        cells = np.ascontiguousarray(cells, dtype=CELL_DTYPE)
+        a6 = np.ascontiguousarray(a6, dtype=np.float64)
+        binv = np.ascontiguousarray(binv, dtype=np.float64)
+        nc = cells.shape[0]
+        KH = np.zeros((nc, 20, 20))
+        FH = np.zeros((nc, 20))
+        rep = np.zeros(nc, dtype=REPORT_DTYPE)
+        st = self._lib.msfec_qned_build(self._h, nc, cells.ctypes.data_as(_vp), _d(a6), _d(binv),
+                                        ctypes.byref(load), _d(KH), _d(FH), rep.ctypes.data_as(_vp))
+        self.check(st, allow=(ERROR_NOT_CONVERGED,))
+        return KH, FH, rep, st
+
+    def qned_basis(self):
+        n = self._lib.msfec_qned_basis_size(self._h)
+        out = np.zeros(n)
+        self.check(self._lib.msfec_qned_get_basis(self._h, _d(out), n))
+        return out
 
     def nedrt_basis(self):
         n = self._lib.msfec_nedrt_basis_size(self._h)

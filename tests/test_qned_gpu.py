@@ -1,0 +1,55 @@
+"""GPU parity of the Q_Ned (Q1 sigma x Nedelec u) basis build against the FP64
+oracle (C ABI). Stated tolerances (both precisions; mixed = FP32 MINRES +
+FP64 refinement): K_H, F_H max abs error <= 1e-9 * max |entry| of the cell;
+basis max|phi - phi_oracle| <= 1e-8 * max|phi_oracle| per function."""
+import numpy as np
+import pytest
+
+import workloads
+from oracle import nedrt_oracle as NR
+from oracle import qned_oracle as Q
+
+pytestmark = pytest.mark.gpu
+TOL_KH = 1e-9
+TOL_PHI = 1e-8
+
+
+def _rel(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def _coefs(cells, seed):
+    """A (SPD tensor, from the Ned_RT workload's A^-1) and B^-1 per fine cell."""
+    cen = workloads.fine_centres(cells)
+    rng = np.random.default_rng(seed)
+    nf = cen.shape[0]
+    g = rng.standard_normal((nf, 3))
+    R = workloads.haar_rotations(rng, nf)
+    A = np.einsum("cij,cj,ckj->cik", R, np.exp(0.5 * g), R)
+    a6 = NR.ainv_to_sym6(A)
+    binv = 1.0 / (1.0 - 0.9 * np.sin(2 * np.pi * 14.0 * cen[:, 0]))
+    return A, a6, binv
+
+
+@pytest.mark.parametrize("precision", ("mixed", "fp64"))
+@pytest.mark.parametrize("m,depth", [(1, 2), (1, 3)])
+def test_qned_basis_matches_oracle(gpu, precision, m, depth):
+    cells = workloads.coarse_grid(m, depth)
+    A, a6, binv = _coefs(cells, seed=7 + depth)
+    load = gpu.make_load(gpu.LOAD_VEC_TRIG, (1.0, 1.0, 0.0, 0.0))
+    h = gpu.Handle(precision=gpu.PRECISION_MIXED if precision == "mixed" else gpu.PRECISION_FP64)
+    KH, FH, rep, st = h.qned_build(cells, a6, binv, load)
+    assert st == gpu.SUCCESS and rep["converged"].all(), rep
+    ref = Q.build(cells, binv, A, load.kind, list(load.params))
+    for c in range(len(cells)):
+        assert _rel(KH[c], ref["KH"][c]) <= TOL_KH, (c, _rel(KH[c], ref["KH"][c]))
+        assert _rel(FH[c], ref["FH"][c]) <= TOL_KH
+    phi = h.qned_basis()
+    off = 0
+    for c, po in enumerate(ref["Phi"]):
+        pg = phi[off:off + po.size].reshape(po.shape)
+        off += po.size
+        for b in range(20):
+            assert _rel(pg[b], po[b]) <= TOL_PHI, (c, b, _rel(pg[b], po[b]))
+    print(f"{precision} depth {depth}: max K_H rel err {max(_rel(KH[c], ref['KH'][c]) for c in range(len(cells))):.2e}, "
+          f"max iterations {rep['iterations'].max()}")
