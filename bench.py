@@ -77,6 +77,11 @@ class Workload:
             self.kind = "nedrt"
             self.cells, self.ainv6, self.bdiv, self.load = workloads.nedrt_tensor(m=16, depth=4, seed=5)
             self.cfg = {"workload": "nedrt_tensor_coarse16^3_L4_18rhs", "coarse_cells": 4096, "depth": 4, "seed": 5}
+        elif name == "qned_small":
+            self.kind = "qned"
+            self.cells, self.a6, self.binv, self.load = workloads.qned_tensor(m=8, depth=3, seed=2)
+            self.cfg = {"workload": "qned_tensor_coarse8^3_L3_20rhs", "coarse_cells": 512, "depth": 3, "seed": 2,
+                        "B^-1": "1/(1-0.9 sin(2 pi 14 x))", "load": "vec trig"}
         elif name == "q1_uneven":
             self.kind = "q1"
             self.cells, self.a, self.r, self.load = workloads.q1_uneven(m=16, seed=3)
@@ -99,12 +104,16 @@ class Workload:
     def work(self, lo=0, hi=None):
         import workloads
         c = self.cells[lo:hi]
+        if self.kind == "qned":
+            return workloads.qned_work_dof_rhs(c)
         return workloads.nedrt_work_dof_rhs(c) if self.kind == "nedrt" else workloads.work_dof_rhs(c)
 
     def per_cell_work(self):
         n = 1 << self.cells["depth"].astype(np.int64)
         if self.kind == "nedrt":
             return (3 * n * (n + 1) ** 2 + 3 * n * n * (n + 1)) * 18
+        if self.kind == "qned":
+            return ((n + 1) ** 3 + 3 * n * (n + 1) ** 2) * 20
         return (n + 1) ** 3 * 8
 
     def shard(self, lo, hi):
@@ -113,6 +122,9 @@ class Workload:
         if self.kind == "nedrt":
             out["ainv6"] = np.ascontiguousarray(self.ainv6[f0:f1])
             out["bdiv"] = np.ascontiguousarray(self.bdiv[f0:f1])
+        elif self.kind == "qned":
+            out["a6"] = np.ascontiguousarray(self.a6[f0:f1])
+            out["binv"] = np.ascontiguousarray(self.binv[f0:f1])
         else:
             out["a"] = np.ascontiguousarray(self.a[f0:f1])
             out["r"] = None if self.r is None else np.ascontiguousarray(self.r[f0:f1])
@@ -256,7 +268,7 @@ def gpu_run(wl, lo, hi, precision, steps, warmup, local, stream, barrier, tune_i
     h = msfec.Handle(precision=precision, device=local)
     h.set_stream(stream.cuda_stream)
     h.set_timing(True)
-    nr = 18 if wl.kind == "nedrt" else 8
+    nr = {"nedrt": 18, "qned": 20}.get(wl.kind, 8)
     d_KH = torch.zeros((nc, nr, nr), dtype=torch.float64, device="cuda")
     d_FH = torch.zeros((nc, nr), dtype=torch.float64, device="cuda")
     d_rep = torch.zeros(max(1, nc) * msfec.REPORT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
@@ -267,6 +279,13 @@ def gpu_run(wl, lo, hi, precision, steps, warmup, local, stream, barrier, tune_i
         def step():
             h.nedrt_build_device(cells, d_x.data_ptr(), d_y.data_ptr(), wl.load, d_KH.data_ptr(),
                                  d_FH.data_ptr(), d_rep.data_ptr())
+    elif wl.kind == "qned":
+        d_x = torch.from_numpy(sh["a6"]).cuda()
+        d_y = torch.from_numpy(sh["binv"]).cuda()
+
+        def step():
+            h.qned_build_device(cells, d_x.data_ptr(), d_y.data_ptr(), wl.load, d_KH.data_ptr(),
+                                d_FH.data_ptr(), d_rep.data_ptr())
     else:
         d_x = torch.from_numpy(sh["a"]).cuda()
         d_y = None if sh["r"] is None else torch.from_numpy(sh["r"]).cuda()
@@ -274,7 +293,7 @@ def gpu_run(wl, lo, hi, precision, steps, warmup, local, stream, barrier, tune_i
         def step():
             h.q1_build_device(cells, d_x.data_ptr(), 0 if d_y is None else d_y.data_ptr(), wl.load,
                               d_KH.data_ptr(), d_FH.data_ptr(), d_rep.data_ptr())
-    if tune_info is not None and nc > 0:
+    if tune_info is not None and nc > 0 and wl.kind != "qned":
         import sharding
         k = min(nc, 64 if wl.kind == "nedrt" else 512)  # several waves of items, seconds of trials
         f = int(sharding.fine_offsets(cells)[k])
@@ -347,9 +366,14 @@ def roofline(wl, lo, hi, solve_ms, gal_ms, rep, kind):
     if wl.kind == "nedrt":
         ndof = int(np.sum(3 * n * (n + 1) ** 2 + 3 * n * n * (n + 1)))
         nrhs, coef_bytes = 18, 7 * 8
-        # FP32 flops of one MINRES iteration of one item: cell operator (2 x 336 per
-        # fine cell) + vector recurrences (~30 per DoF)
-        flops_iter = 2 * 336 * n ** 3 + 30 * (3 * n * (n + 1) ** 2 + 3 * n * n * (n + 1))
+        # FP32 flops of one MINRES iteration of one item: tensor-product cell operator
+        # fused with the delta dot product (~330 per fine cell) + recurrences (~20 per DoF)
+        flops_iter = 330 * n ** 3 + 20 * (3 * n * (n + 1) ** 2 + 3 * n * n * (n + 1))
+    elif wl.kind == "qned":
+        ndof = int(np.sum((n + 1) ** 3 + 3 * n * (n + 1) ** 2))
+        nrhs, coef_bytes = 20, 7 * 8
+        # factored cell operator (vertex mass, M_N Grad, C^T M_RT C, dot: ~300 per fine cell)
+        flops_iter = 300 * n ** 3 + 20 * ((n + 1) ** 3 + 3 * n * (n + 1) ** 2)
     else:
         ndof = int(np.sum((n + 1) ** 3))
         nrhs, coef_bytes = 8, 8 * (1 if wl.r is None else 2)
@@ -359,7 +383,7 @@ def roofline(wl, lo, hi, solve_ms, gal_ms, rep, kind):
     alg_solve = nfine * coef_bytes + ndof * nrhs * 8 * 2
     alg_gal = ndof * nrhs * 8 * 2 + len(c) * (nrhs * nrhs + nrhs) * 8
     iters = rep["iterations"].astype(np.float64)  # max over the cell's RHS (upper estimate)
-    per_cell_flops = flops_iter * iters * (nrhs if wl.kind == "nedrt" else 8)
+    per_cell_flops = flops_iter * iters * (nrhs if wl.kind in ("nedrt", "qned") else 8)
     tflops = float(np.sum(per_cell_flops)) / (solve_ms * 1e-3) / 1e12
     return {"bound": "hbm", "kernel": f"{kind}_solve_kernel (persistent, on-chip Krylov state)",
             "achieved": alg_solve / (solve_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
@@ -591,8 +615,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="nedrt_small",
-                    choices=["nedrt_small", "nedrt_l4", "nedrt_large", "q1_uneven", "q1_small", "q1_adjoint_fwd"])
-    ap.add_argument("--extra", default="q1_uneven", help="comma-separated workloads reported beside the headline")
+                    choices=["nedrt_small", "nedrt_l4", "nedrt_large", "qned_small", "q1_uneven", "q1_small",
+                             "q1_adjoint_fwd"])
+    ap.add_argument("--extra", default="q1_uneven,qned_small",
+                    help="comma-separated workloads reported beside the headline")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")

@@ -390,6 +390,13 @@ class Handle:
         self.check(st, allow=(ERROR_NOT_CONVERGED,))
         return KH, FH, rep, st
 
+    def qned_build_device(self, cells, d_a6, d_binv, load, d_KH, d_FH, d_reports):
+        cells = np.ascontiguousarray(cells, dtype=CELL_DTYPE)
+        st = self._lib.msfec_qned_build_device(self._h, cells.shape[0], cells.ctypes.data_as(_vp),
+                                               _vp(d_a6), _vp(d_binv), ctypes.byref(load),
+                                               _vp(d_KH), _vp(d_FH), _vp(d_reports or 0))
+        return self.check(st)
+
     def qned_basis(self):
         n = self._lib.msfec_qned_basis_size(self._h)
         out = np.zeros(n)

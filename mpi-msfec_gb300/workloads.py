@@ -121,6 +121,27 @@ def nedrt_tensor(m=8, depth=3, seed=2, kb=14.0):
     return cells, ainv6, bdiv, load
 
 
+def qned_tensor(m=8, depth=3, seed=2, kb=14.0):
+    """Q_Ned workload; returns cells, A as [fine, 6] (a00 a11 a22 a01 a02 a12; A = R diag(e^g) R^T,
+    g ~ N(0, 1/4), R Haar), B^-1 = 1 / (1 - 0.9 sin(2 pi 14 x)), vector trig load."""
+    rng = np.random.default_rng(seed)
+    cells = coarse_grid(m, depth)
+    nf = int(np.sum(fine_counts(cells)[0]))
+    g = 0.5 * rng.standard_normal((nf, 3))
+    Rr = haar_rotations(rng, nf)
+    A = np.einsum("cij,cj,ckj->cik", Rr, np.exp(g), Rr)
+    a6 = np.stack([A[:, 0, 0], A[:, 1, 1], A[:, 2, 2], A[:, 0, 1], A[:, 0, 2], A[:, 1, 2]], 1)
+    x = fine_centres(cells)[:, 0]
+    binv = 1.0 / (1.0 - 0.9 * np.sin(2 * np.pi * kb * x))
+    load = make_load(LOAD_VEC_TRIG, (1.0, 1.0, 0.0, 0.0))
+    return cells, a6, binv, load
+
+
+def qned_work_dof_rhs(cells):
+    n = 1 << cells["depth"].astype(np.int64)
+    return int(np.sum((n + 1) ** 3 + 3 * n * (n + 1) ** 2) * 20)
+
+
 def nedrt_work_dof_rhs(cells):
     n = 1 << cells["depth"].astype(np.int64)
     return int(np.sum(3 * n * (n + 1) ** 2 + 3 * n * n * (n + 1)) * 18)
