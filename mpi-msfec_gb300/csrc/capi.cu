@@ -54,7 +54,8 @@ cudaError_t q1_gradient_launch(const Q1Cell *cells, int ncells, const double *a,
                                const double *U, const double *lam, double *grad, cudaStream_t st);
 cudaError_t nedrt_solve_launch(bool fp64, const NRParams &prm, size_t smem, int grid, cudaStream_t st);
 cudaError_t nedrt_solve_launch_split(const NRParams &prm, size_t smem, int grid, cudaStream_t st);
-cudaError_t qned_solve_launch(bool fp64, const QNParams &prm, size_t smem, int grid, cudaStream_t st);
+cudaError_t qned_solve_launch(bool fp64, bool two_per_sm, const QNParams &prm, size_t smem, int grid,
+                              cudaStream_t st);
 cudaError_t qned_galerkin_launch(const NRCell *cells, int ncells, const double *phi, const double *y,
                                  const msfec_load &load, double *eload, double *KH, double *FH,
                                  msfec_cell_report *rep, const NRStat *stats, cudaStream_t st);
@@ -826,7 +827,9 @@ msfec_status qned_build_impl(msfec_handle *h, int ncells, const msfec_cell *cell
   const size_t ws_floats = qn_workspace_floats(nmax, fp64 ? 8 : 4);
   const bool use_smem = ws_floats * 4 <= kNRSmemLimit;
   const size_t smem = use_smem ? ws_floats * 4 : 0;
-  const int grid = std::min<int>((int)items.size(), h->num_sms);
+  // mixed precision with a workspace that fits twice per SM: two 256-thread CTAs per SM
+  const bool two_per_sm = !fp64 && use_smem && smem <= kNRSplitSmemLimit;
+  const int grid = std::min<int>((int)items.size(), (two_per_sm ? 2 : 1) * h->num_sms);
   cudaStream_t st = h->stream;
   MSFEC_CUDA_TRY(h, h->qn_cells.reserve(ncells));
   MSFEC_CUDA_TRY(h, h->qn_items.reserve(items.size()));
@@ -860,7 +863,8 @@ msfec_status qned_build_impl(msfec_handle *h, int ncells, const msfec_cell *cell
   prm.max_refine = h->cfg.max_refine;
   if (h->cfg.verbose)
     fprintf(stderr, "[msfec] qned plan: %d cells, %zu items, workspace %zu floats (%s), grid %d, %s\n", ncells,
-            items.size(), ws_floats, use_smem ? "shared" : "global", grid, fp64 ? "fp64" : "mixed");
+            items.size(), ws_floats, two_per_sm ? "shared, 2 CTAs/SM" : (use_smem ? "shared" : "global"), grid,
+            fp64 ? "fp64" : "mixed");
   msfec_load ld;
   if (load) {
     ld = *load;
@@ -868,7 +872,7 @@ msfec_status qned_build_impl(msfec_handle *h, int ncells, const msfec_cell *cell
     std::memset(&ld, 0, sizeof(ld));
   }
   if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[0], st));
-  MSFEC_CUDA_TRY(h, qned_solve_launch(fp64, prm, smem, grid, st));
+  MSFEC_CUDA_TRY(h, qned_solve_launch(fp64, two_per_sm, prm, smem, grid, st));
   if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[1], st));
   MSFEC_CUDA_TRY(h, qned_galerkin_launch(h->qn_cells.ptr, ncells, h->qn_phi.ptr, h->qn_y.ptr, ld, h->qn_eload.ptr,
                                          d_KH, d_FH, d_rep, h->qn_stats.ptr, st));

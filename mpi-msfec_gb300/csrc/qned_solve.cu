@@ -309,11 +309,11 @@ __device__ __forceinline__ void warp_publish(QNShared &sh, int slot, VT v) {
   }
 }
 
-template <typename VT>
+template <typename VT, int NW>
 __device__ __forceinline__ VT slot_total(const QNShared &sh, int slot) {
   VT s = VT(0);
 #pragma unroll
-  for (int w = 0; w < kQNWarps; ++w) {
+  for (int w = 0; w < NW; ++w) {
     if constexpr (sizeof(VT) == 4)
       s += sh.fslot[slot][w];
     else
@@ -322,7 +322,7 @@ __device__ __forceinline__ VT slot_total(const QNShared &sh, int slot) {
   return s;
 }
 
-template <typename VT, int NV>
+template <typename VT, int NV, int NW>
 __device__ __forceinline__ void block_sum(QNShared &sh, VT (&v)[NV], VT (&out)[NV]) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -343,7 +343,7 @@ __device__ __forceinline__ void block_sum(QNShared &sh, VT (&v)[NV], VT (&out)[N
   for (int t = 0; t < NV; ++t) {
     VT s = VT(0);
 #pragma unroll
-    for (int w = 0; w < kQNWarps; ++w) {
+    for (int w = 0; w < NW; ++w) {
       if constexpr (sizeof(VT) == 4)
         s += sh.fred[w][t];
       else
@@ -355,9 +355,11 @@ __device__ __forceinline__ void block_sum(QNShared &sh, VT (&v)[NV], VT (&out)[N
 
 extern __shared__ __align__(256) unsigned char qn_dyn_smem[];
 
-template <typename T, bool SMEM>
+// NT = 512 (one CTA per SM) or 256 (two CTAs per SM, whose barriers and
+// scalar recurrences then overlap; the depth-3 workspace fits twice).
+template <typename T, bool SMEM, int NT>
 __device__ void solve_item(const QNParams &prm, QNShared &sh, int item_id) {
-  constexpr int NT = kQNThreads;
+  constexpr int NW = NT / 32;
   float *ws = SMEM ? reinterpret_cast<float *>(qn_dyn_smem) : prm.scratch + (size_t)blockIdx.x * prm.scratch_floats;
   const NRItem it = prm.items[item_id];
   const NRCell Cc = prm.cells[it.cell];
@@ -539,7 +541,7 @@ __device__ void solve_item(const QNParams &prm, QNShared &sh, int item_id) {
     }
     {
       double tot[2];
-      block_sum<double, 2>(sh, part, tot);
+      block_sum<double, 2, NW>(sh, part, tot);
       if (ir == 0) bnorm2 = tot[0];
       rnorm2 = tot[1];
     }
@@ -566,7 +568,7 @@ __device__ void solve_item(const QNParams &prm, QNShared &sh, int item_id) {
         p1[0] += z * vc[d];
       }
       T t1[1];
-      block_sum<T, 1>(sh, p1, t1);
+      block_sum<T, 1, NW>(sh, p1, t1);
       gam = sqrt(t1[0]);
     }
     const T eta0 = gam;
@@ -609,7 +611,7 @@ __device__ void solve_item(const QNParams &prm, QNShared &sh, int item_id) {
       }
       warp_publish<T>(sh, 0, dpart);
       __syncthreads();
-      const T delta = slot_total<T>(sh, 0) * gi_c * gi_c;
+      const T delta = slot_total<T, NW>(sh, 0) * gi_c * gi_c;
       T gpart = T(0);
       const T gg = gam * gi_p;
       for (int d = tid; d < N; d += NT) {
@@ -627,7 +629,7 @@ __device__ void solve_item(const QNParams &prm, QNShared &sh, int item_id) {
       }
       warp_publish<T>(sh, 1, gpart);
       __syncthreads();
-      const T gnew = sqrt(fmax(slot_total<T>(sh, 1), T(0)));
+      const T gnew = sqrt(fmax(slot_total<T, NW>(sh, 1), T(0)));
       const T a0 = cc * delta - c_prev * ss * gam;
       const T a1 = sqrt(a0 * a0 + gnew * gnew);
       const T a2 = ss * delta + c_prev * cc * gam;
@@ -698,18 +700,22 @@ __device__ void solve_item(const QNParams &prm, QNShared &sh, int item_id) {
   __syncthreads();
 }
 
-template <typename T>
-__global__ void __launch_bounds__(kQNThreads, 1) qned_solve_kernel(QNParams prm) {
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT, 512 / NT) qned_solve_kernel(QNParams prm) {
   __shared__ QNShared sh;
   for (;;) {
     if (threadIdx.x == 0) sh.item = atomicAdd(prm.queue, 1);
     __syncthreads();
     const int item = sh.item;
     if (item >= prm.n_items) break;
-    if (prm.use_smem)
-      solve_item<T, true>(prm, sh, item);
-    else
-      solve_item<T, false>(prm, sh, item);
+    if constexpr (NT == 256) {
+      solve_item<T, true, 256>(prm, sh, item);
+    } else {
+      if (prm.use_smem)
+        solve_item<T, true, NT>(prm, sh, item);
+      else
+        solve_item<T, false, NT>(prm, sh, item);
+    }
   }
 }
 
@@ -866,14 +872,24 @@ __global__ void qned_report_kernel(const NRStat *__restrict__ stats, int ncells,
 
 }  // namespace qnimpl
 
-cudaError_t qned_solve_launch(bool fp64, const QNParams &prm, size_t smem, int grid, cudaStream_t st) {
+cudaError_t qned_solve_launch(bool fp64, bool two_per_sm, const QNParams &prm, size_t smem, int grid,
+                              cudaStream_t st) {
+  if (two_per_sm) {  // mixed precision, shared workspace that fits twice per SM
+    auto k = qnimpl::qned_solve_kernel<float, 256>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (e != cudaSuccess) return e;
+    k<<<grid, 256, smem, st>>>(prm);
+    return cudaGetLastError();
+  }
   if (fp64) {
-    auto k = qnimpl::qned_solve_kernel<double>;
+    auto k = qnimpl::qned_solve_kernel<double, kQNThreads>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     k<<<grid, kQNThreads, smem, st>>>(prm);
   } else {
-    auto k = qnimpl::qned_solve_kernel<float>;
+    auto k = qnimpl::qned_solve_kernel<float, kQNThreads>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     k<<<grid, kQNThreads, smem, st>>>(prm);
