@@ -407,6 +407,42 @@ int64_t msfec_qned_basis_size(const msfec_handle *handle);
 msfec_status msfec_qned_get_basis(msfec_handle *handle, double *Phi,
                                   int64_t capacity);
 
+/*
+ * Raviart-Thomas x DQ0 (RT_DQ) basis build from host buffers (synchronous).
+ * Replaces RTDQBasis::run (source/RT_DQ/rt_dq_basis.cc:1114-1216) for every
+ * cell of the batch, followed by get_global_element_matrix /
+ * get_global_element_rhs (:1096-1106).
+ *   ainv6  A^-1 per fine cell, 6 doubles (a00 a11 a22 a01 a02 a12), SPD: the
+ *          sigma mass weight (the reference's DiffusionInverse_A); the
+ *          reaction rate is 0 (source/equation_data/eqn_coeff_R.cc:7-14)
+ *   load   MSFEC_LOAD_ZERO, _CONSTANT or _SIN_PRODUCT (scalar global load
+ *          (v, f), F_H only)
+ *   KH     [ncells][7][7]: rows/cols 0..5 coarse faces (GeometryInfo<3>
+ *          face order), 6 the coarse DQ0 value; FH [ncells][7] (face rows 0)
+ * The local problems are pure-Neumann ones (is_laplace): sigma is unique,
+ * the local pressure is fixed up to a constant and, as in the reference
+ * (set_u_to_std, :1039-1044), the stored u block of every basis is 1.
+ * Depth 1..4. Tolerance nedrt_rtol (the same mixed-form solver).
+ */
+msfec_status msfec_rtdq_build(msfec_handle *handle, int32_t ncells,
+                              const msfec_cell *cells, const double *ainv6,
+                              const msfec_load *load, double *KH, double *FH,
+                              msfec_cell_report *reports);
+
+/* Device-pointer variant (asynchronous on the handle's stream); cells on the host. */
+msfec_status msfec_rtdq_build_device(msfec_handle *handle, int32_t ncells,
+                                     const msfec_cell *cells,
+                                     const double *d_ainv6,
+                                     const msfec_load *load, double *d_KH,
+                                     double *d_FH,
+                                     msfec_cell_report *d_reports);
+
+/* Basis of the last RT_DQ build: per cell 6 rows of NF + NC fine DoFs (faces
+   x|y|z as for Ned_RT, then cells i + n(j + n k)). */
+int64_t msfec_rtdq_basis_size(const msfec_handle *handle);
+msfec_status msfec_rtdq_get_basis(msfec_handle *handle, double *Phi,
+                                  int64_t capacity);
+
 /* Basis of the last Ned_RT build: per cell 18 rows (coarse basis order) of
    NE + NF fine DoFs (edges x|y|z then faces x|y|z, lexicographic), sigma and u
    of every basis function. Size in doubles, and copy to host. */

@@ -18,6 +18,7 @@
 #include "nedrt_common.cuh"
 #include "q1_common.cuh"
 #include "qned_common.cuh"
+#include "rtdq_common.cuh"
 
 namespace msfec {
 cudaError_t q1_solve_launch_f32_c1(bool has_r, const Q1Params &prm, size_t smem, int grid, cudaStream_t st);
@@ -59,6 +60,11 @@ cudaError_t qned_solve_launch(bool fp64, bool two_per_sm, const QNParams &prm, s
 cudaError_t qned_galerkin_launch(const NRCell *cells, int ncells, const double *phi, const double *y,
                                  const msfec_load &load, double *eload, double *KH, double *FH,
                                  msfec_cell_report *rep, const NRStat *stats, cudaStream_t st);
+cudaError_t rtdq_solve_launch(bool fp64, bool two_per_sm, const RTParams &prm, size_t smem, int grid,
+                              cudaStream_t st);
+cudaError_t rtdq_galerkin_launch(const NRCell *cells, int ncells, const double *phi, const double *y,
+                                 const msfec_load &load, double *KH, double *FH, msfec_cell_report *rep,
+                                 const NRStat *stats, cudaStream_t st);
 cudaError_t nedrt_split_occupancy(size_t smem, int *blocks_per_sm);
 cudaError_t nedrt_adjoint_prepare_launch(const NRCell *cells, int ncells, const double *phi, const double *U,
                                          const double *lam, const msfec_load &load, int npoints, const int *cell_of,
@@ -183,6 +189,13 @@ struct msfec_handle {
   DevBuf<NRStat> qn_stats;
   DevBuf<float> qn_scratch;
   int64_t qn_basis_doubles = 0;
+  // RT_DQ batch buffers
+  DevBuf<NRCell> rt_cells;
+  DevBuf<NRItem> rt_items;
+  DevBuf<double> rt_phi, rt_y, rt_ainv, rt_KH, rt_FH;
+  DevBuf<NRStat> rt_stats;
+  DevBuf<float> rt_scratch;
+  int64_t rt_basis_doubles = 0;
   int q1_ncells = 0;
   int64_t q1_basis_doubles = 0;
   std::vector<Q1Cell> h_cells;
@@ -887,6 +900,100 @@ msfec_status qned_build_impl(msfec_handle *h, int ncells, const msfec_cell *cell
   return MSFEC_SUCCESS;
 }
 
+// RT_DQ batch: plan (cells deepest first, 6 items per cell), launches.
+msfec_status rtdq_build_impl(msfec_handle *h, int ncells, const msfec_cell *cells, const double *d_ainv,
+                             const msfec_load *load, double *d_KH, double *d_FH, msfec_cell_report *d_rep) {
+  const bool fp64 = h->cfg.precision == MSFEC_PRECISION_FP64;
+  std::vector<NRCell> hc(ncells);
+  int64_t fine = 0, dofs = 0;
+  int nmax = 0;
+  for (int c = 0; c < ncells; ++c) {
+    NRCell &q = hc[c];
+    const int n = 1 << cells[c].depth;
+    for (int d = 0; d < 3; ++d) {
+      q.origin[d] = cells[c].origin[d];
+      q.h[d] = cells[c].size[d] / n;
+    }
+    q.depth = cells[c].depth;
+    q.n = n;
+    q.coef_off = fine;
+    q.dof_off = dofs;
+    int NFx, NF, NC;
+    rt_counts(n, NFx, NF, NC);
+    fine += NC;
+    dofs += NF + NC;
+    nmax = std::max(nmax, n);
+  }
+  std::vector<int> order(ncells);
+  for (int c = 0; c < ncells; ++c) order[c] = c;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cells[x].depth > cells[y].depth; });
+  std::vector<NRItem> items;
+  items.reserve((size_t)ncells * kRTBases);
+  for (int c : order)
+    for (int b = 0; b < kRTBases; ++b) items.push_back(NRItem{c, b, 0});
+  const size_t ws_floats = rt_workspace_floats(nmax, fp64 ? 8 : 4);
+  const bool use_smem = ws_floats * 4 <= kNRSmemLimit;
+  const size_t smem = use_smem ? ws_floats * 4 : 0;
+  const bool two_per_sm = !fp64 && use_smem && smem <= kNRSplitSmemLimit;
+  const int grid = std::min<int>((int)items.size(), (two_per_sm ? 2 : 1) * h->num_sms);
+  cudaStream_t st = h->stream;
+  MSFEC_CUDA_TRY(h, h->rt_cells.reserve(ncells));
+  MSFEC_CUDA_TRY(h, h->rt_items.reserve(items.size()));
+  MSFEC_CUDA_TRY(h, h->queue.reserve(2));
+  MSFEC_CUDA_TRY(h, h->rt_phi.reserve((size_t)dofs * kRTBases));
+  MSFEC_CUDA_TRY(h, h->rt_y.reserve((size_t)dofs * kRTBases));
+  MSFEC_CUDA_TRY(h, h->rt_stats.reserve((size_t)ncells * kRTBases));
+  if (!use_smem) MSFEC_CUDA_TRY(h, h->rt_scratch.reserve(ws_floats * grid));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->rt_cells.ptr, hc.data(), hc.size() * sizeof(NRCell), cudaMemcpyHostToDevice, st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->rt_items.ptr, items.data(), items.size() * sizeof(NRItem),
+                                    cudaMemcpyHostToDevice, st));
+  MSFEC_CUDA_TRY(h, cudaMemsetAsync(h->queue.ptr, 0, sizeof(int), st));
+  RTParams prm{};
+  prm.cells = h->rt_cells.ptr;
+  prm.items = h->rt_items.ptr;
+  prm.n_items = (int)items.size();
+  prm.queue = h->queue.ptr;
+  prm.ainv6 = d_ainv;
+  prm.phi = h->rt_phi.ptr;
+  prm.y = h->rt_y.ptr;
+  prm.stats = h->rt_stats.ptr;
+  prm.scratch = use_smem ? nullptr : h->rt_scratch.ptr;
+  prm.scratch_floats = ws_floats;
+  prm.use_smem = use_smem ? 1 : 0;
+  prm.rtol = h->cfg.nedrt_rtol;
+  prm.inner_rtol = h->cfg.inner_rtol;
+  prm.max_iter = std::max(h->cfg.max_iter, 8000);
+  prm.max_refine = h->cfg.max_refine;
+  if (h->cfg.verbose)
+    fprintf(stderr, "[msfec] rtdq plan: %d cells, %zu items, workspace %zu floats (%s), grid %d, %s\n", ncells,
+            items.size(), ws_floats, two_per_sm ? "shared, 2 CTAs/SM" : (use_smem ? "shared" : "global"), grid,
+            fp64 ? "fp64" : "mixed");
+  msfec_load ld;
+  if (load) {
+    ld = *load;
+  } else {
+    std::memset(&ld, 0, sizeof(ld));
+  }
+  if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[0], st));
+  MSFEC_CUDA_TRY(h, rtdq_solve_launch(fp64, two_per_sm, prm, smem, grid, st));
+  if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[1], st));
+  MSFEC_CUDA_TRY(h, rtdq_galerkin_launch(h->rt_cells.ptr, ncells, h->rt_phi.ptr, h->rt_y.ptr, ld, d_KH, d_FH, d_rep,
+                                         h->rt_stats.ptr, st));
+  if (h->timing) {
+    MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[2], st));
+    MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[3], st));
+  }
+  h->ev_recorded = h->timing;
+  h->last_launches = d_rep ? 3 : 2;
+  h->last_graph = 0;
+  h->rt_basis_doubles = dofs * kRTBases;
+  return MSFEC_SUCCESS;
+}
+
+bool scalar_load_ok(const msfec_load *l) {
+  return !l || l->kind == MSFEC_LOAD_ZERO || l->kind == MSFEC_LOAD_CONSTANT || l->kind == MSFEC_LOAD_SIN_PRODUCT;
+}
+
 bool nr_load_ok(const msfec_load *l) {
   return !l || l->kind == MSFEC_LOAD_ZERO || l->kind == MSFEC_LOAD_VEC_TRIG;
 }
@@ -1007,6 +1114,11 @@ void msfec_destroy(msfec_handle *h) {
       b->release();
     h->qn_stats.release();
     h->qn_scratch.release();
+    h->rt_cells.release();
+    h->rt_items.release();
+    for (DevBuf<double> *b : {&h->rt_phi, &h->rt_y, &h->rt_ainv, &h->rt_KH, &h->rt_FH}) b->release();
+    h->rt_stats.release();
+    h->rt_scratch.release();
     h->q1_graph.reset();
     h->nr_graph.reset();
     if (h->aux_stream) cudaStreamSynchronize(h->aux_stream);
@@ -1724,6 +1836,83 @@ msfec_status msfec_qned_build(msfec_handle *h, int32_t ncells, const msfec_cell 
   if (reports) std::memcpy(reports, rep.data(), rep.size() * sizeof(msfec_cell_report));
   for (const auto &r : rep)
     if (!r.converged) return fail(h, MSFEC_ERROR_NOT_CONVERGED, "at least one Q_Ned local solve missed nedrt_rtol");
+  return MSFEC_SUCCESS;
+}
+
+msfec_status msfec_rtdq_build_device(msfec_handle *h, int32_t ncells, const msfec_cell *cells, const double *d_ainv6,
+                                     const msfec_load *load, double *d_KH, double *d_FH,
+                                     msfec_cell_report *d_reports) {
+  if (!h) return MSFEC_ERROR_INVALID_ARGUMENT;
+  if (ncells < 0 || (ncells > 0 && (!cells || !d_ainv6 || !d_KH || !d_FH)))
+    return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "null pointer or negative cell count");
+  for (int c = 0; c < ncells; ++c)
+    if (!cell_ok(cells[c]) || cells[c].depth > kNRMaxDepth)
+      return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "cell " + std::to_string(c) + " invalid (RT_DQ depth 1..4)");
+  if (!load_ok(load) || !scalar_load_ok(load)) return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "invalid RT_DQ load");
+  if (ncells == 0) {
+    h->rt_basis_doubles = 0;
+    return MSFEC_SUCCESS;
+  }
+  DeviceGuard g(h->device);
+  return rtdq_build_impl(h, ncells, cells, d_ainv6, load, d_KH, d_FH, d_reports);
+}
+
+msfec_status msfec_rtdq_build(msfec_handle *h, int32_t ncells, const msfec_cell *cells, const double *ainv6,
+                              const msfec_load *load, double *KH, double *FH, msfec_cell_report *reports) {
+  if (!h) return MSFEC_ERROR_INVALID_ARGUMENT;
+  if (ncells < 0 || (ncells > 0 && (!cells || !ainv6 || !KH || !FH)))
+    return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "null pointer or negative cell count");
+  int64_t nfine = 0;
+  for (int c = 0; c < ncells; ++c) {
+    if (!cell_ok(cells[c]) || cells[c].depth > kNRMaxDepth)
+      return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "cell " + std::to_string(c) + " invalid (RT_DQ depth 1..4)");
+    const int64_t n = 1LL << cells[c].depth;
+    nfine += n * n * n;
+  }
+  if (!load_ok(load) || !scalar_load_ok(load)) return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "invalid RT_DQ load");
+  for (int64_t e = 0; e < nfine; ++e) {
+    const double *a = ainv6 + 6 * e;
+    const double m1 = a[0], m2 = a[0] * a[1] - a[3] * a[3];
+    const double m3 = a[0] * (a[1] * a[2] - a[5] * a[5]) - a[3] * (a[3] * a[2] - a[5] * a[4]) +
+                      a[4] * (a[3] * a[5] - a[1] * a[4]);
+    bool ok = m1 > 0.0 && m2 > 0.0 && m3 > 0.0;
+    for (int q = 0; q < 6; ++q) ok = ok && std::isfinite(a[q]);
+    if (!ok) return fail(h, MSFEC_ERROR_NUMERICAL, "A^-1 not SPD / finite at fine cell " + std::to_string(e));
+  }
+  if (ncells == 0) return msfec_rtdq_build_device(h, 0, cells, nullptr, load, nullptr, nullptr, nullptr);
+  DeviceGuard g(h->device);
+  cudaStream_t st = h->stream;
+  MSFEC_CUDA_TRY(h, h->rt_ainv.reserve(nfine * 6));
+  MSFEC_CUDA_TRY(h, h->rt_KH.reserve((size_t)ncells * kRTCoarse * kRTCoarse));
+  MSFEC_CUDA_TRY(h, h->rt_FH.reserve((size_t)ncells * kRTCoarse));
+  MSFEC_CUDA_TRY(h, h->rep.reserve(ncells));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->rt_ainv.ptr, ainv6, nfine * 6 * sizeof(double), cudaMemcpyHostToDevice, st));
+  msfec_status s = rtdq_build_impl(h, ncells, cells, h->rt_ainv.ptr, load, h->rt_KH.ptr, h->rt_FH.ptr, h->rep.ptr);
+  if (s != MSFEC_SUCCESS) return s;
+  std::vector<msfec_cell_report> rep(ncells);
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(KH, h->rt_KH.ptr, (size_t)ncells * kRTCoarse * kRTCoarse * sizeof(double),
+                                    cudaMemcpyDeviceToHost, st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(FH, h->rt_FH.ptr, (size_t)ncells * kRTCoarse * sizeof(double),
+                                    cudaMemcpyDeviceToHost, st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(rep.data(), h->rep.ptr, (size_t)ncells * sizeof(msfec_cell_report),
+                                    cudaMemcpyDeviceToHost, st));
+  MSFEC_CUDA_TRY(h, cudaStreamSynchronize(st));
+  if (reports) std::memcpy(reports, rep.data(), rep.size() * sizeof(msfec_cell_report));
+  for (const auto &r : rep)
+    if (!r.converged) return fail(h, MSFEC_ERROR_NOT_CONVERGED, "at least one RT_DQ local solve missed nedrt_rtol");
+  return MSFEC_SUCCESS;
+}
+
+int64_t msfec_rtdq_basis_size(const msfec_handle *h) { return h ? h->rt_basis_doubles : 0; }
+
+msfec_status msfec_rtdq_get_basis(msfec_handle *h, double *Phi, int64_t capacity) {
+  if (!h || !Phi) return MSFEC_ERROR_INVALID_ARGUMENT;
+  if (h->rt_basis_doubles <= 0) return fail(h, MSFEC_ERROR_INVALID_STATE, "no RT_DQ basis built yet");
+  if (capacity < h->rt_basis_doubles) return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "capacity too small");
+  DeviceGuard g(h->device);
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(Phi, h->rt_phi.ptr, h->rt_basis_doubles * sizeof(double), cudaMemcpyDeviceToHost,
+                                    h->stream));
+  MSFEC_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
   return MSFEC_SUCCESS;
 }
 

@@ -40,6 +40,7 @@ EXPORTED = [
     "msfec_nedrt_get_basis", "msfec_q1_backward", "msfec_nedrt_build_noalloc",
     "msfec_set_graph", "msfec_autotune", "msfec_q1_fine_solve", "msfec_nedrt_backward",
     "msfec_qned_build", "msfec_qned_build_device", "msfec_qned_basis_size", "msfec_qned_get_basis",
+    "msfec_rtdq_build", "msfec_rtdq_build_device", "msfec_rtdq_basis_size", "msfec_rtdq_get_basis",
 ]
 
 
@@ -150,6 +151,14 @@ def load_library(path: str = LIB_PATH):
     L.msfec_qned_basis_size.restype = ctypes.c_int64
     L.msfec_qned_get_basis.argtypes = [_vp, _dp, ctypes.c_int64]
     L.msfec_qned_get_basis.restype = ctypes.c_int
+    L.msfec_rtdq_build.argtypes = [_vp, ctypes.c_int32, _vp, _dp, ctypes.POINTER(Load), _dp, _dp, _vp]
+    L.msfec_rtdq_build.restype = ctypes.c_int
+    L.msfec_rtdq_build_device.argtypes = [_vp, ctypes.c_int32, _vp, _vp, ctypes.POINTER(Load), _vp, _vp, _vp]
+    L.msfec_rtdq_build_device.restype = ctypes.c_int
+    L.msfec_rtdq_basis_size.argtypes = [_vp]
+    L.msfec_rtdq_basis_size.restype = ctypes.c_int64
+    L.msfec_rtdq_get_basis.argtypes = [_vp, _dp, ctypes.c_int64]
+    L.msfec_rtdq_get_basis.restype = ctypes.c_int
     L.msfec_set_graph.argtypes = [_vp, ctypes.c_int32]
     L.msfec_set_graph.restype = ctypes.c_int
     _lib = L
@@ -401,6 +410,32 @@ class Handle:
         n = self._lib.msfec_qned_basis_size(self._h)
         out = np.zeros(n)
         self.check(self._lib.msfec_qned_get_basis(self._h, _d(out), n))
+        return out
+
+    def rtdq_build(self, cells, ainv6, load):
+        """RT_DQ basis build from host arrays; returns (KH [c,7,7], FH [c,7], reports, status)."""
+        cells = np.ascontiguousarray(cells, dtype=CELL_DTYPE)
+        ainv6 = np.ascontiguousarray(ainv6, dtype=np.float64)
+        nc = cells.shape[0]
+        KH = np.zeros((nc, 7, 7))
+        FH = np.zeros((nc, 7))
+        rep = np.zeros(nc, dtype=REPORT_DTYPE)
+        st = self._lib.msfec_rtdq_build(self._h, nc, cells.ctypes.data_as(_vp), _d(ainv6), ctypes.byref(load),
+                                        _d(KH), _d(FH), rep.ctypes.data_as(_vp))
+        self.check(st, allow=(ERROR_NOT_CONVERGED,))
+        return KH, FH, rep, st
+
+    def rtdq_build_device(self, cells, d_ainv6, load, d_KH, d_FH, d_reports):
+        cells = np.ascontiguousarray(cells, dtype=CELL_DTYPE)
+        st = self._lib.msfec_rtdq_build_device(self._h, cells.shape[0], cells.ctypes.data_as(_vp),
+                                               _vp(d_ainv6), ctypes.byref(load),
+                                               _vp(d_KH), _vp(d_FH), _vp(d_reports or 0))
+        return self.check(st)
+
+    def rtdq_basis(self):
+        n = self._lib.msfec_rtdq_basis_size(self._h)
+        out = np.zeros(n)
+        self.check(self._lib.msfec_rtdq_get_basis(self._h, _d(out), n))
         return out
 
     def nedrt_basis(self):

@@ -137,6 +137,19 @@ def qned_tensor(m=8, depth=3, seed=2, kb=14.0):
     return cells, a6, binv, load
 
 
+def rtdq_tensor(m=8, depth=3, seed=2):
+    """RT_DQ workload; returns cells, A^-1 as [fine, 6] (A^-1 = R diag(e^-g) R^T, g ~ N(0, 1),
+    R Haar: the Ned_RT coefficient law), scalar sin-product load."""
+    cells, ainv6, _, _ = nedrt_tensor(m, depth, seed)
+    load = make_load(LOAD_SIN_PRODUCT, (1.0, 1.0, 0.0, 0.0))
+    return cells, ainv6, load
+
+
+def rtdq_work_dof_rhs(cells):
+    n = 1 << cells["depth"].astype(np.int64)
+    return int(np.sum(3 * n * n * (n + 1) + n ** 3) * 6)
+
+
 def qned_work_dof_rhs(cells):
     n = 1 << cells["depth"].astype(np.int64)
     return int(np.sum((n + 1) ** 3 + 3 * n * (n + 1) ** 2) * 20)
