@@ -82,6 +82,11 @@ class Workload:
             self.cells, self.a6, self.binv, self.load = workloads.qned_tensor(m=8, depth=3, seed=2)
             self.cfg = {"workload": "qned_tensor_coarse8^3_L3_20rhs", "coarse_cells": 512, "depth": 3, "seed": 2,
                         "B^-1": "1/(1-0.9 sin(2 pi 14 x))", "load": "vec trig"}
+        elif name == "rtdq_small":
+            self.kind = "rtdq"
+            self.cells, self.ainv6, self.load = workloads.rtdq_tensor(m=8, depth=3, seed=2)
+            self.cfg = {"workload": "rtdq_tensor_coarse8^3_L3_6rhs", "coarse_cells": 512, "depth": 3, "seed": 2,
+                        "load": "sin product"}
         elif name == "q1_uneven":
             self.kind = "q1"
             self.cells, self.a, self.r, self.load = workloads.q1_uneven(m=16, seed=3)
@@ -106,6 +111,8 @@ class Workload:
         c = self.cells[lo:hi]
         if self.kind == "qned":
             return workloads.qned_work_dof_rhs(c)
+        if self.kind == "rtdq":
+            return workloads.rtdq_work_dof_rhs(c)
         return workloads.nedrt_work_dof_rhs(c) if self.kind == "nedrt" else workloads.work_dof_rhs(c)
 
     def per_cell_work(self):
@@ -114,6 +121,8 @@ class Workload:
             return (3 * n * (n + 1) ** 2 + 3 * n * n * (n + 1)) * 18
         if self.kind == "qned":
             return ((n + 1) ** 3 + 3 * n * (n + 1) ** 2) * 20
+        if self.kind == "rtdq":
+            return (3 * n * n * (n + 1) + n ** 3) * 6
         return (n + 1) ** 3 * 8
 
     def shard(self, lo, hi):
@@ -125,6 +134,8 @@ class Workload:
         elif self.kind == "qned":
             out["a6"] = np.ascontiguousarray(self.a6[f0:f1])
             out["binv"] = np.ascontiguousarray(self.binv[f0:f1])
+        elif self.kind == "rtdq":
+            out["ainv6"] = np.ascontiguousarray(self.ainv6[f0:f1])
         else:
             out["a"] = np.ascontiguousarray(self.a[f0:f1])
             out["r"] = None if self.r is None else np.ascontiguousarray(self.r[f0:f1])
@@ -185,6 +196,24 @@ class ClockSampler:
 
 
 # --------------------------------------------------------------------------- CPU (oracle)
+def _mixed_oracle_chunk(args):
+    """Q_Ned / RT_DQ oracle (SuperLU per cell) on a chunk of cells, in a worker process."""
+    sys.path.insert(0, REPO)
+    sys.path.insert(0, PKG)
+    kind, cells, coef, load_kind, params = args
+    t0 = time.perf_counter()
+    if kind == "qned":
+        from oracle import nedrt_oracle as N
+        from oracle import qned_oracle as Q
+        a6, binv = coef
+        Q.build(cells, binv, N.sym6_to_ainv(a6), load_kind, params, want_phi=False)
+    else:
+        from oracle import nedrt_oracle as N
+        from oracle import rtdq_oracle as R
+        R.build(cells, N.sym6_to_ainv(coef), load_kind, params, want_phi=False)
+    return time.perf_counter() - t0
+
+
 def _nedrt_oracle_chunk(args):
     sys.path.insert(0, REPO)
     sys.path.insert(0, PKG)
@@ -198,8 +227,10 @@ def _nedrt_oracle_chunk(args):
 def cpu_sample(wl, target_s, nthreads):
     """Stratified sample (every depth represented) sized for ~target_s of CPU work."""
     depths = sorted(set(int(d) for d in wl.cells["depth"]))
-    if wl.kind == "nedrt":
+    if wl.kind in ("nedrt", "qned"):
         per_cell = {1: 5e-3, 2: 3e-2, 3: 0.6, 4: 12.0}
+    elif wl.kind == "rtdq":
+        per_cell = {1: 2e-3, 2: 2e-2, 3: 0.25, 4: 5.0}
     else:
         per_cell = {1: 1e-4, 2: 5e-4, 3: 8e-3, 4: 0.1, 5: 1.6}
     per_depth = target_s * nthreads / max(1, len(depths))
@@ -229,12 +260,19 @@ def time_oracle(wl, sel, nthreads):
         desc = "CG+SSOR(1.6) 1e-12 per RHS (C++, OpenMP over cells)"
     else:
         chunks = []
+        fine = lambda arr, part: np.concatenate([arr[wl.foff[c]:wl.foff[c + 1]] for c in part])  # noqa: E731
         for part in np.array_split(np.asarray(sel), nthreads):
             if len(part) == 0:
                 continue
-            a6 = np.concatenate([wl.ainv6[wl.foff[c]:wl.foff[c + 1]] for c in part])
-            bd = np.concatenate([wl.bdiv[wl.foff[c]:wl.foff[c + 1]] for c in part])
-            chunks.append((wl.cells[part], a6, bd, wl.load.kind, list(wl.load.params)))
+            if wl.kind == "nedrt":
+                chunks.append((wl.cells[part], fine(wl.ainv6, part), fine(wl.bdiv, part), wl.load.kind,
+                               list(wl.load.params)))
+            elif wl.kind == "qned":
+                chunks.append(("qned", wl.cells[part], (fine(wl.a6, part), fine(wl.binv, part)), wl.load.kind,
+                               list(wl.load.params)))
+            else:
+                chunks.append(("rtdq", wl.cells[part], fine(wl.ainv6, part), wl.load.kind, list(wl.load.params)))
+        worker = _nedrt_oracle_chunk if wl.kind == "nedrt" else _mixed_oracle_chunk
         ctx = mp.get_context("spawn")
         saved = {k: os.environ.get(k) for k in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")}
         for k in saved:
@@ -246,11 +284,12 @@ def time_oracle(wl, sel, nthreads):
             else:
                 os.environ[k] = v
         with pool:
-            pool.map(_nedrt_oracle_chunk, chunks[:1])  # warm the workers' imports
+            pool.map(worker, chunks[:1])  # warm the workers' imports
             t0 = time.perf_counter()
-            pool.map(_nedrt_oracle_chunk, chunks)
+            pool.map(worker, chunks)
             dt = time.perf_counter() - t0
-        desc = "sparse direct (SuperLU, one factorisation per cell, 18 solves), process per core"
+        nb = {"nedrt": 18, "qned": 20, "rtdq": 6}[wl.kind]
+        desc = f"sparse direct (SuperLU, one factorisation per cell, {nb} solves), process per core"
     work = int(np.sum(wl.per_cell_work()[sel]))
     return work / dt, dt, f"{len(sel)} of {len(wl.cells)} cells (every depth); {desc}; {dt:.1f} s"
 
@@ -268,7 +307,7 @@ def gpu_run(wl, lo, hi, precision, steps, warmup, local, stream, barrier, tune_i
     h = msfec.Handle(precision=precision, device=local)
     h.set_stream(stream.cuda_stream)
     h.set_timing(True)
-    nr = {"nedrt": 18, "qned": 20}.get(wl.kind, 8)
+    nr = {"nedrt": 18, "qned": 20, "rtdq": 7}.get(wl.kind, 8)
     d_KH = torch.zeros((nc, nr, nr), dtype=torch.float64, device="cuda")
     d_FH = torch.zeros((nc, nr), dtype=torch.float64, device="cuda")
     d_rep = torch.zeros(max(1, nc) * msfec.REPORT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
@@ -286,6 +325,11 @@ def gpu_run(wl, lo, hi, precision, steps, warmup, local, stream, barrier, tune_i
         def step():
             h.qned_build_device(cells, d_x.data_ptr(), d_y.data_ptr(), wl.load, d_KH.data_ptr(),
                                 d_FH.data_ptr(), d_rep.data_ptr())
+    elif wl.kind == "rtdq":
+        d_x = torch.from_numpy(sh["ainv6"]).cuda()
+
+        def step():
+            h.rtdq_build_device(cells, d_x.data_ptr(), wl.load, d_KH.data_ptr(), d_FH.data_ptr(), d_rep.data_ptr())
     else:
         d_x = torch.from_numpy(sh["a"]).cuda()
         d_y = None if sh["r"] is None else torch.from_numpy(sh["r"]).cuda()
@@ -293,7 +337,7 @@ def gpu_run(wl, lo, hi, precision, steps, warmup, local, stream, barrier, tune_i
         def step():
             h.q1_build_device(cells, d_x.data_ptr(), 0 if d_y is None else d_y.data_ptr(), wl.load,
                               d_KH.data_ptr(), d_FH.data_ptr(), d_rep.data_ptr())
-    if tune_info is not None and nc > 0 and wl.kind != "qned":
+    if tune_info is not None and nc > 0 and wl.kind not in ("qned", "rtdq"):
         import sharding
         k = min(nc, 64 if wl.kind == "nedrt" else 512)  # several waves of items, seconds of trials
         f = int(sharding.fine_offsets(cells)[k])
@@ -339,6 +383,16 @@ def e2e_run(wl, lo, hi, local, stream, barrier, steps):
         call = lambda: h.nedrt_build(cells, x, y, wl.load)  # noqa: E731
         h2d = x.nbytes + y.nbytes
         nr = 18
+    elif wl.kind == "qned":
+        x, y = pin(sh["a6"]), pin(sh["binv"])
+        call = lambda: h.qned_build(cells, x, y, wl.load)  # noqa: E731
+        h2d = x.nbytes + y.nbytes
+        nr = 20
+    elif wl.kind == "rtdq":
+        x = pin(sh["ainv6"])
+        call = lambda: h.rtdq_build(cells, x, wl.load)  # noqa: E731
+        h2d = x.nbytes
+        nr = 7
     else:
         x, y = pin(sh["a"]), pin(sh["r"])
         call = lambda: h.q1_build(cells, x, y, wl.load)  # noqa: E731
@@ -374,6 +428,11 @@ def roofline(wl, lo, hi, solve_ms, gal_ms, rep, kind):
         nrhs, coef_bytes = 20, 7 * 8
         # factored cell operator (vertex mass, M_N Grad, C^T M_RT C, dot: ~300 per fine cell)
         flops_iter = 300 * n ** 3 + 20 * ((n + 1) ** 3 + 3 * n * (n + 1) ** 2)
+    elif wl.kind == "rtdq":
+        ndof = int(np.sum(3 * n * n * (n + 1) + n ** 3))
+        nrhs, coef_bytes = 6, 6 * 8
+        # factored RT0 mass + divergence + dot (~100 per fine cell) + recurrences (~20 per DoF)
+        flops_iter = 100 * n ** 3 + 20 * (3 * n * n * (n + 1) + n ** 3)
     else:
         ndof = int(np.sum((n + 1) ** 3))
         nrhs, coef_bytes = 8, 8 * (1 if wl.r is None else 2)
@@ -383,7 +442,7 @@ def roofline(wl, lo, hi, solve_ms, gal_ms, rep, kind):
     alg_solve = nfine * coef_bytes + ndof * nrhs * 8 * 2
     alg_gal = ndof * nrhs * 8 * 2 + len(c) * (nrhs * nrhs + nrhs) * 8
     iters = rep["iterations"].astype(np.float64)  # max over the cell's RHS (upper estimate)
-    per_cell_flops = flops_iter * iters * (nrhs if wl.kind in ("nedrt", "qned") else 8)
+    per_cell_flops = flops_iter * iters * (nrhs if wl.kind in ("nedrt", "qned", "rtdq") else 8)
     tflops = float(np.sum(per_cell_flops)) / (solve_ms * 1e-3) / 1e12
     return {"bound": "hbm", "kernel": f"{kind}_solve_kernel (persistent, on-chip Krylov state)",
             "achieved": alg_solve / (solve_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
@@ -615,9 +674,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="nedrt_small",
-                    choices=["nedrt_small", "nedrt_l4", "nedrt_large", "qned_small", "q1_uneven", "q1_small",
+                    choices=["nedrt_small", "nedrt_l4", "nedrt_large", "qned_small", "rtdq_small", "q1_uneven", "q1_small",
                              "q1_adjoint_fwd"])
-    ap.add_argument("--extra", default="q1_uneven,qned_small",
+    ap.add_argument("--extra", default="q1_uneven,qned_small,rtdq_small",
                     help="comma-separated workloads reported beside the headline")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--skip-fp64", action="store_true")
