@@ -96,6 +96,11 @@ typedef struct msfec_config {
      The mixed local system has condition number ~1e4 at depth 3, so 1e-14
      is needed for a 1e-10 basis error. */
   double nedrt_rtol;
+  /* Face (Schur) block preconditioner of the mixed local solvers (Ned_RT):
+     0 = multilevel (diagonal + coarse RT levels n/2 .. 4 + exact level 2),
+     1 = diagonal only. */
+  int32_t nedrt_precond;
+  int32_t reserved;
 } msfec_config;
 
 typedef struct msfec_cell {
@@ -116,7 +121,7 @@ typedef struct msfec_cell_report {
 typedef struct msfec_handle msfec_handle;
 
 /* Fills cfg with defaults: device 0, MIXED, rtol 1e-12, inner_rtol 1e-6,
-   max_iter 2000, max_refine 6, nedrt_rtol 1e-14. */
+   max_iter 2000, max_refine 6, nedrt_rtol 1e-14, nedrt_precond 0. */
 void msfec_config_default(msfec_config *cfg);
 
 msfec_status msfec_create(msfec_handle **handle, const msfec_config *cfg);

@@ -53,8 +53,11 @@ cudaError_t q1_adjoint_rhs_launch(const Q1Cell *cells, int ncells, const msfec_l
                                   cudaStream_t st);
 cudaError_t q1_gradient_launch(const Q1Cell *cells, int ncells, const double *a, const double *phi, const double *sol,
                                const double *U, const double *lam, double *grad, cudaStream_t st);
-cudaError_t nedrt_solve_launch(bool fp64, const NRParams &prm, size_t smem, int grid, cudaStream_t st);
-cudaError_t nedrt_solve_launch_split(const NRParams &prm, size_t smem, int grid, cudaStream_t st);
+cudaError_t nedrt_solve_launch(bool fp64, bool ml, const NRParams &prm, size_t smem, int grid, cudaStream_t st);
+cudaError_t nedrt_solve_launch_split(bool ml, const NRParams &prm, size_t smem, int grid, cudaStream_t st);
+cudaError_t nedrt_ml_setup_launch(const NRCell *cells, int ncells, const double *ainv6, const double *bdiv,
+                                  float *coarse, float *scratch, size_t scratch_floats, size_t smem, int grid,
+                                  cudaStream_t st);
 cudaError_t qned_solve_launch(bool fp64, bool two_per_sm, const QNParams &prm, size_t smem, int grid,
                               cudaStream_t st);
 cudaError_t qned_galerkin_launch(const NRCell *cells, int ncells, const double *phi, const double *y,
@@ -65,7 +68,7 @@ cudaError_t rtdq_solve_launch(bool fp64, bool two_per_sm, const RTParams &prm, s
 cudaError_t rtdq_galerkin_launch(const NRCell *cells, int ncells, const double *phi, const double *y,
                                  const msfec_load &load, double *KH, double *FH, msfec_cell_report *rep,
                                  const NRStat *stats, cudaStream_t st);
-cudaError_t nedrt_split_occupancy(size_t smem, int *blocks_per_sm);
+cudaError_t nedrt_split_occupancy(bool ml, size_t smem, int *blocks_per_sm);
 cudaError_t nedrt_adjoint_prepare_launch(const NRCell *cells, int ncells, const double *phi, const double *U,
                                          const double *lam, const msfec_load &load, int npoints, const int *cell_of,
                                          const double *pts, const double *dJdu, const double *ainv6,
@@ -174,6 +177,8 @@ struct msfec_handle {
   DevBuf<double> nr_phi, nr_y;
   DevBuf<NRStat> nr_stats;
   DevBuf<float> nr_scratch;
+  DevBuf<float> nr_coarse, nr_mlscratch;  // multilevel preconditioner data per cell, setup workspace
+  bool nr_ml_valid = false;               // the last Ned_RT build left multilevel data for its cells
   DevBuf<double> nr_ainv, nr_bdiv, nr_KH, nr_FH;
   int64_t nr_basis_doubles = 0;
   std::vector<msfec_cell> nr_h_cells;  // batch of the Ned_RT basis held in nr_phi
@@ -679,6 +684,7 @@ msfec_status q1_backward_impl(msfec_handle *h, int ncells, const msfec_cell *cel
 
 constexpr int kNRMaxDepth = 4;
 constexpr size_t kNRSmemLimit = 200 * 1024;
+constexpr size_t kNRSmemTotalLimit = 224 * 1024;  // workspace + multilevel region (227 KB minus static)
 constexpr size_t kNRSplitSmemLimit = 108 * 1024;  // two CTAs per SM (228 KB, minus static shared memory)
 
 msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cells, const double *d_ainv,
@@ -714,6 +720,18 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
     dofs += NE + NF;
     nmax = std::max(nmax, n);
   }
+  // multilevel face preconditioner for every cell of depth >= 2 (nedrt_precond 0)
+  bool ml = h->cfg.nedrt_precond == 0 && nmax >= 4;
+  int64_t coarse_floats = 0;
+  int n_ml = 0;
+  for (int c = 0; c < ncells; ++c) {
+    hc[c].coarse_off = -1;
+    if (ml && hc[c].n >= 4) {
+      hc[c].coarse_off = coarse_floats;
+      coarse_floats += nr_ml_data_floats(hc[c].n);
+      ++n_ml;
+    }
+  }
   // items: (cell, basis), deepest cells first
   std::vector<int> order(ncells);
   for (int c = 0; c < ncells; ++c) order[c] = c;
@@ -738,8 +756,17 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
     smem = nr_split_smem_floats(nmax) * 4;
     ws_floats = nr_split_global_floats(nmax);  // global slot per CTA
     use_smem = true;
+  }
+  // the multilevel region follows the shared workspace (if any)
+  const size_t ml_offset = smem;
+  const size_t ml_bytes = ml ? nr_ml_layout(nmax, fp64 ? 8 : 4).bytes : 0;
+  if (ml && smem + ml_bytes > (split ? kNRSplitSmemLimit : kNRSmemTotalLimit)) ml = false;
+  if (!ml)
+    for (auto &q : hc) q.coarse_off = -1;
+  if (ml) smem += ml_bytes;
+  if (split) {
     int occ = 0;
-    MSFEC_CUDA_TRY(h, nedrt_split_occupancy(smem, &occ));
+    MSFEC_CUDA_TRY(h, nedrt_split_occupancy(ml, smem, &occ));
     if (occ <= 0) return fail(h, MSFEC_ERROR_NOT_SUPPORTED, "split Ned_RT solver cannot be resident");
     grid = std::min<int>((int)items.size(), occ * h->num_sms);
   } else if (!use_smem) {  // resident CTAs = workspace slots (L2 footprint), possibly autotuned
@@ -753,6 +780,14 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
   MSFEC_CUDA_TRY(h, h->nr_y.reserve((size_t)dofs * 18));
   MSFEC_CUDA_TRY(h, h->nr_stats.reserve((size_t)ncells * 18));
   if (!use_smem || split) MSFEC_CUDA_TRY(h, h->nr_scratch.reserve(ws_floats * grid));
+  const int ml_grid = std::min(n_ml, h->num_sms);
+  int NEx0, NFx0, NE0, NF0;
+  nr_counts(nmax, NEx0, NFx0, NE0, NF0);
+  const size_t ml_scratch = 4 * (((size_t)NE0 + NF0 + 63) / 64 * 64);
+  if (ml) {
+    MSFEC_CUDA_TRY(h, h->nr_coarse.reserve((size_t)coarse_floats));
+    MSFEC_CUDA_TRY(h, h->nr_mlscratch.reserve(ml_scratch * ml_grid));
+  }
   MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->nr_cells.ptr, hc.data(), hc.size() * sizeof(NRCell), cudaMemcpyHostToDevice, st));
   MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->nr_items.ptr, items.data(), items.size() * sizeof(NRItem),
                                     cudaMemcpyHostToDevice, st));
@@ -773,10 +808,12 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
   prm.inner_rtol = h->cfg.inner_rtol;
   prm.max_iter = std::max(h->cfg.max_iter, 8000);  // per refinement step (MINRES, kappa ~ 1e4)
   prm.max_refine = h->cfg.max_refine;
+  prm.coarse = ml ? h->nr_coarse.ptr : nullptr;
+  prm.ml_offset = ml_offset;
   if (h->cfg.verbose)
-    fprintf(stderr, "[msfec] nedrt plan: %d cells, %zu items, workspace %zu floats (%s), grid %d, %s\n", ncells,
+    fprintf(stderr, "[msfec] nedrt plan: %d cells, %zu items, workspace %zu floats (%s), grid %d, %s, %s\n", ncells,
             items.size(), ws_floats, split ? "split, 2 CTAs/SM" : (use_smem ? "shared" : "global"), grid,
-            fp64 ? "fp64" : "mixed");
+            fp64 ? "fp64" : "mixed", ml ? "multilevel" : "diagonal");
   msfec_load ld;
   if (load) {
     ld = *load;
@@ -786,8 +823,12 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
   auto seq = [&](bool timed) -> cudaError_t {
     cudaError_t e = cudaMemsetAsync(h->queue.ptr, 0, sizeof(int), st);
     if (e == cudaSuccess && timed) e = cudaEventRecord(h->ev[0], st);
+    if (e == cudaSuccess && ml)
+      e = nedrt_ml_setup_launch(h->nr_cells.ptr, ncells, d_ainv, d_bdiv, h->nr_coarse.ptr, h->nr_mlscratch.ptr,
+                                ml_scratch, (size_t)nr_ml_data_floats(nmax) * 4, ml_grid, st);
     if (e == cudaSuccess)
-      e = split ? nedrt_solve_launch_split(prm, smem, grid, st) : nedrt_solve_launch(fp64, prm, smem, grid, st);
+      e = split ? nedrt_solve_launch_split(ml, prm, smem, grid, st)
+                : nedrt_solve_launch(fp64, ml, prm, smem, grid, st);
     if (e == cudaSuccess && timed) e = cudaEventRecord(h->ev[1], st);
     if (e == cudaSuccess)
       e = nedrt_galerkin_launch(h->nr_cells.ptr, ncells, h->nr_phi.ptr, h->nr_y.ptr, ld, d_KH, d_FH, d_rep,
@@ -796,8 +837,9 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
     if (e == cudaSuccess && timed) e = cudaEventRecord(h->ev[3], st);
     return e;
   };
-  const msfec_status s = run_sequence(h, h->nr_graph, std::move(key), d_rep ? 3 : 2, seq);
+  const msfec_status s = run_sequence(h, h->nr_graph, std::move(key), (d_rep ? 3 : 2) + (ml ? 1 : 0), seq);
   if (s != MSFEC_SUCCESS) return s;
+  h->nr_ml_valid = ml;
   h->nr_graph_basis = dofs * 18;
   h->nr_h_cells.assign(cells, cells + ncells);
   h->nr_basis_doubles = dofs * 18;
@@ -824,6 +866,7 @@ msfec_status qned_build_impl(msfec_handle *h, int ncells, const msfec_cell *cell
     q.n = n;
     q.coef_off = fine;
     q.dof_off = dofs;
+    q.coarse_off = -1;
     int NV, NEx, NE;
     qn_counts(n, NV, NEx, NE);
     fine += (int64_t)n * n * n;
@@ -918,6 +961,7 @@ msfec_status rtdq_build_impl(msfec_handle *h, int ncells, const msfec_cell *cell
     q.n = n;
     q.coef_off = fine;
     q.dof_off = dofs;
+    q.coarse_off = -1;
     int NFx, NF, NC;
     rt_counts(n, NFx, NF, NC);
     fine += NC;
@@ -1041,7 +1085,7 @@ msfec_status msfec_create(msfec_handle **out, const msfec_config *cfg) {
     msfec_config_default(&c);
   if (c.precision != MSFEC_PRECISION_FP64 && c.precision != MSFEC_PRECISION_MIXED) return MSFEC_ERROR_INVALID_ARGUMENT;
   if (!(c.rtol > 0.0) || !(c.inner_rtol > 0.0) || c.inner_rtol >= 1.0 || c.max_iter < 1 || c.max_refine < 1 ||
-      !(c.nedrt_rtol > 0.0) || c.q1_launch < 0 || c.q1_launch > 2)
+      !(c.nedrt_rtol > 0.0) || c.q1_launch < 0 || c.q1_launch > 2 || c.nedrt_precond < 0 || c.nedrt_precond > 1)
     return MSFEC_ERROR_INVALID_ARGUMENT;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || c.device < 0 || c.device >= ndev) return MSFEC_ERROR_CUDA;
@@ -1740,7 +1784,16 @@ msfec_status msfec_nedrt_backward(msfec_handle *h, int32_t ncells, const msfec_c
   prm.inner_rtol = h->cfg.inner_rtol;
   prm.max_iter = std::max(h->cfg.max_iter, 8000);
   prm.max_refine = h->cfg.max_refine;
-  MSFEC_CUDA_TRY(h, nedrt_solve_launch(fp64, prm, smem, grid, st));
+  // the forward build's multilevel data serves the transposed solves (same cells, same S A S form)
+  size_t smem_a = smem;
+  const size_t ml_bytes = nr_ml_layout(nmax, fp64 ? 8 : 4).bytes;
+  const bool ml = h->nr_ml_valid && nmax >= 4 && smem + ml_bytes <= kNRSmemTotalLimit;
+  if (ml) {
+    prm.coarse = h->nr_coarse.ptr;
+    prm.ml_offset = smem;
+    smem_a += ml_bytes;
+  }
+  MSFEC_CUDA_TRY(h, nedrt_solve_launch(fp64, ml, prm, smem_a, grid, st));
   if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[1], st));
   MSFEC_CUDA_TRY(h, nedrt_adjoint_gradient_launch(h->nr_cells.ptr, ncells, h->nr_ainv.ptr, h->nr_bdiv.ptr,
                                                   h->nra_comb.ptr, h->nra_work.ptr, h->nra_x.ptr, h->nra_ga.ptr,
@@ -2049,6 +2102,7 @@ __global__ void __launch_bounds__(kNRPlanThreads)
     q.n = n;
     q.coef_off = pf;
     q.dof_off = pd;
+    q.coarse_off = -1;  // no multilevel data in the static pool: diagonal preconditioner
     cells[c] = q;
     const long long slot = first[dep] + ((pk >> (16 * (dep - 1))) & 0xFFFF);
     for (int b = 0; b < 18; ++b) items[slot * 18 + b] = NRItem{c, b, 0};
@@ -2155,7 +2209,7 @@ msfec_status msfec_nedrt_build_noalloc(msfec_handle *h, int32_t ncells, const ms
   prm.max_iter = std::max(h->cfg.max_iter, 8000);
   prm.max_refine = h->cfg.max_refine;
   if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[0], st));
-  MSFEC_CUDA_TRY(h, nedrt_solve_launch(fp64, prm, smem, grid, st));
+  MSFEC_CUDA_TRY(h, nedrt_solve_launch(fp64, false, prm, smem, grid, st));  // diagonal preconditioner
   if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[1], st));
   msfec_load ld;
   if (load) {

@@ -25,6 +25,7 @@ struct NRCell {
   int n;
   long long coef_off;  // first fine cell in ainv6 / bdiv
   long long dof_off;   // sum of previous cells' DoF counts; Phi base = 18 * dof_off
+  long long coarse_off;  // first float of the cell's multilevel preconditioner data, -1: none
 };
 
 struct NRItem {
@@ -58,6 +59,8 @@ struct NRParams {
   const double *src_floor;  // source mode: [cell] lower bound of the ||f|| the stopping test scales
   float *scratch;       // global workspace when the item does not fit shared memory
   size_t scratch_floats;  // per CTA
+  const float *coarse;    // multilevel preconditioner data (per cell at coarse_off); null: diagonal only
+  size_t ml_offset;       // byte offset of the multilevel region in the dynamic shared memory
   int use_smem;
   double rtol;
   double inner_rtol;
@@ -99,6 +102,53 @@ __host__ __device__ inline size_t nr_split_global_floats(int n) {
   nr_counts(n, NEx, NFx, NE, NF);
   const size_t Np = ((size_t)NE + NF + 63) / 64 * 64;
   return Np + (8 * (size_t)n * n * n + 63) / 64 * 64;
+}
+
+// ---- multilevel (BPX) preconditioner of the face (Schur) block
+// Face-space hierarchy of a cell with n = 2^L fine cells per side: levels
+// m = n/2, n/4, ..., 2 (k = 1 .. L-1). Level m holds the lowest-order RT
+// functions of the m^3 sub-box grid whose flux sits on an interior plane
+// P = 1..m-1: 3 (m-1) m^2 functions, index (d (m-1) + P-1) m^2 + b m + a for
+// normal d and patch (a, b) on the two other axes in increasing order.
+__host__ __device__ inline int nr_ml_count(int m) { return 3 * (m - 1) * m * m; }
+
+// Per-cell data (floats): inverse diagonals of the Galerkin operators of the
+// levels n/2 .. 4, then the 12 x 12 inverse of the level-2 operator.
+__host__ __device__ inline int nr_ml_data_floats(int n) {
+  if (n < 4) return 0;
+  int s = 144;
+  for (int m = n / 2; m >= 4; m /= 2) s += nr_ml_count(m);
+  return s;
+}
+
+// Layout of the solver's multilevel region (bytes from its start): restriction
+// accumulator and correction of level n/2 (precision T), the restricted /
+// corrected vectors of the levels below, the cell's data, one 16-bit code per
+// face DoF (and pad) giving its level-n/2 parents, and one per function of the
+// levels n/2 .. 4 giving its parents one level down.
+struct NRMLLayout {
+  int F1;
+  size_t off_y, off_wk, off_data, off_codes, off_lcodes, bytes;
+};
+
+__host__ __device__ inline NRMLLayout nr_ml_layout(int n, int tsize) {
+  NRMLLayout l{};
+  if (n < 4) return l;
+  int NEx, NFx, NE, NF;
+  nr_counts(n, NEx, NFx, NE, NF);
+  const size_t Np = ((size_t)NE + NF + 63) / 64 * 64;
+  l.F1 = nr_ml_count(n / 2);
+  size_t fw = 0, nl = 0;
+  for (int m = n / 4; m >= 2; m /= 2) fw += nr_ml_count(m);
+  for (int m = n / 2; m >= 4; m /= 2) nl += nr_ml_count(m);
+  auto al16 = [](size_t b) { return (b + 15) / 16 * 16; };
+  l.off_y = (size_t)l.F1 * tsize;
+  l.off_wk = 2 * (size_t)l.F1 * tsize;
+  l.off_data = al16(l.off_wk + 2 * fw * tsize);
+  l.off_codes = al16(l.off_data + (size_t)nr_ml_data_floats(n) * 4);
+  l.off_lcodes = al16(l.off_codes + (Np - NE) * 2);
+  l.bytes = al16(l.off_lcodes + nl * 2);
+  return l;
 }
 
 }  // namespace msfec

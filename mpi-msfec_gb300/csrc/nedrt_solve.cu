@@ -40,8 +40,8 @@ struct NRShared {
   float Cf[12][6];       // (curl tau_l, v_f) on the fine cell
   NRFactors<float> Ff;  // tensor-product factors of the current item's cell
   NRFactors<double> Fd;
-  alignas(16) float fslot[2][kNRWarps];  // per-warp partials of the two fused MINRES reductions
-  double dslot[2][kNRWarps];
+  alignas(16) float fslot[3][kNRWarps];  // per-warp partials of the fused MINRES reductions
+  double dslot[3][kNRWarps];              // (slot 2: multilevel share of gamma^2)
   int item;
 };
 
@@ -405,12 +405,222 @@ __device__ __forceinline__ void block_sum(NRShared &sh, VT (&v)[NV], VT (&out)[N
   }
 }
 
+// ---------------- multilevel (BPX) preconditioner of the face block ----------------
+// z = P v on the faces is diag^-1 v + sum over the levels m = n/2, ..., 2 of
+// P_m X_m P_m^T v: X_m the inverse diagonal of the Galerkin operator
+// P_m^T S P_m (levels n/2 .. 4) or its exact inverse (level 2, 12 functions),
+// S = D + C^T diag(M)^-1 C the Schur complement with M lumped. The level
+// functions nest (index map in nedrt_common.cuh): a level-m function is
+// the sum of the level-2m functions at planes 2P-1, 2P, 2P+1 of its four
+// child patches, weights 1/8, 1/4, 1/8; a fine face (level n, planes 0..n)
+// maps to level n/2 by the same rule. The products are evaluated as a
+// restriction cascade, an exact 12 x 12 solve and a prolongation cascade.
+
+__device__ __forceinline__ int ml_index(int lm, int d, int P, int a, int b) {
+  const int m = 1 << lm;
+  return ((d * (m - 1) + P - 1) << (2 * lm)) + (b << lm) + a;
+}
+
+// Parents of the level-2m (or fine) function / face (d, p, x, y) at level m = 2^lm.
+__device__ __forceinline__ int ml_parents(int lm, int d, int p, int x, int y, int (&j)[2], float (&w)[2]) {
+  const int m = 1 << lm;
+  const int a = x >> 1, b = y >> 1;
+  int cnt = 0;
+  if (!(p & 1)) {
+    const int P = p >> 1;
+    if (P >= 1 && P <= m - 1) {
+      j[0] = ml_index(lm, d, P, a, b);
+      w[0] = 0.25f;
+      cnt = 1;
+    }
+  } else {
+    const int P0 = p >> 1;
+    if (P0 >= 1) {
+      j[cnt] = ml_index(lm, d, P0, a, b);
+      w[cnt++] = 0.125f;
+    }
+    if (P0 + 1 <= m - 1) {
+      j[cnt] = ml_index(lm, d, P0 + 1, a, b);
+      w[cnt++] = 0.125f;
+    }
+  }
+  return cnt;
+}
+
+// 16-bit code of a fine face's level-n/2 parents: bits 0-11 the first parent,
+// bit 12 first valid, bit 13 second valid (first + m^2), bit 14 odd plane
+// (weights 1/8, else 1/4).
+__device__ __forceinline__ unsigned short ml_code(int lm, int d, int p, int x, int y) {
+  int j[2];
+  float w[2];
+  const int cnt = ml_parents(lm, d, p, x, y, j, w);
+  if (cnt == 0) return 0;
+  return (unsigned short)(j[0] | 0x1000 | (cnt == 2 ? 0x2000 : 0) | ((p & 1) ? 0x4000 : 0));
+}
+
+template <typename T>
+__device__ __forceinline__ T ml_code_prolong(unsigned code, const T *y, int m2) {
+  if (!(code & 0x1000u)) return T(0);
+  const int j = code & 0xFFF;
+  T s = y[j];
+  if (code & 0x2000u) s += y[j + m2];
+  return s * ((code & 0x4000u) ? T(0.125) : T(0.25));
+}
+
+// (d, P, a, b) of function J of level 2^lm.
+__device__ __forceinline__ void ml_decode(int lm, int J, int &d, int &P, int &a, int &b) {
+  const int m = 1 << lm;
+  const int per = (m - 1) << (2 * lm);
+  d = (J >= per) + (J >= 2 * per);
+  const int rem = J - d * per;
+  P = (rem >> (2 * lm)) + 1;
+  b = (rem >> lm) & (m - 1);
+  a = rem & (m - 1);
+}
+
+// Restriction of a level-2^lmc vector to function J of level 2^(lmc-1).
+template <typename T>
+__device__ __forceinline__ T ml_restrict_one(const T *rc, int lmc, int J) {
+  int d, P, a, b;
+  ml_decode(lmc - 1, J, d, P, a, b);
+  T s = T(0);
+#pragma unroll
+  for (int q = -1; q <= 1; ++q) {
+    const T w = q == 0 ? T(0.25) : T(0.125);
+#pragma unroll
+    for (int yy = 0; yy < 2; ++yy)
+#pragma unroll
+      for (int xx = 0; xx < 2; ++xx) s += w * rc[ml_index(lmc, d, 2 * P + q, 2 * a + xx, 2 * b + yy)];
+  }
+  return s;
+}
+
+// Fine face DoF of normal d at plane p, transverse position (x, y).
+__device__ __forceinline__ int face_dof(const NRGeom &g, int d, int p, int x, int y) {
+  const int n = g.n;
+  if (d == 0) return g.NE + p + (n + 1) * (x + n * y);
+  if (d == 1) return g.NE + g.NFx + x + n * (p + (n + 1) * y);
+  return g.NE + 2 * g.NFx + x + n * (y + n * p);
+}
+
+template <typename VT>
+__device__ __forceinline__ void warp_publish(NRShared &sh, int slot, VT v);
+template <typename VT, int NW>
+__device__ __forceinline__ VT slot_total(const NRShared &sh, int slot);
+
+// Coarse part of z = P v, all threads of the block: level-n/2 restriction of
+// the face part of v (a gather, one thread per function), the cascade of
+// restrictions, the exact level-2 solve (warp 0, shuffles), the prolongations
+// with the diagonal terms; writes the level-n/2 coefficients y1 (the fine
+// prolongation is left to the caller) and returns the coarse share of
+// gamma^2 = v^T (P - diag^-1) v, identical in every thread. One barrier per
+// level and direction (three at depth 3). wk: the vectors of the levels below
+// n/2; dat: inverse diagonals and the level-2 inverse; lc: parent codes of the
+// level n/2 .. 4 functions one level down.
+template <typename T, int NW>
+__device__ T ml_coarse_block(NRShared &sh, const NRGeom &g, const T *vsrc, T *r1, T *y1, T *wk, const float *dat,
+                             const unsigned short *lc) {
+  constexpr int NT = NW * 32;
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int L = g.L, K = L - 1;  // levels k = 1..K with 2^(L-k) cells per side; k = K is level 2
+  T *rk[4], *yk[4];
+  const float *dk[4];
+  int oc[4];
+  rk[1] = r1;
+  yk[1] = y1;
+  int ow = 0, od = 0;
+  oc[1] = 0;
+  for (int k = 1; k <= K; ++k) {
+    const int F = nr_ml_count(1 << (L - k));
+    if (k >= 2) {
+      rk[k] = wk + ow;
+      yk[k] = wk + ow + F;
+      ow += 2 * F;
+      oc[k] = oc[k - 1] + nr_ml_count(1 << (L - k + 1));
+    }
+    if (k < K) {
+      dk[k] = dat + od;
+      od += F;
+    }
+  }
+  const float *S2 = dat + od;
+  T part = T(0);
+  {  // fine -> level n/2: planes 2P-1, 2P, 2P+1 (weights 1/8, 1/4, 1/8) of the 2 x 2 child patches
+    const int lm = L - 1, F = nr_ml_count(1 << lm), n = g.n;
+    for (int j = tid; j < F; j += NT) {
+      int d, P, a, b;
+      ml_decode(lm, j, d, P, a, b);
+      // DoF strides along the normal and the two transverse axes of a face family
+      const int ps = d == 0 ? 1 : (d == 1 ? n : n * n);
+      const int xs = d == 0 ? n + 1 : 1;
+      const int ys = d == 0 ? (n + 1) * n : (d == 1 ? n * (n + 1) : n);
+      const T *v0 = vsrc + face_dof(g, d, 2 * P - 1, 2 * a, 2 * b);
+      T s = T(0);
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        const T *vq = v0 + q * ps;
+        s += (q == 1 ? T(0.25) : T(0.125)) * ((vq[0] + vq[xs]) + (vq[ys] + vq[xs + ys]));
+      }
+      r1[j] = s;
+      if (K > 1) part += s * (T)dk[1][j] * s;
+      if (K == 2) {  // level-2 restriction accumulated here (12 targets)
+        int jj[2];
+        float ww[2];
+        const int cnt = ml_parents(lm - 1, d, P, a, b, jj, ww);
+        for (int t = 0; t < cnt; ++t) atomicAdd(rk[2] + jj[t], (T)ww[t] * s);
+      }
+    }
+    __syncthreads();
+  }
+  for (int k = 2; k < K; ++k) {  // the diagonal levels below n/2
+    const int F = nr_ml_count(1 << (L - k));
+    for (int J = tid; J < F; J += NT) {
+      const T r = ml_restrict_one(rk[k - 1], L - k + 1, J);
+      rk[k][J] = r;
+      part += r * (T)dk[k][J] * r;
+      if (k + 1 == K) {
+        int d, P, a, b, jj[2];
+        float ww[2];
+        ml_decode(L - k, J, d, P, a, b);
+        const int cnt = ml_parents(L - k - 1, d, P, a, b, jj, ww);
+        for (int t = 0; t < cnt; ++t) atomicAdd(rk[K] + jj[t], (T)ww[t] * r);
+      }
+    }
+    __syncthreads();
+  }
+  if (tid < 32) {  // level 2: exact solve in warp 0 (rk[K] complete; cleared for the next call)
+    T yK = T(0), rme = T(0);
+    if (lane < 12) {
+#pragma unroll
+      for (int q = 0; q < 12; ++q) yK += (T)S2[lane * 12 + q] * rk[K][q];
+      rme = rk[K][lane];
+    }
+    __syncwarp();
+    if (lane < 12) {
+      yk[K][lane] = yK;
+      part += rme * yK;
+      if (K > 1) rk[K][lane] = T(0);
+    }
+  }
+  if (K == 1) warp_publish<T>(sh, 2, part);
+  __syncthreads();
+  for (int k = K - 1; k >= 1; --k) {  // prolongations with the diagonal terms
+    const int F = nr_ml_count(1 << (L - k));
+    const int mp2 = 1 << (2 * (L - k - 1));
+    for (int j = tid; j < F; j += NT)
+      yk[k][j] = (T)dk[k][j] * rk[k][j] + ml_code_prolong(lc[oc[k] + j], yk[k + 1], mp2);
+    if (k == 1) warp_publish<T>(sh, 2, part);
+    __syncthreads();
+  }
+  return slot_total<T, NW>(sh, 2);
+}
+
 extern __shared__ __align__(256) unsigned char nr_dyn_smem[];
 
 // One (cell, basis) item. SMEM: the workspace is the dynamic shared memory
 // (known at compile time, so every vector access is a shared-memory access),
 // otherwise this CTA's slot of the global scratch.
-template <typename T, bool SMEM, int NT>
+template <typename T, bool SMEM, int NT, bool ML>
 __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
   // NT = 256 (two CTAs per SM, mixed precision, shared workspace): the
   // correction x and the float coefficients live in this CTA's global slot so
@@ -514,6 +724,49 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
   }
   __syncthreads();
 
+  // ---- multilevel part of the preconditioner (block-uniform switch): the
+  // cell's data from HBM, the faces' level-n/2 parent codes
+  const bool ml = ML && prm.coarse != nullptr && Cc.coarse_off >= 0;
+  const NRMLLayout mll = nr_ml_layout(n, (int)sizeof(T));
+  unsigned char *mlb = nr_dyn_smem + prm.ml_offset;
+  T *ml_rr = reinterpret_cast<T *>(mlb);
+  T *ml_y = reinterpret_cast<T *>(mlb + mll.off_y);
+  T *ml_wk = reinterpret_cast<T *>(mlb + mll.off_wk);
+  float *ml_dat = reinterpret_cast<float *>(mlb + mll.off_data);
+  unsigned short *ml_codes = reinterpret_cast<unsigned short *>(mlb + mll.off_codes);
+  unsigned short *ml_lcodes = reinterpret_cast<unsigned short *>(mlb + mll.off_lcodes);
+  const int m2 = 1 << (2 * (g.L - 1));
+  if (ml) {
+    const float *src = prm.coarse + Cc.coarse_off;
+    const int nd = nr_ml_data_floats(n);
+    for (int t = tid; t < nd; t += NT) ml_dat[t] = src[t];
+    for (int t = tid; t < mll.F1; t += NT) ml_rr[t] = T(0);
+    for (int t = tid; t < (int)((mll.off_data - mll.off_wk) / sizeof(T)); t += NT) ml_wk[t] = T(0);
+    for (int u = tid; u < (int)Np - g.NE; u += NT) {
+      const int d = g.NE + u;
+      unsigned short code = 0;
+      if (d < N) {
+        int dir, i, j, k;
+        dof_geometry(g, d, dir, i, j, k);
+        const int fd = dir - 3;
+        const int p = fd == 0 ? i : (fd == 1 ? j : k);
+        const int x = fd == 0 ? j : i;
+        const int y = fd == 2 ? j : k;
+        code = ml_code(g.L - 1, fd, p, x, y);
+      }
+      ml_codes[u] = code;
+    }
+    for (int k = 1, o = 0; (1 << (g.L - k)) >= 4; o += nr_ml_count(1 << (g.L - k)), ++k) {
+      const int lm = g.L - k;
+      for (int j = tid; j < nr_ml_count(1 << lm); j += NT) {
+        int d, p, x, y;
+        ml_decode(lm, j, d, p, x, y);
+        ml_lcodes[o + j] = ml_code(lm - 1, d, p, x, y);
+      }
+    }
+    __syncthreads();
+  }
+
   double bnorm2 = 0.0, rnorm2 = 0.0;
   int conv = 0, its = 0, flags = 0, nref = 0;
 
@@ -605,192 +858,378 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
     conv = !fp32_res && (rnorm2 <= prm.rtol * prm.rtol * bnorm2);
     if (conv || ir >= prm.max_refine) break;
 
-    // ---------------- MINRES on A_II d = r, precision T ----------------
-    // Preconditioned Lanczos + MINRES (Paige-Saunders recurrences in the form
-    // of Elman, Silvester & Wathen, preconditioner pd, x0 = 0) in two
-    // block-wide phases per iteration, each ending in one barrier:
-    //   phase 1: az = A z~_j cell by cell, fused with delta~ = z~_j^T S A z~_j,
-    //            plus the w / x update of iteration j-1 (it needs a1, which
-    //            depends on gamma_j, known only after phase 2 of j-1);
-    //   phase 2: v~_{j+1} = (S az - delta v~_j) / g_j - gamma_j v~_{j-1} / g_{j-1},
-    //            z~_{j+1} = P v~_{j+1}, gamma_{j+1}^2 = z~_{j+1}^T v~_{j+1}.
-    // The Lanczos vectors are kept unnormalised (v_j = v~_j / g_j, g_j =
-    // gamma_j), so there is no normalisation pass; each phase's reduction is
-    // published per warp and summed by every thread after the barrier.
-    for (int d = tid; d < (int)Np; d += NT) {  // pads included: the float4 passes cover [0, Np)
-      vB[d] = T(0);
-      wA[d] = T(0);
-      wB[d] = T(0);
-      xk[d] = T(0);
-      az[d] = T(0);
-    }
-    T *vc = vA, *vp = vB;  // v~_j, v~_{j-1}
-    T *wo = wA, *wc = wB;  // w_{j-1}, w_j
-    T gam;                 // gamma_j
-    {
-      T p1[1] = {T(0)};
+    if (ML && ml) {
+      // ---------------- MINRES with the multilevel face preconditioner ----------------
+      // The recurrences of the diagonal path below, with z~_j = P v~_j no longer
+      // recomputable from v~_j alone: zt holds the full z~_j, and each iteration
+      // runs three block-wide phases and the coarse step, each ending in barriers:
+      //   phase 1: az = A z~_j, delta~;
+      //   phase 2: v~_{j+1}; az <- diag^-1 v~_{j+1} (the fine part of z~_{j+1});
+      //            gamma^2 partials;
+      //   coarse:  level-n/2 coefficients y of the coarse part of z~_{j+1} and
+      //            its share of gamma_{j+1}^2 (ml_coarse_block);
+      //   phase 3: w_j from z~_j (still in zt), x += c eta w_j, then
+      //            zt <- az + P_{n/2} y (the full z~_{j+1}), az <- 0.
       for (int d = tid; d < (int)Np; d += NT) {
-        const T z = (T)pd[d] * vc[d];
-        zt[d] = z;
-        p1[0] += z * vc[d];
+        vB[d] = T(0);
+        wA[d] = T(0);
+        wB[d] = T(0);
+        xk[d] = T(0);
+        az[d] = T(0);
       }
-      T t1[1];
-      block_sum<T, 1, NW>(sh, p1, t1);
-      gam = sqrt(t1[0]);
-    }
-    const T eta0 = gam;
-    T eta = gam, c_prev = T(1), cc = T(1), s_prev = T(0), ss = T(0);
-    T gi_c = gam > T(0) ? T(1) / gam : T(0), gi_p = T(0);  // 1/gamma_j, 1/gamma_{j-1}
-    const double tol_abs = prm.rtol * sqrt(bnorm2);
-    // inner target on |eta| (preconditioned residual): for the mixed path a
-    // relative reduction inner_rtol, relaxed on the last refinement step to
-    // what the outer tolerance still asks (0.1 tol_abs / ||r||); for FP64 the
-    // outer tolerance itself. Both are mapped through eta0 / ||r||.
-    const double outer = 0.1 * tol_abs / fmax(sqrt(rnorm2), 1e-300);
-    const T target = (T)((kMixed ? fmax(prm.inner_rtol, outer) : outer) * (double)eta0);
-    bool active = gam > T(0) && isfinite(gam);
-    bool pending = false;  // w / x update of the last iteration not yet applied
-    T p_step = T(0), p_a2 = T(0), p_a3 = T(0), p_ia1 = T(0);
-    __syncthreads();
-    for (int iter = 0; active && iter < prm.max_iter; ++iter) {
-      // ---- phase 1
-      T dpart = T(0);
-      for (int c = tid; c < nc; c += NT) {
-        int e[12], f[6];
-        cell_dofs(g, c, e, f);
-        const bool eb[12] = {}, fb[6] = {};
-        if constexpr (kMixed) {
-          const float4 c0 = reinterpret_cast<const float4 *>(cf)[2 * c];
-          const float4 c1 = reinterpret_cast<const float4 *>(cf)[2 * c + 1];
-          const float ai[6] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y};
-          dpart += cell_apply_s<float, float, float, 0, true>(zt, az, Ff, ai, c1.z, e, f, eb, fb);
-        } else {
-          const double *a = ag + 6 * (size_t)c;
-          const double ai[6] = {a[0], a[1], a[2], a[3], a[4], a[5]};
-          dpart += cell_apply_s<double, double, double, 0, true>(zt, az, Fd, ai, bg[c] * invV, e, f, eb, fb);
+      T *vc = vA, *vp = vB;
+      T *wo = wA, *wc = wB;
+      T gam;
+      {
+        T p1[1] = {T(0)};
+        for (int d = tid; d < (int)Np; d += NT) {
+          const T z = (T)pd[d] * vc[d];
+          zt[d] = z;
+          p1[0] += z * vc[d];
         }
+        T t1[1];
+        block_sum<T, 1, NW>(sh, p1, t1);  // its barriers also complete vc
+        const T gc = ml_coarse_block<T, NW>(sh, g, vc, ml_rr, ml_y, ml_wk, ml_dat, ml_lcodes);
+        gam = sqrt(fmax(t1[0] + gc, T(0)));
+        for (int d = g.NE + tid; d < N; d += NT) zt[d] += ml_code_prolong(ml_codes[d - g.NE], ml_y, m2);
+        __syncthreads();
       }
-      if (pending) {  // w_j = (z_{j-1} - a3 w_{j-2} - a2 w_{j-1}) / a1, x += c eta w_j
-        if constexpr (kMixed) {  // 4 DoFs per thread and vector access (pads are 0)
+      const T eta0 = gam;
+      T eta = gam, c_prev = T(1), cc = T(1), s_prev = T(0), ss = T(0);
+      T gi_c = gam > T(0) ? T(1) / gam : T(0), gi_p = T(0);
+      const double tol_abs = prm.rtol * sqrt(bnorm2);
+      const double outer = 0.1 * tol_abs / fmax(sqrt(rnorm2), 1e-300);
+      const T target = (T)((kMixed ? fmax(prm.inner_rtol, outer) : outer) * (double)eta0);
+      bool active = gam > T(0) && isfinite(gam);
+      for (int iter = 0; active && iter < prm.max_iter; ++iter) {
+        // ---- phase 1
+        T dpart = T(0);
+        for (int c = tid; c < nc; c += NT) {
+          int e[12], f[6];
+          cell_dofs(g, c, e, f);
+          const bool eb[12] = {}, fb[6] = {};
+          if constexpr (kMixed) {
+            const float4 c0 = reinterpret_cast<const float4 *>(cf)[2 * c];
+            const float4 c1 = reinterpret_cast<const float4 *>(cf)[2 * c + 1];
+            const float ai[6] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y};
+            dpart += cell_apply_s<float, float, float, 0, true>(zt, az, Ff, ai, c1.z, e, f, eb, fb);
+          } else {
+            const double *a = ag + 6 * (size_t)c;
+            const double ai[6] = {a[0], a[1], a[2], a[3], a[4], a[5]};
+            dpart += cell_apply_s<double, double, double, 0, true>(zt, az, Fd, ai, bg[c] * invV, e, f, eb, fb);
+          }
+        }
+        warp_publish<T>(sh, 0, dpart);
+        __syncthreads();
+        const T delta = slot_total<T, NW>(sh, 0) * gi_c * gi_c;
+        // ---- phase 2
+        T gpart = T(0);
+        const T gg = gam * gi_p;
+        if constexpr (kMixed) {  // 4 DoFs per access; face quads start at NE (NE % 4 == 0 for n >= 4)
           const float4 *pd4 = reinterpret_cast<const float4 *>(pd);
-          const float4 *vp4 = reinterpret_cast<const float4 *>(vp);
-          float4 *wo4 = reinterpret_cast<float4 *>(wo);
-          const float4 *wc4 = reinterpret_cast<const float4 *>(wc);
-          float4 *xk4 = reinterpret_cast<float4 *>(xk);
+          const float4 *vc4 = reinterpret_cast<const float4 *>(vc);
+          float4 *vp4 = reinterpret_cast<float4 *>(vp);
+          float4 *az4 = reinterpret_cast<float4 *>(az);
           for (int q = tid; q < (int)(Np / 4); q += NT) {
-            const float4 pv = pd4[q], v = vp4[q], a = wo4[q], b = wc4[q];
-            float4 x = xk4[q], wn;
-            wn.x = (pv.x * v.x * gi_p - p_a3 * a.x - p_a2 * b.x) * p_ia1;
-            wn.y = (pv.y * v.y * gi_p - p_a3 * a.y - p_a2 * b.y) * p_ia1;
-            wn.z = (pv.z * v.z * gi_p - p_a3 * a.z - p_a2 * b.z) * p_ia1;
-            wn.w = (pv.w * v.w * gi_p - p_a3 * a.w - p_a2 * b.w) * p_ia1;
-            x.x += p_step * wn.x;
-            x.y += p_step * wn.y;
-            x.z += p_step * wn.z;
-            x.w += p_step * wn.w;
-            wo4[q] = wn;
-            xk4[q] = x;
+            const float4 pv = pd4[q], a = az4[q], c = vc4[q], v = vp4[q];
+            const bool face = 4 * q >= g.NE;
+            const float sg = face ? -1.0f : 1.0f;
+            auto lane = [&](float pdd, float ad, float cd, float vd) {
+              return pdd > 0.0f ? (sg * ad - delta * cd) * gi_c - gg * vd : 0.0f;
+            };
+            float4 vn, z;
+            vn.x = lane(pv.x, a.x, c.x, v.x);
+            vn.y = lane(pv.y, a.y, c.y, v.y);
+            vn.z = lane(pv.z, a.z, c.z, v.z);
+            vn.w = lane(pv.w, a.w, c.w, v.w);
+            z.x = pv.x * vn.x;
+            z.y = pv.y * vn.y;
+            z.z = pv.z * vn.z;
+            z.w = pv.w * vn.w;
+            vp4[q] = vn;
+            az4[q] = z;
+            gpart += z.x * vn.x + z.y * vn.y + z.z * vn.z + z.w * vn.w;
           }
         } else {
           for (int d = tid; d < N; d += NT) {
-            const T z = (T)pd[d] * vp[d] * gi_p;
-            const T wn = (z - p_a3 * wo[d] - p_a2 * wc[d]) * p_ia1;
+            const float pdd = pd[d];
+            T vn = T(0);
+            if (pdd > 0.0f) {
+              const T a = d < g.NE ? az[d] : -az[d];
+              vn = (a - delta * vc[d]) * gi_c - gg * vp[d];
+            }
+            vp[d] = vn;
+            const T z = (T)pdd * vn;
+            az[d] = z;
+            gpart += z * vn;
+          }
+        }
+        warp_publish<T>(sh, 1, gpart);
+        __syncthreads();
+        // ---- coarse step (reads v~_{j+1}, now in vp)
+        const T gc = ml_coarse_block<T, NW>(sh, g, vp, ml_rr, ml_y, ml_wk, ml_dat, ml_lcodes);
+        const T gnew = sqrt(fmax(slot_total<T, NW>(sh, 1) + gc, T(0)));
+        const T a0 = cc * delta - c_prev * ss * gam;
+        const T a1 = sqrt(a0 * a0 + gnew * gnew);
+        const T a2 = ss * delta + c_prev * cc * gam;
+        const T a3 = s_prev * gam;
+        if (!(a1 > T(0)) || !isfinite(a1)) {
+          flags |= 1;
+          break;
+        }
+        const T cn = a0 / a1, sn = gnew / a1;
+        const T step = cn * eta, ia1 = T(1) / a1;
+        // ---- phase 3
+        if constexpr (kMixed) {
+          const float4 *az4 = reinterpret_cast<const float4 *>(az);
+          float4 *zt4 = reinterpret_cast<float4 *>(zt);
+          float4 *wo4 = reinterpret_cast<float4 *>(wo);
+          const float4 *wc4 = reinterpret_cast<const float4 *>(wc);
+          float4 *xk4 = reinterpret_cast<float4 *>(xk);
+          float4 *azw = reinterpret_cast<float4 *>(az);
+          for (int q = tid; q < (int)(Np / 4); q += NT) {
+            const float4 z = zt4[q], a = wo4[q], b = wc4[q], fz = az4[q];
+            float4 x = xk4[q], wn, nz = fz;
+            wn.x = (z.x * gi_c - a3 * a.x - a2 * b.x) * ia1;
+            wn.y = (z.y * gi_c - a3 * a.y - a2 * b.y) * ia1;
+            wn.z = (z.z * gi_c - a3 * a.z - a2 * b.z) * ia1;
+            wn.w = (z.w * gi_c - a3 * a.w - a2 * b.w) * ia1;
+            x.x += step * wn.x;
+            x.y += step * wn.y;
+            x.z += step * wn.z;
+            x.w += step * wn.w;
+            if (4 * q >= g.NE) {
+              const uint2 cw = reinterpret_cast<const uint2 *>(ml_codes)[q - g.NE / 4];
+              nz.x += ml_code_prolong(cw.x & 0xFFFFu, (const float *)ml_y, m2);
+              nz.y += ml_code_prolong(cw.x >> 16, (const float *)ml_y, m2);
+              nz.z += ml_code_prolong(cw.y & 0xFFFFu, (const float *)ml_y, m2);
+              nz.w += ml_code_prolong(cw.y >> 16, (const float *)ml_y, m2);
+            }
+            wo4[q] = wn;
+            xk4[q] = x;
+            zt4[q] = nz;
+            azw[q] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+          }
+        } else {
+          for (int d = tid; d < (int)Np; d += NT) {
+            const T wn = (zt[d] * gi_c - a3 * wo[d] - a2 * wc[d]) * ia1;
             wo[d] = wn;
-            xk[d] += p_step * wn;
+            xk[d] += step * wn;
+            T nz = az[d];
+            if (d >= g.NE) nz += ml_code_prolong(ml_codes[d - g.NE], ml_y, m2);
+            zt[d] = nz;
+            az[d] = T(0);
           }
         }
-        T *t = wo;
-        wo = wc;
-        wc = t;
-      }
-      warp_publish<T>(sh, 0, dpart);
-      __syncthreads();
-      const T delta = slot_total<T, NW>(sh, 0) * gi_c * gi_c;
-      // ---- phase 2
-      T gpart = T(0);
-      const T gg = gam * gi_p;
-      if constexpr (kMixed) {  // 4 DoFs per thread and vector access (pads are 0)
-        const float4 *pd4 = reinterpret_cast<const float4 *>(pd);
-        const float4 *vc4 = reinterpret_cast<const float4 *>(vc);
-        float4 *vp4 = reinterpret_cast<float4 *>(vp);
-        float4 *az4 = reinterpret_cast<float4 *>(az);
-        float4 *zt4 = reinterpret_cast<float4 *>(zt);
-        for (int q = tid; q < (int)(Np / 4); q += NT) {
-          const float4 pv = pd4[q], a = az4[q], c = vc4[q], v = vp4[q];
-          const int d0 = 4 * q;
-          auto lane = [&](float pdd, float ad, float cd, float vd, int d) {
-            const float sa = d < g.NE ? ad : -ad;
-            return pdd > 0.0f ? (sa - delta * cd) * gi_c - gg * vd : 0.0f;
-          };
-          float4 vn, z;
-          vn.x = lane(pv.x, a.x, c.x, v.x, d0);
-          vn.y = lane(pv.y, a.y, c.y, v.y, d0 + 1);
-          vn.z = lane(pv.z, a.z, c.z, v.z, d0 + 2);
-          vn.w = lane(pv.w, a.w, c.w, v.w, d0 + 3);
-          z.x = pv.x * vn.x;
-          z.y = pv.y * vn.y;
-          z.z = pv.z * vn.z;
-          z.w = pv.w * vn.w;
-          vp4[q] = vn;
-          az4[q] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-          zt4[q] = z;
-          gpart += z.x * vn.x + z.y * vn.y + z.z * vn.z + z.w * vn.w;
+        {
+          T *t = wo;
+          wo = wc;
+          wc = t;
+          t = vc;  // v~_{j+1} becomes current
+          vc = vp;
+          vp = t;
         }
-      } else {
-        for (int d = tid; d < N; d += NT) {
-          const float pdd = pd[d];
-          T vn = T(0);
-          if (pdd > 0.0f) {
-            const T a = d < g.NE ? az[d] : -az[d];
-            vn = (a - delta * vc[d]) * gi_c - gg * vp[d];
-          }
-          vp[d] = vn;
-          az[d] = T(0);
-          const T z = (T)pdd * vn;
-          zt[d] = z;
-          gpart += z * vn;
-        }
+        __syncthreads();
+        gi_p = gi_c;
+        gi_c = gnew > T(0) ? T(1) / gnew : T(0);
+        ++its;
+        eta = -sn * eta;
+        gam = gnew;
+        c_prev = cc;
+        cc = cn;
+        s_prev = ss;
+        ss = sn;
+        if (fabs(eta) <= target || gnew == T(0)) active = false;
       }
-      warp_publish<T>(sh, 1, gpart);
       __syncthreads();
-      const T gnew = sqrt(fmax(slot_total<T, NW>(sh, 1), T(0)));
-      const T a0 = cc * delta - c_prev * ss * gam;
-      const T a1 = sqrt(a0 * a0 + gnew * gnew);
-      const T a2 = ss * delta + c_prev * cc * gam;
-      const T a3 = s_prev * gam;
-      if (!(a1 > T(0)) || !isfinite(a1)) {
-        flags |= 1;
-        break;
+    } else {
+      // ---------------- MINRES on A_II d = r, precision T ----------------
+      // Preconditioned Lanczos + MINRES (Paige-Saunders recurrences in the form
+      // of Elman, Silvester & Wathen, preconditioner pd, x0 = 0) in two
+      // block-wide phases per iteration, each ending in one barrier:
+      //   phase 1: az = A z~_j cell by cell, fused with delta~ = z~_j^T S A z~_j,
+      //            plus the w / x update of iteration j-1 (it needs a1, which
+      //            depends on gamma_j, known only after phase 2 of j-1);
+      //   phase 2: v~_{j+1} = (S az - delta v~_j) / g_j - gamma_j v~_{j-1} / g_{j-1},
+      //            z~_{j+1} = P v~_{j+1}, gamma_{j+1}^2 = z~_{j+1}^T v~_{j+1}.
+      // The Lanczos vectors are kept unnormalised (v_j = v~_j / g_j, g_j =
+      // gamma_j), so there is no normalisation pass; each phase's reduction is
+      // published per warp and summed by every thread after the barrier.
+      for (int d = tid; d < (int)Np; d += NT) {  // pads included: the float4 passes cover [0, Np)
+        vB[d] = T(0);
+        wA[d] = T(0);
+        wB[d] = T(0);
+        xk[d] = T(0);
+        az[d] = T(0);
       }
-      const T cn = a0 / a1, sn = gnew / a1;
-      p_step = cn * eta;
-      p_a2 = a2;
-      p_a3 = a3;
-      p_ia1 = T(1) / a1;
-      pending = true;
+      T *vc = vA, *vp = vB;  // v~_j, v~_{j-1}
+      T *wo = wA, *wc = wB;  // w_{j-1}, w_j
+      T gam;                 // gamma_j
       {
-        T *t = vc;  // v~_{j+1} becomes current
-        vc = vp;
-        vp = t;
+        T p1[1] = {T(0)};
+        for (int d = tid; d < (int)Np; d += NT) {
+          const T z = (T)pd[d] * vc[d];
+          zt[d] = z;
+          p1[0] += z * vc[d];
+        }
+        T t1[1];
+        block_sum<T, 1, NW>(sh, p1, t1);
+        gam = sqrt(t1[0]);
       }
-      gi_p = gi_c;
-      gi_c = gnew > T(0) ? T(1) / gnew : T(0);
-      ++its;
-      eta = -sn * eta;
-      gam = gnew;
-      c_prev = cc;
-      cc = cn;
-      s_prev = ss;
-      ss = sn;
-      if (fabs(eta) <= target || gnew == T(0)) active = false;
+      const T eta0 = gam;
+      T eta = gam, c_prev = T(1), cc = T(1), s_prev = T(0), ss = T(0);
+      T gi_c = gam > T(0) ? T(1) / gam : T(0), gi_p = T(0);  // 1/gamma_j, 1/gamma_{j-1}
+      const double tol_abs = prm.rtol * sqrt(bnorm2);
+      // inner target on |eta| (preconditioned residual): for the mixed path a
+      // relative reduction inner_rtol, relaxed on the last refinement step to
+      // what the outer tolerance still asks (0.1 tol_abs / ||r||); for FP64 the
+      // outer tolerance itself. Both are mapped through eta0 / ||r||.
+      const double outer = 0.1 * tol_abs / fmax(sqrt(rnorm2), 1e-300);
+      const T target = (T)((kMixed ? fmax(prm.inner_rtol, outer) : outer) * (double)eta0);
+      bool active = gam > T(0) && isfinite(gam);
+      bool pending = false;  // w / x update of the last iteration not yet applied
+      T p_step = T(0), p_a2 = T(0), p_a3 = T(0), p_ia1 = T(0);
+      __syncthreads();
+      for (int iter = 0; active && iter < prm.max_iter; ++iter) {
+        // ---- phase 1
+        T dpart = T(0);
+        for (int c = tid; c < nc; c += NT) {
+          int e[12], f[6];
+          cell_dofs(g, c, e, f);
+          const bool eb[12] = {}, fb[6] = {};
+          if constexpr (kMixed) {
+            const float4 c0 = reinterpret_cast<const float4 *>(cf)[2 * c];
+            const float4 c1 = reinterpret_cast<const float4 *>(cf)[2 * c + 1];
+            const float ai[6] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y};
+            dpart += cell_apply_s<float, float, float, 0, true>(zt, az, Ff, ai, c1.z, e, f, eb, fb);
+          } else {
+            const double *a = ag + 6 * (size_t)c;
+            const double ai[6] = {a[0], a[1], a[2], a[3], a[4], a[5]};
+            dpart += cell_apply_s<double, double, double, 0, true>(zt, az, Fd, ai, bg[c] * invV, e, f, eb, fb);
+          }
+        }
+        if (pending) {  // w_j = (z_{j-1} - a3 w_{j-2} - a2 w_{j-1}) / a1, x += c eta w_j
+          if constexpr (kMixed) {  // 4 DoFs per thread and vector access (pads are 0)
+            const float4 *pd4 = reinterpret_cast<const float4 *>(pd);
+            const float4 *vp4 = reinterpret_cast<const float4 *>(vp);
+            float4 *wo4 = reinterpret_cast<float4 *>(wo);
+            const float4 *wc4 = reinterpret_cast<const float4 *>(wc);
+            float4 *xk4 = reinterpret_cast<float4 *>(xk);
+            for (int q = tid; q < (int)(Np / 4); q += NT) {
+              const float4 pv = pd4[q], v = vp4[q], a = wo4[q], b = wc4[q];
+              float4 x = xk4[q], wn;
+              wn.x = (pv.x * v.x * gi_p - p_a3 * a.x - p_a2 * b.x) * p_ia1;
+              wn.y = (pv.y * v.y * gi_p - p_a3 * a.y - p_a2 * b.y) * p_ia1;
+              wn.z = (pv.z * v.z * gi_p - p_a3 * a.z - p_a2 * b.z) * p_ia1;
+              wn.w = (pv.w * v.w * gi_p - p_a3 * a.w - p_a2 * b.w) * p_ia1;
+              x.x += p_step * wn.x;
+              x.y += p_step * wn.y;
+              x.z += p_step * wn.z;
+              x.w += p_step * wn.w;
+              wo4[q] = wn;
+              xk4[q] = x;
+            }
+          } else {
+            for (int d = tid; d < N; d += NT) {
+              const T z = (T)pd[d] * vp[d] * gi_p;
+              const T wn = (z - p_a3 * wo[d] - p_a2 * wc[d]) * p_ia1;
+              wo[d] = wn;
+              xk[d] += p_step * wn;
+            }
+          }
+          T *t = wo;
+          wo = wc;
+          wc = t;
+        }
+        warp_publish<T>(sh, 0, dpart);
+        __syncthreads();
+        const T delta = slot_total<T, NW>(sh, 0) * gi_c * gi_c;
+        // ---- phase 2
+        T gpart = T(0);
+        const T gg = gam * gi_p;
+        if constexpr (kMixed) {  // 4 DoFs per thread and vector access (pads are 0)
+          const float4 *pd4 = reinterpret_cast<const float4 *>(pd);
+          const float4 *vc4 = reinterpret_cast<const float4 *>(vc);
+          float4 *vp4 = reinterpret_cast<float4 *>(vp);
+          float4 *az4 = reinterpret_cast<float4 *>(az);
+          float4 *zt4 = reinterpret_cast<float4 *>(zt);
+          for (int q = tid; q < (int)(Np / 4); q += NT) {
+            const float4 pv = pd4[q], a = az4[q], c = vc4[q], v = vp4[q];
+            const int d0 = 4 * q;
+            auto lane = [&](float pdd, float ad, float cd, float vd, int d) {
+              const float sa = d < g.NE ? ad : -ad;
+              return pdd > 0.0f ? (sa - delta * cd) * gi_c - gg * vd : 0.0f;
+            };
+            float4 vn, z;
+            vn.x = lane(pv.x, a.x, c.x, v.x, d0);
+            vn.y = lane(pv.y, a.y, c.y, v.y, d0 + 1);
+            vn.z = lane(pv.z, a.z, c.z, v.z, d0 + 2);
+            vn.w = lane(pv.w, a.w, c.w, v.w, d0 + 3);
+            z.x = pv.x * vn.x;
+            z.y = pv.y * vn.y;
+            z.z = pv.z * vn.z;
+            z.w = pv.w * vn.w;
+            vp4[q] = vn;
+            az4[q] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            zt4[q] = z;
+            gpart += z.x * vn.x + z.y * vn.y + z.z * vn.z + z.w * vn.w;
+          }
+        } else {
+          for (int d = tid; d < N; d += NT) {
+            const float pdd = pd[d];
+            T vn = T(0);
+            if (pdd > 0.0f) {
+              const T a = d < g.NE ? az[d] : -az[d];
+              vn = (a - delta * vc[d]) * gi_c - gg * vp[d];
+            }
+            vp[d] = vn;
+            az[d] = T(0);
+            const T z = (T)pdd * vn;
+            zt[d] = z;
+            gpart += z * vn;
+          }
+        }
+        warp_publish<T>(sh, 1, gpart);
+        __syncthreads();
+        const T gnew = sqrt(fmax(slot_total<T, NW>(sh, 1), T(0)));
+        const T a0 = cc * delta - c_prev * ss * gam;
+        const T a1 = sqrt(a0 * a0 + gnew * gnew);
+        const T a2 = ss * delta + c_prev * cc * gam;
+        const T a3 = s_prev * gam;
+        if (!(a1 > T(0)) || !isfinite(a1)) {
+          flags |= 1;
+          break;
+        }
+        const T cn = a0 / a1, sn = gnew / a1;
+        p_step = cn * eta;
+        p_a2 = a2;
+        p_a3 = a3;
+        p_ia1 = T(1) / a1;
+        pending = true;
+        {
+          T *t = vc;  // v~_{j+1} becomes current
+          vc = vp;
+          vp = t;
+        }
+        gi_p = gi_c;
+        gi_c = gnew > T(0) ? T(1) / gnew : T(0);
+        ++its;
+        eta = -sn * eta;
+        gam = gnew;
+        c_prev = cc;
+        cc = cn;
+        s_prev = ss;
+        ss = sn;
+        if (fabs(eta) <= target || gnew == T(0)) active = false;
+      }
+      if (pending)
+        for (int d = tid; d < N; d += NT) {
+          const T z = (T)pd[d] * vp[d] * gi_p;
+          const T wn = (z - p_a3 * wo[d] - p_a2 * wc[d]) * p_ia1;
+          xk[d] += p_step * wn;
+        }
+      __syncthreads();
     }
-    if (pending)
-      for (int d = tid; d < N; d += NT) {
-        const T z = (T)pd[d] * vp[d] * gi_p;
-        const T wn = (z - p_a3 * wo[d] - p_a2 * wc[d]) * p_ia1;
-        xk[d] += p_step * wn;
-      }
-    __syncthreads();
     // ---------------- phi_I += x (FP64, HBM) ----------------
     for (int d = tid; d < N; d += NT)
       if (pd[d] > 0.0f) phi[d] += (double)xk[d];
@@ -827,7 +1266,8 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
   __syncthreads();
 }
 
-template <typename T, int NT>
+// ML: multilevel face preconditioner (cells with coarse data), else diagonal.
+template <typename T, int NT, bool ML>
 __global__ void __launch_bounds__(NT, 512 / NT) nedrt_solve_kernel(NRParams prm) {
   __shared__ NRShared sh;
   for (;;) {
@@ -836,12 +1276,12 @@ __global__ void __launch_bounds__(NT, 512 / NT) nedrt_solve_kernel(NRParams prm)
     const int item = sh.item;
     if (item >= prm.n_items) break;
     if constexpr (NT == 256) {
-      solve_item<T, true, 256>(prm, sh, item);  // split workspace: shared vectors + global x / coefficients
+      solve_item<T, true, 256, ML>(prm, sh, item);  // split workspace: shared vectors + global x / coefficients
     } else {
       if (prm.use_smem)
-        solve_item<T, true, NT>(prm, sh, item);
+        solve_item<T, true, NT, ML>(prm, sh, item);
       else
-        solve_item<T, false, NT>(prm, sh, item);
+        solve_item<T, false, NT, ML>(prm, sh, item);
     }
   }
 }
@@ -1297,42 +1737,270 @@ __global__ void __launch_bounds__(kAdjThreads) nr_adj_gradient_kernel(const NRCe
   }
 }
 
+// ---------------- multilevel preconditioner setup ----------------
+constexpr int kMLSetupThreads = 512;
+
+// Values at fine face (d, q, x, y) of the level-(n >> k) functions: up to two
+// (index, weight, plane) triples; the hat along the normal times the flux share.
+__device__ __forceinline__ int ml_fine_weights(int L, int k, int d, int q, int x, int y, int (&j)[2], float (&w)[2],
+                                               int (&P)[2]) {
+  const int lm = L - k, m = 1 << lm, r = 1 << k;
+  const int a = x >> k, b = y >> k, P0 = q >> k, rem = q & (r - 1);
+  const float inv = 1.0f / (float)(r * r);
+  int cnt = 0;
+  if (P0 >= 1 && P0 <= m - 1) {
+    j[cnt] = ml_index(lm, d, P0, a, b);
+    P[cnt] = P0;
+    w[cnt++] = (float)(r - rem) / (float)r * inv;
+  }
+  if (rem != 0 && P0 + 1 >= 1 && P0 + 1 <= m - 1) {
+    j[cnt] = ml_index(lm, d, P0 + 1, a, b);
+    P[cnt] = P0 + 1;
+    w[cnt++] = (float)rem / (float)r * inv;
+  }
+  return cnt;
+}
+
+// One CTA per coarse cell (persistent over the batch): for the cell's levels
+// n/2 .. 4 the inverse diagonal of P_m^T S P_m and for level 2 the inverse of
+// the 12 x 12 P_2^T S P_2, S = D + C^T diag(M)^-1 C on the interior faces. S is
+// applied as two masked passes of the element operator (faces -> edges, edge
+// scaling by diag(M)^-1, edges -> faces); it couples faces up to two fine
+// planes apart along their normal (face -> edges of both adjacent cells ->
+// their faces) and one cell across. A diagonal level is probed colour by
+// colour (normal d, P mod 3, a and b mod 2: functions of one colour then have
+// disjoint S-neighbourhoods, so one application of S to their sum gives all
+// their diagonal entries: 36 probes per level); level 2 function by function.
+// scratch per CTA: edge diagonal, probe vector, two accumulators (4 Np floats).
+__global__ void __launch_bounds__(kMLSetupThreads) nr_ml_setup_kernel(const NRCell *__restrict__ cells, int ncells,
+                                                                     const double *__restrict__ ainv6,
+                                                                     const double *__restrict__ bdiv,
+                                                                     float *__restrict__ coarse,
+                                                                     float *__restrict__ scratch,
+                                                                     size_t scratch_floats) {
+  __shared__ NRShared sh;
+  __shared__ double s2[144];
+  float *acc = reinterpret_cast<float *>(nr_dyn_smem);  // the cell's data, accumulated then inverted
+  constexpr int NT = kMLSetupThreads;
+  const int tid = threadIdx.x;
+  for (int cell = blockIdx.x; cell < ncells; cell += gridDim.x) {
+    const NRCell Cc = cells[cell];
+    if (Cc.coarse_off < 0) continue;  // block-uniform
+    NRGeom g;
+    g.n = Cc.n;
+    g.L = Cc.depth;
+    nr_counts(g.n, g.NEx, g.NFx, g.NE, g.NF);
+    g.N = g.NE + g.NF;
+    const int n = g.n, N = g.N, nc = n * n * n, L = g.L;
+    const size_t Np = ((size_t)N + 63) / 64 * 64;
+    float *md = scratch + (size_t)blockIdx.x * scratch_floats;
+    float *x = md + Np, *a1 = x + Np, *a2 = a1 + Np;
+    const double invV = 1.0 / (Cc.h[0] * Cc.h[1] * Cc.h[2]);
+    const double *ag = ainv6 + 6 * Cc.coef_off;
+    const double *bg = bdiv + Cc.coef_off;
+    if (tid == 0) make_factors(Cc.h, sh.Ff);
+    for (int t = tid; t < 144; t += NT) {
+      const int p = t / 48, q = (t / 16) % 3, l4 = (t / 4) % 4, m4 = t % 4;
+      sh.Gf[p][q][l4][m4] = (float)table_G(Cc.h, p, q, l4, m4);
+    }
+    const int nd = nr_ml_data_floats(n);
+    for (int t = tid; t < nd; t += NT) acc[t] = 0.0f;
+    for (int d = tid; d < N; d += NT) md[d] = 0.0f;
+    __syncthreads();
+    for (int c = tid; c < nc; c += NT) {
+      int e[12], f[6];
+      cell_dofs(g, c, e, f);
+      const double *a = ag + 6 * (size_t)c;
+#pragma unroll
+      for (int l = 0; l < 12; ++l) atomicAdd(md + e[l], (float)a[l >> 2] * sh.Gf[l >> 2][l >> 2][l & 3][l & 3]);
+    }
+    __syncthreads();
+    // probe loop: pr < 36 (K - 1) diagonal-level colours, then the 12 level-2 functions
+    const int K = L - 1;
+    const int nprobe = 36 * (K - 1) + 12;
+    for (int pr = 0; pr < nprobe; ++pr) {
+      const bool exact = pr >= 36 * (K - 1);
+      const int k = exact ? K : 1 + pr / 36;  // level 2^(L-k)
+      const int col = pr % 36;
+      const int cd = col / 12, cP = (col >> 2) % 3, ca = (col >> 1) & 1, cb = col & 1;
+      const int J = pr - 36 * (K - 1);  // exact: the probed function
+      int od = 0;  // data offset of level k
+      for (int kk = 1; kk < k; ++kk) od += nr_ml_count(1 << (L - kk));
+      const int lm = L - k;
+      // probe vector on the interior faces; accumulators cleared
+      for (int d = tid; d < N; d += NT) {
+        float v = 0.0f;
+        if (d >= g.NE) {
+          int dir, i, jj, kk;
+          dof_geometry(g, d, dir, i, jj, kk);
+          const int fd = dir - 3;
+          const int q = fd == 0 ? i : (fd == 1 ? jj : kk);
+          const int xx = fd == 0 ? jj : i, yy = fd == 2 ? jj : kk;
+          int fj[2], fP[2];
+          float fw[2];
+          const int cnt = ml_fine_weights(L, k, fd, q, xx, yy, fj, fw, fP);
+          for (int t = 0; t < cnt; ++t) {
+            if (exact) {
+              if (fj[t] == J) v += fw[t];
+            } else if (fd == cd && fP[t] % 3 == cP && ((xx >> k) & 1) == ca && ((yy >> k) & 1) == cb) {
+              v += fw[t];
+            }
+          }
+        }
+        x[d] = v;
+        a1[d] = 0.0f;
+        a2[d] = 0.0f;
+      }
+      __syncthreads();
+      const bool eb[12] = {}, fb[6] = {};
+      for (int c = tid; c < nc; c += NT) {  // a1 = A (0, x)
+        int e[12], f[6];
+        cell_dofs(g, c, e, f);
+        const double *a = ag + 6 * (size_t)c;
+        const float ai[6] = {(float)a[0], (float)a[1], (float)a[2], (float)a[3], (float)a[4], (float)a[5]};
+        cell_apply_s<float, float, float, 3, false>(x, a1, sh.Ff, ai, (float)(bg[c] * invV), e, f, eb, fb);
+      }
+      __syncthreads();
+      for (int d = tid; d < g.NE; d += NT) {  // t = diag(M)^-1 C x on the interior edges (A (0, x) = (-C x, D x))
+        int dir, i, jj, kk;
+        const bool bnd = dof_geometry(g, d, dir, i, jj, kk);
+        x[d] = (!bnd && md[d] > 0.0f) ? -a1[d] / md[d] : 0.0f;
+      }
+      __syncthreads();
+      for (int c = tid; c < nc; c += NT) {  // a2 = A (t, 0) = (M t, C^T t)
+        int e[12], f[6];
+        cell_dofs(g, c, e, f);
+        const double *a = ag + 6 * (size_t)c;
+        const float ai[6] = {(float)a[0], (float)a[1], (float)a[2], (float)a[3], (float)a[4], (float)a[5]};
+        cell_apply_s<float, float, float, 2, false>(x, a2, sh.Ff, ai, (float)(bg[c] * invV), e, f, eb, fb);
+      }
+      __syncthreads();
+      for (int d = g.NE + tid; d < N; d += NT) {  // (S x)_f = a1_f + a2_f against the probed functions
+        int dir, i, jj, kk;
+        const bool bnd = dof_geometry(g, d, dir, i, jj, kk);
+        if (bnd) continue;
+        const float sf = a1[d] + a2[d];
+        const int fd = dir - 3;
+        const int q = fd == 0 ? i : (fd == 1 ? jj : kk);
+        const int xx = fd == 0 ? jj : i, yy = fd == 2 ? jj : kk;
+        int fj[2], fP[2];
+        float fw[2];
+        const int cnt = ml_fine_weights(L, k, fd, q, xx, yy, fj, fw, fP);
+        for (int t = 0; t < cnt; ++t) {
+          if (exact) {
+            atomicAdd(acc + od + fj[t] * 12 + J, fw[t] * sf);
+          } else if (fd == cd && fP[t] % 3 == cP && ((xx >> k) & 1) == ca && ((yy >> k) & 1) == cb) {
+            atomicAdd(acc + od + fj[t], fw[t] * sf);
+          }
+        }
+      }
+      __syncthreads();
+    }
+    // invert: diagonal levels entrywise; level 2 by Gauss-Jordan (FP64, symmetrised)
+    int od2 = 0;
+    for (int kk = 1; kk < K; ++kk) od2 += nr_ml_count(1 << (L - kk));
+    for (int t = tid; t < od2; t += NT) acc[t] = acc[t] > 0.0f ? 1.0f / acc[t] : 0.0f;
+    for (int t = tid; t < 144; t += NT) {
+      const int r = t / 12, c = t % 12;
+      s2[t] = 0.5 * ((double)acc[od2 + r * 12 + c] + (double)acc[od2 + c * 12 + r]);
+    }
+    __syncthreads();
+    if (tid == 0) {
+      double inv[144];
+      for (int t = 0; t < 144; ++t) inv[t] = (t / 12 == t % 12) ? 1.0 : 0.0;
+      bool ok = true;
+      for (int c = 0; c < 12 && ok; ++c) {
+        int piv = c;
+        for (int r = c + 1; r < 12; ++r)
+          if (fabs(s2[r * 12 + c]) > fabs(s2[piv * 12 + c])) piv = r;
+        if (!(fabs(s2[piv * 12 + c]) > 0.0)) {
+          ok = false;
+          break;
+        }
+        if (piv != c)
+          for (int t = 0; t < 12; ++t) {
+            double u = s2[c * 12 + t];
+            s2[c * 12 + t] = s2[piv * 12 + t];
+            s2[piv * 12 + t] = u;
+            u = inv[c * 12 + t];
+            inv[c * 12 + t] = inv[piv * 12 + t];
+            inv[piv * 12 + t] = u;
+          }
+        const double ip = 1.0 / s2[c * 12 + c];
+        for (int t = 0; t < 12; ++t) {
+          s2[c * 12 + t] *= ip;
+          inv[c * 12 + t] *= ip;
+        }
+        for (int r = 0; r < 12; ++r) {
+          if (r == c) continue;
+          const double fct = s2[r * 12 + c];
+          if (fct == 0.0) continue;
+          for (int t = 0; t < 12; ++t) {
+            s2[r * 12 + t] -= fct * s2[c * 12 + t];
+            inv[r * 12 + t] -= fct * inv[c * 12 + t];
+          }
+        }
+      }
+      for (int r = 0; r < 12; ++r)
+        for (int c = 0; c < 12; ++c)  // symmetric by construction of the stored value
+          acc[od2 + r * 12 + c] = ok ? (float)(0.5 * (inv[r * 12 + c] + inv[c * 12 + r])) : 0.0f;
+    }
+    __syncthreads();
+    float *out = coarse + Cc.coarse_off;
+    for (int t = tid; t < nd; t += NT) out[t] = acc[t];
+    __syncthreads();
+  }
+}
+
 }  // namespace nrimpl
 
-cudaError_t nedrt_solve_launch(bool fp64, const NRParams &prm, size_t smem, int grid, cudaStream_t st) {
-  if (fp64) {
-    auto k = nrimpl::nedrt_solve_kernel<double, kNRThreads>;
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+template <typename T, int NT, bool ML>
+static cudaError_t launch_solve(const NRParams &prm, size_t smem, int grid, cudaStream_t st, bool carveout) {
+  auto k = nrimpl::nedrt_solve_kernel<T, NT, ML>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  if (carveout) {
+    e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if (e != cudaSuccess) return e;
-    k<<<grid, kNRThreads, smem, st>>>(prm);
-  } else {
-    auto k = nrimpl::nedrt_solve_kernel<float, kNRThreads>;
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    k<<<grid, kNRThreads, smem, st>>>(prm);
   }
+  k<<<grid, NT, smem, st>>>(prm);
   return cudaGetLastError();
+}
+
+// ml: the multilevel variant (prm.coarse set); smem includes its region.
+cudaError_t nedrt_solve_launch(bool fp64, bool ml, const NRParams &prm, size_t smem, int grid, cudaStream_t st) {
+  if (fp64) return ml ? launch_solve<double, kNRThreads, true>(prm, smem, grid, st, false)
+                      : launch_solve<double, kNRThreads, false>(prm, smem, grid, st, false);
+  return ml ? launch_solve<float, kNRThreads, true>(prm, smem, grid, st, false)
+            : launch_solve<float, kNRThreads, false>(prm, smem, grid, st, false);
 }
 
 // Mixed precision, two 256-thread CTAs per SM with the split workspace
 // (shared: preconditioner + 6 FP32 vectors; global slot: x + coefficients).
-cudaError_t nedrt_solve_launch_split(const NRParams &prm, size_t smem, int grid, cudaStream_t st) {
-  auto k = nrimpl::nedrt_solve_kernel<float, 256>;
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-  if (e != cudaSuccess) return e;
-  k<<<grid, 256, smem, st>>>(prm);
-  return cudaGetLastError();
+cudaError_t nedrt_solve_launch_split(bool ml, const NRParams &prm, size_t smem, int grid, cudaStream_t st) {
+  return ml ? launch_solve<float, 256, true>(prm, smem, grid, st, true)
+            : launch_solve<float, 256, false>(prm, smem, grid, st, true);
 }
 
-cudaError_t nedrt_split_occupancy(size_t smem, int *blocks_per_sm) {
-  auto k = nrimpl::nedrt_solve_kernel<float, 256>;
+cudaError_t nedrt_split_occupancy(bool ml, size_t smem, int *blocks_per_sm) {
+  auto k = ml ? nrimpl::nedrt_solve_kernel<float, 256, true> : nrimpl::nedrt_solve_kernel<float, 256, false>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
   if (e != cudaSuccess) return e;
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k, 256, smem);
+}
+
+// Multilevel preconditioner data of every cell with coarse_off >= 0.
+cudaError_t nedrt_ml_setup_launch(const NRCell *cells, int ncells, const double *ainv6, const double *bdiv,
+                                  float *coarse, float *scratch, size_t scratch_floats, size_t smem, int grid,
+                                  cudaStream_t st) {
+  if (ncells <= 0 || grid <= 0) return cudaSuccess;
+  auto k = nrimpl::nr_ml_setup_kernel;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k<<<grid, nrimpl::kMLSetupThreads, smem, st>>>(cells, ncells, ainv6, bdiv, coarse, scratch, scratch_floats);
+  return cudaGetLastError();
 }
 
 cudaError_t nedrt_galerkin_launch(const NRCell *cells, int ncells, const double *phi, const double *y,

@@ -48,7 +48,8 @@ class Config(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("precision", ctypes.c_int32), ("rtol", ctypes.c_double),
                 ("inner_rtol", ctypes.c_double), ("max_iter", ctypes.c_int32),
                 ("max_refine", ctypes.c_int32), ("verbose", ctypes.c_int32),
-                ("q1_launch", ctypes.c_int32), ("nedrt_rtol", ctypes.c_double)]
+                ("q1_launch", ctypes.c_int32), ("nedrt_rtol", ctypes.c_double),
+                ("nedrt_precond", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 class Cell(ctypes.Structure):
@@ -198,7 +199,7 @@ class Handle:
     """One msfec handle (device buffers + stream)."""
 
     def __init__(self, precision=PRECISION_MIXED, device=0, rtol=None, inner_rtol=None,
-                 max_iter=None, max_refine=None, verbose=0, nedrt_rtol=None, q1_launch=0):
+                 max_iter=None, max_refine=None, verbose=0, nedrt_rtol=None, q1_launch=0, nedrt_precond=0):
         L = load_library()
         cfg = Config()
         L.msfec_config_default(ctypes.byref(cfg))
@@ -216,6 +217,7 @@ class Handle:
             cfg.nedrt_rtol = nedrt_rtol
         cfg.verbose = int(verbose or os.environ.get("MSFEC_VERBOSE", "0"))
         cfg.q1_launch = int(q1_launch)
+        cfg.nedrt_precond = int(nedrt_precond)
         self.cfg = cfg
         h = _vp()
         st = L.msfec_create(ctypes.byref(h), ctypes.byref(cfg))

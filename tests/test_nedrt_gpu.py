@@ -92,3 +92,27 @@ def test_invalid_tensor_rejected(gpu):
     with pytest.raises(gpu.MsfecError) as e:
         h.nedrt_build(c5, ainv6, bdiv, load)
     assert e.value.status == gpu.ERROR_INVALID_ARGUMENT
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("depth", [2, 3, 4])
+def test_multilevel_preconditioner_matches_diagonal(gpu, precision, depth):
+    """The multilevel face preconditioner (default) and the diagonal one give the
+    same K_H to the stated tolerance; the multilevel one needs fewer iterations."""
+    cells, ainv6, bdiv, load = workloads.nedrt_tensor(m=1 if depth == 4 else 2, depth=depth, seed=11 + depth)
+    out = {}
+    for pc in (0, 1):
+        h = gpu.Handle(precision=gpu.PRECISION_MIXED if precision == "mixed" else gpu.PRECISION_FP64,
+                       nedrt_precond=pc)
+        KH, FH, rep, st = h.nedrt_build(cells, ainv6, bdiv, load)
+        assert st == gpu.SUCCESS and rep["converged"].all(), (pc, rep)
+        out[pc] = (KH, FH, rep)
+    for c in range(len(cells)):
+        assert _rel(out[0][0][c], out[1][0][c]) <= TOL_KH
+    if depth <= 3:
+        ref = N.build(cells, N.sym6_to_ainv(ainv6), bdiv, load.kind, list(load.params), want_phi=False)
+        for c in range(len(cells)):
+            assert _rel(out[0][0][c], ref["KH"][c]) <= TOL_KH
+    it_ml, it_d = out[0][2]["iterations"].max(), out[1][2]["iterations"].max()
+    print(f"{precision} depth {depth}: iterations multilevel {it_ml}, diagonal {it_d}")
+    assert it_ml < it_d
