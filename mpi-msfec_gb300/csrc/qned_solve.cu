@@ -154,10 +154,15 @@ __device__ __forceinline__ void rt_mass(const QNFactors<TA> &F, const TA (&A)[3]
 // atomically). MASK: 0 none, 1 keep only lattice-boundary values of z (lift
 // of the Dirichlet data), 2 keep only vertex values, 3 keep only edge values.
 // With DOT returns sum_d S_d z_d (A_e z_e)_d, S = +1 on vertices, -1 on edges.
-template <typename TA, typename TV, typename TO, int MASK, bool DOT>
+// MERGE: the warp holds complete x-rows of consecutive cells c (n >= 4, all
+// lanes active): contributions to the DoFs shared with the x-neighbour (4
+// vertices + 4 edges on the plane between them) and then with the
+// y-neighbour in the warp (2 vertices + 3 edges) are summed by shuffles before
+// the shared-memory atomics.
+template <typename TA, typename TV, typename TO, int MASK, bool DOT, bool MERGE = false>
 __device__ __forceinline__ TA cell_apply(const TV *__restrict__ z, TO *out, const QNFactors<TA> &F,
                                          const TA (&ai)[6], TA binv, const int (&vi)[8], const int (&ei)[12],
-                                         const bool (&vb)[8], const bool (&eb)[12]) {
+                                         const bool (&vb)[8], const bool (&eb)[12], int c = 0, int L = 0) {
   TA zv[8], ze[12];
 #pragma unroll
   for (int t = 0; t < 8; ++t) {
@@ -204,15 +209,62 @@ __device__ __forceinline__ TA cell_apply(const TV *__restrict__ z, TO *out, cons
     }
   }
   TA dot = TA(0);
+  if constexpr (DOT) {
 #pragma unroll
-  for (int t = 0; t < 8; ++t) {
-    atomicAdd(out + vi[t], (TO)yv[t]);
-    if (DOT) dot += zv[t] * yv[t];
+    for (int t = 0; t < 8; ++t) dot += zv[t] * yv[t];
+#pragma unroll
+    for (int l = 0; l < 12; ++l) dot -= ze[l] * ye[l];
   }
+  if constexpr (MERGE) {
+    const int n = 1 << L, lane = threadIdx.x & 31;
+    const int i = c & (n - 1), j = (c >> L) & (n - 1);
+    // plane x = i: vertices 0 2 4 6, y-edges 4 6, z-edges 8 10; plane x = i+1: the same with bit 0 set
+    TA lf[8] = {yv[0], yv[2], yv[4], yv[6], ye[4], ye[6], ye[8], ye[10]};
+    const TA rt[8] = {yv[1], yv[3], yv[5], yv[7], ye[5], ye[7], ye[9], ye[11]};
 #pragma unroll
-  for (int l = 0; l < 12; ++l) {
-    atomicAdd(out + ei[l], (TO)ye[l]);
-    if (DOT) dot -= ze[l] * ye[l];
+    for (int t = 0; t < 8; ++t) {
+      const TA v = __shfl_up_sync(0xffffffffu, rt[t], 1);
+      if (i > 0) lf[t] += v;
+    }
+    if (i == n - 1) {
+      atomicAdd(out + vi[1], (TO)rt[0]);
+      atomicAdd(out + vi[3], (TO)rt[1]);
+      atomicAdd(out + vi[5], (TO)rt[2]);
+      atomicAdd(out + vi[7], (TO)rt[3]);
+      atomicAdd(out + ei[5], (TO)rt[4]);
+      atomicAdd(out + ei[7], (TO)rt[5]);
+      atomicAdd(out + ei[9], (TO)rt[6]);
+      atomicAdd(out + ei[11], (TO)rt[7]);
+    }
+    atomicAdd(out + ei[4], (TO)lf[4]);
+    atomicAdd(out + ei[6], (TO)lf[5]);
+    // plane y = j: vertices 0 4, x-edges 0 2, z-edge 8; plane y = j+1: vertices 2 6, x-edges 1 3, z-edge 10
+    TA bt[5] = {lf[0], lf[2], ye[0], ye[2], lf[6]};
+    const TA tp[5] = {lf[1], lf[3], ye[1], ye[3], lf[7]};
+    const bool below = lane >= n && j > 0;
+    const bool above = lane + n < 32 && j < n - 1;
+#pragma unroll
+    for (int t = 0; t < 5; ++t) {
+      const TA v = __shfl_up_sync(0xffffffffu, tp[t], n);
+      if (below) bt[t] += v;
+    }
+    if (!above) {
+      atomicAdd(out + vi[2], (TO)tp[0]);
+      atomicAdd(out + vi[6], (TO)tp[1]);
+      atomicAdd(out + ei[1], (TO)tp[2]);
+      atomicAdd(out + ei[3], (TO)tp[3]);
+      atomicAdd(out + ei[10], (TO)tp[4]);
+    }
+    atomicAdd(out + vi[0], (TO)bt[0]);
+    atomicAdd(out + vi[4], (TO)bt[1]);
+    atomicAdd(out + ei[0], (TO)bt[2]);
+    atomicAdd(out + ei[2], (TO)bt[3]);
+    atomicAdd(out + ei[8], (TO)bt[4]);
+  } else {
+#pragma unroll
+    for (int t = 0; t < 8; ++t) atomicAdd(out + vi[t], (TO)yv[t]);
+#pragma unroll
+    for (int l = 0; l < 12; ++l) atomicAdd(out + ei[l], (TO)ye[l]);
   }
   return dot;
 }
@@ -591,11 +643,14 @@ __device__ void solve_item(const QNParams &prm, QNShared &sh, int item_id) {
           const float4 c0 = reinterpret_cast<const float4 *>(cf)[2 * c];
           const float4 c1 = reinterpret_cast<const float4 *>(cf)[2 * c + 1];
           const float ai[6] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y};
-          dpart += cell_apply<float, float, float, 0, true>(zt, az, Ff, ai, c1.z, v, e, vb, eb);
+          dpart += n >= 4 ? cell_apply<float, float, float, 0, true, true>(zt, az, Ff, ai, c1.z, v, e, vb, eb, c, g.L)
+                          : cell_apply<float, float, float, 0, true>(zt, az, Ff, ai, c1.z, v, e, vb, eb);
         } else {
           const double *a = ag + 6 * (size_t)c;
           const double ai[6] = {a[0], a[1], a[2], a[3], a[4], a[5]};
-          dpart += cell_apply<double, double, double, 0, true>(zt, az, Fd, ai, bg[c], v, e, vb, eb);
+          dpart += n >= 4 ? cell_apply<double, double, double, 0, true, true>(zt, az, Fd, ai, bg[c], v, e, vb, eb, c,
+                                                                               g.L)
+                          : cell_apply<double, double, double, 0, true>(zt, az, Fd, ai, bg[c], v, e, vb, eb);
         }
       }
       if (pending) {
