@@ -558,28 +558,32 @@ __device__ __forceinline__ void warp_publish(NRShared &sh, int slot, VT v);
 template <typename VT, int NW>
 __device__ __forceinline__ VT slot_total(const NRShared &sh, int slot);
 
-// Coarse part of z = P v, all threads of the block: level-n/2 restriction of
-// the face part of v (a gather, one thread per function), the cascade of
-// restrictions, the exact level-2 solve (warp 0, shuffles), the prolongations
-// with the diagonal terms; writes the level-n/2 coefficients y1 (the fine
-// prolongation is left to the caller) and returns the coarse share of
-// gamma^2 = v^T (P - diag^-1) v, identical in every thread. One barrier per
-// level and direction (three at depth 3). wk: the vectors of the levels below
-// n/2; dat: inverse diagonals and the level-2 inverse; lc: parent codes of the
-// level n/2 .. 4 functions one level down.
-template <typename T, int NW>
+// Coarse part of z = P v, all threads of the block, K = L - 1 coarse levels
+// (k = 1..K with 2^(L-k) cells per side; level K is level 2): the level-n/2
+// restriction of the face part of v (a gather, one thread per function; at
+// K == 2 also the level-2 restriction, by 12-target atomics), the restrictions
+// of the levels below (K == 3), the exact level-2 solve in every warp (lanes
+// 0..11, kept in a register), the prolongations with the diagonal terms (the
+// level above level 2 reads its parents by shuffles); writes the level-n/2
+// coefficients y1 (the fine prolongation is left to the caller) and returns
+// the coarse share of gamma^2 = v^T (P - diag^-1) v, identical in every
+// thread. Barriers: 2 at K <= 2, 4 at K == 3. wk: the vectors of the levels
+// below n/2; dat: inverse diagonals and the level-2 inverse; lc: parent codes
+// of the level n/2 .. 4 functions one level down.
+template <typename T, int NW, int K>
 __device__ T ml_coarse_block(NRShared &sh, const NRGeom &g, const T *vsrc, T *r1, T *y1, T *wk, const float *dat,
                              const unsigned short *lc) {
   constexpr int NT = NW * 32;
-  const int tid = threadIdx.x, lane = tid & 31;
-  const int L = g.L, K = L - 1;  // levels k = 1..K with 2^(L-k) cells per side; k = K is level 2
-  T *rk[4], *yk[4];
-  const float *dk[4];
-  int oc[4];
+  constexpr int L = K + 1;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  T *rk[K + 1], *yk[K + 1];
+  const float *dk[K + 1];
+  int oc[K + 1];
   rk[1] = r1;
   yk[1] = y1;
   int ow = 0, od = 0;
   oc[1] = 0;
+#pragma unroll
   for (int k = 1; k <= K; ++k) {
     const int F = nr_ml_count(1 << (L - k));
     if (k >= 2) {
@@ -596,7 +600,8 @@ __device__ T ml_coarse_block(NRShared &sh, const NRGeom &g, const T *vsrc, T *r1
   const float *S2 = dat + od;
   T part = T(0);
   {  // fine -> level n/2: planes 2P-1, 2P, 2P+1 (weights 1/8, 1/4, 1/8) of the 2 x 2 child patches
-    const int lm = L - 1, F = nr_ml_count(1 << lm), n = g.n;
+    constexpr int lm = L - 1;
+    const int F = nr_ml_count(1 << lm), n = g.n;
     for (int j = tid; j < F; j += NT) {
       int d, P, a, b;
       ml_decode(lm, j, d, P, a, b);
@@ -612,8 +617,8 @@ __device__ T ml_coarse_block(NRShared &sh, const NRGeom &g, const T *vsrc, T *r1
         s += (q == 1 ? T(0.25) : T(0.125)) * ((vq[0] + vq[xs]) + (vq[ys] + vq[xs + ys]));
       }
       r1[j] = s;
-      if (K > 1) part += s * (T)dk[1][j] * s;
-      if (K == 2) {  // level-2 restriction accumulated here (12 targets)
+      if constexpr (K > 1) part += s * (T)dk[1][j] * s;
+      if constexpr (K == 2) {  // level-2 restriction accumulated here (12 targets)
         int jj[2];
         float ww[2];
         const int cnt = ml_parents(lm - 1, d, P, a, b, jj, ww);
@@ -622,7 +627,8 @@ __device__ T ml_coarse_block(NRShared &sh, const NRGeom &g, const T *vsrc, T *r1
     }
     __syncthreads();
   }
-  for (int k = 2; k < K; ++k) {  // the diagonal levels below n/2
+#pragma unroll
+  for (int k = 2; k < K; ++k) {  // the diagonal levels below n/2 (K == 3: level 4)
     const int F = nr_ml_count(1 << (L - k));
     for (int J = tid; J < F; J += NT) {
       const T r = ml_restrict_one(rk[k - 1], L - k + 1, J);
@@ -638,31 +644,61 @@ __device__ T ml_coarse_block(NRShared &sh, const NRGeom &g, const T *vsrc, T *r1
     }
     __syncthreads();
   }
-  if (tid < 32) {  // level 2: exact solve in warp 0 (rk[K] complete; cleared for the next call)
-    T yK = T(0), rme = T(0);
-    if (lane < 12) {
+  // level 2, exact, in every warp: lane q < 12 holds y_K[q]
+  T yK = T(0), rme = T(0);
+  if (lane < 12) {
 #pragma unroll
-      for (int q = 0; q < 12; ++q) yK += (T)S2[lane * 12 + q] * rk[K][q];
-      rme = rk[K][lane];
-    }
-    __syncwarp();
-    if (lane < 12) {
-      yk[K][lane] = yK;
-      part += rme * yK;
-      if (K > 1) rk[K][lane] = T(0);
-    }
+    for (int q = 0; q < 12; ++q) yK += (T)S2[lane * 12 + q] * rk[K][q];
+    rme = rk[K][lane];
   }
-  if (K == 1) warp_publish<T>(sh, 2, part);
-  __syncthreads();
-  for (int k = K - 1; k >= 1; --k) {  // prolongations with the diagonal terms
-    const int F = nr_ml_count(1 << (L - k));
-    const int mp2 = 1 << (2 * (L - k - 1));
-    for (int j = tid; j < F; j += NT)
-      yk[k][j] = (T)dk[k][j] * rk[k][j] + ml_code_prolong(lc[oc[k] + j], yk[k + 1], mp2);
-    if (k == 1) warp_publish<T>(sh, 2, part);
+  if (tid < 12) part += rme * yK;  // counted once
+  if constexpr (K == 1) {
+    if (tid < 12) y1[tid] = yK;
+    warp_publish<T>(sh, 2, part);
     __syncthreads();
+    return slot_total<T, NW>(sh, 2);
+  } else {
+    {  // level K-1 from the register y_K (warp-uniform trip count: every lane takes part in the shuffles)
+      constexpr int k = K - 1;
+      const int F = nr_ml_count(1 << (L - k));
+      for (int base = warp * 32; base < F; base += NT) {
+        const int j = base + lane;
+        const bool ok = j < F;
+        const unsigned code = ok ? lc[oc[k] + j] : 0u;
+        const int j0 = code & 0xFFF, j1 = j0 + 4;  // level 2: 4 functions per plane
+        const T a0 = __shfl_sync(0xffffffffu, yK, j0 & 31);
+        const T a1 = __shfl_sync(0xffffffffu, yK, j1 & 31);
+        if (ok) {
+          T pr = T(0);
+          if (code & 0x1000u) pr = a0 + ((code & 0x2000u) ? a1 : T(0));
+          pr *= (code & 0x4000u) ? T(0.125) : T(0.25);
+          yk[k][j] = (T)dk[k][j] * rk[k][j] + pr;
+        }
+      }
+      if (k == 1) warp_publish<T>(sh, 2, part);
+      __syncthreads();
+    }
+#pragma unroll
+    for (int k = K - 2; k >= 1; --k) {  // the levels above, from shared memory
+      const int F = nr_ml_count(1 << (L - k));
+      const int mp2 = 1 << (2 * (L - k - 1));
+      for (int j = tid; j < F; j += NT)
+        yk[k][j] = (T)dk[k][j] * rk[k][j] + ml_code_prolong(lc[oc[k] + j], yk[k + 1], mp2);
+      if (k == 1) warp_publish<T>(sh, 2, part);
+      __syncthreads();
+    }
+    if (tid < 12) rk[K][tid] = T(0);  // every warp has read it; the next accumulation is barriers away
+    return slot_total<T, NW>(sh, 2);
   }
-  return slot_total<T, NW>(sh, 2);
+}
+
+// Dispatch on the cell's depth (2..4).
+template <typename T, int NW>
+__device__ __forceinline__ T ml_coarse(NRShared &sh, const NRGeom &g, const T *vsrc, T *r1, T *y1, T *wk,
+                                       const float *dat, const unsigned short *lc) {
+  if (g.L == 2) return ml_coarse_block<T, NW, 1>(sh, g, vsrc, r1, y1, wk, dat, lc);
+  if (g.L == 3) return ml_coarse_block<T, NW, 2>(sh, g, vsrc, r1, y1, wk, dat, lc);
+  return ml_coarse_block<T, NW, 3>(sh, g, vsrc, r1, y1, wk, dat, lc);
 }
 
 extern __shared__ __align__(256) unsigned char nr_dyn_smem[];
@@ -940,7 +976,7 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
         }
         T t1[1];
         block_sum<T, 1, NW>(sh, p1, t1);  // its barriers also complete vc
-        const T gc = ml_coarse_block<T, NW>(sh, g, vc, ml_rr, ml_y, ml_wk, ml_dat, ml_lcodes);
+        const T gc = ml_coarse<T, NW>(sh, g, vc, ml_rr, ml_y, ml_wk, ml_dat, ml_lcodes);
         gam = sqrt(fmax(t1[0] + gc, T(0)));
         for (int d = g.NE + tid; d < N; d += NT) zt[d] += ml_code_prolong(ml_codes[d - g.NE], ml_y, m2);
         __syncthreads();
@@ -1021,7 +1057,7 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
         warp_publish<T>(sh, 1, gpart);
         __syncthreads();
         // ---- coarse step (reads v~_{j+1}, now in vp)
-        const T gc = ml_coarse_block<T, NW>(sh, g, vp, ml_rr, ml_y, ml_wk, ml_dat, ml_lcodes);
+        const T gc = ml_coarse<T, NW>(sh, g, vp, ml_rr, ml_y, ml_wk, ml_dat, ml_lcodes);
         const T gnew = sqrt(fmax(slot_total<T, NW>(sh, 1) + gc, T(0)));
         const T a0 = cc * delta - c_prev * ss * gam;
         const T a1 = sqrt(a0 * a0 + gnew * gnew);
