@@ -98,29 +98,33 @@ __device__ double table_C(const double h[3], int l, int f) {
 }
 
 __device__ __forceinline__ void cell_dofs(const NRGeom &g, int c, int (&e)[12], int (&f)[6]) {
-  const int n = g.n;
+  // one base index per DoF family, the neighbours at constant strides
+  const int n = g.n, n1 = n + 1;
   const int i = c & (n - 1), j = (c >> g.L) & (n - 1), k = c >> (2 * g.L);
-  auto ex = [&](int a, int b, int cc) { return a + n * (b + (n + 1) * cc); };
-  auto ey = [&](int a, int b, int cc) { return g.NEx + a + (n + 1) * (b + n * cc); };
-  auto ez = [&](int a, int b, int cc) { return 2 * g.NEx + a + (n + 1) * (b + (n + 1) * cc); };
-  e[0] = ex(i, j, k);
-  e[1] = ex(i, j + 1, k);
-  e[2] = ex(i, j, k + 1);
-  e[3] = ex(i, j + 1, k + 1);
-  e[4] = ey(i, j, k);
-  e[5] = ey(i + 1, j, k);
-  e[6] = ey(i, j, k + 1);
-  e[7] = ey(i + 1, j, k + 1);
-  e[8] = ez(i, j, k);
-  e[9] = ez(i + 1, j, k);
-  e[10] = ez(i, j + 1, k);
-  e[11] = ez(i + 1, j + 1, k);
-  f[0] = g.NE + i + (n + 1) * (j + n * k);
-  f[1] = g.NE + (i + 1) + (n + 1) * (j + n * k);
-  f[2] = g.NE + g.NFx + i + n * (j + (n + 1) * k);
-  f[3] = g.NE + g.NFx + i + n * ((j + 1) + (n + 1) * k);
-  f[4] = g.NE + 2 * g.NFx + i + n * (j + n * k);
-  f[5] = g.NE + 2 * g.NFx + i + n * (j + n * (k + 1));
+  const int ex = i + n * (j + n1 * k);
+  const int ey = g.NEx + i + n1 * (j + n * k);
+  const int ez = 2 * g.NEx + i + n1 * (j + n1 * k);
+  e[0] = ex;
+  e[1] = ex + n;
+  e[2] = ex + n * n1;
+  e[3] = ex + n * n1 + n;
+  e[4] = ey;
+  e[5] = ey + 1;
+  e[6] = ey + n1 * n;
+  e[7] = ey + n1 * n + 1;
+  e[8] = ez;
+  e[9] = ez + 1;
+  e[10] = ez + n1;
+  e[11] = ez + n1 + 1;
+  const int fx = g.NE + i + n1 * (j + n * k);
+  const int fy = g.NE + g.NFx + i + n * (j + n1 * k);
+  const int fz = g.NE + 2 * g.NFx + i + n * (j + n * k);
+  f[0] = fx;
+  f[1] = fx + 1;
+  f[2] = fy;
+  f[3] = fy + n;
+  f[4] = fz;
+  f[5] = fz + n * n;
 }
 
 // (dir, i, j, k) of DoF d; returns true for a lattice-boundary DoF.
