@@ -73,13 +73,9 @@ __device__ __forceinline__ void rt_mass(const RTFactors<TA> &F, const TA (&A)[3]
 // the cell DoF by its owning thread). MASK: 0 none, 1 keep only
 // lattice-boundary face values and no cell value (lift of the boundary data),
 // 2 keep only face values. With DOT returns z_f . (A z)_f - z_c (A z)_c.
-// MERGE: the warp holds complete x-rows of consecutive cells c (n >= 4, all
-// lanes active): the x-face and y-face a cell shares with its x- and
-// y-neighbour in the warp are summed by shuffles before the atomics.
-template <typename TA, typename TV, typename TO, int MASK, bool DOT, bool MERGE = false>
+template <typename TA, typename TV, typename TO, int MASK, bool DOT>
 __device__ __forceinline__ TA cell_apply(const TV *__restrict__ z, TO *out, const RTFactors<TA> &F,
-                                         const TA (&ai)[6], const int (&fi)[6], int ci, const bool (&fb)[6],
-                                         int c = 0, int L = 0) {
+                                         const TA (&ai)[6], const int (&fi)[6], int ci, const bool (&fb)[6]) {
   TA zf[6];
 #pragma unroll
   for (int t = 0; t < 6; ++t) {
@@ -98,28 +94,10 @@ __device__ __forceinline__ TA cell_apply(const TV *__restrict__ z, TO *out, cons
   }
   const TA yc = (zf[1] - zf[0]) + (zf[3] - zf[2]) + (zf[5] - zf[4]);
   TA dot = TA(0);
-  if constexpr (DOT) {
 #pragma unroll
-    for (int t = 0; t < 6; ++t) dot += zf[t] * yf[t];
-  }
-  if constexpr (MERGE) {
-    const int n = 1 << L, lane = threadIdx.x & 31;
-    const int i = c & (n - 1), j = (c >> L) & (n - 1);
-    TA lx = yf[0];
-    const TA vx = __shfl_up_sync(0xffffffffu, yf[1], 1);
-    if (i > 0) lx += vx;
-    if (i == n - 1) atomicAdd(out + fi[1], (TO)yf[1]);
-    atomicAdd(out + fi[0], (TO)lx);
-    TA by = yf[2];
-    const TA vy = __shfl_up_sync(0xffffffffu, yf[3], n);
-    if (lane >= n && j > 0) by += vy;
-    if (!(lane + n < 32 && j < n - 1)) atomicAdd(out + fi[3], (TO)yf[3]);
-    atomicAdd(out + fi[2], (TO)by);
-    atomicAdd(out + fi[4], (TO)yf[4]);
-    atomicAdd(out + fi[5], (TO)yf[5]);
-  } else {
-#pragma unroll
-    for (int t = 0; t < 6; ++t) atomicAdd(out + fi[t], (TO)yf[t]);
+  for (int t = 0; t < 6; ++t) {
+    atomicAdd(out + fi[t], (TO)yf[t]);
+    if (DOT) dot += zf[t] * yf[t];
   }
   out[ci] += (TO)yc;
   if (DOT) dot -= zc * yc;
@@ -430,13 +408,11 @@ __device__ void solve_item(const RTParams &prm, RTShared &sh, int item_id) {
           const float4 c0 = reinterpret_cast<const float4 *>(cf)[2 * c];
           const float4 c1 = reinterpret_cast<const float4 *>(cf)[2 * c + 1];
           const float ai[6] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y};
-          dpart += n >= 4 ? cell_apply<float, float, float, 0, true, true>(zt, az, Ff, ai, f, ci, fb, c, g.L)
-                          : cell_apply<float, float, float, 0, true>(zt, az, Ff, ai, f, ci, fb);
+          dpart += cell_apply<float, float, float, 0, true>(zt, az, Ff, ai, f, ci, fb);
         } else {
           const double *a = ag + 6 * (size_t)c;
           const double ai[6] = {a[0], a[1], a[2], a[3], a[4], a[5]};
-          dpart += n >= 4 ? cell_apply<double, double, double, 0, true, true>(zt, az, Fd, ai, f, ci, fb, c, g.L)
-                          : cell_apply<double, double, double, 0, true>(zt, az, Fd, ai, f, ci, fb);
+          dpart += cell_apply<double, double, double, 0, true>(zt, az, Fd, ai, f, ci, fb);
         }
       }
       if (pending) {

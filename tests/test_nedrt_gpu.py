@@ -116,3 +116,23 @@ def test_multilevel_preconditioner_matches_diagonal(gpu, precision, depth):
     it_ml, it_d = out[0][2]["iterations"].max(), out[1][2]["iterations"].max()
     print(f"{precision} depth {depth}: iterations multilevel {it_ml}, diagonal {it_d}")
     assert it_ml < it_d
+
+
+def test_multilevel_mixed_depth_batch(gpu):
+    """One launch over cells of depths 1-4: every item picks its own level count
+    (diagonal only at depth 1) inside the shared multilevel region sized for the
+    deepest cell; K_H equals the diagonal-preconditioner build."""
+    parts = [workloads.nedrt_tensor(m=1, depth=d, seed=20 + d) for d in (2, 4, 1, 3, 2)]
+    cells = np.concatenate([p[0] for p in parts])
+    ainv6 = np.concatenate([p[1] for p in parts])
+    bdiv = np.concatenate([p[2] for p in parts])
+    load = parts[0][3]
+    out = {}
+    for pc in (0, 1):
+        h = gpu.Handle(nedrt_precond=pc)
+        KH, FH, rep, st = h.nedrt_build(cells, ainv6, bdiv, load)
+        assert st == gpu.SUCCESS and rep["converged"].all(), (pc, rep)
+        out[pc] = (KH, FH)
+    for c in range(len(cells)):
+        assert _rel(out[0][0][c], out[1][0][c]) <= TOL_KH, c
+        assert _rel(out[0][1][c], out[1][1][c]) <= TOL_KH, c
