@@ -411,6 +411,12 @@ def e2e_run(wl, lo, hi, local, stream, barrier, steps):
     return dt, h2d, d2h
 
 
+# DRAM bytes per coarse cell of one Ned_RT depth-3 solve launch (mixed precision, multilevel
+# preconditioner): ncu dram__bytes_read.sum + dram__bytes_write.sum of `bench.py --probe nedrt_256cells`
+# (profiles/nedrt_solve_kernel_L3_traffic.md), 358.2 MB / 256 cells; traffic grows with the cells.
+NEDRT_L3_TRAFFIC_PER_CELL = 358.2e6 / 256
+
+
 def roofline(wl, lo, hi, solve_ms, gal_ms, rep, kind):
     """Roofline of the dominant (solver) kernel and of the Galerkin kernel."""
     peak, peak_kind = peaks()
@@ -446,7 +452,9 @@ def roofline(wl, lo, hi, solve_ms, gal_ms, rep, kind):
     tflops = float(np.sum(per_cell_flops)) / (solve_ms * 1e-3) / 1e12
     return {"bound": "hbm", "kernel": f"{kind}_solve_kernel (persistent, on-chip Krylov state)",
             "achieved": alg_solve / (solve_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
-            "frac": alg_solve / (solve_ms * 1e-3) / 1e9 / peak, "traffic": None,
+            "frac": alg_solve / (solve_ms * 1e-3) / 1e9 / peak,
+            "traffic": (NEDRT_L3_TRAFFIC_PER_CELL * len(c)
+                        if wl.kind == "nedrt" and bool(np.all(c["depth"] == 3)) else None),
             "algorithmic_bytes": alg_solve, "launch_ms": solve_ms, "peak_source": peak_kind,
             "note": "Krylov vectors stay in shared memory/registers: HBM carries only coefficients "
                     "in and basis + K*basis out, so this fraction is low by design; the on-chip "
@@ -659,6 +667,9 @@ def probe(name):
     if name == "nedrt_one_cell":
         cells, ainv6, bdiv, load = workloads.nedrt_tensor(m=1, depth=3, seed=2)
         KH, FH, rep, st = h.nedrt_build(cells, ainv6, bdiv, load)
+    elif name == "nedrt_256cells":  # first half of the headline batch: basis + K*basis 271 MB > L2
+        cells, ainv6, bdiv, load = workloads.nedrt_tensor(m=8, depth=3, seed=2)
+        KH, FH, rep, st = h.nedrt_build(cells[:256], ainv6[:256 * 512], bdiv[:256 * 512], load)
     else:
         depth, m = (5, 1) if name == "q1_depth5_one_cell" else (3, 2)
         cells, a, r, load = workloads.q1_lognormal(m=m, depth=depth, seed=9, reaction=False)
@@ -683,7 +694,7 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-extra", action="store_true")
     ap.add_argument("--skip-adjoint", action="store_true")
-    ap.add_argument("--probe", default=None, choices=["nedrt_one_cell", "q1_depth5_one_cell", "q1_depth3_8cells"],
+    ap.add_argument("--probe", default=None, choices=["nedrt_one_cell", "nedrt_256cells", "q1_depth5_one_cell", "q1_depth3_8cells"],
                     help="run one small mixed build and exit (the case profiled with ncu --set full)")
     args = ap.parse_args()
     if args.probe:
