@@ -255,4 +255,226 @@ void NedRTBatch::solution(int slot, const std::vector<double> &w, std::vector<do
 }
 
 }  // namespace NedRT
+
+namespace QNed {
+
+QNedBasis::QNedBasis(const ParametersBasis &parameters, const std::string &parameter_filename,
+                     const CoarseCell &global_cell, const std::string &first_cell, unsigned local_subdomain,
+                     std::shared_ptr<QNedBatch> batch)
+    : parameters_(parameters),
+      parameter_filename_(parameter_filename),
+      cell_(global_cell),
+      first_cell_(first_cell),
+      local_subdomain_(local_subdomain),
+      batch_(std::move(batch)),
+      global_weights_(20, 0.0) {}
+
+void QNedBasis::run() {
+  if (slot_ < 0) slot_ = batch_->enqueue(cell_, parameters_.n_refine_local);
+}
+
+const FullMatrix &QNedBasis::get_global_element_matrix() const {
+  if (slot_ < 0) throw BasisError(MSFEC_ERROR_INVALID_STATE, "QNedBasis: run() was not called");
+  return batch_->matrix(slot_);
+}
+
+const Vector &QNedBasis::get_global_element_rhs() const {
+  if (slot_ < 0) throw BasisError(MSFEC_ERROR_INVALID_STATE, "QNedBasis: run() was not called");
+  return batch_->rhs(slot_);
+}
+
+const std::string &QNedBasis::get_filename_global() const { return parameters_.filename_global; }
+
+void QNedBasis::set_global_weights(const std::vector<double> &global_weights) {
+  if (global_weights.size() != 20) throw BasisError(MSFEC_ERROR_INVALID_ARGUMENT, "QNedBasis: 20 weights expected");
+  global_weights_ = global_weights;
+}
+
+void QNedBasis::set_output_flag() { output_flag_ = cell_.id == first_cell_; }
+
+void QNedBasis::global_solution(std::vector<double> &sigma, std::vector<double> &u) const {
+  if (slot_ < 0) throw BasisError(MSFEC_ERROR_INVALID_STATE, "QNedBasis: run() was not called");
+  batch_->solution(slot_, global_weights_, sigma, u);
+}
+
+QNedBatch::QNedBatch(QNedCoefficients coeff, int device, int precision)
+    : coeff_(std::move(coeff)), gpu_(device, precision) {}
+
+int QNedBatch::enqueue(const CoarseCell &cell, unsigned depth) {
+  if (built_) {
+    cells_.clear();
+    built_ = false;
+  }
+  cells_.push_back(make_cell(cell, depth));
+  return (int)cells_.size() - 1;
+}
+
+void QNedBatch::flush() {
+  if (built_) return;
+  std::vector<double> a6, binv;
+  for (const msfec_cell &c : cells_)
+    for_each_fine_centre(c, [&](const Point &p) {
+      const std::array<double, 9> m = coeff_.diffusion(p);
+      const double s[6] = {m[0], m[4], m[8], m[1], m[2], m[5]};
+      a6.insert(a6.end(), s, s + 6);
+      binv.push_back(coeff_.inverse_b(p));
+    });
+  const int nc = (int)cells_.size();
+  std::vector<double> KH((size_t)nc * 400), FH((size_t)nc * 20);
+  reports_.assign(nc, msfec_cell_report{});
+  check(gpu_.handle(),
+        msfec_qned_build(gpu_.handle(), nc, cells_.data(), a6.data(), binv.data(), &coeff_.load, KH.data(),
+                         FH.data(), reports_.data()),
+        "msfec_qned_build");
+  KH_.assign(nc, FullMatrix(20, 20));
+  FH_.assign(nc, Vector(20));
+  for (int c = 0; c < nc; ++c) {
+    std::memcpy(KH_[c].data.data(), &KH[(size_t)c * 400], 400 * sizeof(double));
+    std::memcpy(FH_[c].data.data(), &FH[(size_t)c * 20], 20 * sizeof(double));
+  }
+  basis_.resize((size_t)msfec_qned_basis_size(gpu_.handle()));
+  check(gpu_.handle(), msfec_qned_get_basis(gpu_.handle(), basis_.data(), (int64_t)basis_.size()),
+        "msfec_qned_get_basis");
+  basis_off_.assign(nc + 1, 0);
+  for (int c = 0; c < nc; ++c) {
+    const size_t n = (size_t)1 << cells_[c].depth;
+    basis_off_[c + 1] = basis_off_[c] + 20 * ((n + 1) * (n + 1) * (n + 1) + 3 * n * (n + 1) * (n + 1));
+  }
+  built_ = true;
+}
+
+const FullMatrix &QNedBatch::matrix(int slot) {
+  flush();
+  return KH_.at(slot);
+}
+
+const Vector &QNedBatch::rhs(int slot) {
+  flush();
+  return FH_.at(slot);
+}
+
+void QNedBatch::solution(int slot, const std::vector<double> &w, std::vector<double> &sigma, std::vector<double> &u) {
+  flush();
+  const size_t n = (size_t)1 << cells_[slot].depth;
+  const size_t NV = (n + 1) * (n + 1) * (n + 1), NE = 3 * n * (n + 1) * (n + 1), N = NV + NE;
+  const double *phi = basis_.data() + basis_off_[slot];
+  sigma.assign(NV, 0.0);
+  u.assign(NE, 0.0);
+  for (int b = 0; b < 8; ++b)
+    for (size_t d = 0; d < NV; ++d) sigma[d] += w[b] * phi[(size_t)b * N + d];
+  for (int b = 8; b < 20; ++b)
+    for (size_t d = 0; d < NE; ++d) u[d] += w[b] * phi[(size_t)b * N + NV + d];
+}
+
+}  // namespace QNed
+
+namespace RTDQ {
+
+RTDQBasis::RTDQBasis(const ParametersBasis &parameters, const std::string &parameter_filename,
+                     const CoarseCell &global_cell, const std::string &first_cell, unsigned local_subdomain,
+                     std::shared_ptr<RTDQBatch> batch)
+    : parameters_(parameters),
+      parameter_filename_(parameter_filename),
+      cell_(global_cell),
+      first_cell_(first_cell),
+      local_subdomain_(local_subdomain),
+      batch_(std::move(batch)),
+      global_weights_(7, 0.0) {}
+
+void RTDQBasis::run() {
+  if (slot_ < 0) slot_ = batch_->enqueue(cell_, parameters_.n_refine_local);
+}
+
+const FullMatrix &RTDQBasis::get_global_element_matrix() const {
+  if (slot_ < 0) throw BasisError(MSFEC_ERROR_INVALID_STATE, "RTDQBasis: run() was not called");
+  return batch_->matrix(slot_);
+}
+
+const Vector &RTDQBasis::get_global_element_rhs() const {
+  if (slot_ < 0) throw BasisError(MSFEC_ERROR_INVALID_STATE, "RTDQBasis: run() was not called");
+  return batch_->rhs(slot_);
+}
+
+const std::string &RTDQBasis::get_filename_global() const { return parameters_.filename_global; }
+
+void RTDQBasis::set_global_weights(const std::vector<double> &global_weights) {
+  if (global_weights.size() != 7) throw BasisError(MSFEC_ERROR_INVALID_ARGUMENT, "RTDQBasis: 7 weights expected");
+  global_weights_ = global_weights;
+}
+
+void RTDQBasis::set_output_flag() { output_flag_ = cell_.id == first_cell_; }
+
+void RTDQBasis::global_solution(std::vector<double> &sigma, std::vector<double> &u) const {
+  if (slot_ < 0) throw BasisError(MSFEC_ERROR_INVALID_STATE, "RTDQBasis: run() was not called");
+  batch_->solution(slot_, global_weights_, sigma, u);
+}
+
+RTDQBatch::RTDQBatch(RTDQCoefficients coeff, int device, int precision)
+    : coeff_(std::move(coeff)), gpu_(device, precision) {}
+
+int RTDQBatch::enqueue(const CoarseCell &cell, unsigned depth) {
+  if (built_) {
+    cells_.clear();
+    built_ = false;
+  }
+  cells_.push_back(make_cell(cell, depth));
+  return (int)cells_.size() - 1;
+}
+
+void RTDQBatch::flush() {
+  if (built_) return;
+  std::vector<double> ainv6;
+  for (const msfec_cell &c : cells_)
+    for_each_fine_centre(c, [&](const Point &p) {
+      const std::array<double, 9> m = coeff_.diffusion_inverse(p);
+      const double s[6] = {m[0], m[4], m[8], m[1], m[2], m[5]};
+      ainv6.insert(ainv6.end(), s, s + 6);
+    });
+  const int nc = (int)cells_.size();
+  std::vector<double> KH((size_t)nc * 49), FH((size_t)nc * 7);
+  reports_.assign(nc, msfec_cell_report{});
+  check(gpu_.handle(),
+        msfec_rtdq_build(gpu_.handle(), nc, cells_.data(), ainv6.data(), &coeff_.load, KH.data(), FH.data(),
+                         reports_.data()),
+        "msfec_rtdq_build");
+  KH_.assign(nc, FullMatrix(7, 7));
+  FH_.assign(nc, Vector(7));
+  for (int c = 0; c < nc; ++c) {
+    std::memcpy(KH_[c].data.data(), &KH[(size_t)c * 49], 49 * sizeof(double));
+    std::memcpy(FH_[c].data.data(), &FH[(size_t)c * 7], 7 * sizeof(double));
+  }
+  basis_.resize((size_t)msfec_rtdq_basis_size(gpu_.handle()));
+  check(gpu_.handle(), msfec_rtdq_get_basis(gpu_.handle(), basis_.data(), (int64_t)basis_.size()),
+        "msfec_rtdq_get_basis");
+  basis_off_.assign(nc + 1, 0);
+  for (int c = 0; c < nc; ++c) {
+    const size_t n = (size_t)1 << cells_[c].depth;
+    basis_off_[c + 1] = basis_off_[c] + 6 * (3 * n * n * (n + 1) + n * n * n);
+  }
+  built_ = true;
+}
+
+const FullMatrix &RTDQBatch::matrix(int slot) {
+  flush();
+  return KH_.at(slot);
+}
+
+const Vector &RTDQBatch::rhs(int slot) {
+  flush();
+  return FH_.at(slot);
+}
+
+void RTDQBatch::solution(int slot, const std::vector<double> &w, std::vector<double> &sigma, std::vector<double> &u) {
+  flush();
+  const size_t n = (size_t)1 << cells_[slot].depth;
+  const size_t NF = 3 * n * n * (n + 1), NC = n * n * n, N = NF + NC;
+  const double *phi = basis_.data() + basis_off_[slot];
+  sigma.assign(NF, 0.0);
+  for (int b = 0; b < 6; ++b)
+    for (size_t d = 0; d < NF; ++d) sigma[d] += w[b] * phi[(size_t)b * N + d];
+  u.assign(NC, 0.0);
+  for (size_t d = 0; d < NC; ++d) u[d] = w[6] * phi[NF + d];  // basis 0's u block (1 after the build)
+}
+
+}  // namespace RTDQ
 }  // namespace msfec_host

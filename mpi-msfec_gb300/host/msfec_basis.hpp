@@ -217,4 +217,141 @@ class NedRTBatch : public std::enable_shared_from_this<NedRTBatch> {
 };
 
 }  // namespace NedRT
+
+namespace QNed {
+
+// A(x) (SPD 3x3, the curl-curl weight: the reference's Diffusion_A), B^-1(x) > 0
+// (the sigma mass weight: DiffusionInverse_B), vector load as an msfec_load.
+struct QNedCoefficients {
+  std::function<std::array<double, 9>(const Point &)> diffusion;
+  std::function<double(const Point &)> inverse_b;
+  msfec_load load{MSFEC_LOAD_ZERO, 0, {0, 0, 0, 0}};
+};
+
+class QNedBatch;
+
+// QNedBasis (include/Q_Ned/q_ned_basis.h) with the same methods; the coarse
+// element matrix is 20 x 20 (8 vertices, then 12 lines).
+class QNedBasis {
+ public:
+  QNedBasis() = delete;
+  QNedBasis(const ParametersBasis &parameters, const std::string &parameter_filename,
+            const CoarseCell &global_cell, const std::string &first_cell, unsigned local_subdomain,
+            std::shared_ptr<QNedBatch> batch);
+  QNedBasis(const QNedBasis &other) = default;
+
+  void run();
+  const FullMatrix &get_global_element_matrix() const;
+  const Vector &get_global_element_rhs() const;
+  const std::string &get_filename_global() const;
+  void set_global_weights(const std::vector<double> &global_weights);
+  void set_output_flag();
+  // Fine DoF vectors of the local multiscale solution: sigma (vertex DoFs) from
+  // the 8 H1 bases and u (edge DoFs) from the 12 curl bases
+  // (QNedBasis::set_global_weights, q_ned_basis.cc:1158-1183).
+  void global_solution(std::vector<double> &sigma, std::vector<double> &u) const;
+
+ private:
+  friend class QNedBatch;
+  ParametersBasis parameters_;
+  std::string parameter_filename_;
+  CoarseCell cell_;
+  std::string first_cell_;
+  unsigned local_subdomain_;
+  std::shared_ptr<QNedBatch> batch_;
+  int slot_ = -1;
+  std::vector<double> global_weights_;
+  bool output_flag_ = false;
+};
+
+class QNedBatch : public std::enable_shared_from_this<QNedBatch> {
+ public:
+  QNedBatch(QNedCoefficients coeff, int device = 0, int precision = MSFEC_PRECISION_MIXED);
+  int enqueue(const CoarseCell &cell, unsigned depth);
+  void flush();
+  const FullMatrix &matrix(int slot);
+  const Vector &rhs(int slot);
+  void solution(int slot, const std::vector<double> &w, std::vector<double> &sigma, std::vector<double> &u);
+
+ private:
+  QNedCoefficients coeff_;
+  BasisBatch gpu_;
+  std::vector<msfec_cell> cells_;
+  std::vector<FullMatrix> KH_;
+  std::vector<Vector> FH_;
+  std::vector<double> basis_;
+  std::vector<size_t> basis_off_;
+  std::vector<msfec_cell_report> reports_;
+  bool built_ = false;
+};
+
+}  // namespace QNed
+
+namespace RTDQ {
+
+// A^-1(x) (SPD 3x3, the sigma mass weight: DiffusionInverse_A), scalar load as
+// an msfec_load (ZERO, CONSTANT or SIN_PRODUCT); the reaction rate is 0.
+struct RTDQCoefficients {
+  std::function<std::array<double, 9>(const Point &)> diffusion_inverse;
+  msfec_load load{MSFEC_LOAD_ZERO, 0, {0, 0, 0, 0}};
+};
+
+class RTDQBatch;
+
+// RTDQBasis (include/RT_DQ/rt_dq_basis.h) with the same methods; the coarse
+// element matrix is 7 x 7 (6 faces, then the DQ0 value).
+class RTDQBasis {
+ public:
+  RTDQBasis() = delete;
+  RTDQBasis(const ParametersBasis &parameters, const std::string &parameter_filename,
+            const CoarseCell &global_cell, const std::string &first_cell, unsigned local_subdomain,
+            std::shared_ptr<RTDQBatch> batch);
+  RTDQBasis(const RTDQBasis &other) = default;
+
+  void run();
+  const FullMatrix &get_global_element_matrix() const;
+  const Vector &get_global_element_rhs() const;
+  const std::string &get_filename_global() const;
+  void set_global_weights(const std::vector<double> &global_weights);
+  void set_output_flag();
+  // Fine DoF vectors of the local multiscale solution: sigma (face DoFs) from the
+  // 6 bases, u (cell DoFs) = weight 6 times basis 0's u block, which is 1
+  // (RTDQBasis::set_global_weights, rt_dq_basis.cc:1011-1036).
+  void global_solution(std::vector<double> &sigma, std::vector<double> &u) const;
+
+ private:
+  friend class RTDQBatch;
+  ParametersBasis parameters_;
+  std::string parameter_filename_;
+  CoarseCell cell_;
+  std::string first_cell_;
+  unsigned local_subdomain_;
+  std::shared_ptr<RTDQBatch> batch_;
+  int slot_ = -1;
+  std::vector<double> global_weights_;
+  bool output_flag_ = false;
+};
+
+class RTDQBatch : public std::enable_shared_from_this<RTDQBatch> {
+ public:
+  RTDQBatch(RTDQCoefficients coeff, int device = 0, int precision = MSFEC_PRECISION_MIXED);
+  int enqueue(const CoarseCell &cell, unsigned depth);
+  void flush();
+  const FullMatrix &matrix(int slot);
+  const Vector &rhs(int slot);
+  void solution(int slot, const std::vector<double> &w, std::vector<double> &sigma, std::vector<double> &u);
+
+ private:
+  RTDQCoefficients coeff_;
+  BasisBatch gpu_;
+  std::vector<msfec_cell> cells_;
+  std::vector<FullMatrix> KH_;
+  std::vector<Vector> FH_;
+  std::vector<double> basis_;
+  std::vector<size_t> basis_off_;
+  std::vector<msfec_cell_report> reports_;
+  bool built_ = false;
+};
+
+}  // namespace RTDQ
 }  // namespace msfec_host
