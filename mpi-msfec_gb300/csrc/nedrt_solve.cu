@@ -9,9 +9,11 @@
 //   run solve loop                ned_rt_basis.cc:1338-1381
 //   solve_iterative (Schur CG + ILU/GMRES there) ned_rt_basis.cc:636-847
 // The saddle-point system is solved (in its symmetric form, face rows negated)
-// with MINRES preconditioned by
-// diag(M)^-1 (+) diag(D + C^T diag(M)^-1 C)^-1 on the interior DoFs, FP32 inside
-// FP64 iterative refinement (MINRES in FP64 for the plain FP64 path); the
+// with MINRES preconditioned by diag(M)^-1 on the edges and, on the faces,
+// either diag(D + C^T diag(M)^-1 C)^-1 or (default) that diagonal plus the
+// multilevel coarse-RT correction built below (ml_coarse_block,
+// nr_ml_setup_kernel), FP32 inside FP64 iterative refinement (MINRES in FP64
+// for the plain FP64 path); the
 // operator is applied matrix-free, cell by cell, from the per-cell A^-1 / B in
 // tensor-product form (1D P1 mass factors), accumulating into shared memory
 // with atomics; the closed-form element tables feed the preconditioner.
