@@ -728,7 +728,7 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
     hc[c].coarse_off = -1;
     if (ml && hc[c].n >= 4) {
       hc[c].coarse_off = coarse_floats;
-      coarse_floats += nr_ml_data_floats(hc[c].n);
+      coarse_floats += nr_ml_cell_floats(hc[c].n);
       ++n_ml;
     }
   }

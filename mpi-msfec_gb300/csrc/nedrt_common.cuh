@@ -121,6 +121,17 @@ __host__ __device__ inline int nr_ml_data_floats(int n) {
   return s;
 }
 
+// After that data, per cell: the inverse of the assembled diagonal of the
+// Schur operator on every face (0 on the boundary), the fine level of the
+// multilevel operator; the solver reads it into its preconditioner vector.
+__host__ __device__ inline int nr_ml_fine_floats(int n) {
+  if (n < 4) return 0;
+  int NEx, NFx, NE, NF;
+  nr_counts(n, NEx, NFx, NE, NF);
+  return NF;
+}
+__host__ __device__ inline int nr_ml_cell_floats(int n) { return nr_ml_data_floats(n) + nr_ml_fine_floats(n); }
+
 // Layout of the solver's multilevel region (bytes from its start): restriction
 // accumulator and correction of level n/2 (precision T), the restricted /
 // corrected vectors of the levels below, the cell's data, one 16-bit code per

@@ -833,6 +833,9 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
     const float *src = prm.coarse + Cc.coarse_off;
     const int nd = nr_ml_data_floats(n);
     for (int t = tid; t < nd; t += NT) ml_dat[t] = src[t];
+    // fine level: the inverse assembled diagonal of S replaces the cell-lumped one on the faces
+    for (int u = tid; u < g.NF; u += NT)
+      if (pd[g.NE + u] > 0.0f) pd[g.NE + u] = src[nd + u];
     for (int t = tid; t < mll.F1; t += NT) ml_rr[t] = T(0);
     for (int t = tid; t < (int)((mll.off_data - mll.off_wk) / sizeof(T)); t += NT) ml_wk[t] = T(0);
     for (int u = tid; u < (int)Np - g.NE; u += NT) {
@@ -1914,15 +1917,21 @@ __global__ void __launch_bounds__(kMLSetupThreads) nr_ml_setup_kernel(const NRCe
       for (int l = 0; l < 12; ++l) atomicAdd(md + e[l], (float)a[l >> 2] * sh.Gf[l >> 2][l >> 2][l & 3][l & 3]);
     }
     __syncthreads();
-    // probe loop: pr < 36 (K - 1) diagonal-level colours, then the 12 level-2 functions
+    // probe loop: 36 colours of single fine faces (the assembled diagonal of S,
+    // written straight to the cell's fine block), 36 (K - 1) diagonal-level
+    // colours, then the 12 level-2 functions
     const int K = L - 1;
-    const int nprobe = 36 * (K - 1) + 12;
+    const int nprobe = 36 + 36 * (K - 1) + 12;
+    float *fine_out = coarse + Cc.coarse_off + nd;
+    for (int u = tid; u < g.NF; u += NT) fine_out[u] = 0.0f;  // boundary faces keep 0
     for (int pr = 0; pr < nprobe; ++pr) {
-      const bool exact = pr >= 36 * (K - 1);
-      const int k = exact ? K : 1 + pr / 36;  // level 2^(L-k)
-      const int col = pr % 36;
+      const bool fine = pr < 36;
+      const int pl = pr - 36;
+      const bool exact = !fine && pl >= 36 * (K - 1);
+      const int k = fine ? 0 : (exact ? K : 1 + pl / 36);  // level 2^(L-k); k = 0: the fine faces
+      const int col = fine ? pr : pl % 36;
       const int cd = col / 12, cP = (col >> 2) % 3, ca = (col >> 1) & 1, cb = col & 1;
-      const int J = pr - 36 * (K - 1);  // exact: the probed function
+      const int J = pl - 36 * (K - 1);  // exact: the probed function
       int od = 0;  // data offset of level k
       for (int kk = 1; kk < k; ++kk) od += nr_ml_count(1 << (L - kk));
       const int lm = L - k;
@@ -1931,10 +1940,17 @@ __global__ void __launch_bounds__(kMLSetupThreads) nr_ml_setup_kernel(const NRCe
         float v = 0.0f;
         if (d >= g.NE) {
           int dir, i, jj, kk;
-          dof_geometry(g, d, dir, i, jj, kk);
+          const bool fbnd = dof_geometry(g, d, dir, i, jj, kk);
           const int fd = dir - 3;
           const int q = fd == 0 ? i : (fd == 1 ? jj : kk);
           const int xx = fd == 0 ? jj : i, yy = fd == 2 ? jj : kk;
+          if (fine) {
+            v = (!fbnd && fd == cd && q % 3 == cP && (xx & 1) == ca && (yy & 1) == cb) ? 1.0f : 0.0f;
+            x[d] = v;
+            a1[d] = 0.0f;
+            a2[d] = 0.0f;
+            continue;
+          }
           int fj[2], fP[2];
           float fw[2];
           const int cnt = ml_fine_weights(L, k, fd, q, xx, yy, fj, fw, fP);
@@ -1982,6 +1998,11 @@ __global__ void __launch_bounds__(kMLSetupThreads) nr_ml_setup_kernel(const NRCe
         const int fd = dir - 3;
         const int q = fd == 0 ? i : (fd == 1 ? jj : kk);
         const int xx = fd == 0 ? jj : i, yy = fd == 2 ? jj : kk;
+        if (fine) {  // faces of one colour are S-decoupled: (S x)_f = S_ff
+          if (fd == cd && q % 3 == cP && (xx & 1) == ca && (yy & 1) == cb)
+            fine_out[d - g.NE] = sf > 0.0f ? 1.0f / sf : 0.0f;
+          continue;
+        }
         int fj[2], fP[2];
         float fw[2];
         const int cnt = ml_fine_weights(L, k, fd, q, xx, yy, fj, fw, fP);

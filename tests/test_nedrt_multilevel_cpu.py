@@ -174,3 +174,20 @@ def test_cascade_equals_explicit_bpx(system):
     assert np.abs(z - explicit).max() <= 1e-12 * np.abs(explicit).max()
     # and the coarse share of gamma^2
     assert abs(v @ z - (r1 @ (r1 / D1) + r2 @ y2)) <= 1e-12 * abs(v @ z)
+
+
+def test_fine_face_probing_gives_assembled_diagonal(system):
+    """The setup kernel's 36 single-face colours (normal, plane mod 3, x and y
+    parity): one application of S per colour returns S_ff for all its faces."""
+    L, n, S, geo, pos, uI = system
+    got = np.zeros(len(uI))
+    for col in range(36):
+        cd, cP, ca, cb = col // 12, (col >> 2) % 3, (col >> 1) & 1, col & 1
+        sel = [pos[u] for u in uI if geo[u][0] == cd and geo[u][1] % 3 == cP and geo[u][2] % 2 == ca
+               and geo[u][3] % 2 == cb]
+        x = np.zeros(len(uI))
+        x[sel] = 1.0
+        s = S @ x
+        got[sel] = s[sel]
+    ref = S.diagonal()
+    assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
