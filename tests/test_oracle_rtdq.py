@@ -77,3 +77,42 @@ def test_pressure_constant_does_not_change_sigma():
     x0 = np.concatenate([Phi[3, :NF], P[3]])
     x1 = np.concatenate([Phi[3, :NF], P[3] + 7.5])
     assert np.abs((A @ x0 - A @ x1)[I]).max() < 1e-12
+
+
+def test_reference_schur_cg_gives_the_oracle_sigma():
+    """The reference's solve_iterative (rt_dq_basis.cc:615-820), restated: CG on
+    the Schur complement S = B M^-1 B^T of the condensed system, right-hand side
+    B M^-1 f - g with its mean removed (:683-698), zero start; then
+    sigma = M^-1 (f + B^T u). Its sigma equals the oracle's (bordered, mean-zero
+    pressure) to the CG tolerance, and its pressure is mean-zero as well."""
+    import scipy.sparse.linalg as spla
+    cells, ainv6, _ = workloads.rtdq_tensor(m=1, depth=2, seed=8)
+    ainv = NR.sym6_to_ainv(ainv6)
+    n = 4
+    NF, NC = RQ.counts(n)
+    Phi, P, _, _ = RQ.build_cell(cells["origin"][0], cells["size"][0], 2, ainv)
+    A = RQ.assemble(n, cells["size"][0], ainv)
+    bnd = RQ.boundary_mask(n)
+    I = np.where(~bnd)[0]
+    If, Ic = I[I < NF], I[I >= NF]
+    M = A[If][:, If].tocsc()
+    Bt = -A[If][:, Ic]          # face rows: -B^T
+    B = A[Ic][:, If]
+    Mlu = spla.splu(M)
+    for b in range(6):
+        G = np.zeros(NF + NC)
+        G[:NF] = NR.coarse_face_dofs(n, b)
+        G[I] = 0.0
+        rhs = np.zeros(NF + NC)
+        rhs[NF:] = (1.0 if b & 1 else -1.0) / NC
+        r = rhs - A @ G
+        f, g = r[If], r[Ic]
+        s_rhs = B @ Mlu.solve(f) - g
+        s_rhs -= s_rhs.mean()
+        S = spla.LinearOperator((len(Ic), len(Ic)), matvec=lambda u: -(B @ Mlu.solve(Bt @ u)))
+        u, info = spla.cg(S, s_rhs, rtol=1e-13, maxiter=2000)
+        assert info == 0
+        sigma = Mlu.solve(f + Bt @ u)
+        assert np.abs(sigma - Phi[b, If]).max() <= 1e-10 * np.abs(Phi[b, :NF]).max()
+        assert abs(u.mean()) <= 1e-10 * np.abs(u).max()
+        assert np.abs(u - P[b][Ic - NF]).max() <= 1e-8 * np.abs(u).max()
