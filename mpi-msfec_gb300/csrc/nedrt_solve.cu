@@ -1934,7 +1934,6 @@ __global__ void __launch_bounds__(kMLSetupThreads) nr_ml_setup_kernel(const NRCe
       const int J = pl - 36 * (K - 1);  // exact: the probed function
       int od = 0;  // data offset of level k
       for (int kk = 1; kk < k; ++kk) od += nr_ml_count(1 << (L - kk));
-      const int lm = L - k;
       // probe vector on the interior faces; accumulators cleared
       for (int d = tid; d < N; d += NT) {
         float v = 0.0f;
