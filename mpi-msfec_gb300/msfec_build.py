@@ -77,7 +77,7 @@ def build(verbose: bool = False) -> str:
 def build_host(objs=()):
     """QBasis/NedRTBasis/QNedBasis/RTDQBasis shim + coarse solvers (g++, links the CUDA library) and the
     example drivers."""
-    srcs = [os.path.join(HOST, f) for f in ("msfec_basis.cpp", "coarse_q1.cpp", "coarse_nedrt.cpp")]
+    srcs = [os.path.join(HOST, f) for f in ("msfec_basis.cpp", "coarse_q1.cpp", "coarse_nedrt.cpp", "coarse_pairings.cpp")]
     deps = srcs + [os.path.join(HOST, "msfec_basis.hpp"), LIB] + glob.glob(os.path.join(INCLUDE, "*.h"))
     if not os.path.exists(HOSTLIB) or any(os.path.getmtime(d) > os.path.getmtime(HOSTLIB) for d in deps):
         cmd = [CXX, "-O2", "-std=c++17", "-fPIC", "-shared", "-I", INCLUDE, "-o", HOSTLIB] + srcs + \
