@@ -1,0 +1,79 @@
+"""Global multiscale Q_Ned and RT_DQ solutions from GPU-built K_H / F_H / basis
+vs the FP64 oracles' (host coarse assembly + solve, the reference's
+QNedMultiscale / RTDQMultiscale flow, then set_global_weights' fine
+reconstruction). Stated tolerance: relative L2 difference <= 1e-9 of the
+coarse solution and of the fine sigma_h, u_h."""
+import numpy as np
+import pytest
+
+import workloads
+from oracle import nedrt_oracle as NR
+from oracle import qned_oracle as Q
+from oracle import rtdq_oracle as RQ
+from test_coarse_pairings import host_solve, qned_maps, rtdq_maps
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-9
+
+
+def _rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+@pytest.mark.parametrize("precision", ("mixed", "fp64"))
+def test_global_qned_solution_matches_oracle(gpu, precision):
+    m, depth = 2, 2
+    cells, a6, binv, load = workloads.qned_tensor(m=m, depth=depth, seed=14)
+    h = gpu.Handle(precision=gpu.PRECISION_MIXED if precision == "mixed" else gpu.PRECISION_FP64)
+    KH, FH, rep, st = h.qned_build(cells, a6, binv, load)
+    assert st == gpu.SUCCESS and rep["converged"].all()
+    ref = Q.build(cells, binv, NR.sym6_to_ainv(a6), load.kind, list(load.params))
+    g, fixed = qned_maps(m)
+    n = 1 << depth
+    NV, NE = Q.counts(n)
+    phi = h.qned_basis().reshape(m ** 3, 20, NV + NE)
+    phi_r = np.array(ref["Phi"])
+    rng = np.random.default_rng(5)
+    # the trig load acts on u only (its coarse solution has no vertex part); a
+    # generic vertex load exercises the sigma / u coupling as well
+    extra = np.concatenate([rng.standard_normal((m ** 3, 8)), np.zeros((m ** 3, 12))], 1)
+    for F_add in (0.0, extra):
+        U = host_solve("msfec_host_qned_coarse_solve", fixed.size, KH, FH + F_add, m)
+        Ur = host_solve("msfec_host_qned_coarse_solve", fixed.size, ref["KH"], ref["FH"] + F_add, m)
+        assert _rel(U, Ur) <= TOL
+        # sigma from the 8 H1 bases' sigma block, u from the 12 curl bases' u block
+        sig = np.einsum("cb,cbd->cd", U[g[:, :8]], phi[:, :8, :NV])
+        sig_r = np.einsum("cb,cbd->cd", Ur[g[:, :8]], phi_r[:, :8, :NV])
+        u = np.einsum("cb,cbd->cd", U[g[:, 8:]], phi[:, 8:, NV:])
+        u_r = np.einsum("cb,cbd->cd", Ur[g[:, 8:]], phi_r[:, 8:, NV:])
+        assert np.linalg.norm(u_r) > 0
+        assert _rel(u, u_r) <= TOL
+        # the coarse curl-curl block is singular on gradients, so the vertex
+        # unknowns stay ~1e-12 of u even under a vertex load: compared only if not negligible
+        if np.linalg.norm(sig_r) > 1e-6 * np.linalg.norm(u_r):
+            assert _rel(sig, sig_r) <= TOL
+
+
+@pytest.mark.parametrize("precision", ("mixed", "fp64"))
+def test_global_rtdq_solution_matches_oracle(gpu, precision):
+    m, depth = 2, 2
+    cells, ainv6, load = workloads.rtdq_tensor(m=m, depth=depth, seed=15)
+    h = gpu.Handle(precision=gpu.PRECISION_MIXED if precision == "mixed" else gpu.PRECISION_FP64)
+    KH, FH, rep, st = h.rtdq_build(cells, ainv6, load)
+    assert st == gpu.SUCCESS and rep["converged"].all()
+    ref = RQ.build(cells, NR.sym6_to_ainv(ainv6), load.kind, list(load.params))
+    g, fixed = rtdq_maps(m)
+    n = 1 << depth
+    NF, NC = RQ.counts(n)
+    phi = h.rtdq_basis().reshape(m ** 3, 6, NF + NC)
+    phi_r = np.array(ref["Phi"])
+    U = host_solve("msfec_host_rtdq_coarse_solve", fixed.size, KH, FH, m)
+    Ur = host_solve("msfec_host_rtdq_coarse_solve", fixed.size, ref["KH"], ref["FH"], m)
+    assert _rel(U, Ur) <= TOL
+    # sigma from the 6 bases, u = weight 6 times basis 0's u block (1)
+    sig = np.einsum("cb,cbd->cd", U[g[:, :6]], phi[:, :, :NF])
+    sig_r = np.einsum("cb,cbd->cd", Ur[g[:, :6]], phi_r[:, :, :NF])
+    u = U[g[:, 6]][:, None] * phi[:, 0, NF:]
+    u_r = Ur[g[:, 6]][:, None] * phi_r[:, 0, NF:]
+    assert _rel(sig, sig_r) <= TOL
+    assert _rel(u, u_r) <= TOL
