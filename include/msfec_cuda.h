@@ -261,6 +261,29 @@ msfec_status msfec_q1_fine_solve(msfec_handle *handle, const msfec_cell *domain,
                                  msfec_cell_report *report);
 
 /*
+ * Standard fine-scale Ned_RT solve (the reference's NedRTStd path,
+ * source/Ned_RT/ned_rt_ref.cc:110-330, as an independent accuracy reference
+ * for the Ned_RT multiscale solution): the mixed system
+ *   (A^-1 sigma, tau) - (u, curl tau) = 0
+ *   (curl sigma, v) + (B div u, div v) = (f, v)
+ * on the box `domain` (uniformly refined depth times, depth 1..4) with the
+ * reference's boundary treatment: its essential projections are disabled
+ * (ned_rt_ref.cc:119-133), so every boundary edge and face is free (natural
+ * conditions), and the reaction term is zero (eqn_coeff_R.cc:8-14). The
+ * persistent Ned_RT solver runs one source item over the whole lattice with
+ * the diagonal preconditioner. Host buffers, synchronous.
+ *   ainv6, bdiv  per fine cell, as for msfec_nedrt_build
+ *   load         MSFEC_LOAD_ZERO or MSFEC_LOAD_VEC_TRIG
+ *   x            [NE + NF]: sigma on the fine edges, then u on the fine faces,
+ *                in the lattice order of the Ned_RT basis vectors
+ * report may be NULL.
+ */
+msfec_status msfec_nedrt_fine_solve(msfec_handle *handle, const msfec_cell *domain,
+                                    const double *ainv6, const double *bdiv,
+                                    const msfec_load *load, double *x,
+                                    msfec_cell_report *report);
+
+/*
  * Ned_RT (lowest-order Nedelec sigma x Raviart-Thomas u) basis build from
  * host buffers (synchronous). Replaces NedRTBasis::run
  * (source/Ned_RT/ned_rt_basis.cc:1279-1428) for every cell of the batch,

@@ -77,6 +77,8 @@ cudaError_t nedrt_adjoint_prepare_launch(const NRCell *cells, int ncells, const 
 cudaError_t nedrt_adjoint_gradient_launch(const NRCell *cells, int ncells, const double *ainv6, const double *bdiv,
                                           const double *comb, const double *work, const double *xsol, double *ga,
                                           double *gb, cudaStream_t st);
+cudaError_t nedrt_face_load_launch(const NRCell *cells, int ncells, const msfec_load &load, double *b,
+                                   cudaStream_t st);
 cudaError_t nedrt_galerkin_launch(const NRCell *cells, int ncells, const double *phi, const double *y,
                                   const msfec_load &load, double *KH, double *FH, msfec_cell_report *rep,
                                   const NRStat *stats, cudaStream_t st);
@@ -187,6 +189,12 @@ struct msfec_handle {
       nra_floor;
   DevBuf<int> nra_cell;
   DevBuf<NRItem> nra_items;
+  // Ned_RT standard fine solve: the domain as one cell
+  DevBuf<NRCell> nrf_cell;
+  DevBuf<NRItem> nrf_item;
+  DevBuf<double> nrf_b, nrf_x, nrf_floor;
+  DevBuf<NRStat> nrf_stats;
+  DevBuf<float> nrf_scratch;
   // Q_Ned state of the last build
   DevBuf<NRCell> qn_cells;
   DevBuf<NRItem> qn_items;
@@ -1042,6 +1050,20 @@ bool nr_load_ok(const msfec_load *l) {
   return !l || l->kind == MSFEC_LOAD_ZERO || l->kind == MSFEC_LOAD_VEC_TRIG;
 }
 
+// A^-1 SPD (leading principal minors) and finite, B positive and finite, per fine cell.
+msfec_status nr_coef_check(msfec_handle *h, const double *ainv6, const double *bdiv, int64_t nfine) {
+  for (int64_t e = 0; e < nfine; ++e) {
+    const double *a = ainv6 + 6 * e;
+    const double m1 = a[0], m2 = a[0] * a[1] - a[3] * a[3];
+    const double m3 = a[0] * (a[1] * a[2] - a[5] * a[5]) - a[3] * (a[3] * a[2] - a[5] * a[4]) +
+                      a[4] * (a[3] * a[5] - a[1] * a[4]);
+    bool ok = m1 > 0.0 && m2 > 0.0 && m3 > 0.0 && bdiv[e] > 0.0 && std::isfinite(bdiv[e]);
+    for (int q = 0; q < 6; ++q) ok = ok && std::isfinite(a[q]);
+    if (!ok) return fail(h, MSFEC_ERROR_NUMERICAL, "A^-1 not SPD / finite or B not positive at fine cell " + std::to_string(e));
+  }
+  return MSFEC_SUCCESS;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1152,6 +1174,13 @@ void msfec_destroy(msfec_handle *h) {
       b->release();
     h->nra_cell.release();
     h->nra_items.release();
+    h->nrf_cell.release();
+    h->nrf_item.release();
+    h->nrf_b.release();
+    h->nrf_x.release();
+    h->nrf_floor.release();
+    h->nrf_stats.release();
+    h->nrf_scratch.release();
     h->qn_cells.release();
     h->qn_items.release();
     for (DevBuf<double> *b : {&h->qn_phi, &h->qn_y, &h->qn_eload, &h->qn_a6, &h->qn_binv, &h->qn_KH, &h->qn_FH})
@@ -1502,6 +1531,117 @@ msfec_status msfec_q1_fine_solve(msfec_handle *h, const msfec_cell *domain, cons
   return MSFEC_SUCCESS;
 }
 
+msfec_status msfec_nedrt_fine_solve(msfec_handle *h, const msfec_cell *domain, const double *ainv6,
+                                    const double *bdiv, const msfec_load *load, double *x,
+                                    msfec_cell_report *report) {
+  if (!h) return MSFEC_ERROR_INVALID_ARGUMENT;
+  if (!domain || !ainv6 || !bdiv || !x) return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "null pointer");
+  if (!cell_ok(*domain) || domain->depth > kNRMaxDepth)
+    return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "domain box invalid (Ned_RT depth 1..4)");
+  if (!load_ok(load) || !nr_load_ok(load)) return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "invalid Ned_RT load");
+  const int n = 1 << domain->depth;
+  const int64_t nfine = (int64_t)n * n * n;
+  {
+    const msfec_status cs = nr_coef_check(h, ainv6, bdiv, nfine);
+    if (cs != MSFEC_SUCCESS) return cs;
+  }
+  const bool fp64 = h->cfg.precision == MSFEC_PRECISION_FP64;
+  DeviceGuard g(h->device);
+  cudaStream_t st = h->stream;
+  NRCell hc;
+  for (int d = 0; d < 3; ++d) {
+    hc.origin[d] = domain->origin[d];
+    hc.h[d] = domain->size[d] / n;
+  }
+  hc.depth = domain->depth;
+  hc.n = n;
+  hc.coef_off = 0;
+  hc.dof_off = 0;
+  hc.coarse_off = -1;  // diagonal preconditioner
+  int NEx, NFx, NE, NF;
+  nr_counts(n, NEx, NFx, NE, NF);
+  const size_t N = (size_t)NE + NF;
+  // one source item with natural boundary conditions (mode 2): right-hand side 0 of cell 0
+  const NRItem item{0, 0, 2};
+  const size_t ws_floats = nr_workspace_floats(n, fp64 ? 8 : 4);
+  const bool use_smem = ws_floats * 4 <= kNRSmemLimit;
+  MSFEC_CUDA_TRY(h, h->nr_ainv.reserve(nfine * 6));
+  MSFEC_CUDA_TRY(h, h->nr_bdiv.reserve(nfine));
+  MSFEC_CUDA_TRY(h, h->nrf_cell.reserve(1));
+  MSFEC_CUDA_TRY(h, h->nrf_item.reserve(1));
+  MSFEC_CUDA_TRY(h, h->nrf_b.reserve(kNRSrcRhs * N));
+  MSFEC_CUDA_TRY(h, h->nrf_x.reserve(kNRSrcRhs * N));
+  MSFEC_CUDA_TRY(h, h->nrf_floor.reserve(1));
+  MSFEC_CUDA_TRY(h, h->nrf_stats.reserve(18));
+  MSFEC_CUDA_TRY(h, h->queue.reserve(2));
+  if (!use_smem) MSFEC_CUDA_TRY(h, h->nrf_scratch.reserve(ws_floats));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->nr_ainv.ptr, ainv6, nfine * 6 * sizeof(double), cudaMemcpyHostToDevice, st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->nr_bdiv.ptr, bdiv, nfine * sizeof(double), cudaMemcpyHostToDevice, st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->nrf_cell.ptr, &hc, sizeof(NRCell), cudaMemcpyHostToDevice, st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->nrf_item.ptr, &item, sizeof(NRItem), cudaMemcpyHostToDevice, st));
+  MSFEC_CUDA_TRY(h, cudaMemsetAsync(h->nrf_b.ptr, 0, N * sizeof(double), st));
+  MSFEC_CUDA_TRY(h, cudaMemsetAsync(h->nrf_x.ptr, 0, N * sizeof(double), st));
+  MSFEC_CUDA_TRY(h, cudaMemsetAsync(h->nrf_floor.ptr, 0, sizeof(double), st));
+  MSFEC_CUDA_TRY(h, cudaMemsetAsync(h->nrf_stats.ptr, 0, 18 * sizeof(NRStat), st));
+  MSFEC_CUDA_TRY(h, cudaMemsetAsync(h->queue.ptr, 0, sizeof(int), st));
+  msfec_load ld;
+  if (load) {
+    ld = *load;
+  } else {
+    std::memset(&ld, 0, sizeof(ld));
+  }
+  if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[0], st));
+  MSFEC_CUDA_TRY(h, nedrt_face_load_launch(h->nrf_cell.ptr, 1, ld, h->nrf_b.ptr, st));
+  NRParams prm{};
+  prm.cells = h->nrf_cell.ptr;
+  prm.items = h->nrf_item.ptr;
+  prm.n_items = 1;
+  prm.queue = h->queue.ptr;
+  prm.ainv6 = h->nr_ainv.ptr;
+  prm.bdiv = h->nr_bdiv.ptr;
+  prm.phi = h->nrf_x.ptr;  // not written by source items
+  prm.y = h->nrf_x.ptr;
+  prm.stats = h->nrf_stats.ptr;
+  prm.src_rhs = h->nrf_b.ptr;
+  prm.src_out = h->nrf_x.ptr;
+  prm.src_floor = h->nrf_floor.ptr;
+  prm.scratch = use_smem ? nullptr : h->nrf_scratch.ptr;
+  prm.scratch_floats = ws_floats;
+  prm.use_smem = use_smem ? 1 : 0;
+  prm.coarse = nullptr;
+  prm.ml_offset = 0;
+  prm.rtol = h->cfg.nedrt_rtol;
+  prm.inner_rtol = h->cfg.inner_rtol;
+  prm.max_iter = std::max(h->cfg.max_iter, 20000);
+  prm.max_refine = h->cfg.max_refine;
+  MSFEC_CUDA_TRY(h, nedrt_solve_launch(fp64, false, prm, use_smem ? ws_floats * 4 : 0, 1, st));
+  if (h->timing) {
+    MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[1], st));
+    MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[2], st));
+    MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[3], st));
+  }
+  h->ev_recorded = h->timing;
+  h->last_launches = 2;
+  h->last_graph = 0;
+  NRStat stat;
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(x, h->nrf_x.ptr, N * sizeof(double), cudaMemcpyDeviceToHost, st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(&stat, h->nrf_stats.ptr, sizeof(NRStat), cudaMemcpyDeviceToHost, st));
+  MSFEC_CUDA_TRY(h, cudaStreamSynchronize(st));
+  const bool ok = stat.converged && !(stat.flags & 1);
+  if (report) {
+    report->iterations = stat.iters;
+    report->refinements = stat.refinements;
+    report->converged = ok ? 1 : 0;
+    report->reserved = 0;
+    report->residual = stat.rel_residual;
+  }
+  if (!ok)
+    return fail(h, MSFEC_ERROR_NOT_CONVERGED,
+                "Ned_RT fine-scale solve missed rtol (relative residual " + std::to_string(stat.rel_residual) + ", " +
+                    std::to_string(stat.iters) + " iterations)");
+  return MSFEC_SUCCESS;
+}
+
 msfec_status msfec_nedrt_build_device(msfec_handle *h, int32_t ncells, const msfec_cell *cells, const double *d_ainv6,
                                       const double *d_bdiv, const msfec_load *load, double *d_KH, double *d_FH,
                                       msfec_cell_report *d_reports) {
@@ -1534,15 +1674,9 @@ msfec_status msfec_nedrt_build(msfec_handle *h, int32_t ncells, const msfec_cell
     nfine += n * n * n;
   }
   if (!load_ok(load) || !nr_load_ok(load)) return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "invalid Ned_RT load");
-  for (int64_t e = 0; e < nfine; ++e) {
-    const double *a = ainv6 + 6 * e;
-    // SPD check of the 3x3 A^-1 (leading principal minors) and B > 0
-    const double m1 = a[0], m2 = a[0] * a[1] - a[3] * a[3];
-    const double m3 = a[0] * (a[1] * a[2] - a[5] * a[5]) - a[3] * (a[3] * a[2] - a[5] * a[4]) +
-                      a[4] * (a[3] * a[5] - a[1] * a[4]);
-    bool ok = m1 > 0.0 && m2 > 0.0 && m3 > 0.0 && bdiv[e] > 0.0 && std::isfinite(bdiv[e]);
-    for (int q = 0; q < 6; ++q) ok = ok && std::isfinite(a[q]);
-    if (!ok) return fail(h, MSFEC_ERROR_NUMERICAL, "A^-1 not SPD / finite or B not positive at fine cell " + std::to_string(e));
+  {
+    const msfec_status cs = nr_coef_check(h, ainv6, bdiv, nfine);
+    if (cs != MSFEC_SUCCESS) return cs;
   }
   if (ncells == 0) return msfec_nedrt_build_device(h, 0, cells, nullptr, nullptr, load, nullptr, nullptr, nullptr);
   DeviceGuard g(h->device);

@@ -31,7 +31,8 @@ struct NRCell {
 struct NRItem {
   int cell;
   int basis;  // 0..17 (basis mode); right-hand side 0..3 of the cell (source mode)
-  int mode;   // 0 basis function, 1 source: zero Dirichlet data, load from src_rhs
+  int mode;   // 0 basis function, 1 source: zero Dirichlet data, load from src_rhs,
+              // 2 source with natural boundary conditions: every DoF free (standard fine solve)
 };
 
 constexpr int kNRSrcRhs = 4;  // source-mode right-hand sides per cell (adjoint)

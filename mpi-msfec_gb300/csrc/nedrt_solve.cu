@@ -730,7 +730,8 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
   const int n = g.n, N = g.N;
   const int nc = n * n * n;
   const int bb = it.basis;
-  const bool src = it.mode == 1;
+  const bool src = it.mode >= 1;
+  const bool natural = it.mode == 2;  // every DoF free (no Dirichlet rows)
   const bool merge = n >= 4;  // full warps of complete x-rows in the apply (block-uniform)
   const int tid = threadIdx.x;
   constexpr bool kMixed = sizeof(T) == 4;
@@ -813,13 +814,13 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
   for (int d = tid; d < N; d += NT) {
     int dir, i, j, k;
     const bool bnd = dof_geometry(g, d, dir, i, j, k);
-    pd[d] = bnd ? 0.0f : 1.0f / pd[d];
+    pd[d] = (bnd && !natural) ? 0.0f : 1.0f / pd[d];
   }
   __syncthreads();
 
   // ---- multilevel part of the preconditioner (block-uniform switch): the
   // cell's data from HBM, the faces' level-n/2 parent codes
-  const bool ml = ML && prm.coarse != nullptr && Cc.coarse_off >= 0;
+  const bool ml = ML && prm.coarse != nullptr && Cc.coarse_off >= 0 && !natural;
   const NRMLLayout mll = nr_ml_layout(n, (int)sizeof(T));
   unsigned char *mlb = nr_dyn_smem + prm.ml_offset;
   T *ml_rr = reinterpret_cast<T *>(mlb);
@@ -2146,6 +2147,14 @@ cudaError_t nedrt_adjoint_prepare_launch(const NRCell *cells, int ncells, const 
     nrimpl::nr_adj_point_kernel<<<(npoints + 127) / 128, 128, 0, st>>>(cells, npoints, cell_of, pts, dJdu, e);
   nrimpl::nr_adj_rhs_kernel<<<ncells, nrimpl::kAdjThreads, 0, st>>>(cells, ainv6, bdiv, comb, bload, e, work, rhs,
                                                                      floor_out);
+  return cudaGetLastError();
+}
+
+// Face load b_f = (v_f, f) of every fine face of every cell (b zeroed by the caller).
+cudaError_t nedrt_face_load_launch(const NRCell *cells, int ncells, const msfec_load &load, double *b,
+                                   cudaStream_t st) {
+  if (ncells <= 0) return cudaSuccess;
+  nrimpl::nr_adj_face_load_kernel<<<ncells, nrimpl::kAdjThreads, 0, st>>>(cells, load, b);
   return cudaGetLastError();
 }
 

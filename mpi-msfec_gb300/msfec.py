@@ -41,6 +41,7 @@ EXPORTED = [
     "msfec_set_graph", "msfec_autotune", "msfec_q1_fine_solve", "msfec_nedrt_backward",
     "msfec_qned_build", "msfec_qned_build_device", "msfec_qned_basis_size", "msfec_qned_get_basis",
     "msfec_rtdq_build", "msfec_rtdq_build_device", "msfec_rtdq_basis_size", "msfec_rtdq_get_basis",
+    "msfec_nedrt_fine_solve",
 ]
 
 
@@ -143,6 +144,8 @@ def load_library(path: str = LIB_PATH):
     L.msfec_autotune.restype = ctypes.c_int
     L.msfec_q1_fine_solve.argtypes = [_vp, _vp, _dp, _dp, ctypes.POINTER(Load), _dp, _vp]
     L.msfec_q1_fine_solve.restype = ctypes.c_int
+    L.msfec_nedrt_fine_solve.argtypes = [_vp, _vp, _dp, _dp, ctypes.POINTER(Load), _dp, _vp]
+    L.msfec_nedrt_fine_solve.restype = ctypes.c_int
     L.msfec_nedrt_backward.argtypes = [_vp, ctypes.c_int32, _vp, _dp, _dp, ctypes.POINTER(Load), ctypes.c_int32,
                                        _dp, _dp, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32), _dp, _dp, _dp, _dp]
     L.msfec_nedrt_backward.restype = ctypes.c_int
@@ -313,6 +316,21 @@ class Handle:
                                            _d(u), rep.ctypes.data_as(_vp))
         self.check(st, allow=(ERROR_NOT_CONVERGED,))
         return u, rep[0], st
+
+    def nedrt_fine_solve(self, domain, ainv6, bdiv, load):
+        """msfec_nedrt_fine_solve: standard fine-scale Ned_RT solve (natural boundary
+        conditions) on one box; returns (x = [sigma edges, u faces], report, status)."""
+        domain = np.ascontiguousarray(domain, dtype=CELL_DTYPE).reshape(1)
+        ainv6 = np.ascontiguousarray(ainv6, dtype=np.float64)
+        bdiv = np.ascontiguousarray(bdiv, dtype=np.float64)
+        n = 1 << int(domain["depth"][0])
+        x = np.zeros(3 * n * (n + 1) ** 2 + 3 * (n + 1) * n * n)
+        rep = np.zeros(1, dtype=REPORT_DTYPE)
+        ld = load if load is not None else make_load()
+        st = self._lib.msfec_nedrt_fine_solve(self._h, domain.ctypes.data_as(_vp), _d(ainv6), _d(bdiv),
+                                              ctypes.byref(ld), _d(x), rep.ctypes.data_as(_vp))
+        self.check(st, allow=(ERROR_NOT_CONVERGED,))
+        return x, rep[0], st
 
     def autotune(self, kind, cells, coef0, coef1, load):
         """msfec_autotune on a sample batch; returns (choice, n_candidates, times_ms)."""

@@ -319,6 +319,21 @@ def build_cell(origin, size, depth, ainv, bdiv, load_kind=LOAD_VEC_ZERO, load_pa
     return Phi, KH, FH
 
 
+def standard_solve(origin, size, depth, ainv, bdiv, load_kind=LOAD_VEC_ZERO, load_params=(0, 0, 0, 0)):
+    """Standard fine-scale Ned_RT solution on one box: the reference's NedRTStd
+    (ned_rt_ref.cc:110-330). Its constraints hold hanging nodes only (the
+    boundary projections at :119-133 are disabled), so every edge and face is
+    free; its reaction rate is zero (eqn_coeff_R.cc:8-14) and without an exact
+    solution it adds no boundary integral (:275-321). System: the unconstrained
+    [[M, -C], [C^T, D]] x = [0; (v, f)], sparse direct. Returns x [NE + NF]."""
+    n = 1 << int(depth)
+    NE, NF = counts(n)
+    A = assemble(n, size, ainv, bdiv)
+    rhs = np.zeros(NE + NF)
+    rhs[NE:] = face_load(n, origin, size, load_kind, load_params)
+    return spla.spsolve(A.tocsc(), rhs)
+
+
 def build(cells, ainv, bdiv, load_kind=LOAD_VEC_ZERO, load_params=(0, 0, 0, 0), want_phi=True,
           basis="solve"):
     """Batch over coarse cells; ainv [sum n^3, 3, 3], bdiv [sum n^3]."""

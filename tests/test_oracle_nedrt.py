@@ -110,3 +110,60 @@ def test_committed_nedrt_fixture_reproduces():
     res = N.build(cells, N.sym6_to_ainv(ainv6), bdiv, load.kind, list(load.params), want_phi=False)
     assert np.abs(res["KH"] - g["KH"]).max() <= 1e-9 * np.abs(g["KH"]).max()
     assert np.abs(res["FH"] - g["FH"]).max() <= 1e-9 * np.abs(g["FH"]).max()
+
+
+def _edge_index(n, d, i, j, k):
+    Ex = n * (n + 1) ** 2
+    return [i + n * (j + (n + 1) * k), Ex + i + (n + 1) * (j + n * k),
+            2 * Ex + i + (n + 1) * (j + (n + 1) * k)][d]
+
+
+def _face_index(n, d, i, j, k):
+    Fx = (n + 1) * n * n
+    return [i + (n + 1) * (j + n * k), Fx + i + n * (j + (n + 1) * k), 2 * Fx + i + n * (j + n * k)][d]
+
+
+def cyclic_image(n):
+    """DoF map of the rotation (x, y, z) -> (z, x, y) of the unit cube: the DoF
+    of direction d at lattice position (i, j, k) goes to direction d+1 at
+    (k, i, j) (tangential line integrals and normal fluxes keep their sign)."""
+    NE, NF = N.counts(n)
+    img = np.zeros(NE + NF, dtype=np.int64)
+    off = 0
+    for d, i, j, k in N.edge_geometry(n):
+        img[off:off + len(i)] = _edge_index(n, (d + 1) % 3, k, i, j)
+        off += len(i)
+    for d, i, j, k in N.face_geometry(n):
+        img[off:off + len(i)] = NE + _face_index(n, (d + 1) % 3, k, i, j)
+        off += len(i)
+    return img
+
+
+def test_standard_solve_natural_boundary():
+    """NedRTStd restatement: every DoF free (no Dirichlet rows), residual of the
+    full system at rounding, the boundary fluxes and tangential fields nonzero."""
+    cells, ainv6, bdiv, load = workloads.nedrt_tensor(m=1, depth=2, seed=5)
+    c = cells[0]
+    x = N.standard_solve(c["origin"], c["size"], 2, N.sym6_to_ainv(ainv6), bdiv, load.kind, list(load.params))
+    n = 4
+    NE, NF = N.counts(n)
+    A = N.assemble(n, c["size"], N.sym6_to_ainv(ainv6), bdiv)
+    rhs = np.zeros(NE + NF)
+    rhs[NE:] = N.face_load(n, c["origin"], c["size"], load.kind, list(load.params))
+    assert np.linalg.norm(A @ x - rhs) <= 1e-12 * np.linalg.norm(rhs)
+    bnd = N.boundary_mask(n)
+    assert np.abs(x[bnd]).max() > 1e-3 * np.abs(x).max()
+
+
+def test_standard_solve_cyclic_symmetry():
+    """Isotropic constant coefficients and the cyclic vector trig load on the unit
+    cube: the solution is invariant under the rotation (x, y, z) -> (z, x, y)."""
+    depth, n = 3, 8
+    ainv = np.tile(np.eye(3) * 0.7, (n ** 3, 1, 1))
+    bdiv = np.full(n ** 3, 1.3)
+    x = N.standard_solve(np.zeros(3), np.ones(3), depth, ainv, bdiv, N.LOAD_VEC_TRIG, [1.0, 1.0, 0.0, 0.0])
+    img = cyclic_image(n)
+    y = np.empty_like(x)
+    y[img] = x
+    assert np.abs(x).max() > 0
+    assert np.abs(y - x).max() <= 1e-10 * np.abs(x).max()
