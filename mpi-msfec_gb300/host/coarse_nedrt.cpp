@@ -1,11 +1,17 @@
 // Global coarse Ned_RT assembly and solve on a structured m^3 coarse grid of the
-// unit cube with essential conditions (coarse edges tangential to the
-// boundary and coarse boundary faces are zero): the consumer of the 18x18
-// K_H / 18 F_H of every cell. Restates NedRTMultiscale::assemble_system
-// (source/Ned_RT/ned_rt_global.cc:191-311, distribute_local_to_global of the
-// element matrices) and its solve (ned_rt_global.cc:313-461, a Schur
-// complement solver there; preconditioned MINRES on the symmetric form here,
-// FP64 on the host).
+// unit cube: the consumer of the 18x18 K_H / 18 F_H of every cell. Restates
+// NedRTMultiscale::assemble_system (source/Ned_RT/ned_rt_global.cc:191-311,
+// distribute_local_to_global of the element matrices) and its solve
+// (ned_rt_global.cc:313-461, a Schur complement solver there; preconditioned
+// MINRES on the symmetric form here, FP64 on the host).
+//
+// Boundary conditions: NedRTMultiscale::setup_constraints
+// (ned_rt_global.cc:165-188) holds hanging-node constraints only, its
+// curl- and div-conforming boundary projections being commented out, so every
+// coarse DoF is free (natural conditions; the system is nonsingular on the
+// cube): msfec_host_nedrt_coarse_solve. The variant with essential conditions
+// (coarse edges tangential to the boundary and coarse boundary faces zero) is
+// msfec_host_nedrt_coarse_solve_essential.
 //
 // Coarse DoFs: edges in the fine-lattice numbering with n = m (x-edges
 // i + m(j + (m+1)k), then y-, z-edges), then faces (x-faces
@@ -84,12 +90,14 @@ extern "C" int msfec_host_nedrt_cell_dofs(int m, int cell, int *g18) {
   return 0;
 }
 
-extern "C" int msfec_host_nedrt_coarse_solve(int m, const double *KH, const double *FH, double *U, double rtol,
-                                             int max_iter, int *iters) {
+namespace {
+
+int nedrt_coarse_solve(int m, const double *KH, const double *FH, double *U, double rtol, int max_iter, int *iters,
+                       bool essential) {
   if (m < 1 || !KH || !FH || !U) return 1;
   const int Ex = m * (m + 1) * (m + 1), Fx = (m + 1) * m * m, NE = 3 * Ex;
   const size_t N = (size_t)3 * Ex + 3 * Fx;
-  const std::vector<char> bnd = boundary(m);
+  const std::vector<char> bnd = essential ? boundary(m) : std::vector<char>(N, 0);
   // assemble the symmetric form (face rows negated) on interior DoFs as CSR
   std::vector<std::vector<std::pair<int, double>>> rows(N);
   std::vector<double> b(N, 0.0);
@@ -208,4 +216,19 @@ extern "C" int msfec_host_nedrt_coarse_solve(int m, const double *KH, const doub
   for (size_t t = 0; t < N; ++t) U[t] = x[t];
   if (iters) *iters = it;
   return std::sqrt(rr) <= rtol * bnorm || bnorm == 0.0 ? 0 : 2;
+}
+
+}  // namespace
+
+// The reference's NedRTMultiscale system: natural conditions, every coarse DoF
+// free. U [NE + NF]; returns 0, 1 (bad arguments) or 2 (rtol not reached).
+extern "C" int msfec_host_nedrt_coarse_solve(int m, const double *KH, const double *FH, double *U, double rtol,
+                                             int max_iter, int *iters) {
+  return nedrt_coarse_solve(m, KH, FH, U, rtol, max_iter, iters, false);
+}
+
+// Essential conditions: boundary-tangential coarse edges and boundary coarse faces fixed at 0.
+extern "C" int msfec_host_nedrt_coarse_solve_essential(int m, const double *KH, const double *FH, double *U,
+                                                       double rtol, int max_iter, int *iters) {
+  return nedrt_coarse_solve(m, KH, FH, U, rtol, max_iter, iters, true);
 }

@@ -21,8 +21,9 @@ def host_lib():
     L.msfec_host_q1_coarse_solve.argtypes = [ctypes.c_int, dp, dp, dp, ctypes.c_double, ctypes.c_int,
                                              ctypes.POINTER(ctypes.c_int)]
     L.msfec_host_q1_coarse_solve.restype = ctypes.c_int
-    L.msfec_host_nedrt_coarse_solve.argtypes = L.msfec_host_q1_coarse_solve.argtypes
-    L.msfec_host_nedrt_coarse_solve.restype = ctypes.c_int
+    for name in ("msfec_host_nedrt_coarse_solve", "msfec_host_nedrt_coarse_solve_essential"):
+        getattr(L, name).argtypes = L.msfec_host_q1_coarse_solve.argtypes
+        getattr(L, name).restype = ctypes.c_int
     return L
 
 
@@ -76,7 +77,9 @@ def test_shim_library_and_example_build():
     assert hasattr(L, "msfec_host_q1_coarse_solve") and hasattr(L, "msfec_host_nedrt_coarse_solve")
 
 
-def nedrt_coarse_solve(m, KH, FH, rtol=1e-13):
+def nedrt_coarse_solve(m, KH, FH, rtol=1e-13, essential=False):
+    """Host coarse Ned_RT solve: natural conditions (the reference's
+    NedRTMultiscale) by default, or boundary DoFs fixed at 0."""
     L = host_lib()
     from oracle import nedrt_oracle as N
     NE, NF = N.counts(m)
@@ -85,16 +88,18 @@ def nedrt_coarse_solve(m, KH, FH, rtol=1e-13):
     dp = ctypes.POINTER(ctypes.c_double)
     KH = np.ascontiguousarray(KH, dtype=np.float64)
     FH = np.ascontiguousarray(FH, dtype=np.float64)
-    st = L.msfec_host_nedrt_coarse_solve(m, KH.ctypes.data_as(dp), FH.ctypes.data_as(dp), U.ctypes.data_as(dp),
-                                         rtol, 50000, ctypes.byref(it))
+    f = L.msfec_host_nedrt_coarse_solve_essential if essential else L.msfec_host_nedrt_coarse_solve
+    st = f(m, KH.ctypes.data_as(dp), FH.ctypes.data_as(dp), U.ctypes.data_as(dp), rtol, 50000, ctypes.byref(it))
     assert st == 0, (st, it.value)
     return U
 
 
-def scipy_nedrt_coarse(m, KH, FH):
+def scipy_nedrt_coarse(m, KH, FH, essential=False):
     """Independent assembly (global maps of the oracle) and sparse direct solve."""
     from oracle import nedrt_adjoint as NA
     g, bnd = NA.coarse_maps(m)
+    if not essential:
+        bnd = np.zeros_like(bnd)
     n = bnd.size
     K = sp.coo_matrix((np.asarray(KH).ravel(), (np.repeat(g, 18, axis=1).ravel(), np.tile(g, (1, 18)).ravel())),
                       shape=(n, n)).tocsr()
@@ -106,14 +111,19 @@ def scipy_nedrt_coarse(m, KH, FH):
     return U
 
 
+@pytest.mark.parametrize("essential", [False, True])
 @pytest.mark.parametrize("m", [2, 3])
-def test_nedrt_coarse_solver_matches_scipy(m):
+def test_nedrt_coarse_solver_matches_scipy(m, essential):
+    from oracle import nedrt_adjoint as NA
     from oracle import nedrt_oracle as N
     cells, ainv6, bdiv, load = workloads.nedrt_tensor(m=m, depth=1, seed=8)
     res = N.build(cells, N.sym6_to_ainv(ainv6), bdiv, load.kind, list(load.params), want_phi=False)
     rng = np.random.default_rng(m)
-    # a generic face load as well as the (divergence-free) trig load of the workload
+    # the trig load of the workload and a generic face load on top of it
     for FH in (res["FH"], res["FH"] + np.concatenate([np.zeros((m ** 3, 12)), rng.standard_normal((m ** 3, 6))], 1)):
-        U = nedrt_coarse_solve(m, res["KH"], FH)
-        Us = scipy_nedrt_coarse(m, res["KH"], FH)
+        U = nedrt_coarse_solve(m, res["KH"], FH, essential=essential)
+        Us = scipy_nedrt_coarse(m, res["KH"], FH, essential=essential)
         assert np.abs(U - Us).max() <= 1e-10 * np.abs(Us).max()
+        if not essential:  # natural conditions: the boundary DoFs carry the solution too
+            _, bnd = NA.coarse_maps(m)
+            assert np.abs(Us[bnd]).max() > 1e-3 * np.abs(Us).max()

@@ -41,8 +41,8 @@ def test_global_nedrt_solution_matches_oracle(gpu, precision):
     assert st == gpu.SUCCESS and rep["converged"].all()
     ref = N.build(cells, N.sym6_to_ainv(ainv6), bdiv, load.kind, list(load.params))
     rng = np.random.default_rng(5)
-    # the trig load is divergence-free (its coarse solution has no edge part);
-    # a generic face load exercises the edge/face coupling as well
+    # the workload's trig load and a generic face load on top of it; the coarse
+    # solve has the reference's natural conditions (every coarse DoF free)
     extra = np.concatenate([np.zeros((m ** 3, 12)), rng.standard_normal((m ** 3, 6))], 1)
     g, _ = NA.coarse_maps(m)
     n = 1 << depth

@@ -167,3 +167,65 @@ def test_standard_solve_cyclic_symmetry():
     y[img] = x
     assert np.abs(x).max() > 0
     assert np.abs(y - x).max() <= 1e-10 * np.abs(x).max()
+
+
+def _global_fine_field(m, n, cells_vec):
+    """Scatter per-coarse-cell fine vectors (edges, faces of an n^3 lattice) into
+    the global (m n)^3 lattice; shared interface DoFs agree (conforming basis)."""
+    D = m * n
+    GE, GF = N.counts(D)
+    x = np.zeros(GE + GF)
+    for c in range(m ** 3):
+        ci, cj, ck = c % m, (c // m) % m, c // (m * m)
+        sig, u = cells_vec(c)
+        off = 0
+        for d, a, b, q in N.edge_geometry(n):
+            x[_edge_index(D, d, ci * n + a, cj * n + b, ck * n + q)] = sig[off:off + len(a)]
+            off += len(a)
+        off = 0
+        for d, a, b, q in N.face_geometry(n):
+            x[GE + _face_index(D, d, ci * n + a, cj * n + b, ck * n + q)] = u[off:off + len(a)]
+            off += len(a)
+    return x
+
+
+def _multiscale_vs_standard(m, depth, seed):
+    from oracle import nedrt_adjoint as NA
+    from test_coarse_solve import scipy_nedrt_coarse
+    n = 1 << depth
+    D = m * n
+    cells, ainv6, bdiv, load = workloads.nedrt_tensor(m=m, depth=depth, seed=seed)
+    ainv = N.sym6_to_ainv(ainv6)
+    ref = N.build(cells, ainv, bdiv, load.kind, list(load.params))
+    U = scipy_nedrt_coarse(m, ref["KH"], ref["FH"])  # natural conditions, as NedRTMultiscale
+    g, _ = NA.coarse_maps(m)
+    NE, _ = N.counts(n)
+    Phi = np.array(ref["Phi"])
+    # set_global_weights: sigma from the edge bases' sigma blocks, u from the face bases' u blocks
+    x = _global_fine_field(m, n, lambda c: (U[g[c, :12]] @ Phi[c, :12, :NE], U[g[c, 12:]] @ Phi[c, 12:, NE:]))
+    nf = n ** 3
+    ga, gb = np.zeros((D ** 3, 3, 3)), np.zeros(D ** 3)
+    t = np.arange(nf)
+    i, j, k = t % n, (t // n) % n, t // (n * n)
+    for c in range(m ** 3):
+        ci, cj, ck = c % m, (c // m) % m, c // (m * m)
+        G = (ci * n + i) + D * ((cj * n + j) + D * (ck * n + k))
+        ga[G] = ainv[c * nf:(c + 1) * nf]
+        gb[G] = bdiv[c * nf:(c + 1) * nf]
+    xs = N.standard_solve(np.zeros(3), np.ones(3), int(np.log2(D)), ga, gb, load.kind, list(load.params))
+    GE, _ = N.counts(D)
+    es = np.linalg.norm(x[:GE] - xs[:GE]) / np.linalg.norm(xs[:GE])
+    eu = np.linalg.norm(x[GE:] - xs[GE:]) / np.linalg.norm(xs[GE:])
+    return es, eu
+
+
+def test_multiscale_vs_standard_solution():
+    """Error of the Ned_RT multiscale solution (coarse solve with the reference's
+    natural conditions, fine reconstruction by set_global_weights) against the
+    standard fine-scale solution (NedRTStd) on the same fine grid and rough
+    coefficient: bounded, and smaller on the finer coarse grid."""
+    es2, eu2 = _multiscale_vs_standard(2, 2, 3)  # coarse 2^3 x depth 2 vs fine 8^3
+    es4, eu4 = _multiscale_vs_standard(4, 2, 3)  # coarse 4^3 x depth 2 vs fine 16^3
+    print(f"multiscale vs standard Ned_RT: 2^3 sigma {es2:.3e} u {eu2:.3e}; 4^3 sigma {es4:.3e} u {eu4:.3e}")
+    assert max(es2, eu2) < 0.7 and max(es4, eu4) < 0.55
+    assert es4 < es2 and eu4 < eu2
