@@ -9,6 +9,7 @@
    workloads, the parity target of the CUDA path.
 3. nedrt_*.npz: FP64 oracle (sparse direct, SuperLU) K_H / F_H of a seeded
    Ned_RT workload.
+4. qned_*.npz, rtdq_*.npz: the same for seeded Q_Ned and RT_DQ workloads.
 
 Usage: python tests/golden/make_golden.py [--reference DIR]
 """
@@ -25,6 +26,8 @@ sys.path.insert(0, REPO)
 
 from oracle import oracle  # noqa: E402
 from oracle import nedrt_oracle  # noqa: E402
+from oracle import qned_oracle  # noqa: E402
+from oracle import rtdq_oracle  # noqa: E402
 import workloads  # noqa: E402
 
 
@@ -69,6 +72,15 @@ def main():
     res = nedrt_oracle.build(cells, nedrt_oracle.sym6_to_ainv(ainv6), bdiv, load.kind, list(load.params),
                              want_phi=False)
     np.savez_compressed(os.path.join(HERE, "nedrt_tensor_m2_L2_seed2.npz"), KH=res["KH"], FH=res["FH"])
+    # Q_Ned: coarse 2^3, depth 2, seeded tensor A and B^-1 (seed 4)
+    cells, a6, binv, load = workloads.qned_tensor(m=2, depth=2, seed=4)
+    res = qned_oracle.build(cells, binv, nedrt_oracle.sym6_to_ainv(a6), load.kind, list(load.params),
+                            want_phi=False)
+    np.savez_compressed(os.path.join(HERE, "qned_tensor_m2_L2_seed4.npz"), KH=res["KH"], FH=res["FH"])
+    # RT_DQ: coarse 2^3, depth 2, seeded tensor A^-1 (seed 6)
+    cells, ainv6, load = workloads.rtdq_tensor(m=2, depth=2, seed=6)
+    res = rtdq_oracle.build(cells, nedrt_oracle.sym6_to_ainv(ainv6), load.kind, list(load.params), want_phi=False)
+    np.savez_compressed(os.path.join(HERE, "rtdq_tensor_m2_L2_seed6.npz"), KH=res["KH"], FH=res["FH"])
 
 
 if __name__ == "__main__":

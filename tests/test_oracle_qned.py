@@ -87,3 +87,13 @@ def test_oracle_basis_properties():
     # partition of unity: sum of the vertex bases' sigma blocks is 1 (constant in the kernel of grad)
     assert np.abs(Phi[:8, :NV].sum(0) - 1.0).max() < 1e-10
     assert Am.shape == (NV + NE, NV + NE) and len(I) > 0
+
+
+def test_committed_qned_fixture_reproduces():
+    """The oracle against its committed K_H / F_H (tests/golden/make_golden.py)."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "qned_tensor_m2_L2_seed4.npz"))
+    cells, a6, binv, load = workloads.qned_tensor(m=2, depth=2, seed=4)
+    res = Q.build(cells, binv, NR.sym6_to_ainv(a6), load.kind, list(load.params), want_phi=False)
+    assert np.abs(res["KH"] - g["KH"]).max() <= 1e-9 * np.abs(g["KH"]).max()
+    assert np.abs(res["FH"] - g["FH"]).max() <= 1e-9 * np.abs(g["FH"]).max()

@@ -116,3 +116,13 @@ def test_reference_schur_cg_gives_the_oracle_sigma():
         assert np.abs(sigma - Phi[b, If]).max() <= 1e-10 * np.abs(Phi[b, :NF]).max()
         assert abs(u.mean()) <= 1e-10 * np.abs(u).max()
         assert np.abs(u - P[b][Ic - NF]).max() <= 1e-8 * np.abs(u).max()
+
+
+def test_committed_rtdq_fixture_reproduces():
+    """The oracle against its committed K_H / F_H (tests/golden/make_golden.py)."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "rtdq_tensor_m2_L2_seed6.npz"))
+    cells, ainv6, load = workloads.rtdq_tensor(m=2, depth=2, seed=6)
+    res = RQ.build(cells, NR.sym6_to_ainv(ainv6), load.kind, list(load.params), want_phi=False)
+    assert np.abs(res["KH"] - g["KH"]).max() <= 1e-9 * np.abs(g["KH"]).max()
+    assert np.abs(res["FH"] - g["FH"]).max() <= 1e-9 * np.abs(g["FH"]).max()

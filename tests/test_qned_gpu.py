@@ -53,3 +53,18 @@ def test_qned_basis_matches_oracle(gpu, precision, m, depth):
             assert _rel(pg[b], po[b]) <= TOL_PHI, (c, b, _rel(pg[b], po[b]))
     print(f"{precision} depth {depth}: max K_H rel err {max(_rel(KH[c], ref['KH'][c]) for c in range(len(cells))):.2e}, "
           f"max iterations {rep['iterations'].max()}")
+
+
+@pytest.mark.parametrize("precision", ("mixed", "fp64"))
+def test_qned_matches_golden(gpu, precision):
+    """GPU build against the committed oracle fixture (coarse 2^3 x depth 2,
+    tests/golden/make_golden.py), same per-cell tolerance as above."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "qned_tensor_m2_L2_seed4.npz"))
+    cells, a6, binv, load = workloads.qned_tensor(m=2, depth=2, seed=4)
+    h = gpu.Handle(precision=gpu.PRECISION_MIXED if precision == "mixed" else gpu.PRECISION_FP64)
+    KH, FH, rep, st = h.qned_build(cells, a6, binv, load)
+    assert st == gpu.SUCCESS and rep["converged"].all(), rep
+    for c in range(len(cells)):
+        assert _rel(KH[c], g["KH"][c]) <= TOL_KH, (c, _rel(KH[c], g["KH"][c]))
+        assert _rel(FH[c], g["FH"][c]) <= TOL_KH, (c, _rel(FH[c], g["FH"][c]))

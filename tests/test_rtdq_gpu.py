@@ -99,3 +99,18 @@ def test_rtdq_rejects_bad_input(gpu):
         h.rtdq_build(deep, np.tile(ainv6, (64, 1)), gpu.make_load(gpu.LOAD_ZERO, (0, 0, 0, 0)))
     KH, FH, rep, st = h.rtdq_build(cells[:0], ainv6[:0], gpu.make_load(gpu.LOAD_ZERO, (0, 0, 0, 0)))
     assert st == gpu.SUCCESS and KH.shape == (0, 7, 7)
+
+
+@pytest.mark.parametrize("precision", ("mixed", "fp64"))
+def test_rtdq_matches_golden(gpu, precision):
+    """GPU build against the committed oracle fixture (coarse 2^3 x depth 2,
+    tests/golden/make_golden.py), same per-cell tolerance as above."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "rtdq_tensor_m2_L2_seed6.npz"))
+    cells, ainv6, load = workloads.rtdq_tensor(m=2, depth=2, seed=6)
+    h = gpu.Handle(precision=gpu.PRECISION_MIXED if precision == "mixed" else gpu.PRECISION_FP64)
+    KH, FH, rep, st = h.rtdq_build(cells, ainv6, load)
+    assert st == gpu.SUCCESS and rep["converged"].all(), rep
+    for c in range(len(cells)):
+        assert _rel(KH[c], g["KH"][c]) <= TOL_KH, (c, _rel(KH[c], g["KH"][c]))
+        assert _rel(FH[c], g["FH"][c]) <= TOL_KH, (c, _rel(FH[c], g["FH"][c]))
