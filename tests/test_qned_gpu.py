@@ -68,3 +68,43 @@ def test_qned_matches_golden(gpu, precision):
     for c in range(len(cells)):
         assert _rel(KH[c], g["KH"][c]) <= TOL_KH, (c, _rel(KH[c], g["KH"][c]))
         assert _rel(FH[c], g["FH"][c]) <= TOL_KH, (c, _rel(FH[c], g["FH"][c]))
+
+
+def test_qned_mixed_depth_batch(gpu):
+    """Ragged batch: depths 2 and 3 in one persistent launch (deepest items
+    first, workspace sized by the deepest cell), per cell against the oracle."""
+    cells = workloads.coarse_grid(2, 2)
+    cells["depth"] = [3, 2, 2, 3, 2, 3, 3, 2]
+    A, a6, binv = _coefs(cells, seed=21)
+    load = gpu.make_load(gpu.LOAD_VEC_TRIG, (1.0, 1.0, 0.0, 0.0))
+    h = gpu.Handle()
+    KH, FH, rep, st = h.qned_build(cells, a6, binv, load)
+    assert st == gpu.SUCCESS and rep["converged"].all(), rep
+    ref = Q.build(cells, binv, A, load.kind, list(load.params), want_phi=False)
+    for c in range(len(cells)):
+        assert _rel(KH[c], ref["KH"][c]) <= TOL_KH, (c, _rel(KH[c], ref["KH"][c]))
+        assert _rel(FH[c], ref["FH"][c]) <= TOL_KH, (c, _rel(FH[c], ref["FH"][c]))
+
+
+def test_qned_rejects_bad_input(gpu):
+    """Host-side validation (no kernel runs): scalar load, B^-1 <= 0, A not SPD,
+    depth 5; an empty batch succeeds with empty outputs."""
+    cells = workloads.coarse_grid(1, 2)
+    A, a6, binv = _coefs(cells, seed=3)
+    h = gpu.Handle()
+    with pytest.raises(gpu.MsfecError):
+        h.qned_build(cells, a6, binv, gpu.make_load(gpu.LOAD_SIN_PRODUCT, (1.0, 1.0, 0.0, 0.0)))
+    bad = binv.copy()
+    bad[3] = -1.0
+    with pytest.raises(gpu.MsfecError):
+        h.qned_build(cells, a6, bad, gpu.make_load())
+    nspd = a6.copy()
+    nspd[5, 0] = -1.0
+    with pytest.raises(gpu.MsfecError):
+        h.qned_build(cells, nspd, binv, gpu.make_load())
+    deep = cells.copy()
+    deep["depth"] = 5
+    with pytest.raises(gpu.MsfecError):
+        h.qned_build(deep, np.tile(a6, (512, 1)), np.tile(binv, 512), gpu.make_load())
+    KH, FH, rep, st = h.qned_build(cells[:0], a6[:0], binv[:0], gpu.make_load())
+    assert st == gpu.SUCCESS and KH.shape == (0, 20, 20) and FH.shape == (0, 20)
