@@ -2,7 +2,8 @@
 // the reference's NedRTMultiscale::run (source/Ned_RT/ned_rt_global.cc) -
 // basis objects per coarse cell in a std::map (ned_rt_global.cc:49-99), run(),
 // 18x18 element matrices into the global coarse system, coarse solve (host
-// MINRES), weights back to every cell (set_global_weights,
+// MINRES, natural boundary conditions as in NedRTMultiscale::setup_constraints,
+// ned_rt_global.cc:165-188), weights back to every cell (set_global_weights,
 // ned_rt_basis.cc:1155-1181), fine sigma / u of the multiscale solution.
 // Usage: example_nedrt <m> <depth>   (coarse m^3 cells of the unit cube)
 #include <cmath>
