@@ -66,6 +66,44 @@ def test_kernel_closed_form_tables_match_quadrature():
     assert np.allclose(Ce, C, rtol=1e-13, atol=1e-14)
 
 
+def kernel_edge_mass_form(h, ai, x, y):
+    """Same factored form as edge_mass_form in csrc/nedrt_solve.cu (the A part of
+    the adjoint gradient): x^T M_e y without the 12 x 12 table."""
+    A = np.array([[ai[0], ai[3], ai[4]], [ai[3], ai[1], ai[5]], [ai[4], ai[5], ai[2]]])
+    my = np.zeros(12)
+    for p in range(3):
+        o1, o2 = _other(p)
+        k = A[p, p] * h[o1] * h[o2] / (36.0 * h[p])
+        t = [2.0 * y[4 * p + l] + y[4 * p + (l ^ 1)] for l in range(4)]
+        for l in range(4):
+            my[4 * p + l] = k * (2.0 * t[l] + t[l ^ 2])
+    for p in range(3):
+        for q in range(3):
+            if q == p:
+                continue
+            r = 3 - p - q
+            s1 = sum(y[4 * q + m] for m in range(4) if _edge_pos(q, m, r))
+            s0 = sum(y[4 * q + m] for m in range(4) if not _edge_pos(q, m, r))
+            k = A[p, q] * h[r] / 24.0
+            for l in range(4):
+                my[4 * p + l] += k * (s0 + 2.0 * s1 if _edge_pos(p, l, r) else 2.0 * s0 + s1)
+    return float(np.dot(x, my))
+
+
+def test_kernel_edge_mass_form_matches_quadrature():
+    rng = np.random.default_rng(4)
+    for _ in range(5):
+        h = rng.uniform(0.05, 0.6, 3)
+        G = rng.standard_normal((3, 3))
+        ainv = G @ G.T + 0.5 * np.eye(3)
+        ai = [ainv[0, 0], ainv[1, 1], ainv[2, 2], ainv[0, 1], ainv[0, 2], ainv[1, 2]]
+        Me, _, _ = N.element_matrices(h, ainv[None], np.ones(1))
+        x, y = rng.standard_normal(12), rng.standard_normal(12)
+        ref = x @ Me[0] @ y
+        scale = np.abs(x) @ np.abs(Me[0]) @ np.abs(y)
+        assert abs(kernel_edge_mass_form(h, ai, x, y) - ref) <= 1e-13 * scale
+
+
 def test_standard_basis_galerkin_is_refinement_invariant():
     # The reference's set_to_std sanity path (ned_rt_basis.cc:1312-1335): with
     # constant coefficients the coarse functions' Galerkin matrix does not
