@@ -5,9 +5,10 @@ Problem: coarse 2^3 x depth 2 on the unit cube, tensor A^-1 and B of the
 Ned_RT workload scaled by exp(-ta), exp(tb) per fine cell, vector trig load,
 J = 1/2 sum_k |u_h(x_k) - d_k|^2 at 40 points. The coarse problem (assembly,
 solve, transposed adjoint solve) is the harness's (scipy). Stated tolerances:
-  GPU vs oracle   |g - g_ref| <= 1e-8 max|g_ref|  (both gradients; the A
-                  gradient vanishes for this divergence-free load, so it is
-                  compared against the B gradient's scale)
+  GPU vs oracle   |g - g_ref| <= 1e-8 max|g_ref|  (both gradients; on the 2^3
+                  grid the A gradient vanishes for this divergence-free load,
+                  so it is compared against the B gradient's scale; the last
+                  test runs coarse 3^3, where it does not vanish)
   FD (h = 1e-5)   |fd - g.d| <= 1e-6 sum|g_i d_i| (cancellation-aware)
   mixed vs FP64   1e-8 relative
 """
@@ -119,3 +120,19 @@ def test_nedrt_gradient_finite_differences_and_fp64(gpu):
         d = rng.standard_normal(ta.size)
         fda = (P64.forward(ta + hs * d, tb)[0] - P64.forward(ta - hs * d, tb)[0]) / (2 * hs)
         assert abs(fda - ga @ d) <= 1e-6 * np.abs(gb * d).sum()
+
+
+def test_nedrt_gradient_nonvanishing_A_matches_oracle(gpu):
+    """Coarse 3^3 x depth 2: the coarse solution has an edge part, so dJ/d log A
+    does not vanish (max|g_A| ~ 3.5 % of max|g_B|); both gradients against the
+    oracle, each to 1e-8 of its own scale."""
+    P = NedRTMisfit(gpu, m=3, depth=2, seed=5, precision="mixed")
+    rng = np.random.default_rng(9)
+    ta = 0.3 * rng.standard_normal(P.bdiv.size)
+    tb = 0.3 * rng.standard_normal(P.bdiv.size)
+    J, ga, gb = P.gradient(ta, tb)
+    Jr, gar, gbr = P.oracle(ta, tb)
+    assert abs(J - Jr) <= 1e-9 * abs(Jr)
+    assert np.abs(gar).max() > 1e-2 * np.abs(gbr).max()
+    assert np.abs(ga - gar).max() <= 1e-8 * np.abs(gar).max(), np.abs(ga - gar).max() / np.abs(gar).max()
+    assert np.abs(gb - gbr).max() <= 1e-8 * np.abs(gbr).max(), np.abs(gb - gbr).max() / np.abs(gbr).max()
