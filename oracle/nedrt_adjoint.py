@@ -23,9 +23,9 @@ Pi_j the primary block of basis j. eta_j is linear in (lambda_j, U_j) with
 four distinct right-hand sides per cell (edge / face bases x lambda / U), so
 four transposed local solves per cell (A^T = S A S, S = +1 on edges, -1 on
 faces). The reference has no adjoint; this is the derivative of its Ned_RT
-path restated here. For the divergence-free trig load the coarse solution has
-no edge part and does not depend on A (dJ/dta vanishes); B carries the
-sensitivity.
+path restated here. For the divergence-free trig load on a coarse 2^3 grid the
+coarse solution has no edge part and does not depend on A (dJ/dta vanishes; B
+carries the sensitivity); on a 3^3 grid it has one and dJ/dta does not vanish.
 """
 import numpy as np
 import scipy.sparse as sp
