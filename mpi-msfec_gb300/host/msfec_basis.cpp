@@ -3,6 +3,7 @@
 // answers the reference's getters from the batch results.
 #include "msfec_basis.hpp"
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -141,6 +142,54 @@ double Q1Batch::evaluate(int slot, const std::vector<double> &w, const Point &x)
   return out;
 }
 
+static msfec_cell unit_cube(unsigned n_refine) {
+  msfec_cell m;
+  std::memset(&m, 0, sizeof(m));
+  for (int d = 0; d < 3; ++d) m.size[d] = 1.0;
+  m.depth = (int32_t)n_refine;
+  return m;
+}
+
+QStd::QStd(const ParametersStd &parameters, Q1Coefficients coeff)
+    : parameters_(parameters), coeff_(std::move(coeff)), gpu_(parameters.device, parameters.precision) {}
+
+void QStd::run() {
+  const msfec_cell dom = unit_cube(parameters_.n_refine);
+  std::vector<double> a, r;
+  for_each_fine_centre(dom, [&](const Point &p) {
+    a.push_back(coeff_.diffusion(p));
+    if (coeff_.reaction) r.push_back(coeff_.reaction(p));
+  });
+  const size_t n1 = ((size_t)1 << parameters_.n_refine) + 1;
+  u_.assign(n1 * n1 * n1, 0.0);
+  check(gpu_.handle(),
+        msfec_q1_fine_solve(gpu_.handle(), &dom, a.data(), coeff_.reaction ? r.data() : nullptr, &coeff_.load,
+                            u_.data(), &report_),
+        "msfec_q1_fine_solve");
+}
+
+// Lattice coordinate of x along one axis: cell index in [0, n) and the local coordinate in [0, 1].
+static void lattice_coord(double x, int n, int &i, double &t) {
+  const double s = std::fmin(std::fmax(x, 0.0), 1.0) * n;
+  i = std::min((int)s, n - 1);
+  t = s - i;
+}
+
+double QStd::solution_value(const Point &x) const {
+  if (u_.empty()) throw BasisError(MSFEC_ERROR_INVALID_ARGUMENT, "QStd::solution_value before run()");
+  const int n = 1 << parameters_.n_refine, n1 = n + 1;
+  int c[3];
+  double t[3];
+  for (int d = 0; d < 3; ++d) lattice_coord(x[d], n, c[d], t[d]);
+  double v = 0.0;
+  for (int q = 0; q < 8; ++q) {
+    const int a = q & 1, b = (q >> 1) & 1, e = q >> 2;
+    const double w = (a ? t[0] : 1.0 - t[0]) * (b ? t[1] : 1.0 - t[1]) * (e ? t[2] : 1.0 - t[2]);
+    v += w * u_[(size_t)(c[0] + a) + (size_t)n1 * ((c[1] + b) + (size_t)n1 * (c[2] + e))];
+  }
+  return v;
+}
+
 }  // namespace Q
 
 namespace NedRT {
@@ -252,6 +301,52 @@ void NedRTBatch::solution(int slot, const std::vector<double> &w, std::vector<do
     for (size_t d = 0; d < NE; ++d) sigma[d] += w[b] * phi[(size_t)b * N + d];
   for (int b = 12; b < 18; ++b)
     for (size_t d = 0; d < NF; ++d) u[d] += w[b] * phi[(size_t)b * N + NE + d];
+}
+
+NedRTStd::NedRTStd(const ParametersStd &parameters, NedRTCoefficients coeff)
+    : parameters_(parameters), coeff_(std::move(coeff)), gpu_(parameters.device, parameters.precision) {}
+
+void NedRTStd::run() {
+  const msfec_cell dom = Q::unit_cube(parameters_.n_refine);
+  std::vector<double> ainv6, b;
+  for_each_fine_centre(dom, [&](const Point &p) {
+    const std::array<double, 9> m = coeff_.diffusion_inverse(p);
+    const double s6[6] = {m[0], m[4], m[8], m[1], m[2], m[5]};
+    ainv6.insert(ainv6.end(), s6, s6 + 6);
+    b.push_back(coeff_.div_weight(p));
+  });
+  const size_t n = (size_t)1 << parameters_.n_refine;
+  const size_t NE = 3 * n * (n + 1) * (n + 1), NF = 3 * (n + 1) * n * n;
+  std::vector<double> x(NE + NF, 0.0);
+  check(gpu_.handle(),
+        msfec_nedrt_fine_solve(gpu_.handle(), &dom, ainv6.data(), b.data(), &coeff_.load, x.data(), &report_),
+        "msfec_nedrt_fine_solve");
+  sigma_.assign(x.begin(), x.begin() + NE);
+  u_.assign(x.begin() + NE, x.end());
+}
+
+Point NedRTStd::u_value(const Point &x) const {
+  if (u_.empty()) throw BasisError(MSFEC_ERROR_INVALID_ARGUMENT, "NedRTStd::u_value before run()");
+  const int n = 1 << parameters_.n_refine;
+  const size_t Fx = (size_t)(n + 1) * n * n;
+  int c[3];
+  double t[3];
+  for (int d = 0; d < 3; ++d) Q::lattice_coord(x[d], n, c[d], t[d]);
+  const double h = 1.0 / n, area = h * h;
+  // face (normal d, lattice position) -> index in the face block
+  auto face = [&](int d, int i, int j, int k) -> size_t {
+    if (d == 0) return (size_t)i + (size_t)(n + 1) * (j + (size_t)n * k);
+    if (d == 1) return Fx + (size_t)i + (size_t)n * (j + (size_t)(n + 1) * k);
+    return 2 * Fx + (size_t)i + (size_t)n * (j + (size_t)n * k);
+  };
+  Point v{};
+  for (int d = 0; d < 3; ++d) {
+    int lo[3] = {c[0], c[1], c[2]}, hi[3] = {c[0], c[1], c[2]};
+    hi[d] += 1;
+    // flux DoF / face area, linear along the normal (lowest-order RT)
+    v[d] = ((1.0 - t[d]) * u_[face(d, lo[0], lo[1], lo[2])] + t[d] * u_[face(d, hi[0], hi[1], hi[2])]) / area;
+  }
+  return v;
 }
 
 }  // namespace NedRT

@@ -4,6 +4,8 @@
 // global coarse solvers consume the result unchanged:
 //   Q::QBasis          include/Q/q_basis.h:77-139
 //   NedRT::NedRTBasis  include/Ned_RT/ned_rt_basis.h:99-153
+// and, as accuracy references, the standard fine-scale solvers Q::QStd and
+// NedRT::NedRTStd (constructor + run(), solution returned instead of written).
 // ctor -> run() -> get_global_element_matrix() / get_global_element_rhs()
 // -> (coarse solve) -> set_global_weights().
 //
@@ -73,6 +75,18 @@ struct ParametersBasis {
   bool use_direct_solver = false;  // accepted for compatibility; the GPU path is iterative
   int precision = MSFEC_PRECISION_MIXED;
   std::string filename_global = "multiscale_solution";
+};
+
+// The knobs of ParametersStd the standard fine-scale solvers read
+// (include/Q/q_parameters.h:18-42): the unit cube refined n_refine times
+// (2^n_refine fine cells per axis). Output file names are not used (the
+// solution is returned instead of written as VTU).
+struct ParametersStd {
+  unsigned n_refine = 5;
+  bool verbose = false;
+  bool use_direct_solver = false;  // accepted for compatibility; the GPU path is iterative
+  int precision = MSFEC_PRECISION_MIXED;
+  int device = 0;
 };
 
 // One GPU handle and the pending cells of one batch.
@@ -150,6 +164,32 @@ class Q1Batch : public std::enable_shared_from_this<Q1Batch> {
   bool built_ = false;
 };
 
+// Standard fine-scale Q1 solve on the unit cube: the reference's QStd
+// (include/Q/q_ref.h:84-110, source/Q/q_ref.cc:139-363) through
+// msfec_q1_fine_solve, homogeneous Dirichlet data, coefficients from the same
+// callbacks as the basis batch (sampled at fine-cell centres).
+class QStd {
+ public:
+  QStd() = delete;
+  QStd(const ParametersStd &parameters, Q1Coefficients coeff);
+  QStd(const QStd &) = delete;
+  QStd &operator=(const QStd &) = delete;
+
+  void run();  // one GPU solve; throws BasisError
+  // Nodal values, node = i + (n+1)(j + (n+1)k), n = 2^n_refine (after run()).
+  const std::vector<double> &solution() const { return u_; }
+  // u_h(x) by trilinear interpolation (x clamped to the unit cube).
+  double solution_value(const Point &x) const;
+  const msfec_cell_report &report() const { return report_; }
+
+ private:
+  ParametersStd parameters_;
+  Q1Coefficients coeff_;
+  BasisBatch gpu_;
+  std::vector<double> u_;
+  msfec_cell_report report_{};
+};
+
 }  // namespace Q
 
 namespace NedRT {
@@ -214,6 +254,33 @@ class NedRTBatch : public std::enable_shared_from_this<NedRTBatch> {
   std::vector<size_t> basis_off_;
   std::vector<msfec_cell_report> reports_;
   bool built_ = false;
+};
+
+// Standard fine-scale Ned_RT solve on the unit cube: the reference's NedRTStd
+// (include/Ned_RT/ned_rt_ref.h:99-120, source/Ned_RT/ned_rt_ref.cc:110-330)
+// through msfec_nedrt_fine_solve, natural boundary conditions as there.
+class NedRTStd {
+ public:
+  NedRTStd() = delete;
+  NedRTStd(const ParametersStd &parameters, NedRTCoefficients coeff);
+  NedRTStd(const NedRTStd &) = delete;
+  NedRTStd &operator=(const NedRTStd &) = delete;
+
+  void run();  // one GPU solve; throws BasisError
+  // sigma on the fine edges (x-, then y-, then z-edges) and u on the fine faces
+  // (x-, y-, z-faces), lattice order of msfec_nedrt_fine_solve (after run()).
+  const std::vector<double> &sigma() const { return sigma_; }
+  const std::vector<double> &u() const { return u_; }
+  // The lowest-order RT field u_h(x) (x clamped to the unit cube).
+  Point u_value(const Point &x) const;
+  const msfec_cell_report &report() const { return report_; }
+
+ private:
+  ParametersStd parameters_;
+  NedRTCoefficients coeff_;
+  BasisBatch gpu_;
+  std::vector<double> sigma_, u_;
+  msfec_cell_report report_{};
 };
 
 }  // namespace NedRT

@@ -21,6 +21,7 @@ HOSTLIB = os.path.join(LIBDIR, "libmsfec_host.so")
 EXAMPLE = os.path.join(LIBDIR, "example_q1")
 EXAMPLE_NR = os.path.join(LIBDIR, "example_nedrt")
 EXAMPLE_PAIR = os.path.join(LIBDIR, "example_pairings")
+EXAMPLE_STD = os.path.join(LIBDIR, "example_std")
 HOST = os.path.join(HERE, "host")
 CXX = os.environ.get("CXX", "g++")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
@@ -75,8 +76,8 @@ def build(verbose: bool = False) -> str:
 
 
 def build_host(objs=()):
-    """QBasis/NedRTBasis/QNedBasis/RTDQBasis shim + coarse solvers (g++, links the CUDA library) and the
-    example drivers."""
+    """QBasis/NedRTBasis/QNedBasis/RTDQBasis/QStd/NedRTStd shim + coarse solvers (g++, links the CUDA
+    library) and the example drivers."""
     srcs = [os.path.join(HOST, f) for f in ("msfec_basis.cpp", "coarse_q1.cpp", "coarse_nedrt.cpp", "coarse_pairings.cpp")]
     deps = srcs + [os.path.join(HOST, "msfec_basis.hpp"), LIB] + glob.glob(os.path.join(INCLUDE, "*.h"))
     if not os.path.exists(HOSTLIB) or any(os.path.getmtime(d) > os.path.getmtime(HOSTLIB) for d in deps):
@@ -86,7 +87,7 @@ def build_host(objs=()):
         if r.returncode != 0:
             raise RuntimeError("host shim build failed:\n" + r.stderr)
     for src_name, out in (("example_q1.cpp", EXAMPLE), ("example_nedrt.cpp", EXAMPLE_NR),
-                          ("example_pairings.cpp", EXAMPLE_PAIR)):
+                          ("example_pairings.cpp", EXAMPLE_PAIR), ("example_std.cpp", EXAMPLE_STD)):
         ex = os.path.join(HOST, src_name)
         if not os.path.exists(out) or os.path.getmtime(ex) > os.path.getmtime(out) or \
                 os.path.getmtime(HOSTLIB) > os.path.getmtime(out):

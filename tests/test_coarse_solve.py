@@ -73,6 +73,8 @@ def test_shim_library_and_example_build():
     import msfec_build
     msfec_build.build()
     assert os.path.exists(msfec_build.HOSTLIB) and os.path.exists(msfec_build.EXAMPLE)
+    for ex in (msfec_build.EXAMPLE_NR, msfec_build.EXAMPLE_PAIR, msfec_build.EXAMPLE_STD):
+        assert os.path.exists(ex), ex
     L = ctypes.CDLL(msfec_build.HOSTLIB)
     assert hasattr(L, "msfec_host_q1_coarse_solve") and hasattr(L, "msfec_host_nedrt_coarse_solve")
 
