@@ -1050,18 +1050,39 @@ bool nr_load_ok(const msfec_load *l) {
   return !l || l->kind == MSFEC_LOAD_ZERO || l->kind == MSFEC_LOAD_VEC_TRIG;
 }
 
-// A^-1 SPD (leading principal minors) and finite, B positive and finite, per fine cell.
-msfec_status nr_coef_check(msfec_handle *h, const double *ainv6, const double *bdiv, int64_t nfine) {
+// Symmetric 3x3 tensor (a00 a11 a22 a01 a02 a12) finite and SPD (leading principal minors).
+bool sym6_spd(const double *a) {
+  for (int q = 0; q < 6; ++q)
+    if (!std::isfinite(a[q])) return false;
+  const double m1 = a[0], m2 = a[0] * a[1] - a[3] * a[3];
+  const double m3 = a[0] * (a[1] * a[2] - a[5] * a[5]) - a[3] * (a[3] * a[2] - a[5] * a[4]) +
+                    a[4] * (a[3] * a[5] - a[1] * a[4]);
+  return m1 > 0.0 && m2 > 0.0 && m3 > 0.0;
+}
+
+// Per fine cell: the tensor SPD and finite, the scalar (if any) positive and finite.
+msfec_status tensor_coef_check(msfec_handle *h, const double *six, const double *scalar, int64_t nfine,
+                               const char *what) {
   for (int64_t e = 0; e < nfine; ++e) {
-    const double *a = ainv6 + 6 * e;
-    const double m1 = a[0], m2 = a[0] * a[1] - a[3] * a[3];
-    const double m3 = a[0] * (a[1] * a[2] - a[5] * a[5]) - a[3] * (a[3] * a[2] - a[5] * a[4]) +
-                      a[4] * (a[3] * a[5] - a[1] * a[4]);
-    bool ok = m1 > 0.0 && m2 > 0.0 && m3 > 0.0 && bdiv[e] > 0.0 && std::isfinite(bdiv[e]);
-    for (int q = 0; q < 6; ++q) ok = ok && std::isfinite(a[q]);
-    if (!ok) return fail(h, MSFEC_ERROR_NUMERICAL, "A^-1 not SPD / finite or B not positive at fine cell " + std::to_string(e));
+    const bool ok = sym6_spd(six + 6 * e) && (!scalar || (scalar[e] > 0.0 && std::isfinite(scalar[e])));
+    if (!ok) return fail(h, MSFEC_ERROR_NUMERICAL, std::string(what) + " at fine cell " + std::to_string(e));
   }
   return MSFEC_SUCCESS;
+}
+
+// Q1 coefficients per fine cell: a positive and finite, the reaction (if any) non-negative and finite.
+msfec_status q1_coef_check(msfec_handle *h, const double *a, const double *reaction, int64_t nfine) {
+  for (int64_t e = 0; e < nfine; ++e) {
+    if (!(a[e] > 0.0) || !std::isfinite(a[e])) return fail(h, MSFEC_ERROR_NUMERICAL, "coefficient a not positive/finite");
+    if (reaction && (!(reaction[e] >= 0.0) || !std::isfinite(reaction[e])))
+      return fail(h, MSFEC_ERROR_NUMERICAL, "reaction coefficient negative or non-finite");
+  }
+  return MSFEC_SUCCESS;
+}
+
+// Ned_RT coefficients: A^-1 SPD and finite, B positive and finite.
+msfec_status nr_coef_check(msfec_handle *h, const double *ainv6, const double *bdiv, int64_t nfine) {
+  return tensor_coef_check(h, ainv6, bdiv, nfine, "A^-1 not SPD / finite or B not positive");
 }
 
 }  // namespace
@@ -1250,10 +1271,9 @@ msfec_status msfec_q1_build(msfec_handle *h, int32_t ncells, const msfec_cell *c
     nfine += n * n * n;
   }
   if (!load_ok(load)) return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "invalid load");
-  for (int64_t e = 0; e < nfine; ++e) {
-    if (!(a[e] > 0.0) || !std::isfinite(a[e])) return fail(h, MSFEC_ERROR_NUMERICAL, "coefficient a not positive/finite");
-    if (reaction && (!(reaction[e] >= 0.0) || !std::isfinite(reaction[e])))
-      return fail(h, MSFEC_ERROR_NUMERICAL, "reaction coefficient negative or non-finite");
+  {
+    const msfec_status cs = q1_coef_check(h, a, reaction, nfine);
+    if (cs != MSFEC_SUCCESS) return cs;
   }
   if (ncells == 0) return msfec_q1_build_device(h, 0, cells, nullptr, nullptr, load, nullptr, nullptr, nullptr);
   DeviceGuard g(h->device);
@@ -1381,6 +1401,10 @@ msfec_status msfec_q1_backward(msfec_handle *h, int32_t ncells, const msfec_cell
     if (cell_of[p] < 0 || cell_of[p] >= ncells) return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "cell_of out of range");
   if (!load_ok(load) || (load && load->kind == MSFEC_LOAD_VEC_TRIG))
     return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "invalid Q1 load");
+  {
+    const msfec_status cs = q1_coef_check(h, a, reaction, nfine);
+    if (cs != MSFEC_SUCCESS) return cs;
+  }
   DeviceGuard g(h->device);
   cudaStream_t st = h->stream;
   MSFEC_CUDA_TRY(h, h->a.reserve(nfine));
@@ -1437,10 +1461,9 @@ msfec_status msfec_q1_fine_solve(msfec_handle *h, const msfec_cell *domain, cons
     return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "invalid Q1 load");
   const int n = 1 << domain->depth;
   const int64_t nfine = (int64_t)n * n * n, nodes = (int64_t)(n + 1) * (n + 1) * (n + 1);
-  for (int64_t e = 0; e < nfine; ++e) {
-    if (!(a[e] > 0.0) || !std::isfinite(a[e])) return fail(h, MSFEC_ERROR_NUMERICAL, "coefficient a not positive/finite");
-    if (reaction && (!(reaction[e] >= 0.0) || !std::isfinite(reaction[e])))
-      return fail(h, MSFEC_ERROR_NUMERICAL, "reaction coefficient negative or non-finite");
+  {
+    const msfec_status cs = q1_coef_check(h, a, reaction, nfine);
+    if (cs != MSFEC_SUCCESS) return cs;
   }
   const bool fp64 = h->cfg.precision == MSFEC_PRECISION_FP64;
   const bool has_r = reaction != nullptr;
@@ -1817,6 +1840,10 @@ msfec_status msfec_nedrt_backward(msfec_handle *h, int32_t ncells, const msfec_c
         return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "non-finite point or dJ/du");
   }
   if (!load_ok(load) || !nr_load_ok(load)) return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "invalid Ned_RT load");
+  {
+    const msfec_status cs = nr_coef_check(h, ainv6, bdiv, nfine);
+    if (cs != MSFEC_SUCCESS) return cs;
+  }
   const bool fp64 = h->cfg.precision == MSFEC_PRECISION_FP64;
   DeviceGuard g(h->device);
   cudaStream_t st = h->stream;
@@ -1990,14 +2017,9 @@ msfec_status msfec_qned_build(msfec_handle *h, int32_t ncells, const msfec_cell 
     nfine += n * n * n;
   }
   if (!load_ok(load) || !nr_load_ok(load)) return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "invalid Q_Ned load");
-  for (int64_t e = 0; e < nfine; ++e) {
-    const double *a = a6 + 6 * e;
-    const double m1 = a[0], m2 = a[0] * a[1] - a[3] * a[3];
-    const double m3 = a[0] * (a[1] * a[2] - a[5] * a[5]) - a[3] * (a[3] * a[2] - a[5] * a[4]) +
-                      a[4] * (a[3] * a[5] - a[1] * a[4]);
-    bool ok = m1 > 0.0 && m2 > 0.0 && m3 > 0.0 && binv[e] > 0.0 && std::isfinite(binv[e]);
-    for (int q = 0; q < 6; ++q) ok = ok && std::isfinite(a[q]);
-    if (!ok) return fail(h, MSFEC_ERROR_NUMERICAL, "A not SPD / finite or B^-1 not positive at fine cell " + std::to_string(e));
+  {
+    const msfec_status cs = tensor_coef_check(h, a6, binv, nfine, "A not SPD / finite or B^-1 not positive");
+    if (cs != MSFEC_SUCCESS) return cs;
   }
   if (ncells == 0) return msfec_qned_build_device(h, 0, cells, nullptr, nullptr, load, nullptr, nullptr, nullptr);
   DeviceGuard g(h->device);
@@ -2057,14 +2079,9 @@ msfec_status msfec_rtdq_build(msfec_handle *h, int32_t ncells, const msfec_cell 
     nfine += n * n * n;
   }
   if (!load_ok(load) || !scalar_load_ok(load)) return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "invalid RT_DQ load");
-  for (int64_t e = 0; e < nfine; ++e) {
-    const double *a = ainv6 + 6 * e;
-    const double m1 = a[0], m2 = a[0] * a[1] - a[3] * a[3];
-    const double m3 = a[0] * (a[1] * a[2] - a[5] * a[5]) - a[3] * (a[3] * a[2] - a[5] * a[4]) +
-                      a[4] * (a[3] * a[5] - a[1] * a[4]);
-    bool ok = m1 > 0.0 && m2 > 0.0 && m3 > 0.0;
-    for (int q = 0; q < 6; ++q) ok = ok && std::isfinite(a[q]);
-    if (!ok) return fail(h, MSFEC_ERROR_NUMERICAL, "A^-1 not SPD / finite at fine cell " + std::to_string(e));
+  {
+    const msfec_status cs = tensor_coef_check(h, ainv6, nullptr, nfine, "A^-1 not SPD / finite");
+    if (cs != MSFEC_SUCCESS) return cs;
   }
   if (ncells == 0) return msfec_rtdq_build_device(h, 0, cells, nullptr, load, nullptr, nullptr, nullptr);
   DeviceGuard g(h->device);
