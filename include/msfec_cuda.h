@@ -175,8 +175,9 @@ msfec_status msfec_q1_build_device(msfec_handle *handle, int32_t ncells,
  * basis of the last msfec_q1_build on this handle is reused when the batch is
  * the same (same cells; the caller guarantees the same a); otherwise it is
  * recomputed first (the reference keeps no basis either: basis objects are
- * rebuilt per run, q_global.cc:38-87). No counterpart in the reference, which
- * has no adjoint; it extends QBasis with the gradient of its outputs.
+ * rebuilt per run, q_global.cc:38-87). Coefficients are checked as in
+ * msfec_q1_build (MSFEC_ERROR_NUMERICAL). No counterpart in the reference,
+ * which has no adjoint; it extends QBasis with the gradient of its outputs.
  */
 msfec_status msfec_q1_backward(msfec_handle *handle, int32_t ncells,
                                const msfec_cell *cells, const double *a,
@@ -389,9 +390,11 @@ msfec_status msfec_autotune(msfec_handle *handle, int32_t kind, int32_t ncells,
  * relative to max(||f||, 1e-3 of the cell's adjoint source scale) (the
  * right-hand sides are projections and differences that can cancel to
  * rounding); the basis is rebuilt unless reuse_basis != 0 and the
- * last Ned_RT build on this handle is the same batch. For the divergence-free
- * MSFEC_LOAD_VEC_TRIG load the coarse solution has no edge part and grad_a
- * vanishes to rounding; B carries the sensitivity.
+ * last Ned_RT build on this handle is the same batch. Coefficients are
+ * checked as in msfec_nedrt_build (MSFEC_ERROR_NUMERICAL). grad_a vanishes to
+ * rounding when the coarse solution has no edge part (e.g. the divergence-free
+ * MSFEC_LOAD_VEC_TRIG load on a coarse 2^3 grid with the boundary edges and
+ * faces fixed); B then carries the sensitivity.
  */
 msfec_status msfec_nedrt_backward(msfec_handle *handle, int32_t ncells,
                                   const msfec_cell *cells, const double *ainv6,
