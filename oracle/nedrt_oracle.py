@@ -334,6 +334,38 @@ def standard_solve(origin, size, depth, ainv, bdiv, load_kind=LOAD_VEC_ZERO, loa
     return spla.spsolve(A.tocsc(), rhs)
 
 
+def vec_trig_exact_dofs(n, p0, p1, a):
+    """Exact DoFs on the n^3 lattice of the unit cube of the analytic solution of
+    the standard Ned_RT problem (standard_solve) with A = a I (any B) and the
+    vector trig load f = p0 (sin wy sin wz, sin wz sin wx, sin wx sin wy),
+    w = p1 pi, p1 integer: f is divergence-free and curl curl f = 2 w^2 f, so
+    u = f / (2 a w^2), sigma = a curl u = p0 curl f / (2 w^2) solve
+    A^-1 sigma - curl u = 0, curl sigma - grad(B div u) = f, and u x n = 0,
+    div u = 0 on the boundary (the natural conditions). Edge DoFs: line
+    integrals of sigma along +axis; face DoFs: fluxes of u along +axis."""
+    w = p1 * np.pi
+    h = 1.0 / n
+    NE, NF = counts(n)
+    x = np.zeros(NE + NF)
+
+    def cdiff(s0, s1):  # integral of sin(w s) over [s0, s1]
+        return (np.cos(w * s0) - np.cos(w * s1)) / w
+
+    off = 0
+    for d, i, j, k in edge_geometry(n):
+        pos = [i * h, j * h, k * h]
+        # (curl f)_d = w sin(w x_d) (cos(w x_{d+1}) - cos(w x_{d+2})), cyclic
+        x[off:off + len(i)] = (p0 / (2 * w * w) * w * cdiff(pos[d], pos[d] + h) *
+                               (np.cos(w * pos[(d + 1) % 3]) - np.cos(w * pos[(d + 2) % 3])))
+        off += len(i)
+    for d, i, j, k in face_geometry(n):
+        pos = [i * h, j * h, k * h]
+        o1, o2 = [(1, 2), (0, 2), (0, 1)][d]
+        x[off:off + len(i)] = p0 / (2 * a * w * w) * cdiff(pos[o1], pos[o1] + h) * cdiff(pos[o2], pos[o2] + h)
+        off += len(i)
+    return x
+
+
 def build(cells, ainv, bdiv, load_kind=LOAD_VEC_ZERO, load_params=(0, 0, 0, 0), want_phi=True,
           basis="solve"):
     """Batch over coarse cells; ainv [sum n^3, 3, 3], bdiv [sum n^3]."""

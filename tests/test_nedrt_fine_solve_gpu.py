@@ -62,3 +62,21 @@ def test_nedrt_fine_solve_zero_load_and_invalid(gpu):
     neg[3] = -1.0
     with pytest.raises(gpu.MsfecError):
         h.nedrt_fine_solve(cells, ainv6, neg, gpu.make_load())
+
+
+def test_nedrt_fine_solve_analytic_solution(gpu):
+    """Known answer (oracle's vec_trig_exact_dofs): A^-1 = 0.7 I, B = 1.3, the
+    vector trig load with w = pi; at depth 4 the oracle's discretisation error
+    is 6.9e-7 (edge DoFs) and 3.2e-3 (face DoFs) relative, and the GPU solve
+    must show the same."""
+    depth, n = 4, 16
+    cells = workloads.coarse_grid(1, depth)
+    ainv6 = np.tile([0.7, 0.7, 0.7, 0.0, 0.0, 0.0], (n ** 3, 1))
+    load = gpu.make_load(gpu.LOAD_VEC_TRIG, (1.0, 1.0, 0.0, 0.0))
+    x, rep, st = gpu.Handle().nedrt_fine_solve(cells, ainv6, np.full(n ** 3, 1.3), load)
+    assert st == gpu.SUCCESS
+    xe = NR.vec_trig_exact_dofs(n, 1.0, 1.0, 1.0 / 0.7)
+    NE, _ = NR.counts(n)
+    es = np.linalg.norm(x[:NE] - xe[:NE]) / np.linalg.norm(xe[:NE])
+    eu = np.linalg.norm(x[NE:] - xe[NE:]) / np.linalg.norm(xe[NE:])
+    assert es < 2e-6 and eu < 5e-3, (es, eu)
