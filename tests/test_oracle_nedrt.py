@@ -289,3 +289,34 @@ def test_standard_solve_converges_to_analytic_solution():
     assert err[-1][0] < 1e-6 and err[-1][1] < 5e-3
     for (s0, u0), (s1, u1) in zip(err, err[1:]):
         assert s0 / s1 > 12.0 and u0 / u1 > 3.5, err
+
+
+def test_multiscale_solution_converges_to_analytic_solution():
+    """The whole multiscale Ned_RT pipeline of the oracle (local basis solves,
+    block Galerkin, coarse solve with the reference's natural conditions,
+    set_global_weights reconstruction) against the analytic solution of the
+    constant-coefficient problem (N.vec_trig_exact_dofs): the error falls at
+    first order in the coarse mesh size H (measured: sigma 45.7 % -> 22.3 %,
+    u 58.9 % -> 30.8 % from coarse 2^3 to 4^3 at depth 2)."""
+    from oracle import nedrt_adjoint as NA
+    from test_coarse_solve import scipy_nedrt_coarse
+    a, B, depth = 1.0 / 0.7, 1.3, 2
+    n = 1 << depth
+    err = []
+    for m in (2, 4):
+        cells = workloads.coarse_grid(m, depth)
+        nfc = len(cells) * n ** 3
+        ref = N.build(cells, np.tile(np.eye(3) / a, (nfc, 1, 1)), np.full(nfc, B), N.LOAD_VEC_TRIG,
+                      [1.0, 1.0, 0.0, 0.0])
+        U = scipy_nedrt_coarse(m, ref["KH"], ref["FH"])
+        g, _ = NA.coarse_maps(m)
+        NE, _ = N.counts(n)
+        Phi = np.array(ref["Phi"])
+        x = _global_fine_field(m, n, lambda c: (U[g[c, :12]] @ Phi[c, :12, :NE], U[g[c, 12:]] @ Phi[c, 12:, NE:]))
+        xe = N.vec_trig_exact_dofs(m * n, 1.0, 1.0, a)
+        GE, _ = N.counts(m * n)
+        err.append((np.linalg.norm(x[:GE] - xe[:GE]) / np.linalg.norm(xe[:GE]),
+                    np.linalg.norm(x[GE:] - xe[GE:]) / np.linalg.norm(xe[GE:])))
+    (s2, u2), (s4, u4) = err
+    assert max(s2, u2) < 0.65 and max(s4, u4) < 0.35, err
+    assert s2 / s4 > 1.7 and u2 / u4 > 1.7, err
