@@ -67,3 +67,20 @@ def test_multiscale_vs_fine_error(gpu):
     err = np.linalg.norm(ums - u) / np.linalg.norm(u)
     print(f"multiscale (coarse 4^3 x depth 3) vs fine 32^3: relative nodal L2 error {err:.3e}")
     assert err < 0.5
+
+
+def test_fine_solve_analytic_solution(gpu):
+    """Known answer: constant a = 0.8, no reaction, load sin(pi x) sin(pi y)
+    sin(pi z) on the unit cube have the exact solution u = f / (3 a pi^2); on
+    the 32^3 grid the discretisation error of the nodal values is O(h^2)
+    (the oracle's: 0.16 %), so the GPU solution must be within 0.5 %."""
+    depth, n = 5, 32
+    dom = workloads.coarse_grid(1, depth)
+    h = gpu.Handle()
+    u, rep, st = h.q1_fine_solve(dom, np.full(n ** 3, 0.8), None, gpu.make_load(gpu.LOAD_SIN_PRODUCT, (1.0, 1.0, 0.0, 0.0)))
+    assert st == gpu.SUCCESS
+    N1 = n + 1
+    idx = np.arange(N1 ** 3)
+    i, j, k = idx % N1, (idx // N1) % N1, idx // (N1 * N1)
+    ue = np.sin(np.pi * i / n) * np.sin(np.pi * j / n) * np.sin(np.pi * k / n) / (3 * 0.8 * np.pi ** 2)
+    assert np.abs(u - ue).max() <= 5e-3 * np.abs(ue).max(), np.abs(u - ue).max() / np.abs(ue).max()

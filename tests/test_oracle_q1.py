@@ -147,3 +147,30 @@ def test_committed_q1_fixtures_reproduce(oracle_lib):
 def test_invalid_depth_rejected(oracle_lib):
     res = oracle_lib.q1_build([0, 0, 0], [1, 1, 1], [0], np.ones(1))
     assert res["status"] != 0
+
+
+def test_fine_problem_converges_to_analytic_solution(oracle_lib):
+    """Known answer for the standard fine-scale Q1 problem (the system the fine
+    solve and the local problems discretise): constant a and r with the
+    sin-product load f = sin(pi x) sin(pi y) sin(pi z) have the exact solution
+    u = f / (3 a pi^2 + r), which vanishes on the boundary (homogeneous
+    Dirichlet data). The nodal error falls at O(h^2) (measured: 11.3 %, 2.7 %,
+    0.67 % at depths 2-4)."""
+    a0, r0 = 0.8, 2.0
+    err = []
+    for depth in (2, 3, 4):
+        n = 1 << depth
+        nf = n ** 3
+        K, b = oracle_lib.q1_assemble(np.zeros(3), np.ones(3), depth, np.full(nf, a0), np.full(nf, r0),
+                                      oracle_lib.LOAD_SIN_PRODUCT, [1.0, 1.0, 0.0, 0.0])
+        K = K.tocsr()
+        N1 = n + 1
+        idx = np.arange(N1 ** 3)
+        i, j, k = idx % N1, (idx // N1) % N1, idx // (N1 * N1)
+        I = np.where((i > 0) & (j > 0) & (k > 0) & (i < n) & (j < n) & (k < n))[0]
+        u = np.zeros(N1 ** 3)
+        u[I] = spla.spsolve(K[I][:, I].tocsc(), b[I])
+        ue = np.sin(np.pi * i / n) * np.sin(np.pi * j / n) * np.sin(np.pi * k / n) / (3 * a0 * np.pi ** 2 + r0)
+        err.append(np.abs(u - ue).max() / np.abs(ue).max())
+    assert err[-1] < 2e-2, err
+    assert err[0] / err[1] > 3.5 and err[1] / err[2] > 3.5, err
