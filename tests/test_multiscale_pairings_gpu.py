@@ -10,7 +10,7 @@ import workloads
 from oracle import nedrt_oracle as NR
 from oracle import qned_oracle as Q
 from oracle import rtdq_oracle as RQ
-from test_coarse_pairings import host_solve, qned_maps, rtdq_maps
+from test_coarse_pairings import host_solve, qned_exact_edges, qned_maps, rtdq_exact, rtdq_maps
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-9
@@ -77,3 +77,41 @@ def test_global_rtdq_solution_matches_oracle(gpu, precision):
     u_r = Ur[g[:, 6]][:, None] * phi_r[:, 0, NF:]
     assert _rel(sig, sig_r) <= TOL
     assert _rel(u, u_r) <= TOL
+
+
+def test_rtdq_multiscale_analytic_solution(gpu):
+    """Known answer (test_coarse_pairings.rtdq_exact): constant A = 0.8 I and the
+    sin-product load; the GPU-built coarse 4^3 x depth 2 solution must show the
+    oracle's accuracy (cell values 5.0 % from the exact cell means, face fluxes
+    1.0e-6 from the exact fluxes)."""
+    m, depth, a = 4, 2, 0.8
+    cells = workloads.coarse_grid(m, depth)
+    nfc = len(cells) * (1 << depth) ** 3
+    ainv6 = np.tile([1 / a, 1 / a, 1 / a, 0.0, 0.0, 0.0], (nfc, 1))
+    KH, FH, rep, st = gpu.Handle().rtdq_build(cells, ainv6, gpu.make_load(gpu.LOAD_SIN_PRODUCT, (1.0, 1.0, 0.0, 0.0)))
+    assert st == gpu.SUCCESS and rep["converged"].all()
+    g, fixed = rtdq_maps(m)
+    U = host_solve("msfec_host_rtdq_coarse_solve", fixed.size, KH, FH, m)
+    fl, um = rtdq_exact(m, a)
+    NF = fl.size
+    assert _rel(U[NF:], um) < 0.06 and _rel(U[:NF], fl) < 1e-5, (_rel(U[NF:], um), _rel(U[:NF], fl))
+
+
+def test_qned_multiscale_analytic_solution(gpu):
+    """Known answer (test_coarse_pairings.qned_exact_edges): A = 0.8 I, B^-1 = 1.7
+    and the vector trig load; the GPU-built coarse 4^3 x depth 2 solution must
+    show the oracle's accuracy (edge DoFs 5.2 % from the exact line integrals,
+    vertex DoFs zero as sigma = 0)."""
+    m, depth, a = 4, 2, 0.8
+    cells = workloads.coarse_grid(m, depth)
+    nfc = len(cells) * (1 << depth) ** 3
+    a6 = np.tile([a, a, a, 0.0, 0.0, 0.0], (nfc, 1))
+    KH, FH, rep, st = gpu.Handle().qned_build(cells, a6, np.full(nfc, 1.7),
+                                             gpu.make_load(gpu.LOAD_VEC_TRIG, (1.0, 1.0, 0.0, 0.0)))
+    assert st == gpu.SUCCESS and rep["converged"].all()
+    g, fixed = qned_maps(m)
+    U = host_solve("msfec_host_qned_coarse_solve", fixed.size, KH, FH, m)
+    ue = qned_exact_edges(m, a)
+    NV = (m + 1) ** 3
+    assert np.abs(U[:NV]).max() <= 1e-8 * np.abs(ue).max()
+    assert _rel(U[NV:], ue) < 0.06, _rel(U[NV:], ue)
