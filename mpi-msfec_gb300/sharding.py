@@ -70,6 +70,19 @@ def max_over_ranks(x, dist=None, group=None):
     return float(t.item())
 
 
+def weak_scaling_value(work_local, seconds_local, dist=None, group=None):
+    """Whole-job throughput of a weak-scaling step in which every rank builds
+    its own batch of independent cells: the work of all ranks divided by the
+    slowest rank's time (no data-path collective; only these two scalars are
+    reduced)."""
+    if dist is None:
+        return float(work_local) / float(seconds_local)
+    import torch
+    w = torch.tensor([float(work_local)], dtype=torch.float64)
+    dist.all_reduce(w, op=dist.ReduceOp.SUM, group=group)
+    return float(w.item()) / max_over_ranks(seconds_local, dist, group)
+
+
 def build_sharded(build, cells, fine_arrays, kind, world, rank, dist=None, group=None):
     """Build this rank's share of `cells` with `build(cells_slice, arrays_slice)
     -> (KH, FH)` and return the full (KH, FH) of the batch on every rank.

@@ -3,8 +3,9 @@
 Each rank builds its work-balanced cell range with the FP64 oracle (the GPU
 library is not needed to test the rank logic), the Galerkin blocks are
 all-gathered, and every rank must hold exactly the single-process result.
-Also checks the partition (coverage, order, balance) and the max-over-ranks
-timing reduction.
+Also checks the partition (coverage, order, balance), the max-over-ranks
+timing reduction and the weak-scaling throughput of the benchmark's
+multi-GPU mode (every rank builds a whole batch).
 """
 import os
 import socket
@@ -62,7 +63,11 @@ def _rank_main(rank, world, port, out_dir):
         cells, a, _, _ = workloads.q1_lognormal(m=2, depth=2, seed=11, reaction=False)
         KH, FH = sharding.build_sharded(_oracle_build, cells, [a], "q1", world, rank, dist)
         t = sharding.max_over_ranks(1.0 + rank, dist)
-        np.savez(os.path.join(out_dir, f"rank{rank}.npz"), KH=KH, FH=FH, t=t)
+        # weak scaling (the benchmark's multi-GPU mode): every rank builds the whole batch
+        KHw, FHw = _oracle_build(cells, [a])
+        work = float(workloads.work_dof_rhs(cells))
+        v = sharding.weak_scaling_value(work, 1.0 + rank, dist)
+        np.savez(os.path.join(out_dir, f"rank{rank}.npz"), KH=KH, FH=FH, t=t, KHw=KHw, v=v, work=work)
     finally:
         dist.destroy_process_group()
 
@@ -78,3 +83,5 @@ def test_gloo_two_ranks_match_single_process(oracle_lib):
             g = np.load(os.path.join(d, f"rank{r}.npz"))
             assert np.array_equal(g["KH"], KH_ref) and np.array_equal(g["FH"], FH_ref)
             assert float(g["t"]) == 2.0
+            assert np.array_equal(g["KHw"], KH_ref)
+            assert float(g["v"]) == world * float(g["work"]) / 2.0  # all ranks' work / slowest rank
