@@ -1,14 +1,17 @@
-"""Faithful-iterative mode of the Ned_RT oracle (TEST INFRASTRUCTURE ONLY: the
-checker of the CUDA path in tests/; the product library never imports it).
+"""Faithful-iterative mode of the Ned_RT and Q_Ned oracles (TEST
+INFRASTRUCTURE ONLY: the checker of the CUDA path in tests/; the product
+library never imports it).
 
-Restates the reference's default local solver for the Ned_RT basis problems,
+Restates the reference's default local solver of both mixed pairings,
 NedRTBasis::solve_iterative (konsim83/MPI-MSFEC,
-source/Ned_RT/ned_rt_basis.cc:637-830), on the interior DoFs of one coarse
-cell (the constrained boundary DoFs carry the coarse data, as
+source/Ned_RT/ned_rt_basis.cc:637-830) and QNedBasis::solve_iterative
+(source/Q_Ned/q_ned_basis.cc:628-790, the same scheme), on the interior DoFs
+of one coarse cell (the constrained boundary DoFs carry the coarse data, as
 distribute_local_to_global and distribute leave them):
-  - blocks: M = block(0,0) (A^-1 edge mass), B01 = block(0,1) = -C,
-    B10 = block(1,0) = C^T, B11 = block(1,1) = D (the unconstrained assembly
-    of nedrt_oracle.assemble restricted to interior rows and columns);
+  - blocks of the interior system: M = block(0,0) (first field: Ned_RT sigma
+    edges / Q_Ned sigma vertices), B01 = block(0,1), B10 = block(1,0),
+    B11 = block(1,1) (the unconstrained assembly of the oracle restricted to
+    interior rows and columns);
   - M^-1 (InverseMatrix, include/linear_algebra/inverse_matrix.tpp:21-40):
     GMRES to 1e-6 * |src| preconditioned by ILU(0) of M
     (LocalInnerPreconditioner<3> = SparseILU, preconditioner.h:62-67);
@@ -18,18 +21,18 @@ distribute_local_to_global and distribute leave them):
   - its preconditioner (:756-779): at most 14 CG steps (1e-6 relative) on the
     approximate Schur complement B10 ILU(M)^-1 B01 - B11
     (approximate_schur_complement.tpp:32-41, approximate_inverse.tpp:23-40);
-  - sigma = M^-1 (f - B01 u) (:807-813).
+  - first field = M^-1 (f - B01 u) (:807-813).
 The iterates follow the same algorithm and tolerances; they are not bit for
 bit deal.II's (its GMRES and ILU implementations are not restated line by
 line). The point of this mode: the reference's own basis functions are
 accurate to about the 1e-6 tolerances above, and the direct oracle (and the
-GPU path, at 1e-14 relative residual) is the limit they approach.
+GPU path, at 1e-14 relative residual) is the limit they approach. Use it as
+the interior_solver of nedrt_oracle.build_cell / qned_oracle.build_cell.
 """
 import numpy as np
 import scipy.sparse as sp
 import scipy.sparse.linalg as spla
 
-from . import nedrt_oracle as N
 
 
 def ilu0(A):
@@ -96,8 +99,9 @@ def _cg(apply_A, b, apply_P, rtol, maxiter):
 
 
 def faithful_solve(A_II, NEi, rhs):
-    """Solve the interior block system A_II x = rhs (edges first: NEi of them)
-    by the reference's Schur-complement scheme. Returns (x, schur iterations)."""
+    """Solve the interior block system A_II x = rhs (first field first: NEi
+    DoFs) by the reference's Schur-complement scheme. Returns (x, Schur
+    iterations)."""
     M = A_II[:NEi][:, :NEi].tocsr()
     B01 = A_II[:NEi][:, NEi:].tocsr()
     B10 = A_II[NEi:][:, :NEi].tocsr()
@@ -130,31 +134,14 @@ def faithful_solve(A_II, NEi, rhs):
     return np.concatenate([sigma, u]), its
 
 
-def build_cell_faithful(origin, size, depth, ainv, bdiv, bases=range(18)):
-    """Basis functions of one coarse cell by the faithful-iterative scheme.
-    Returns (Phi [len(bases), NE + NF], Schur iterations per basis)."""
-    n = 1 << int(depth)
-    NE, NF = N.counts(n)
-    A = N.assemble(n, size, ainv, bdiv).tocsr()
-    bnd = N.boundary_mask(n)
-    I = np.where(~bnd)[0]
-    B = np.where(bnd)[0]
-    NEi = int(np.sum(I < NE))
-    A_II = A[I][:, I].tocsr()
-    out, its = [], []
-    for b in bases:
-        g = np.zeros(NE + NF)
-        rhs = np.zeros(NE + NF)
-        if b < 12:
-            g[:NE] = N.coarse_edge_dofs(n, b)
-            rhs[NE:] = N.coarse_curl_rhs(n, size, b)
-        else:
-            g[NE:] = N.coarse_face_dofs(n, b - 12)
-        gb = np.zeros(NE + NF)
-        gb[B] = g[B]
-        x, k = faithful_solve(A_II, NEi, rhs[I] - A[I][:, B] @ gb[B])
-        phi = gb.copy()
-        phi[I] = x
-        out.append(phi)
-        its.append(k)
-    return np.array(out), its
+def interior_solver(A_II, n_first, R):
+    """Solve A_II X = R column by column with the reference's scheme (first
+    field: the leading n_first interior DoFs). Returns X; the Schur iteration
+    counts of the last call are kept in interior_solver.iterations."""
+    cols, its = [], []
+    for k in range(R.shape[1]):
+        x, it = faithful_solve(A_II, n_first, np.asarray(R[:, k]).ravel())
+        cols.append(x)
+        its.append(it)
+    interior_solver.iterations = its
+    return np.array(cols).T

@@ -275,13 +275,16 @@ def face_load(n, origin, size, kind, params):
 
 
 def build_cell(origin, size, depth, ainv, bdiv, load_kind=LOAD_VEC_ZERO, load_params=(0, 0, 0, 0),
-               basis="solve"):
+               basis="solve", interior_solver=None):
     """One coarse cell. Returns (Phi [18, NE+NF], KH [18,18], FH [18]).
 
     basis="solve": the multiscale basis (the reference's run loop,
     ned_rt_basis.cc:1338-1381, direct solver). basis="std": the coarse
     functions themselves (the reference's set_to_std sanity path,
-    ned_rt_basis.cc:1312-1335 / set_sigma_to_std :1183-1217)."""
+    ned_rt_basis.cc:1312-1335 / set_sigma_to_std :1183-1217).
+    interior_solver(A_II, n_interior_edges, R) -> X replaces the direct solve
+    of the interior system (faithful_iterative.interior_solver: the
+    reference's iterative scheme)."""
     n = 1 << int(depth)
     NE, NF = counts(n)
     A = assemble(n, size, ainv, bdiv)
@@ -303,8 +306,10 @@ def build_cell(origin, size, depth, ainv, bdiv, load_kind=LOAD_VEC_ZERO, load_pa
         G = Phi.copy()
         G[:, I] = 0.0  # Dirichlet data only
         R = rhs_all[I, :] - A[I][:, B] @ G[:, B].T
-        lu = spla.splu(A[I][:, I].tocsc())
-        X = lu.solve(R)
+        if interior_solver is None:
+            X = spla.splu(A[I][:, I].tocsc()).solve(R)
+        else:
+            X = interior_solver(A[I][:, I].tocsr(), int(np.sum(I < NE)), R)
         Phi = G
         Phi[:, I] = X.T
     # Galerkin with the unconstrained matrix, primary blocks only (:849-948)

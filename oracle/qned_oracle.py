@@ -150,8 +150,12 @@ def edge_load(n, origin, size, kind, params):
     return out
 
 
-def build_cell(origin, size, depth, binv, a3, load_kind=LOAD_VEC_ZERO, load_params=(0, 0, 0, 0)):
-    """One coarse cell. Returns (Phi [20, NV+NE], KH [20,20], FH [20])."""
+def build_cell(origin, size, depth, binv, a3, load_kind=LOAD_VEC_ZERO, load_params=(0, 0, 0, 0),
+               interior_solver=None):
+    """One coarse cell. Returns (Phi [20, NV+NE], KH [20,20], FH [20]).
+    interior_solver(A_II, n_interior_vertices, R) -> X replaces the direct
+    solve of the interior system (faithful_iterative.interior_solver: the
+    reference's iterative scheme, q_ned_basis.cc:628-790)."""
     n = 1 << int(depth)
     NV, NE = counts(n)
     A = assemble(n, size, binv, a3)
@@ -178,7 +182,10 @@ def build_cell(origin, size, depth, binv, a3, load_kind=LOAD_VEC_ZERO, load_para
     Gb = G.copy()
     Gb[:, I] = 0.0
     R = rhs[I, :] - A[I][:, B] @ Gb[:, B].T
-    X = spla.splu(A[I][:, I].tocsc()).solve(R)
+    if interior_solver is None:
+        X = spla.splu(A[I][:, I].tocsc()).solve(R)
+    else:
+        X = interior_solver(A[I][:, I].tocsr(), int(np.sum(I < NV)), R)
     Phi = Gb
     Phi[:, I] = X.T
     P = np.zeros_like(Phi)
