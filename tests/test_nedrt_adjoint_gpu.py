@@ -62,8 +62,15 @@ class NedRTMisfit:
         return 0.5 * float(np.sum(r ** 2)), (U, r, jac, Phi, lu, NE, NF)
 
     def gradient(self, ta, tb):
+        J, state = self.forward(ta, tb)
+        ga, gb = self.backward(ta, tb, state)
+        return J, ga, gb
+
+    def backward(self, ta, tb, state):
+        """dJ/dta, dJ/dtb through msfec_nedrt_backward, reusing the basis of the
+        forward build (the last Ned_RT build on this handle)."""
         m = self.m
-        J, (U, r, jac, Phi, lu, NE, NF) = self.forward(ta, tb)
+        U, r, jac, Phi, lu, NE, NF = state
         e_cell = np.zeros((m ** 3, NF))
         for p in range(len(self.pts)):
             for fi, d, w in jac[p]:
@@ -77,12 +84,34 @@ class NedRTMisfit:
         a6, b = self.coefs(ta, tb)
         ga, gb = self.h.nedrt_backward(self.cells, a6, b, self.load, U[self.g], lam[self.g], self.cell_of, self.pts,
                                        r, reuse_basis=True)
-        return J, ga, gb
+        return ga, gb
 
     def oracle(self, ta, tb):
         ainv = self.N.sym6_to_ainv(self.ainv6)
         return self.NA.misfit(self.cells, self.m, ainv, self.bdiv, ta, tb, self.load.kind, list(self.load.params),
                               self.cell_of, self.pts, self.data)
+
+
+def make_nedrt_autograd(P):
+    """torch.autograd.Function (ta, tb) -> J over the C ABI forward/backward
+    pair (test harness only): forward = msfec_nedrt_build + coarse solve +
+    misfit, backward = msfec_nedrt_backward on the forward's basis."""
+    import torch
+
+    class NedRTMisfitFn(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, ta, tb):
+            ta_np, tb_np = ta.detach().cpu().double().numpy(), tb.detach().cpu().double().numpy()
+            J, state = P.forward(ta_np, tb_np)
+            ctx.args = (ta_np, tb_np, state)
+            return torch.tensor(J, dtype=torch.float64)
+
+        @staticmethod
+        def backward(ctx, gout):
+            ga, gb = P.backward(*ctx.args)
+            return torch.from_numpy(ga) * gout, torch.from_numpy(gb) * gout
+
+    return NedRTMisfitFn.apply
 
 
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
@@ -136,3 +165,21 @@ def test_nedrt_gradient_nonvanishing_A_matches_oracle(gpu):
     assert np.abs(gar).max() > 1e-2 * np.abs(gbr).max()
     assert np.abs(ga - gar).max() <= 1e-8 * np.abs(gar).max(), np.abs(ga - gar).max() / np.abs(gar).max()
     assert np.abs(gb - gbr).max() <= 1e-8 * np.abs(gbr).max(), np.abs(gb - gbr).max() / np.abs(gbr).max()
+
+
+def test_nedrt_autograd_wrapper(gpu):
+    """The autograd wrapper returns the C ABI's J and gradients (two GPU runs:
+    shared-memory atomics vary the last bits, hence 1e-9)."""
+    import torch
+    P = NedRTMisfit(gpu, precision="mixed")
+    rng = np.random.default_rng(11)
+    ta0 = 0.2 * rng.standard_normal(P.bdiv.size)
+    tb0 = 0.2 * rng.standard_normal(P.bdiv.size)
+    ta = torch.tensor(ta0, requires_grad=True)
+    tb = torch.tensor(tb0, requires_grad=True)
+    J = make_nedrt_autograd(P)(ta, tb)
+    J.backward()
+    J2, ga, gb = P.gradient(ta0, tb0)
+    assert abs(float(J.detach()) - J2) <= 1e-9 * abs(J2)
+    assert np.abs(tb.grad.numpy() - gb).max() <= 1e-9 * np.abs(gb).max()
+    assert np.abs(ta.grad.numpy() - ga).max() <= 1e-9 * np.abs(gb).max()
