@@ -4,7 +4,6 @@ QMultiscale / NedRTMultiscale flow), and the C++ QBasis-compatible shim driver
 on the GPU. Tolerance (stated): relative L2 difference <= 1e-9 of the coarse
 solution, and for Ned_RT also of the fine reconstruction sigma_h, u_h."""
 import json
-import os
 import subprocess
 
 import numpy as np

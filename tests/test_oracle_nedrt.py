@@ -3,7 +3,6 @@ the CUDA kernel uses (restated here in Python from the kernel's formulas)."""
 import os
 
 import numpy as np
-import pytest
 
 from oracle import nedrt_oracle as N
 import workloads

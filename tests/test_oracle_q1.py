@@ -7,7 +7,6 @@ the committed seeded fixtures.
 import os
 
 import numpy as np
-import pytest
 import scipy.sparse as sp
 import scipy.sparse.linalg as spla
 

@@ -3,7 +3,6 @@ oracle (C ABI). Stated tolerances (both precisions; mixed = FP32 MINRES +
 FP64 refinement): K_H, F_H max abs error <= 1e-9 * max |entry| of the cell;
 sigma of every basis max|phi - phi_oracle| <= 1e-8 * max|phi_oracle|; the
 stored u block is exactly 1 (the reference's set_u_to_std)."""
-import ctypes
 
 import numpy as np
 import pytest
