@@ -136,3 +136,26 @@ def test_multilevel_mixed_depth_batch(gpu):
     for c in range(len(cells)):
         assert _rel(out[0][0][c], out[1][0][c]) <= TOL_KH, c
         assert _rel(out[0][1][c], out[1][1][c]) <= TOL_KH, c
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("depth", [2, 3])
+def test_constant_diagonal_coefficients_give_the_standard_basis(gpu, precision, depth):
+    """Known answer: constant diagonal A^-1 and constant B on a non-cubic box;
+    the multiscale basis (primary blocks) is the standard coarse Nedelec / RT
+    functions and K_H their Galerkin matrix (the oracle's set_to_std path)."""
+    n = 1 << depth
+    cells = workloads.coarse_grid(1, depth)
+    cells["size"] = [[1.0, 0.8, 1.3]]
+    ainv6 = np.tile([0.5, 1.0, 2.0, 0.0, 0.0, 0.0], (n ** 3, 1))
+    bdiv = np.full(n ** 3, 1.7)
+    h = _handle(gpu, precision)
+    KH, FH, rep, st = h.nedrt_build(cells, ainv6, bdiv, gpu.make_load())
+    assert st == gpu.SUCCESS and rep["converged"].all(), rep
+    S, KHs, _ = N.build_cell(cells["origin"][0], cells["size"][0], depth, N.sym6_to_ainv(ainv6), bdiv, basis="std")
+    assert _rel(KH[0], KHs) <= 1e-10, _rel(KH[0], KHs)
+    NE, NF = N.counts(n)
+    phi = h.nedrt_basis().reshape(18, NE + NF)
+    for b in range(18):
+        blk = slice(0, NE) if b < 12 else slice(NE, NE + NF)
+        assert _rel(phi[b, blk], S[b, blk]) <= TOL_PHI, (b, _rel(phi[b, blk], S[b, blk]))

@@ -319,3 +319,26 @@ def test_multiscale_solution_converges_to_analytic_solution():
     (s2, u2), (s4, u4) = err
     assert max(s2, u2) < 0.65 and max(s4, u4) < 0.35, err
     assert s2 / s4 > 1.7 and u2 / u4 > 1.7, err
+
+
+def test_constant_diagonal_coefficients_give_the_standard_basis():
+    """Known answer (the Ned_RT analogue of Q1's trilinear basis): with a
+    constant diagonal A^-1 and constant B the coarse Nedelec / RT functions
+    solve the local problems, so the multiscale basis (primary blocks) equals
+    the standard functions of the set_to_std path and K_H its Galerkin matrix,
+    on any box. A full constant tensor breaks it (edge bases differ by ~7 %)."""
+    n, size = 4, np.array([1.0, 0.8, 1.3])
+    NE, _ = N.counts(n)
+    for A3, holds in ((np.diag([0.5, 1.0, 2.0]), True),
+                      (np.array([[1.0, 0.3, 0.1], [0.3, 0.8, -0.2], [0.1, -0.2, 1.5]]), False)):
+        ainv = np.tile(A3, (n ** 3, 1, 1))
+        bdiv = np.full(n ** 3, 1.7)
+        P, KH, _ = N.build_cell(np.zeros(3), size, 2, ainv, bdiv, basis="solve")
+        S, KHs, _ = N.build_cell(np.zeros(3), size, 2, ainv, bdiv, basis="std")
+        de = max(np.abs(P[b, :NE] - S[b, :NE]).max() / np.abs(S[b, :NE]).max() for b in range(12))
+        if holds:
+            df = max(np.abs(P[b, NE:] - S[b, NE:]).max() / np.abs(S[b, NE:]).max() for b in range(12, 18))
+            assert de <= 1e-12 and df <= 1e-12
+            assert np.abs(KH - KHs).max() <= 1e-12 * np.abs(KHs).max()
+        else:
+            assert de > 1e-3
