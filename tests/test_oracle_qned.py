@@ -97,3 +97,20 @@ def test_committed_qned_fixture_reproduces():
     res = Q.build(cells, binv, NR.sym6_to_ainv(a6), load.kind, list(load.params), want_phi=False)
     assert np.abs(res["KH"] - g["KH"]).max() <= 1e-9 * np.abs(g["KH"]).max()
     assert np.abs(res["FH"] - g["FH"]).max() <= 1e-9 * np.abs(g["FH"]).max()
+
+
+def test_constant_diagonal_coefficients_give_the_standard_basis():
+    """Known answer: with a constant diagonal A and constant B^-1 the vertex
+    bases' sigma is the trilinear coarse function and the edge bases' u the
+    coarse Nedelec function (any box); a full constant tensor breaks the
+    latter (~5 %)."""
+    n, size = 4, np.array([1.0, 0.8, 1.3])
+    NV, _ = Q.counts(n)
+    for A3, holds in ((np.diag([0.5, 1.0, 2.0]), True),
+                      (np.array([[1.0, 0.3, 0.1], [0.3, 0.8, -0.2], [0.1, -0.2, 1.5]]), False)):
+        Phi, _, _ = Q.build_cell(np.zeros(3), size, 2, np.full(n ** 3, 1.7), np.tile(A3, (n ** 3, 1, 1)))
+        ev = max(np.abs(Phi[v, :NV] - Q.coarse_vertex_values(n, v)).max() for v in range(8))
+        ee = max(np.abs(Phi[8 + l, NV:] - NR.coarse_edge_dofs(n, l)).max() / np.abs(NR.coarse_edge_dofs(n, l)).max()
+                 for l in range(12))
+        assert ev <= 1e-12
+        assert (ee <= 1e-12) if holds else (ee > 1e-3), ee

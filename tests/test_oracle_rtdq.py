@@ -126,3 +126,18 @@ def test_committed_rtdq_fixture_reproduces():
     res = RQ.build(cells, NR.sym6_to_ainv(ainv6), load.kind, list(load.params), want_phi=False)
     assert np.abs(res["KH"] - g["KH"]).max() <= 1e-9 * np.abs(g["KH"]).max()
     assert np.abs(res["FH"] - g["FH"]).max() <= 1e-9 * np.abs(g["FH"]).max()
+
+
+def test_constant_diagonal_coefficients_give_the_standard_basis():
+    """Known answer: with a constant diagonal A^-1 the coarse RT0 function of
+    face f has constant divergence and a curl-free A^-1 sigma, so it solves its
+    local problem: sigma of every basis is the standard coarse RT function (any
+    box); a full constant tensor breaks it (~12 %)."""
+    n, size = 4, np.array([1.0, 0.8, 1.3])
+    NF, _ = RQ.counts(n)
+    for A3, holds in ((np.diag([0.5, 1.0, 2.0]), True),
+                      (np.array([[1.0, 0.3, 0.1], [0.3, 0.8, -0.2], [0.1, -0.2, 1.5]]), False)):
+        Phi, _, _, _ = RQ.build_cell(np.zeros(3), size, 2, np.tile(A3, (n ** 3, 1, 1)))
+        e = max(np.abs(Phi[f, :NF] - NR.coarse_face_dofs(n, f)).max() / np.abs(NR.coarse_face_dofs(n, f)).max()
+                for f in range(6))
+        assert (e <= 1e-12) if holds else (e > 1e-3), e

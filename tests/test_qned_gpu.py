@@ -108,3 +108,24 @@ def test_qned_rejects_bad_input(gpu):
         h.qned_build(deep, np.tile(a6, (512, 1)), np.tile(binv, 512), gpu.make_load())
     KH, FH, rep, st = h.qned_build(cells[:0], a6[:0], binv[:0], gpu.make_load())
     assert st == gpu.SUCCESS and KH.shape == (0, 20, 20) and FH.shape == (0, 20)
+
+
+@pytest.mark.parametrize("precision", ("mixed", "fp64"))
+def test_qned_constant_diagonal_gives_the_standard_basis(gpu, precision):
+    """Known answer: constant diagonal A, constant B^-1, non-cubic box; the
+    vertex bases' sigma is trilinear, the edge bases' u the coarse Nedelec
+    function."""
+    depth, n = 3, 8
+    cells = workloads.coarse_grid(1, depth)
+    cells["size"] = [[1.0, 0.8, 1.3]]
+    a6 = np.tile([0.5, 1.0, 2.0, 0.0, 0.0, 0.0], (n ** 3, 1))
+    h = gpu.Handle(precision=gpu.PRECISION_MIXED if precision == "mixed" else gpu.PRECISION_FP64)
+    KH, FH, rep, st = h.qned_build(cells, a6, np.full(n ** 3, 1.7), gpu.make_load())
+    assert st == gpu.SUCCESS and rep["converged"].all(), rep
+    NV, NE = Q.counts(n)
+    phi = h.qned_basis().reshape(20, NV + NE)
+    for v in range(8):
+        assert _rel(phi[v, :NV], Q.coarse_vertex_values(n, v)) <= TOL_PHI, v
+    for l in range(12):
+        std = NR.coarse_edge_dofs(n, l)
+        assert _rel(phi[8 + l, NV:], std) <= TOL_PHI, (l, _rel(phi[8 + l, NV:], std))

@@ -113,3 +113,21 @@ def test_rtdq_matches_golden(gpu, precision):
     for c in range(len(cells)):
         assert _rel(KH[c], g["KH"][c]) <= TOL_KH, (c, _rel(KH[c], g["KH"][c]))
         assert _rel(FH[c], g["FH"][c]) <= TOL_KH, (c, _rel(FH[c], g["FH"][c]))
+
+
+@pytest.mark.parametrize("precision", ("mixed", "fp64"))
+def test_rtdq_constant_diagonal_gives_the_standard_basis(gpu, precision):
+    """Known answer: constant diagonal A^-1 on a non-cubic box; sigma of every
+    basis is the standard coarse RT function."""
+    depth, n = 3, 8
+    cells = workloads.coarse_grid(1, depth)
+    cells["size"] = [[1.0, 0.8, 1.3]]
+    ainv6 = np.tile([0.5, 1.0, 2.0, 0.0, 0.0, 0.0], (n ** 3, 1))
+    h = gpu.Handle(precision=gpu.PRECISION_MIXED if precision == "mixed" else gpu.PRECISION_FP64)
+    KH, FH, rep, st = h.rtdq_build(cells, ainv6, gpu.make_load(gpu.LOAD_ZERO, (0, 0, 0, 0)))
+    assert st == gpu.SUCCESS and rep["converged"].all(), rep
+    NF, NC = RQ.counts(n)
+    phi = h.rtdq_basis().reshape(6, NF + NC)
+    for f in range(6):
+        std = NR.coarse_face_dofs(n, f)
+        assert _rel(phi[f, :NF], std) <= TOL_PHI, (f, _rel(phi[f, :NF], std))
