@@ -31,6 +31,17 @@ faces in face order (line l / face f <-> coarse DoF l / 12 + f).
 
 Fine DoF numbering (lexicographic, not deal.II's): x-edges (i<n, j<=n, k<=n)
 i + n(j + (n+1)k), then y-edges, z-edges; x-faces (i<=n, j<n, k<n), y-, z-faces.
+
+Parity partially pinned: no reference test or fixture covers the basis /
+Galerkin path (the reference cannot be built here; its only golden output
+pins the Nedelec DoF functional, reproduced exactly in
+tests/test_golden_nedelec.py). Pinned further by known answers: constant
+diagonal coefficients give the standard coarse functions, the set_to_std
+Galerkin matrix is refinement-invariant, the standard problem converges to
+a closed-form solution at the expected rates, the multiscale solution
+converges in the coarse mesh size, and the reference's own iterative solver
+restated (faithful_iterative.py) reaches this oracle's basis to its 1e-6
+tolerance.
 """
 from __future__ import annotations
 

@@ -27,6 +27,13 @@ GPU path and checked here: grad of a Q1 function lies in the lowest-order
 Nedelec space with edge DoF = difference of the end values, and the curl of
 a Nedelec function lies in RT0 with face flux = the circulation around the
 face, so the element blocks factor as M_N(I) Grad and C^T M_RT(A) C.
+
+Parity partially pinned: no reference test or fixture covers this pairing.
+Pinned by known answers: constant diagonal coefficients give the trilinear /
+coarse Nedelec functions, the multiscale solution converges to a closed-form
+solution in the coarse mesh size, and the reference's own iterative solver
+restated (faithful_iterative.py) reaches this oracle's basis to its 1e-6
+tolerance.
 """
 from __future__ import annotations
 

@@ -27,6 +27,12 @@ sum over fine cells of (B sigma_j)_c = the net outflow of sigma_j, K_H[6][6] =
 0 (R = 0), F_H[6] = the integral of f over the coarse cell.
 Fine DoFs per cell: faces in the Ned_RT numbering (x-, y-, z-faces), then
 cells (lexicographic). Face DoF = flux in the positive axis direction.
+
+Parity partially pinned: no reference test or fixture covers this pairing.
+Pinned by known answers: constant diagonal coefficients give the coarse RT
+functions, the multiscale solution converges to a closed-form solution in the
+coarse mesh size, and the reference's own Schur-complement CG (restated in
+tests/test_oracle_rtdq.py) gives this oracle's sigma.
 """
 from __future__ import annotations
 
