@@ -36,3 +36,17 @@ def test_status_strings_and_defaults_without_gpu():
         assert L.msfec_status_string(s)
     # argument checks happen before any device work
     assert L.msfec_create(None, None) == msfec.ERROR_INVALID_ARGUMENT
+
+
+def test_header_is_plain_c():
+    """The boundary is a C ABI: the header compiles as strict C99 (no C++ or
+    torch types), so cgo / ctypes / JNI bindings can include it directly."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        import pytest
+        pytest.skip("no C compiler")
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-fsyntax-only", "-x", "c",
+                        os.path.join(REPO, "include", "msfec_cuda.h")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
