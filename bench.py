@@ -117,14 +117,8 @@ class Workload:
         return workloads.nedrt_work_dof_rhs(c) if self.kind == "nedrt" else workloads.work_dof_rhs(c)
 
     def per_cell_work(self):
-        n = 1 << self.cells["depth"].astype(np.int64)
-        if self.kind == "nedrt":
-            return (3 * n * (n + 1) ** 2 + 3 * n * n * (n + 1)) * 18
-        if self.kind == "qned":
-            return ((n + 1) ** 3 + 3 * n * (n + 1) ** 2) * 20
-        if self.kind == "rtdq":
-            return (3 * n * n * (n + 1) + n ** 3) * 6
-        return (n + 1) ** 3 * 8
+        import sharding
+        return sharding.cell_work(self.cells, self.kind)
 
     def shard(self, lo, hi):
         f0, f1 = int(self.foff[lo]), int(self.foff[hi])

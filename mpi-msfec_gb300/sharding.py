@@ -5,7 +5,8 @@ exchange, source/Q/q_global.cc:50-86), so a batch is split into contiguous
 cell ranges balanced by fine DoF x RHS, each rank builds its range on its own
 GPU, and nothing crosses ranks during the build. The one collective is the
 gather of the small per-cell Galerkin blocks (64 + 8 doubles per Q1 cell,
-324 + 18 per Ned_RT cell) for the global coarse assembly, which every rank
+324 + 18 per Ned_RT, 400 + 20 per Q_Ned, 49 + 7 per RT_DQ cell) for the
+global coarse assembly, which every rank
 then holds in full. Timing of a sharded step is the maximum over ranks.
 
 The helpers take the per-rank builder and the process group as arguments so
@@ -17,11 +18,20 @@ import numpy as np
 
 
 def cell_work(cells, kind):
-    """Fine DoF x RHS of every cell: Q1 8 (n+1)^3, Ned_RT 18 (N_edge + N_face)."""
+    """Fine DoF x RHS of every cell (the measures of the benchmark's workloads):
+    Q1 8 (n+1)^3, Ned_RT 18 (N_edge + N_face), Q_Ned 20 (N_vertex + N_edge),
+    RT_DQ 6 (N_face + N_cell)."""
     n = 1 << np.asarray(cells["depth"]).astype(np.int64)
+    n_edge, n_face = 3 * n * (n + 1) ** 2, 3 * n * n * (n + 1)
+    if kind == "q1":
+        return (n + 1) ** 3 * 8
     if kind == "nedrt":
-        return (3 * n * (n + 1) ** 2 + 3 * n * n * (n + 1)) * 18
-    return (n + 1) ** 3 * 8
+        return (n_edge + n_face) * 18
+    if kind == "qned":
+        return ((n + 1) ** 3 + n_edge) * 20
+    if kind == "rtdq":
+        return (n_face + n ** 3) * 6
+    raise ValueError(f"unknown pairing {kind!r}")
 
 
 def partition(work, world, rank):

@@ -38,6 +38,17 @@ def test_partition_covers_in_order_and_balances(world):
     assert share.max() <= w.sum() / world + w.max()
 
 
+def test_cell_work_matches_the_workload_measures():
+    """Per-cell work of every pairing sums to the workload generators' totals."""
+    cells = workloads.coarse_grid(2, [1, 2, 3, 2, 1, 3, 2, 1])
+    assert sharding.cell_work(cells, "q1").sum() == workloads.work_dof_rhs(cells)
+    assert sharding.cell_work(cells, "nedrt").sum() == workloads.nedrt_work_dof_rhs(cells)
+    assert sharding.cell_work(cells, "qned").sum() == workloads.qned_work_dof_rhs(cells)
+    assert sharding.cell_work(cells, "rtdq").sum() == workloads.rtdq_work_dof_rhs(cells)
+    with pytest.raises(ValueError):
+        sharding.cell_work(cells, "p2")
+
+
 def test_partition_more_ranks_than_cells():
     w = np.array([5, 1, 1])
     ranges = [sharding.partition(w, 5, r) for r in range(5)]
