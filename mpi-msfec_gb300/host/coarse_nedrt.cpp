@@ -19,7 +19,8 @@
 // GeometryInfo<3> order, then 6 faces. The block system [K_ee K_ef; K_fe K_ff]
 // has K_fe = -K_ef^T (curl coupling), so negating the face rows gives a
 // symmetric indefinite matrix, solved by MINRES with the positive diagonal
-// diag(K_ee) (+) diag(K_ff + K_fe diag(K_ee)^-1 K_ef).
+// diag(K_ee) (+) diag(K_ff - K_fe diag(K_ee)^-1 K_ef), i.e. on face f
+// diag(K_ff) + sum_e K_fe^2 / K_ee (K_fe = -K_ef^T).
 #include <algorithm>
 #include <cmath>
 #include <cstddef>

@@ -10,7 +10,9 @@ global coarse assembly, which every rank
 then holds in full. Timing of a sharded step is the maximum over ranks.
 
 The helpers take the per-rank builder and the process group as arguments so
-that the same code runs over NCCL with the GPU library and over gloo on CPU.
+that the same code runs over NCCL with the GPU library and over gloo on CPU:
+the tensors they exchange live on the current CUDA device when the group's
+backend is NCCL (which accepts CUDA tensors only) and on the host otherwise.
 """
 from __future__ import annotations
 
@@ -53,21 +55,31 @@ def fine_offsets(cells):
     return np.concatenate([[0], np.cumsum(n ** 3)])
 
 
+def exchange_device(dist, group=None):
+    """Device of the tensors a collective of `group` exchanges: the current
+    CUDA device for the NCCL backend, the host for every other backend."""
+    import torch
+    if str(dist.get_backend(group)).lower() == "nccl":
+        return torch.device("cuda", torch.cuda.current_device())
+    return torch.device("cpu")
+
+
 def gather_blocks(local, dist, group=None):
     """All-gather per-rank arrays of per-cell blocks (leading axis = cells of
     the rank's range, in rank order) into the full array on every rank."""
     import torch
     world = dist.get_world_size(group)
-    t = torch.from_numpy(np.ascontiguousarray(local))
-    counts = torch.tensor([t.shape[0]], dtype=torch.int64)
-    all_counts = [torch.zeros(1, dtype=torch.int64) for _ in range(world)]
+    dev = exchange_device(dist, group)
+    t = torch.from_numpy(np.ascontiguousarray(local)).to(dev)
+    counts = torch.tensor([t.shape[0]], dtype=torch.int64, device=dev)
+    all_counts = [torch.zeros(1, dtype=torch.int64, device=dev) for _ in range(world)]
     dist.all_gather(all_counts, counts, group=group)
     cmax = int(max(int(c.item()) for c in all_counts))
-    pad = torch.zeros((cmax,) + tuple(t.shape[1:]), dtype=t.dtype)
+    pad = torch.zeros((cmax,) + tuple(t.shape[1:]), dtype=t.dtype, device=dev)
     pad[: t.shape[0]] = t
     parts = [torch.zeros_like(pad) for _ in range(world)]
     dist.all_gather(parts, pad, group=group)
-    return np.concatenate([p[: int(c.item())].numpy() for p, c in zip(parts, all_counts)])
+    return np.concatenate([p[: int(c.item())].cpu().numpy() for p, c in zip(parts, all_counts)])
 
 
 def max_over_ranks(x, dist=None, group=None):
@@ -75,7 +87,7 @@ def max_over_ranks(x, dist=None, group=None):
     if dist is None:
         return float(x)
     import torch
-    t = torch.tensor([float(x)], dtype=torch.float64)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=exchange_device(dist, group))
     dist.all_reduce(t, op=dist.ReduceOp.MAX, group=group)
     return float(t.item())
 
@@ -88,7 +100,7 @@ def weak_scaling_value(work_local, seconds_local, dist=None, group=None):
     if dist is None:
         return float(work_local) / float(seconds_local)
     import torch
-    w = torch.tensor([float(work_local)], dtype=torch.float64)
+    w = torch.tensor([float(work_local)], dtype=torch.float64, device=exchange_device(dist, group))
     dist.all_reduce(w, op=dist.ReduceOp.SUM, group=group)
     return float(w.item()) / max_over_ranks(seconds_local, dist, group)
 

@@ -53,10 +53,12 @@ def q1_case(name, cells, a, r, load):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("MSFEC_REFERENCE_DIR"),
+                    help="checkout of konsim83/MPI-MSFEC whose test outputs are copied "
+                         "(default: $MSFEC_REFERENCE_DIR; skipped when neither is given)")
     args = ap.parse_args()
     oracle.build()
-    if os.path.isdir(args.reference):
+    if args.reference and os.path.isdir(args.reference):
         copy_reference_golden(args.reference)
     # small Q1 case: coarse 4^3, depth 3, log-normal a, reaction 1, sin load (seed 1)
     q1_case("q1_lognormal_m4_L3_seed1.npz", *workloads.q1_lognormal(m=4, depth=3, seed=1, reaction=True))

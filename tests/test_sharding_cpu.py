@@ -96,3 +96,22 @@ def test_gloo_two_ranks_match_single_process(oracle_lib):
             assert float(g["t"]) == 2.0
             assert np.array_equal(g["KHw"], KH_ref)
             assert float(g["v"]) == world * float(g["work"]) / 2.0  # all ranks' work / slowest rank
+
+
+class _FakeDist:
+    """Stand-in for torch.distributed that reports a backend name."""
+
+    def __init__(self, backend):
+        self.backend = backend
+
+    def get_backend(self, group=None):
+        return self.backend
+
+
+def test_exchange_device_follows_the_backend(monkeypatch):
+    """NCCL collectives take CUDA tensors only: the helpers put their tensors
+    on the current CUDA device for NCCL and on the host for gloo."""
+    import torch
+    assert sharding.exchange_device(_FakeDist("gloo")) == torch.device("cpu")
+    monkeypatch.setattr(torch.cuda, "current_device", lambda: 3)
+    assert sharding.exchange_device(_FakeDist("nccl")) == torch.device("cuda", 3)
