@@ -40,6 +40,13 @@ enum {
   ORACLE_LOAD_SIN_PRODUCT = 2, /* f = p0 sin(p1 pi x) sin(p1 pi y) sin(p1 pi z) */
 };
 
+/* Diffusion coefficient layout of the Q1 oracle (doubles per fine cell). */
+enum {
+  ORACLE_COEF_SCALAR = 0, /* 1: a, the stiffness is a K_unit */
+  ORACLE_COEF_TENSOR = 1, /* 6: a00 a11 a22 a01 a02 a12 of a symmetric A */
+  ORACLE_COEF_GAUSS = 2,  /* 48: those 6 at each 2x2x2 Gauss point, x fastest */
+};
+
 /* Local solver of the oracle. */
 enum {
   ORACLE_SOLVER_DIRECT = 0,   /* banded Cholesky: `use direct solver basis = true` */
@@ -60,6 +67,14 @@ int oracle_q1_build(int ncells, const double *origin, const double *size,
                     double tol, int max_iter, double *Phi, double *KH,
                     double *FH, int *iters, int nthreads);
 
+/* oracle_q1_build with the diffusion coefficient in layout coef_mode. */
+int oracle_q1_build_coef(int ncells, const double *origin, const double *size,
+                         const int *depth, int coef_mode, const double *a,
+                         const double *r, int load_kind,
+                         const double *load_params, int solver, double tol,
+                         int max_iter, double *Phi, double *KH, double *FH,
+                         int *iters, int nthreads);
+
 /*
  * Assemble the unconstrained fine stiffness K (27-point, COO with exactly
  * 27*(n+1)^3 slots, unused slots carry value 0 and row=col=0) and load b for
@@ -69,6 +84,10 @@ int oracle_q1_assemble(const double *origin, const double *size, int depth,
                        const double *a, const double *r, int load_kind,
                        const double *load_params, int *rows, int *cols,
                        double *vals, double *b);
+int oracle_q1_assemble_coef(const double *origin, const double *size, int depth,
+                            int coef_mode, const double *a, const double *r,
+                            int load_kind, const double *load_params, int *rows,
+                            int *cols, double *vals, double *b);
 
 /*
  * Nedelec lowest-order DoF values of a constant field c on the unit cube

@@ -19,6 +19,7 @@ _lib = None
 
 LOAD_ZERO, LOAD_CONSTANT, LOAD_SIN_PRODUCT = 0, 1, 2
 SOLVER_DIRECT, SOLVER_CG_SSOR = 0, 1
+COEF_SCALAR, COEF_TENSOR, COEF_GAUSS = 0, 1, 2
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int)
@@ -43,6 +44,13 @@ def lib():
         L.oracle_q1_assemble.restype = ctypes.c_int
         L.oracle_q1_assemble.argtypes = [_dp, _dp, ctypes.c_int, _dp, _dp, ctypes.c_int, _dp,
                                          _ip, _ip, _dp, _dp]
+        L.oracle_q1_build_coef.restype = ctypes.c_int
+        L.oracle_q1_build_coef.argtypes = [ctypes.c_int, _dp, _dp, _ip, ctypes.c_int, _dp, _dp, ctypes.c_int,
+                                           _dp, ctypes.c_int, ctypes.c_double, ctypes.c_int, _dp, _dp, _dp,
+                                           _ip, ctypes.c_int]
+        L.oracle_q1_assemble_coef.restype = ctypes.c_int
+        L.oracle_q1_assemble_coef.argtypes = [_dp, _dp, ctypes.c_int, ctypes.c_int, _dp, _dp, ctypes.c_int, _dp,
+                                              _ip, _ip, _dp, _dp]
         L.oracle_nedelec_dof_values_unit_cube.restype = ctypes.c_int
         L.oracle_nedelec_dof_values_unit_cube.argtypes = [ctypes.c_int, _dp, _dp, ctypes.c_int]
         _lib = L
@@ -58,9 +66,12 @@ def _i(a):
 
 
 def q1_build(origin, size, depth, a, r=None, load_kind=LOAD_ZERO, load_params=(0, 0, 0, 0),
-             solver=SOLVER_DIRECT, tol=1e-12, max_iter=1000, want_phi=True, nthreads=0):
+             solver=SOLVER_DIRECT, tol=1e-12, max_iter=1000, want_phi=True, nthreads=0, coef_mode=0):
     """Q1 basis build (reference QBasis::run, source/Q/q_basis.cc:518-603).
 
+    coef_mode: COEF_SCALAR (a: one value per fine cell), COEF_TENSOR (6 per
+    fine cell: a00 a11 a22 a01 a02 a12), COEF_GAUSS (48 per fine cell: the 6
+    at each 2x2x2 Gauss point, x fastest).
     Returns dict with KH [c,8,8], FH [c,8], Phi (flat, per cell 8 planes of
     (n+1)^3 nodes) and iters [c,8]."""
     origin = np.ascontiguousarray(origin, dtype=np.float64).reshape(-1, 3)
@@ -76,13 +87,13 @@ def q1_build(origin, size, depth, a, r=None, load_kind=LOAD_ZERO, load_params=(0
     KH = np.zeros((nc, 8, 8))
     FH = np.zeros((nc, 8))
     iters = np.zeros((nc, 8), dtype=np.int32)
-    st = lib().oracle_q1_build(nc, _d(origin), _d(size), _i(depth), _d(a), _d(r), int(load_kind),
-                               _d(lp), int(solver), float(tol), int(max_iter), _d(Phi), _d(KH),
-                               _d(FH), _i(iters), int(nthreads))
+    st = lib().oracle_q1_build_coef(nc, _d(origin), _d(size), _i(depth), int(coef_mode), _d(a), _d(r),
+                                    int(load_kind), _d(lp), int(solver), float(tol), int(max_iter), _d(Phi),
+                                    _d(KH), _d(FH), _i(iters), int(nthreads))
     return {"status": st, "KH": KH, "FH": FH, "Phi": Phi, "iters": iters}
 
 
-def q1_assemble(origin, size, depth, a, r=None, load_kind=LOAD_ZERO, load_params=(0, 0, 0, 0)):
+def q1_assemble(origin, size, depth, a, r=None, load_kind=LOAD_ZERO, load_params=(0, 0, 0, 0), coef_mode=0):
     """Unconstrained fine K (scipy CSR) and load b of one coarse cell."""
     import scipy.sparse as sp
     n = 1 << int(depth)
@@ -96,8 +107,8 @@ def q1_assemble(origin, size, depth, a, r=None, load_kind=LOAD_ZERO, load_params
     a = np.ascontiguousarray(a, dtype=np.float64)
     r = None if r is None else np.ascontiguousarray(r, dtype=np.float64)
     lp = np.ascontiguousarray(load_params, dtype=np.float64)
-    st = lib().oracle_q1_assemble(_d(o), _d(s), int(depth), _d(a), _d(r), int(load_kind), _d(lp),
-                                  _i(rows), _i(cols), _d(vals), _d(b))
+    st = lib().oracle_q1_assemble_coef(_d(o), _d(s), int(depth), int(coef_mode), _d(a), _d(r), int(load_kind),
+                                       _d(lp), _i(rows), _i(cols), _d(vals), _d(b))
     assert st == 0
     K = sp.coo_matrix((vals, (rows, cols)), shape=(nn, nn)).tocsr()
     return K, b

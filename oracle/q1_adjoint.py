@@ -65,14 +65,39 @@ def _element(h):
     return K
 
 
-def misfit(cells, m, theta, load, cell_of, points, data, gradient=True):
-    """Returns (J, grad or None) for a uniform-depth batch on the m^3 coarse grid."""
+def element_tensor(h, A6, gauss):
+    """Element stiffness sum_q grad psi_u . A_q grad psi_v JxW of every fine cell
+    (the reference's quadrature loop, q_basis.cc:222-231). A6: [ne, 6] (one
+    tensor per cell) or [ne, 48] (at the 2x2x2 Gauss points, x fastest).
+    Returns [ne, 8, 8]."""
+    g = 0.5 / np.sqrt(3.0)
+    qp = np.array([0.5 - g, 0.5 + g])
+    G = np.zeros((8, 8, 3))  # [gauss point, vertex, direction], physical gradient
+    for q in range(8):
+        t = [qp[q & 1], qp[(q >> 1) & 1], qp[q >> 2]]
+        for u in range(8):
+            b = [(u >> d) & 1 for d in range(3)]
+            val = [t[d] if b[d] else 1 - t[d] for d in range(3)]
+            der = [(1.0 if b[d] else -1.0) / h[d] for d in range(3)]
+            G[q, u] = [der[0] * val[1] * val[2], val[0] * der[1] * val[2], val[0] * val[1] * der[2]]
+    A6 = np.asarray(A6).reshape(len(A6), 8 if gauss else 1, 6)
+    A6 = np.broadcast_to(A6, (len(A6), 8, 6))
+    A = np.stack([np.stack([A6[..., 0], A6[..., 3], A6[..., 4]], -1),
+                  np.stack([A6[..., 3], A6[..., 1], A6[..., 5]], -1),
+                  np.stack([A6[..., 4], A6[..., 5], A6[..., 2]], -1)], -2)  # [ne, 8, 3, 3]
+    return np.einsum("qud,eqdk,qvk->euv", G, A, G) * (h[0] * h[1] * h[2] / 8.0)
+
+
+def misfit(cells, m, theta, load, cell_of, points, data, gradient=True, coef_mode=0, base=None):
+    """Returns (J, grad or None) for a uniform-depth batch on the m^3 coarse grid.
+    coef_mode 0: a = exp(theta) per fine cell; 1 / 2 (tensor per fine cell / at
+    the Gauss points): A_e = exp(theta_e) base_e, grad = dJ/dtheta."""
     depth = int(cells["depth"][0])
     n = 1 << depth
     N1 = n + 1
-    a = np.exp(theta)
+    a = np.exp(theta) if coef_mode == 0 else np.asarray(base) * np.exp(theta)[:, None]
     res = O.q1_build(cells["origin"], cells["size"], cells["depth"], a, None, load_kind=load.kind,
-                     load_params=list(load.params))
+                     load_params=list(load.params), coef_mode=coef_mode)
     KH, FH = res["KH"], res["FH"]
     Phi = res["Phi"].reshape(m ** 3, 8, -1)
     K, I, nodes = _coarse(m, KH)
@@ -107,7 +132,7 @@ def misfit(cells, m, theta, load, cell_of, points, data, gradient=True):
     for c in range(m ** 3):
         sl = slice(c * n ** 3, (c + 1) * n ** 3)
         Kf, bf = O.q1_assemble(cells["origin"][c], cells["size"][c], depth, a[sl], None, load.kind,
-                               list(load.params))
+                               list(load.params), coef_mode=coef_mode)
         Kf = Kf.tocsr()
         flu = spla.splu(Kf[Iin][:, Iin].tocsc())
         mu = np.zeros(N1 ** 3)
@@ -120,10 +145,14 @@ def misfit(cells, m, theta, load, cell_of, points, data, gradient=True):
         eta[Iin] = flu.solve(src[Iin])
         psiU = U[nodes[c]] @ Phi[c]
         psiL = lam[nodes[c]] @ Phi[c]
-        Kh = _element(np.asarray(cells["size"][c]) / n)
         A_ = (mu + psiU)[enodes]
         B_ = psiL[enodes]
         C_ = eta[enodes]
         D_ = psiU[enodes]
-        grad[sl] = -a[sl] * (np.einsum("eu,uv,ev->e", A_, Kh, B_) + np.einsum("eu,uv,ev->e", C_, Kh, D_))
+        if coef_mode == 0:
+            Kh = _element(np.asarray(cells["size"][c]) / n)
+            grad[sl] = -a[sl] * (np.einsum("eu,uv,ev->e", A_, Kh, B_) + np.einsum("eu,uv,ev->e", C_, Kh, D_))
+        else:  # d K_e / d theta_e = K_e(A_e)
+            Ke = element_tensor(np.asarray(cells["size"][c]) / n, a[sl], coef_mode == 2)
+            grad[sl] = -(np.einsum("eu,euv,ev->e", A_, Ke, B_) + np.einsum("eu,euv,ev->e", C_, Ke, D_))
     return J, grad

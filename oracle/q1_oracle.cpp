@@ -12,10 +12,17 @@
 //
 // The coarse cells handled here are axis-aligned boxes, so the reference's
 // monomial-inverse BasisQ1 reduces to the tensor-product trilinear nodal
-// function and the fine Q1 mapping is affine. The coefficient is one value
-// per fine cell (the seeded workloads), so the 2x2x2 Gauss rule of the
-// reference integrates the element stiffness and mass exactly; the closed
-// forms are used. The load uses the same 2x2x2 Gauss rule as the reference.
+// function and the fine Q1 mapping is affine. Coefficient modes:
+//   scalar  one value a per fine cell (the seeded workloads): the 2x2x2 Gauss
+//           rule of the reference integrates a K_unit exactly, closed form used;
+//   tensor  a symmetric 3x3 A per fine cell (a00 a11 a22 a01 a02 a12);
+//   gauss   A at each of the cell's 2x2x2 Gauss points (8 x 6 values, points
+//           x fastest at 0.5 -+ 1/(2 sqrt 3) of the cell), which is what
+//           Diffusion_A::value_list hands the reference's assembly
+//           (source/equation_data/eqn_coeff_A.cc:162-191);
+// for the last two the element matrix is the reference's quadrature loop
+// itself, sum_q grad psi_i . A(x_q) grad psi_j JxW (q_basis.cc:222-231).
+// The load uses the same 2x2x2 Gauss rule as the reference.
 //
 // Parity partially pinned: no reference test or fixture covers the basis /
 // Galerkin path (the reference cannot be built here). Pinned by known answers:
@@ -76,10 +83,47 @@ void element_matrices(const double h[3], double K[8][8], double M[8][8]) {
     }
 }
 
+// Element stiffness sum_q grad psi_u(x_q) . A_q grad psi_v(x_q) JxW over the
+// 2x2x2 Gauss points q (x fastest) of a box; A6 holds 6 entries per point
+// (a00 a11 a22 a01 a02 a12), stride 0 for one tensor on the whole cell.
+void element_matrix_tensor(const double h[3], const double *A6, int stride, double K[8][8]) {
+  const double g = 0.5 / std::sqrt(3.0);
+  const double qp[2] = {0.5 - g, 0.5 + g};
+  const double jxw = h[0] * h[1] * h[2] / 8.0;
+  for (int u = 0; u < 8; ++u)
+    for (int v = 0; v < 8; ++v) K[u][v] = 0.0;
+  for (int q = 0; q < 8; ++q) {
+    const int qx = q & 1, qy = (q >> 1) & 1, qz = q >> 2;
+    const double *a = A6 + (size_t)q * stride;
+    const double A[3][3] = {{a[0], a[3], a[4]}, {a[3], a[1], a[5]}, {a[4], a[5], a[2]}};
+    const double t[3] = {qp[qx], qp[qy], qp[qz]};
+    double gr[8][3];
+    for (int u = 0; u < 8; ++u) {
+      const int b[3] = {u & 1, (u >> 1) & 1, u >> 2};
+      double val[3], der[3];
+      for (int d = 0; d < 3; ++d) {
+        val[d] = b[d] ? t[d] : 1.0 - t[d];
+        der[d] = (b[d] ? 1.0 : -1.0) / h[d];
+      }
+      gr[u][0] = der[0] * val[1] * val[2];
+      gr[u][1] = val[0] * der[1] * val[2];
+      gr[u][2] = val[0] * val[1] * der[2];
+    }
+    for (int u = 0; u < 8; ++u) {
+      double Ag[3];
+      for (int d = 0; d < 3; ++d) Ag[d] = A[d][0] * gr[u][0] + A[d][1] * gr[u][1] + A[d][2] * gr[u][2];
+      for (int v = 0; v < 8; ++v) K[v][u] += (gr[v][0] * Ag[0] + gr[v][1] * Ag[1] + gr[v][2] * Ag[2]) * jxw;
+    }
+  }
+}
+
 inline int off27(int dx, int dy, int dz) { return (dx + 1) + 3 * (dy + 1) + 9 * (dz + 1); }
 
+// Doubles of the diffusion coefficient per fine cell of each mode.
+inline size_t coef_stride(int mode) { return mode == ORACLE_COEF_TENSOR ? 6 : (mode == ORACLE_COEF_GAUSS ? 48 : 1); }
+
 // Structured assembly: W[node*27 + off27] = K(node, node+offset), b[node].
-void assemble(const Box &bx, const double *a, const double *r, int load_kind,
+void assemble(const Box &bx, int coef_mode, const double *a, const double *r, int load_kind,
               const double *lp, std::vector<double> &W, std::vector<double> &b) {
   const int n = bx.n, N1 = n + 1;
   const size_t nn = (size_t)N1 * N1 * N1;
@@ -94,13 +138,20 @@ void assemble(const Box &bx, const double *a, const double *r, int load_kind,
     for (int j = 0; j < n; ++j)
       for (int i = 0; i < n; ++i) {
         const size_t e = (size_t)i + (size_t)n * (j + (size_t)n * k);
-        const double ae = a[e], re = r ? r[e] : 0.0;
+        const double re = r ? r[e] : 0.0;
+        double Ke[8][8];
+        if (coef_mode == ORACLE_COEF_SCALAR) {
+          for (int u = 0; u < 8; ++u)
+            for (int v = 0; v < 8; ++v) Ke[u][v] = a[e] * K[u][v];
+        } else {
+          element_matrix_tensor(bx.h, a + e * coef_stride(coef_mode), coef_mode == ORACLE_COEF_GAUSS ? 6 : 0, Ke);
+        }
         for (int u = 0; u < 8; ++u) {
           const int ux = u & 1, uy = (u >> 1) & 1, uz = u >> 2;
           const size_t nu = (size_t)(i + ux) + N1 * ((size_t)(j + uy) + N1 * (size_t)(k + uz));
           for (int v = 0; v < 8; ++v) {
             const int vx = v & 1, vy = (v >> 1) & 1, vz = v >> 2;
-            W[nu * 27 + off27(vx - ux, vy - uy, vz - uz)] += ae * K[u][v] + re * M[u][v];
+            W[nu * 27 + off27(vx - ux, vy - uy, vz - uz)] += Ke[u][v] + re * M[u][v];
           }
         }
         if (load_kind != ORACLE_LOAD_ZERO) {
@@ -313,12 +364,12 @@ struct BandChol {
   }
 };
 
-int build_cell(const Box &bx, const double *a, const double *r, int load_kind, const double *lp,
+int build_cell(const Box &bx, int coef_mode, const double *a, const double *r, int load_kind, const double *lp,
                int solver, double tol, int max_iter, double *Phi, double *KH, double *FH, int *iters) {
   const int n = bx.n, N1 = n + 1, m = n - 1;
   const size_t nn = (size_t)N1 * N1 * N1, Ni = (size_t)m * m * m;
   std::vector<double> W, b;
-  assemble(bx, a, r, load_kind, lp, W, b);
+  assemble(bx, coef_mode, a, r, load_kind, lp, W, b);
   std::vector<double> phi(8 * nn), rhs(Ni), x(Ni);
   BandChol chol;
   if (solver == ORACLE_SOLVER_DIRECT && Ni > 0 && chol.factor(n, W) != 0) return 2;
@@ -370,7 +421,16 @@ extern "C" int oracle_q1_build(int ncells, const double *origin, const double *s
                                const double *a, const double *r, int load_kind, const double *load_params,
                                int solver, double tol, int max_iter, double *Phi, double *KH, double *FH,
                                int *iters, int nthreads) {
+  return oracle_q1_build_coef(ncells, origin, size, depth, ORACLE_COEF_SCALAR, a, r, load_kind, load_params,
+                              solver, tol, max_iter, Phi, KH, FH, iters, nthreads);
+}
+
+extern "C" int oracle_q1_build_coef(int ncells, const double *origin, const double *size, const int *depth,
+                                    int coef_mode, const double *a, const double *r, int load_kind,
+                                    const double *load_params, int solver, double tol, int max_iter, double *Phi,
+                                    double *KH, double *FH, int *iters, int nthreads) {
   if (ncells < 0 || !origin || !size || !depth || !a || !KH || !FH) return 1;
+  if (coef_mode < ORACLE_COEF_SCALAR || coef_mode > ORACLE_COEF_GAUSS) return 1;
   std::vector<size_t> coff(ncells + 1, 0), poff(ncells + 1, 0);
   for (int c = 0; c < ncells; ++c) {
     if (depth[c] < 1 || depth[c] > 6) return 1;
@@ -392,7 +452,8 @@ extern "C" int oracle_q1_build(int ncells, const double *origin, const double *s
       bx.o[d] = origin[3 * c + d];
       bx.h[d] = size[3 * c + d] / bx.n;
     }
-    status |= build_cell(bx, a + coff[c], r ? r + coff[c] : nullptr, load_kind, lp, solver, tol, max_iter,
+    status |= build_cell(bx, coef_mode, a + coff[c] * coef_stride(coef_mode), r ? r + coff[c] : nullptr,
+                         load_kind, lp, solver, tol, max_iter,
                          Phi ? Phi + poff[c] : nullptr, KH + 64 * (size_t)c, FH + 8 * (size_t)c,
                          iters ? iters + 8 * (size_t)c : nullptr);
   }
@@ -403,6 +464,14 @@ extern "C" int oracle_q1_build(int ncells, const double *origin, const double *s
 extern "C" int oracle_q1_assemble(const double *origin, const double *size, int depth, const double *a,
                                   const double *r, int load_kind, const double *load_params, int *rows,
                                   int *cols, double *vals, double *b) {
+  return oracle_q1_assemble_coef(origin, size, depth, ORACLE_COEF_SCALAR, a, r, load_kind, load_params, rows, cols,
+                                 vals, b);
+}
+
+extern "C" int oracle_q1_assemble_coef(const double *origin, const double *size, int depth, int coef_mode,
+                                       const double *a, const double *r, int load_kind, const double *load_params,
+                                       int *rows, int *cols, double *vals, double *b) {
+  if (coef_mode < ORACLE_COEF_SCALAR || coef_mode > ORACLE_COEF_GAUSS) return 1;
   if (depth < 1 || depth > 6) return 1;
   Box bx;
   bx.n = 1 << depth;
@@ -412,7 +481,7 @@ extern "C" int oracle_q1_assemble(const double *origin, const double *size, int 
   }
   const double zero_params[4] = {0, 0, 0, 0};
   std::vector<double> W, bb;
-  assemble(bx, a, r, load_kind, load_params ? load_params : zero_params, W, bb);
+  assemble(bx, coef_mode, a, r, load_kind, load_params ? load_params : zero_params, W, bb);
   const int n = bx.n, N1 = n + 1;
   for (int k = 0; k <= n; ++k)
     for (int j = 0; j <= n; ++j)

@@ -190,7 +190,7 @@ def build_cell(origin, size, depth, binv, a3, load_kind=LOAD_VEC_ZERO, load_para
     Gb[:, I] = 0.0
     R = rhs[I, :] - A[I][:, B] @ Gb[:, B].T
     if interior_solver is None:
-        X = spla.splu(A[I][:, I].tocsc()).solve(R)
+        X = NR.solve_refined(A[I][:, I], R)
     else:
         X = interior_solver(A[I][:, I].tocsr(), int(np.sum(I < NV)), R)
     Phi = Gb

@@ -128,7 +128,7 @@ def build_cell(origin, size, depth, ainv, load_kind=LOAD_ZERO, load_params=(0, 0
     R[cel] -= R[cel].mean(0, keepdims=True)
     border = sp.coo_matrix((np.ones(len(cel)), (cel, np.zeros(len(cel), dtype=int))), shape=(nI, 1))
     K = sp.bmat([[AII, border], [border.T, None]]).tocsc()
-    X = spla.splu(K).solve(np.vstack([R, np.zeros((1, 6))]))[:nI]
+    X = NR.solve_refined(K, np.vstack([R, np.zeros((1, 6))]))[:nI]
     Phi = G
     Phi[:, I] = X.T
     P = Phi[:, NF:].copy()
