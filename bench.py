@@ -1,25 +1,31 @@
 #!/usr/bin/env python3
 """Benchmark of the batched MsFEC basis build (fine-DoF x RHS per second).
 
-Headline workload (default): Ned_RT mixed basis build, coarse 8^3 cells of the
-unit cube, 3 local refinement levels (8^3 fine cells, 3672 Nedelec+RT DoFs per
-cell, 12 edge + 6 face coarse-basis RHS), per fine cell A = R diag(e^g) R^T with
-g ~ N(0,1) and R Haar-random (seed 2), B = 1 - 0.9 sin(2 pi 14 x), vector trig
-load. Mixed precision (FP32 MINRES inside FP64 iterative refinement) with the
-plain FP64 path timed beside it. Reported beside the headline: the batched
-uneven-depth Q1 build (coarse 16^3, L ~ U{2..5}, 8 RHS, oscillatory
-coefficient eps = 1/64 times a per-cell log-normal factor).
+Headline workload (default, the largest configuration that fits one GPU):
+Ned_RT mixed basis build, coarse 16^3 cells of the unit cube, 4 local
+refinement levels (16^3 fine cells, 26928 Nedelec+RT DoFs per cell, 12 edge +
+6 face coarse-basis RHS), per fine cell A = R diag(e^g) R^T with g ~ N(0,1)
+and R Haar-random (seed 5), B = 1 - 0.9 sin(2 pi 14 x), vector trig load:
+1.985e9 fine DoF x RHS, 16 GB of basis. Mixed precision (FP32 MINRES inside
+FP64 iterative refinement); the plain FP64 path is timed on a 64-cell sample
+beside it. The 4096 cells are built in batches of 512 (one step = one batch,
+all inputs resident; the steps cycle through the 8 batches), and one build of
+all 4096 cells in a single call is timed once as a cross-check. Reported
+beside the headline: the smaller Ned_RT batch (coarse 8^3 x depth 3), the
+batched uneven-depth Q1 build (coarse 16^3, L ~ U{2..5}), Q_Ned and RT_DQ, the
+adjoints, and the parity of a sample of the headline batch against the FP64
+oracle (checker, after the timed region).
 
-One step = one full build (all local solves + Galerkin K_H, F_H) of every
-cell of this rank's share; inputs resident in HBM for `value`, host buffers
-through the C ABI (H2D + D2H inside the timed region) for `e2e`.
+One step = one build (all local solves + Galerkin K_H, F_H) of one batch of
+this rank's cells; inputs resident in HBM for `value`, host buffers through
+the C ABI (H2D + D2H inside the timed region) for `e2e`.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-N > 1 (torchrun): every rank builds its own full batch of the workload (coarse
-cells are independent: no data-path collective, only the timing max is
-reduced); per-GPU work is fixed -> scaling "weak", value = the DoF x RHS of all
-ranks / the slowest rank's step time.
+N > 1 (torchrun): every rank builds its own full batches of the workload
+(coarse cells are independent: no data-path collective, only the timing max
+is reduced); per-GPU work is fixed -> scaling "weak", value = the DoF x RHS
+of all ranks / the slowest rank's step time.
 """
 from __future__ import annotations
 
@@ -77,7 +83,9 @@ class Workload:
         elif name == "nedrt_large":
             self.kind = "nedrt"
             self.cells, self.ainv6, self.bdiv, self.load = workloads.nedrt_tensor(m=16, depth=4, seed=5)
-            self.cfg = {"workload": "nedrt_tensor_coarse16^3_L4_18rhs", "coarse_cells": 4096, "depth": 4, "seed": 5}
+            self.cfg = {"workload": "nedrt_tensor_coarse16^3_L4_18rhs", "coarse_cells": 4096, "depth": 4, "seed": 5,
+                        "B": "1-0.9 sin(2 pi 14 x)", "load": "vec trig"}
+            self.batch_cells = 512
         elif name == "qned_small":
             self.kind = "qned"
             self.cells, self.a6, self.binv, self.load = workloads.qned_tensor(m=8, depth=3, seed=2)
@@ -103,6 +111,8 @@ class Workload:
             self.cfg = {"workload": "q1_lognormal_coarse8^3_L4_8rhs", "coarse_cells": 512, "seed": 4}
         else:
             raise SystemExit(f"unknown workload {name}")
+        if not hasattr(self, "batch_cells"):
+            self.batch_cells = len(self.cells)
         n = 1 << self.cells["depth"].astype(np.int64)
         self.nfine = n ** 3
         self.foff = np.concatenate([[0], np.cumsum(self.nfine)])
@@ -138,8 +148,13 @@ class Workload:
 
 
 def rank_share(wl):
-    """Weak scaling: each rank's share is the whole batch of the workload."""
+    """Weak scaling: each rank's share is the whole workload."""
     return 0, len(wl.cells)
+
+
+def batches_of(wl, lo, hi):
+    """Consecutive batches of at most wl.batch_cells cells covering [lo, hi)."""
+    return [(a, min(hi, a + wl.batch_cells)) for a in range(lo, hi, wl.batch_cells)] or [(lo, hi)]
 
 
 # --------------------------------------------------------------------------- clocks
@@ -219,11 +234,15 @@ def _nedrt_oracle_chunk(args):
     return time.perf_counter() - t0
 
 
-def cpu_sample(wl, target_s, nthreads):
-    """Stratified sample (every depth represented) sized for ~target_s of CPU work."""
-    depths = sorted(set(int(d) for d in wl.cells["depth"]))
+def cpu_sample(wl, target_s, nthreads, lo=0, hi=None):
+    """Stratified sample of cells [lo, hi) (every depth represented) sized for
+    ~target_s of wall time on nthreads workers (at least one cell per worker
+    when the cells are that many)."""
+    hi = len(wl.cells) if hi is None else hi
+    depth = wl.cells["depth"][lo:hi]
+    depths = sorted(set(int(d) for d in depth))
     if wl.kind in ("nedrt", "qned"):
-        per_cell = {1: 5e-3, 2: 3e-2, 3: 0.6, 4: 12.0}
+        per_cell = {1: 5e-3, 2: 3e-2, 3: 0.6, 4: 7.0}
     elif wl.kind == "rtdq":
         per_cell = {1: 2e-3, 2: 2e-2, 3: 0.25, 4: 5.0}
     else:
@@ -231,10 +250,10 @@ def cpu_sample(wl, target_s, nthreads):
     per_depth = target_s * nthreads / max(1, len(depths))
     idx = []
     for d in depths:
-        cand = np.where(wl.cells["depth"] == d)[0]
-        k = int(max(1, min(len(cand), per_depth / per_cell.get(d, 1.0))))
-        idx.extend(cand[:k].tolist())
-    return np.array(sorted(idx))
+        cand = lo + np.where(depth == d)[0]
+        k = int(max(1, min(len(cand), max(per_depth / per_cell.get(d, 1.0), nthreads / len(depths)))))
+        idx.extend(cand[np.round(np.linspace(0, len(cand) - 1, k)).astype(int)].tolist())
+    return np.array(sorted(set(idx)))
 
 
 def time_oracle(wl, sel, nthreads):
@@ -290,48 +309,49 @@ def time_oracle(wl, sel, nthreads):
 
 
 # --------------------------------------------------------------------------- GPU
-def gpu_run(wl, lo, hi, precision, steps, warmup, local, stream, barrier, tune_info=None):
-    """Device-resident builds; returns per-step ms, mean solve / Galerkin ms, launches, reports.
-    With tune_info (a dict), msfec_autotune first picks the launch shape on a sample of the
-    shard (untimed) and its outcome is stored there."""
+def gpu_run(wl, lo, hi, precision, steps, warmup, local, stream, barrier, tune_info=None, batches=None):
+    """Device-resident builds of this rank's cells [lo, hi), one batch per step
+    (the steps cycle through `batches`, default batches_of(wl, lo, hi)).
+    Returns per-step ms, the work of the timed steps, mean solver / setup /
+    Galerkin ms per launch, launches, the reports of every cell built. With
+    tune_info (a dict), msfec_autotune first picks the launch shape on a sample
+    of the first batch (untimed) and its outcome is stored there."""
     import torch
     import msfec
     sh = wl.shard(lo, hi)
     cells = sh["cells"]
     nc = len(cells)
+    fo = np.concatenate([[0], np.cumsum(wl.nfine[lo:hi])]).astype(np.int64)
+    batches = [(a - lo, b - lo) for a, b in (batches or batches_of(wl, lo, hi))]
     h = msfec.Handle(precision=precision, device=local)
     h.set_stream(stream.cuda_stream)
     h.set_timing(True)
     nr = {"nedrt": 18, "qned": 20, "rtdq": 7}.get(wl.kind, 8)
-    d_KH = torch.zeros((nc, nr, nr), dtype=torch.float64, device="cuda")
-    d_FH = torch.zeros((nc, nr), dtype=torch.float64, device="cuda")
-    d_rep = torch.zeros(max(1, nc) * msfec.REPORT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
-    if wl.kind == "nedrt":
-        d_x = torch.from_numpy(sh["ainv6"]).cuda()
-        d_y = torch.from_numpy(sh["bdiv"]).cuda()
+    d_KH = torch.zeros((max(1, nc), nr, nr), dtype=torch.float64, device="cuda")
+    d_FH = torch.zeros((max(1, nc), nr), dtype=torch.float64, device="cuda")
+    rsz = msfec.REPORT_DTYPE.itemsize
+    d_rep = torch.zeros(max(1, nc) * rsz, dtype=torch.uint8, device="cuda")
+    names = {"nedrt": ("ainv6", "bdiv"), "qned": ("a6", "binv"), "rtdq": ("ainv6", None), "q1": ("a", "r")}[wl.kind]
+    widths = {"ainv6": 6, "a6": 6, "bdiv": 1, "binv": 1, "a": 1, "r": 1}
+    dev = {k: (None if (k is None or sh[k] is None) else torch.from_numpy(sh[k]).cuda()) for k in names}
 
-        def step():
-            h.nedrt_build_device(cells, d_x.data_ptr(), d_y.data_ptr(), wl.load, d_KH.data_ptr(),
-                                 d_FH.data_ptr(), d_rep.data_ptr())
-    elif wl.kind == "qned":
-        d_x = torch.from_numpy(sh["a6"]).cuda()
-        d_y = torch.from_numpy(sh["binv"]).cuda()
+    def ptr(k, a):  # device pointer of the first fine value of batch cell a
+        t = dev[k]
+        return 0 if t is None else t.data_ptr() + int(fo[a]) * widths[k] * 8
 
-        def step():
-            h.qned_build_device(cells, d_x.data_ptr(), d_y.data_ptr(), wl.load, d_KH.data_ptr(),
-                                d_FH.data_ptr(), d_rep.data_ptr())
-    elif wl.kind == "rtdq":
-        d_x = torch.from_numpy(sh["ainv6"]).cuda()
+    def build(a, b):
+        c = cells[a:b]
+        out = (d_KH.data_ptr() + a * nr * nr * 8, d_FH.data_ptr() + a * nr * 8, d_rep.data_ptr() + a * rsz)
+        x, y = ptr(names[0], a), (ptr(names[1], a) if names[1] else 0)
+        if wl.kind == "nedrt":
+            h.nedrt_build_device(c, x, y, wl.load, *out)
+        elif wl.kind == "qned":
+            h.qned_build_device(c, x, y, wl.load, *out)
+        elif wl.kind == "rtdq":
+            h.rtdq_build_device(c, x, wl.load, *out)
+        else:
+            h.q1_build_device(c, x, y, wl.load, *out)
 
-        def step():
-            h.rtdq_build_device(cells, d_x.data_ptr(), wl.load, d_KH.data_ptr(), d_FH.data_ptr(), d_rep.data_ptr())
-    else:
-        d_x = torch.from_numpy(sh["a"]).cuda()
-        d_y = None if sh["r"] is None else torch.from_numpy(sh["r"]).cuda()
-
-        def step():
-            h.q1_build_device(cells, d_x.data_ptr(), 0 if d_y is None else d_y.data_ptr(), wl.load,
-                              d_KH.data_ptr(), d_FH.data_ptr(), d_rep.data_ptr())
     if tune_info is not None and nc > 0 and wl.kind not in ("qned", "rtdq"):
         import sharding
         k = min(nc, 64 if wl.kind == "nedrt" else 512)  # several waves of items, seconds of trials
@@ -343,77 +363,97 @@ def gpu_run(wl, lo, hi, precision, steps, warmup, local, stream, barrier, tune_i
         choice, ncand, times = h.autotune(kind, cells[:k], c0, c1, wl.load)
         tune_info.update({"sample_cells": k, "candidates": ncand, "choice": choice,
                           "times_ms": [round(t, 3) for t in times]})
-    for _ in range(warmup):
-        step()
+    for i in range(warmup):
+        build(*batches[i % len(batches)])
     barrier()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    solve_ms, gal_ms, launches = [], [], 0
+    solve_ms, setup_ms, gal_ms, launches, work = [], [], [], 0, 0
+    pc = wl.per_cell_work()[lo:hi]
     e0.record(stream)
-    for _ in range(steps):
-        step()
+    for i in range(steps):
+        a, b = batches[i % len(batches)]
+        build(a, b)
         t = h.timings()
         solve_ms.append(t["solve_ms"])
+        setup_ms.append(max(0.0, t["setup_ms"]))
         gal_ms.append(t["galerkin_ms"])
         launches += t["kernel_launches"]
+        work += int(np.sum(pc[a:b]))
     e1.record(stream)
     barrier()
     ms = e0.elapsed_time(e1) / steps
+    built = sorted({batches[i % len(batches)] for i in range(max(steps, warmup))})
     rep = np.frombuffer(d_rep.cpu().numpy().tobytes(), dtype=msfec.REPORT_DTYPE)[:nc]
+    rep = np.concatenate([rep[a:b] for a, b in built]) if built else rep
     h.close()
-    return ms, float(np.mean(solve_ms)), float(np.mean(gal_ms)), launches, rep
+    return {"ms": ms, "work": work, "solve_ms": float(np.mean(solve_ms)), "setup_ms": float(np.mean(setup_ms)),
+            "gal_ms": float(np.mean(gal_ms)), "launches": launches, "rep": rep,
+            "batch": batches[0], "nbatches": len(batches)}
 
 
 def e2e_run(wl, lo, hi, local, stream, barrier, steps):
-    """Through the host-buffer C ABI: pinned inputs, H2D + build + D2H per step."""
+    """Through the host-buffer C ABI: pinned inputs, H2D + build + D2H per step,
+    one batch per step (cycling through the batches of [lo, hi))."""
     import torch
     import msfec
     sh = wl.shard(lo, hi)
     cells = sh["cells"]
+    fo = np.concatenate([[0], np.cumsum(wl.nfine[lo:hi])]).astype(np.int64)
+    batches = [(a - lo, b - lo) for a, b in batches_of(wl, lo, hi)]
     h = msfec.Handle(precision=msfec.PRECISION_MIXED, device=local)
     h.set_stream(stream.cuda_stream)
     pin = lambda a: None if a is None else torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
-    if wl.kind == "nedrt":
-        x, y = pin(sh["ainv6"]), pin(sh["bdiv"])
-        call = lambda: h.nedrt_build(cells, x, y, wl.load)  # noqa: E731
-        h2d = x.nbytes + y.nbytes
-        nr = 18
-    elif wl.kind == "qned":
-        x, y = pin(sh["a6"]), pin(sh["binv"])
-        call = lambda: h.qned_build(cells, x, y, wl.load)  # noqa: E731
-        h2d = x.nbytes + y.nbytes
-        nr = 20
-    elif wl.kind == "rtdq":
-        x = pin(sh["ainv6"])
-        call = lambda: h.rtdq_build(cells, x, wl.load)  # noqa: E731
-        h2d = x.nbytes
-        nr = 7
-    else:
-        x, y = pin(sh["a"]), pin(sh["r"])
-        call = lambda: h.q1_build(cells, x, y, wl.load)  # noqa: E731
-        h2d = x.nbytes + (0 if y is None else y.nbytes)
-        nr = 8
-    call()
+    nr = {"nedrt": 18, "qned": 20, "rtdq": 7}.get(wl.kind, 8)
+    names = {"nedrt": ("ainv6", "bdiv"), "qned": ("a6", "binv"), "rtdq": ("ainv6", None), "q1": ("a", "r")}[wl.kind]
+    host = {k: (None if k is None else pin(sh[k])) for k in names}
+
+    def call(a, b):
+        f0, f1 = int(fo[a]), int(fo[b])
+        x = host[names[0]][f0:f1]
+        y = None if (names[1] is None or host[names[1]] is None) else host[names[1]][f0:f1]
+        if wl.kind == "nedrt":
+            h.nedrt_build(cells[a:b], x, y, wl.load)
+        elif wl.kind == "qned":
+            h.qned_build(cells[a:b], x, y, wl.load)
+        elif wl.kind == "rtdq":
+            h.rtdq_build(cells[a:b], x, wl.load)
+        else:
+            h.q1_build(cells[a:b], x, y, wl.load)
+        return x.nbytes + (0 if y is None else y.nbytes) + (b - a) * msfec.CELL_DTYPE.itemsize, \
+            (b - a) * ((nr * nr + nr) * 8 + msfec.REPORT_DTYPE.itemsize)
+
+    call(*batches[0])
     barrier()
+    h2d = d2h = 0
+    pc = wl.per_cell_work()[lo:hi]
+    work = 0
     t0 = time.perf_counter()
-    for _ in range(steps):
-        call()
+    for i in range(steps):
+        a, b = batches[i % len(batches)]
+        bi, bo = call(a, b)
+        h2d += bi
+        d2h += bo
+        work += int(np.sum(pc[a:b]))
     barrier()
     dt = (time.perf_counter() - t0) / steps
     h.close()
-    h2d += len(cells) * msfec.CELL_DTYPE.itemsize
-    d2h = len(cells) * (nr * nr + nr) * 8 + len(cells) * msfec.REPORT_DTYPE.itemsize
-    return dt, h2d, d2h
+    return dt, work / steps, h2d // steps, d2h // steps
 
 
 # DRAM bytes per coarse cell of one Ned_RT depth-3 solve launch (mixed precision, multilevel
 # preconditioner): ncu dram__bytes_read.sum + dram__bytes_write.sum of `bench.py --probe nedrt_256cells`
 # (profiles/nedrt_solve_kernel_L3_traffic.md), 358.2 MB / 256 cells; traffic grows with the cells.
 NEDRT_L3_TRAFFIC_PER_CELL = 358.2e6 / 256
+# The same for depth-4 cells (global MINRES workspace): ncu DRAM bytes of
+# `bench.py --probe nedrt_depth4_8cells` per cell (profiles/nedrt_solve_kernel_L4_8cells.md).
+NEDRT_L4_TRAFFIC_PER_CELL = None
 
 
-def roofline(wl, lo, hi, solve_ms, gal_ms, rep, kind):
-    """Roofline of the dominant (solver) kernel and of the Galerkin kernel."""
+def roofline(wl, lo, hi, solve_ms, setup_ms, gal_ms, rep, kind):
+    """Roofline of the dominant (solver) kernel over one launch = one batch
+    [lo, hi) of cells, and of the Galerkin kernel. rep: reports of the batch's
+    cells (per-RHS iteration sums for the flop model)."""
     peak, peak_kind = peaks()
     c = wl.cells[lo:hi]
     n = 1 << c["depth"].astype(np.int64)
@@ -437,30 +477,27 @@ def roofline(wl, lo, hi, solve_ms, gal_ms, rep, kind):
     else:
         ndof = int(np.sum((n + 1) ** 3))
         nrhs, coef_bytes = 8, 8 * (1 if wl.r is None else 2)
-        # FP32 flops per Krylov iteration of one item: 27-point apply (2 x 35) + recurrences (~20)
+        # FP32 flops per Krylov iteration of one RHS: 27-point apply (2 x 35) + recurrences (~20)
         flops_iter = 90 * (n - 1) ** 3
     # algorithmic HBM bytes of one solver launch: coefficients in, basis and K*basis out (FP64)
     alg_solve = nfine * coef_bytes + ndof * nrhs * 8 * 2
     alg_gal = ndof * nrhs * 8 * 2 + len(c) * (nrhs * nrhs + nrhs) * 8
-    iters = rep["iterations"].astype(np.float64)  # max over the cell's RHS (upper estimate)
-    per_cell_flops = flops_iter * iters * (nrhs if wl.kind in ("nedrt", "qned", "rtdq") else 8)
-    tflops = float(np.sum(per_cell_flops)) / (solve_ms * 1e-3) / 1e12
-    return {"bound": "hbm", "kernel": f"{kind}_solve_kernel (persistent, on-chip Krylov state)",
-            "achieved": alg_solve / (solve_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
-            "frac": alg_solve / (solve_ms * 1e-3) / 1e9 / peak,
-            "traffic": (NEDRT_L3_TRAFFIC_PER_CELL * len(c)
-                        if wl.kind == "nedrt" and bool(np.all(c["depth"] == 3)) else None),
-            "algorithmic_bytes": alg_solve, "launch_ms": solve_ms, "peak_source": peak_kind,
-            "note": "Krylov vectors stay in shared memory/registers: HBM carries only coefficients "
-                    "in and basis + K*basis out, so this fraction is low by design; the on-chip "
-                    "FP32 rate below is the binding roofline",
+    # per-RHS iteration counts: the report's sum over the cell's right-hand sides
+    iters = rep["iterations_sum"].astype(np.float64)
+    tflops = float(np.sum(flops_iter * iters)) / (solve_ms * 1e-3) / 1e12
+    achieved = alg_solve / (solve_ms * 1e-3) / 1e9
+    traffic = None
+    if wl.kind == "nedrt" and NEDRT_L4_TRAFFIC_PER_CELL and bool(np.all(c["depth"] == 4)):
+        traffic = NEDRT_L4_TRAFFIC_PER_CELL * len(c)
+    elif wl.kind == "nedrt" and bool(np.all(c["depth"] == 3)):
+        traffic = NEDRT_L3_TRAFFIC_PER_CELL * len(c)
+    return {"bound": "hbm", "kernel": f"{kind}_solve_kernel", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": traffic, "algorithmic_bytes": alg_solve, "launch_ms": solve_ms,
+            "cells_per_launch": len(c), "setup_ms": setup_ms, "peak_source": peak_kind,
             "onchip": {"bound": "fp32", "achieved_tflops": tflops, "peak_tflops_nominal": FP32_NOMINAL_TFLOPS,
-                       "frac": tflops / FP32_NOMINAL_TFLOPS,
-                       "flops_model": "per Krylov iteration of one RHS: operator + recurrences, "
-                                      "x iterations (max over the cell's RHS)"},
-            "galerkin": {"kernel": f"{kind}_galerkin_kernel (FP64 DMMA m8n8k4)", "launch_ms": gal_ms,
-                         "achieved": alg_gal / (gal_ms * 1e-3) / 1e9,
-                         "frac": alg_gal / (gal_ms * 1e-3) / 1e9 / peak, "algorithmic_bytes": alg_gal}}
+                       "frac": tflops / FP32_NOMINAL_TFLOPS},
+            "galerkin": {"launch_ms": gal_ms, "achieved": alg_gal / (gal_ms * 1e-3) / 1e9,
+                         "frac": alg_gal / (gal_ms * 1e-3) / 1e9 / peak}}
 
 
 def adjoint_timing(local, stream, steps=3):
@@ -500,13 +537,24 @@ def adjoint_timing(local, stream, steps=3):
             "note": "host-buffer C ABI for both; backward = 2 adjoint local problems per cell + gradient kernel"}
 
 
-def adjoint_timing_nedrt(local, stream, steps=3):
-    """Backward / forward time of the Ned_RT adjoint on coarse 8^3 x depth 3 (the
-    headline batch, 512 observation points): forward = msfec_nedrt_build, backward
-    = msfec_nedrt_backward reusing the stored basis (host buffers for both)."""
+def adjoint_timing_nedrt(local, stream, wl=None, lo=0, hi=None, steps=2):
+    """Backward / forward time of the Ned_RT adjoint on cells [lo, hi) of the
+    Ned_RT workload `wl` (default the coarse 8^3 x depth 3 batch), misfit J of
+    the coarse u field at 512 seeded observation points (host buffers for
+    both): forward = msfec_nedrt_build; backward = msfec_nedrt_backward with
+    the basis recomputed (reuse_basis off: the basis is not kept between the
+    passes, as when it does not fit beside the adjoint state) and reusing the
+    stored basis."""
     import msfec
     import workloads
-    cells, ainv6, bdiv, load = workloads.nedrt_tensor(m=8, depth=3, seed=2)
+    if wl is None:
+        cells, ainv6, bdiv, load = workloads.nedrt_tensor(m=8, depth=3, seed=2)
+        name = "nedrt_tensor_coarse8^3_L3"
+    else:
+        hi = len(wl.cells) if hi is None else hi
+        f0, f1 = int(wl.foff[lo]), int(wl.foff[hi])
+        cells, ainv6, bdiv, load = wl.cells[lo:hi], wl.ainv6[f0:f1], wl.bdiv[f0:f1], wl.load
+        name = f"{wl.cfg['workload']} cells [{lo}, {hi})"
     rng = np.random.default_rng(7)
     npts = 512
     cell_of = rng.integers(0, len(cells), npts).astype(np.int32)
@@ -518,21 +566,85 @@ def adjoint_timing_nedrt(local, stream, steps=3):
     h.set_stream(stream.cuda_stream)
     h.nedrt_build(cells, ainv6, bdiv, load)
     h.nedrt_backward(cells, ainv6, bdiv, load, U, lam, cell_of, pts, g)
-    fw, bw = [], []
+    fw, bw, br = [], [], []
     for _ in range(steps):
         t0 = time.perf_counter()
         h.nedrt_build(cells, ainv6, bdiv, load)
         t1 = time.perf_counter()
         h.nedrt_backward(cells, ainv6, bdiv, load, U, lam, cell_of, pts, g, reuse_basis=True)
         t2 = time.perf_counter()
+        h.nedrt_backward(cells, ainv6, bdiv, load, U, lam, cell_of, pts, g, reuse_basis=False)
+        t3 = time.perf_counter()
         fw.append(t1 - t0)
         bw.append(t2 - t1)
+        br.append(t3 - t2)
     h.close()
-    f, b = float(np.median(fw)), float(np.median(bw))
-    return {"workload": "nedrt_tensor_coarse8^3_L3, 512 observation points", "forward_ms": f * 1e3,
-            "backward_ms": b * 1e3, "bwd_over_fwd": b / f,
-            "note": "host-buffer C ABI for both; backward = 4 adjoint local problems per cell (vs 18 basis "
-                    "problems forward) + gradient kernel, d/dlog A and d/dlog B"}
+    f, b, r = float(np.median(fw)), float(np.median(bw)), float(np.median(br))
+    return {"workload": f"{name}, 512 observation points", "forward_ms": f * 1e3,
+            "backward_recompute_basis_ms": r * 1e3, "bwd_recompute_over_fwd": r / f,
+            "backward_reuse_basis_ms": b * 1e3, "bwd_reuse_over_fwd": b / f}
+
+
+def _r(x, digits=4):
+    """Round floats (recursively) to `digits` significant digits: a compact line."""
+    if isinstance(x, float):
+        return float(f"{x:.{digits}g}") if np.isfinite(x) else x
+    if isinstance(x, dict):
+        return {k: _r(v, digits) for k, v in x.items()}
+    if isinstance(x, (list, tuple)):
+        return [_r(v, digits) for v in x]
+    return x
+
+
+def start_parity(wl, lo, hi, ncells=3):
+    """Oracle results of `ncells` cells spread over the first batch of [lo, hi),
+    computed in a spawn-started pool while the GPU runs (checker only)."""
+    if wl.kind not in ("nedrt", "q1"):
+        return None
+    from oracle import parity
+    a, b = batches_of(wl, lo, hi)[0]
+    sel = parity.stratified_sample(wl.cells[a:b], ncells) + a
+    coef = (wl.ainv6, wl.bdiv) if wl.kind == "nedrt" else (wl.a, wl.r)
+    return parity.OracleSample(wl.kind, wl.cells, sel, coef, wl.load, processes=ncells)
+
+
+def finish_parity(wl, lo, hi, sample, local, stream):
+    """GPU builds of the first batch (mixed) and of the sampled cells alone
+    (FP64) through the host C ABI, against the oracle on the sampled cells."""
+    import msfec
+    from oracle import parity
+    a, b = batches_of(wl, lo, hi)[0]
+    sel = sample.sel
+    out = {"cells": [int(c) for c in sel], "batch": [a, b], "tolerance": 1e-10}
+    for prec, tag in ((msfec.PRECISION_MIXED, "mixed"), (msfec.PRECISION_FP64, "fp64")):
+        h = msfec.Handle(precision=prec, device=local)
+        h.set_stream(stream.cuda_stream)
+        if tag == "mixed":
+            sub, first = wl.cells[a:b], a
+        else:  # the sampled cells as a batch of their own
+            sub, first = wl.cells[sel], None
+        f = lambda arr, cs: None if arr is None else np.concatenate(  # noqa: E731
+            [arr[wl.foff[c]:wl.foff[c + 1]] for c in cs])
+        cs = range(a, b) if tag == "mixed" else sel
+        if wl.kind == "nedrt":
+            KHs, FHs, rep, st = h.nedrt_build(sub, f(wl.ainv6, cs), f(wl.bdiv, cs), wl.load)
+            basis = h.nedrt_basis_cells
+        else:
+            KHs, FHs, rep, st = h.q1_build(sub, f(wl.a, cs), f(wl.r, cs), wl.load)
+            basis = h.q1_basis_cells
+        nb = KHs.shape[1]
+        KH = np.zeros((len(wl.cells), nb, nb))
+        FH = np.zeros((len(wl.cells), nb))
+        pos = {int(c): (c - first if first is not None else i) for i, c in enumerate(sel)}
+        if first is not None:
+            KH[a:b], FH[a:b] = KHs, FHs
+        else:
+            KH[sel], FH[sel] = KHs, FHs
+        err = parity.compare(sample, KH, FH, lambda c: basis(sub, int(pos[c]), 1)[0])
+        h.close()
+        out[tag] = {"KH_max_rel": err["KH_max_rel"], "FH_max_rel": err["FH_max_rel"],
+                    "Phi_max_rel": err["Phi_max_rel"], "converged": bool(rep["converged"].all())}
+    return out
 
 
 def run_ours(args):
@@ -559,71 +671,100 @@ def run_ours(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
-    def measure(name, steps, warmup, fp64_steps, with_clocks):
-        wl = Workload(name)
+    def measure(wl, steps, warmup, fp64_steps, with_clocks, full_pass=False):
         lo, hi = rank_share(wl)
-        total = wl.work() * world  # DoF x RHS of all ranks
         sampler = ClockSampler(local)
         if with_clocks:
             sampler.start()
         tune = {}
-        ms, solve_ms, gal_ms, launches, rep = gpu_run(wl, lo, hi, msfec.PRECISION_MIXED, steps, warmup, local,
-                                                      stream, barrier, tune_info=tune)
+        r = gpu_run(wl, lo, hi, msfec.PRECISION_MIXED, steps, warmup, local, stream, barrier, tune_info=tune)
         clocks = sampler.stop() if with_clocks else None
-        ms = reduce_max(ms)
-        out = {"wl": wl, "lo": lo, "hi": hi, "value": total / (ms * 1e-3), "ms_per_step": ms, "clocks": clocks,
-               "launches": launches, "converged": bool(rep["converged"].all()),
-               "max_iterations": int(rep["iterations"].max()) if len(rep) else 0, "work_dof_rhs": total,
-               "roofline": roofline(wl, lo, hi, solve_ms, gal_ms, rep, wl.kind), "autotune": tune}
+        ms = reduce_max(r["ms"])
+        step_work = r["work"] / steps
+        a, b = r["batch"]
+        out = {"lo": lo, "hi": hi, "value": step_work * world / (ms * 1e-3), "ms_per_step": ms, "clocks": clocks,
+               "launches": r["launches"], "converged": bool(r["rep"]["converged"].all()),
+               "max_iterations": int(r["rep"]["iterations"].max()) if len(r["rep"]) else 0,
+               "work_dof_rhs": int(step_work * world), "batches": r["nbatches"],
+               "roofline": roofline(wl, lo + a, lo + b, r["solve_ms"], r["setup_ms"], r["gal_ms"],
+                                    r["rep"][: b - a], wl.kind),
+               "autotune": tune}
         if fp64_steps > 0:
-            tune64 = {}
-            ms64, s64, g64, _, rep64 = gpu_run(wl, lo, hi, msfec.PRECISION_FP64, fp64_steps, 1, local, stream,
-                                               barrier, tune_info=tune64)
-            ms64 = reduce_max(ms64)
-            out["fp64_path"] = {"value": total / (ms64 * 1e-3), "ms_per_step": ms64, "solve_ms": s64,
-                                "steps": fp64_steps, "converged": bool(rep64["converged"].all()),
-                                "mixed_over_fp64": ms64 / ms, "autotune": tune64}
+            ns = min(hi - lo, 64 if wl.kind in ("nedrt", "qned", "rtdq") else 512)
+            r64 = gpu_run(wl, lo, hi, msfec.PRECISION_FP64, fp64_steps, 1, local, stream, barrier,
+                          batches=[(lo, lo + ns)])
+            ms64 = reduce_max(r64["ms"])
+            v64 = r64["work"] / fp64_steps / (ms64 * 1e-3)
+            out["fp64_path"] = {"value": v64 * world, "ms_per_step": ms64, "cells": ns,
+                                "converged": bool(r64["rep"]["converged"].all()),
+                                "mixed_over_fp64": out["value"] / (v64 * world)}
+        if full_pass and len(batches_of(wl, lo, hi)) > 1:
+            rf = gpu_run(wl, lo, hi, msfec.PRECISION_MIXED, 1, 0, local, stream, barrier, batches=[(lo, hi)])
+            dev_ms = reduce_max(rf["solve_ms"] + rf["setup_ms"] + rf["gal_ms"])
+            out["full_pass"] = {"cells": hi - lo, "device_ms": dev_ms,
+                                "value": rf["work"] * world / (dev_ms * 1e-3),
+                                "converged": bool(rf["rep"]["converged"].all())}
         return out
 
-    head = measure(args.workload, args.steps, args.warmup, 0 if args.skip_fp64 else max(1, min(args.steps, 2)),
-                   True)
-    wl, lo, hi = head["wl"], head["lo"], head["hi"]
-    e2e_s, h2d, d2h = e2e_run(wl, lo, hi, local, stream, barrier, max(1, min(args.steps, 3)))
+    wl = Workload(args.workload)
+    lo, hi = rank_share(wl)
+    psample = start_parity(wl, lo, hi) if (rank == 0 and not args.skip_parity) else None
+    head = measure(wl, args.steps, args.warmup, 0 if args.skip_fp64 else max(1, min(args.steps, 2)), True,
+                   full_pass=not args.skip_extra)
+    e2e_s, e2e_work, h2d, d2h = e2e_run(wl, lo, hi, local, stream, barrier, max(1, min(args.steps, 3)))
     e2e_s = reduce_max(e2e_s)
     extras = {}
     if not args.skip_extra and args.extra:
         for name in args.extra.split(","):
-            ex = measure(name, max(3, min(args.steps, 5)), 3, 0 if args.skip_fp64 else 2, False)
-            extras[name] = {k: ex[k] for k in ("value", "ms_per_step", "converged", "max_iterations",
-                                               "work_dof_rhs", "roofline", "fp64_path", "autotune") if k in ex}
-            extras[name]["config"] = ex["wl"].cfg
+            if name == args.workload:
+                continue
+            ex = measure(Workload(name), max(3, min(args.steps, 5)), 3, 0 if args.skip_fp64 else 2, False)
+            rf = ex["roofline"]
+            extras[name] = {"value": ex["value"], "ms_per_step": ex["ms_per_step"], "converged": ex["converged"],
+                            "max_iterations": ex["max_iterations"], "work_dof_rhs": ex["work_dof_rhs"],
+                            "solve_launch_ms": rf["launch_ms"], "hbm_frac": rf["frac"],
+                            "fp32_tflops": rf["onchip"]["achieved_tflops"]}
+            if "fp64_path" in ex:
+                extras[name]["fp64_value"] = ex["fp64_path"]["value"]
+                extras[name]["mixed_over_fp64"] = ex["fp64_path"]["mixed_over_fp64"]
+    adjoint = {}
     if not args.skip_extra and not args.skip_adjoint:
-        extras["adjoint_q1"] = adjoint_timing(local, stream)
-        extras["adjoint_nedrt"] = adjoint_timing_nedrt(local, stream)
+        adjoint["q1"] = adjoint_timing(local, stream)
+        if wl.kind == "nedrt" and bool(np.all(wl.cells["depth"] == 4)):
+            a, b = (lo, hi) if args.adjoint_full else batches_of(wl, lo, hi)[0]
+            adjoint["nedrt"] = adjoint_timing_nedrt(local, stream, wl, a, b, steps=1 if args.adjoint_full else 2)
+        else:
+            adjoint["nedrt"] = adjoint_timing_nedrt(local, stream)
     if rank != 0:
         if dist is not None:
             dist.destroy_process_group()
         return
+    par = finish_parity(wl, lo, hi, psample, local, stream) if psample is not None else None
     cpu = None
     if not args.skip_cpu:
         nthreads = os.cpu_count() or 1
-        sel = cpu_sample(wl, args.cpu_seconds, nthreads)
+        sel = cpu_sample(wl, args.cpu_seconds, nthreads, lo, hi)
         v, dt, desc = time_oracle(wl, sel, nthreads)
         cpu = {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": desc}
+    nb = head["batches"]
     line = {"metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-            "config": dict(wl.cfg, precision="mixed (FP32 Krylov + FP64 refinement)",
+            "config": dict(wl.cfg, batch_cells=wl.batch_cells, batches=nb,
+                           step=(f"one batch of {wl.batch_cells} cells, cycling through the {nb} batches"
+                                 if nb > 1 else "the whole batch"),
+                           precision="mixed (FP32 Krylov + FP64 refinement)",
                            l2="inputs + basis exceed L2 (129 MB): Phi and K*Phi are written fresh every step",
-                           parallelism=f"{world} GPU(s), one full batch of independent coarse cells each"),
+                           parallelism=f"{world} GPU(s), the whole workload on each (weak)"),
             "roofline": head["roofline"], "cpu_baseline": cpu,
-            "e2e": {"value": head["work_dof_rhs"] / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+            "e2e": {"value": e2e_work * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(head["launches"]), "clocks": head["clocks"],
-            "fp64_path": head.get("fp64_path"), "converged": head["converged"],
-            "max_iterations": head["max_iterations"], "work_dof_rhs": head["work_dof_rhs"],
-            "autotune": head.get("autotune"), "extra": extras}
-    print(json.dumps(line), flush=True)
+            "converged": head["converged"], "max_iterations": head["max_iterations"],
+            "work_dof_rhs": head["work_dof_rhs"], "full_pass": head.get("full_pass"),
+            "fp64_path": head.get("fp64_path"), "parity": par, "autotune": head.get("autotune"),
+            "adjoint": adjoint, "extra": extras}
+    print(json.dumps(_r(line)), flush=True)
     if dist is not None:
         dist.destroy_process_group()
 
@@ -634,7 +775,7 @@ def run_reference(args):
         return
     wl = Workload(args.workload)
     nthreads = os.cpu_count() or 1
-    sel = cpu_sample(wl, args.cpu_seconds / 2.0, nthreads)
+    sel = cpu_sample(wl, args.cpu_seconds / 2.0, nthreads, *batches_of(wl, 0, len(wl.cells))[0])
     for _ in range(args.warmup):
         time_oracle(wl, sel[: max(1, len(sel) // 8)], nthreads)
     vals, dts = [], []
@@ -646,11 +787,11 @@ def run_reference(args):
     value = float(np.median(vals))
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": float(np.median(dts) * 1e3), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": wl.cfg,
-            "impl": "reference",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": dict(wl.cfg, batch_cells=wl.batch_cells), "impl": "reference",
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": desc},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
+    print(json.dumps(_r(line)), flush=True)
 
 
 def probe(name):
@@ -661,6 +802,9 @@ def probe(name):
     h.set_timing(True)
     if name == "nedrt_one_cell":
         cells, ainv6, bdiv, load = workloads.nedrt_tensor(m=1, depth=3, seed=2)
+        KH, FH, rep, st = h.nedrt_build(cells, ainv6, bdiv, load)
+    elif name == "nedrt_depth4_8cells":  # 144 depth-4 items: about one wave of the 152 SMs
+        cells, ainv6, bdiv, load = workloads.nedrt_tensor(m=2, depth=4, seed=5)
         KH, FH, rep, st = h.nedrt_build(cells, ainv6, bdiv, load)
     elif name == "nedrt_256cells":  # first half of the headline batch: basis + K*basis 271 MB > L2
         cells, ainv6, bdiv, load = workloads.nedrt_tensor(m=8, depth=3, seed=2)
@@ -679,17 +823,20 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="nedrt_small",
+    ap.add_argument("--workload", default="nedrt_large",
                     choices=["nedrt_small", "nedrt_l4", "nedrt_large", "qned_small", "rtdq_small", "q1_uneven", "q1_small",
                              "q1_adjoint_fwd"])
-    ap.add_argument("--extra", default="q1_uneven,qned_small,rtdq_small",
+    ap.add_argument("--extra", default="nedrt_small,q1_uneven,qned_small,rtdq_small",
                     help="comma-separated workloads reported beside the headline")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-extra", action="store_true")
     ap.add_argument("--skip-adjoint", action="store_true")
-    ap.add_argument("--probe", default=None, choices=["nedrt_one_cell", "nedrt_256cells", "q1_depth5_one_cell", "q1_depth3_8cells"],
+    ap.add_argument("--skip-parity", action="store_true")
+    ap.add_argument("--adjoint-full", action="store_true",
+                    help="time the Ned_RT adjoint on every cell of the headline workload (default: its first batch)")
+    ap.add_argument("--probe", default=None, choices=["nedrt_one_cell", "nedrt_depth4_8cells", "nedrt_256cells", "q1_depth5_one_cell", "q1_depth3_8cells"],
                     help="run one small mixed build and exit (the case profiled with ncu --set full)")
     args = ap.parse_args()
     if args.probe:

@@ -100,8 +100,21 @@ typedef struct msfec_config {
      0 = multilevel (diagonal + coarse RT levels n/2 .. 4 + exact level 2),
      1 = diagonal only. */
   int32_t nedrt_precond;
-  int32_t reserved;
+  /* Layout of the Q1 diffusion coefficient `a` (msfec_q1_coefficient):
+     SCALAR one value per fine cell (default); TENSOR a symmetric positive
+     definite A per fine cell, 6 doubles a00 a11 a22 a01 a02 a12; GAUSS A at
+     each of the fine cell's 2x2x2 Gauss points, 8 x 6 doubles (points x
+     fastest at 0.5 -+ 1/(2 sqrt 3) of the cell), which is what the
+     reference's Diffusion_A::value_list gives its assembly
+     (source/equation_data/eqn_coeff_A.cc:162-191, q_basis.cc:218-231). */
+  int32_t q1_coefficient;
 } msfec_config;
+
+typedef enum msfec_q1_coefficient {
+  MSFEC_Q1_COEF_SCALAR = 0,
+  MSFEC_Q1_COEF_TENSOR = 1,
+  MSFEC_Q1_COEF_GAUSS = 2
+} msfec_q1_coefficient;
 
 typedef struct msfec_cell {
   double origin[3];
@@ -114,7 +127,7 @@ typedef struct msfec_cell_report {
   int32_t iterations;  /* Krylov iterations summed over refinement steps, max over RHS */
   int32_t refinements; /* FP64 residual evaluations */
   int32_t converged;   /* 1 if every RHS of the cell met rtol */
-  int32_t reserved;
+  int32_t iterations_sum; /* Krylov iterations summed over refinement steps and over the cell's RHS */
   double residual;     /* max over RHS of ||r||_2 / ||K_IB g||_2 */
 } msfec_cell_report;
 
@@ -140,7 +153,11 @@ msfec_status msfec_set_precision(msfec_handle *handle, int32_t precision);
  * Replaces QBasis::run (q_basis.cc:518-603) for every cell of the batch,
  * followed by get_global_element_matrix / get_global_element_rhs
  * (q_basis.cc:361-373).
- *   a        diffusion coefficient per fine cell (> 0), FP64
+ *   a        diffusion coefficient per fine cell, FP64, in the handle's
+ *            q1_coefficient layout: a > 0 (SCALAR), an SPD tensor (TENSOR),
+ *            an SPD tensor at each Gauss point (GAUSS). The tensor layouts
+ *            run a cell-wise quadrature apply (the reference's assembly
+ *            loop) instead of the scalar 27-point stencil.
  *   reaction reaction coefficient per fine cell, or NULL for none (the
  *            reference's ReactionRate is zero, eqn_coeff_R.cc:7-14)
  *   KH       [ncells][8][8], FH [ncells][8], reports [ncells] or NULL
@@ -168,7 +185,10 @@ msfec_status msfec_q1_build_device(msfec_handle *handle, int32_t ncells,
  *   U        [ncells][8] coarse solution restricted to each cell (vertex order)
  *   lambda   [ncells][8] coarse adjoint K_H^-1 dJ/dU restricted to each cell
  *   points   [npoints][3] in cell cell_of[p]; dJ_du[p] = dJ / d u_H(points[p])
- *   grad     [fine cells] output, total derivative dJ / d log a_e
+ *   grad     [fine cells] output, total derivative dJ / d log a_e; for the
+ *            tensor layouts (q1_coefficient TENSOR / GAUSS) the derivative
+ *            with respect to theta_e in A_e -> exp(theta_e) A_e (every
+ *            Gauss-point tensor of the fine cell scaled together)
  * Two adjoint local problems per cell (load and observation bubbles) run
  * through the batched local solver; no basis sensitivity is solved for
  * because the multiscale basis is K-harmonic. With reuse_basis != 0 the
@@ -191,7 +211,7 @@ msfec_status msfec_q1_backward(msfec_handle *handle, int32_t ncells,
    handle's stream when timing is enabled (the reference's TimerOutput scopes,
    source/Q/q_global.cc:21-24). Milliseconds; -1 when not measured. */
 typedef struct msfec_timings {
-  float solve_ms;    /* persistent local-solver kernel */
+  float solve_ms;    /* persistent local-solver kernel (alone; see setup_ms) */
   float galerkin_ms; /* Phi^T K Phi / Phi^T f contraction */
   float total_ms;    /* whole build on the device, H2D/D2H excluded */
   int32_t solve_launches;
@@ -199,6 +219,9 @@ typedef struct msfec_timings {
   /* 0: launched directly; 1: captured into a new CUDA graph, then launched;
      2: replayed the cached graph (solve_ms then covers the whole graph) */
   int32_t graph;
+  /* preconditioner setup kernel before the solver (Ned_RT multilevel
+     data); 0 when the build ran none */
+  float setup_ms;
 } msfec_timings;
 
 msfec_status msfec_set_timing(msfec_handle *handle, int32_t enable);
@@ -227,6 +250,15 @@ int64_t msfec_q1_basis_size(const msfec_handle *handle);
 /* Copy the last Q1 build's basis to host memory (capacity in doubles). */
 msfec_status msfec_q1_get_basis(msfec_handle *handle, double *Phi,
                                 int64_t capacity);
+
+/* Copy the basis of cells [first, first + count) of the last Q1 build (in
+   the batch's cell order, 8 (n+1)^3 doubles per cell) to host memory: the
+   per-cell basis of the reference's QBasis objects (each holds its own
+   basis_solution, source/Q/q_basis.h:77-139) without copying the whole
+   batch. capacity in doubles. */
+msfec_status msfec_q1_get_basis_cells(msfec_handle *handle, int32_t first,
+                                      int32_t count, double *Phi,
+                                      int64_t capacity);
 
 /* Device pointer of the last Q1 build's basis (read-only, valid until the
    next build on this handle). */
@@ -322,23 +354,29 @@ msfec_status msfec_nedrt_build_device(msfec_handle *handle, int32_t ncells,
  * callers that must not allocate device memory while they build: a solver
  * whose pooling allocator already holds nearly all of HBM, or a rank whose
  * other streams must not be stalled by the device-wide synchronisation of
- * cudaMalloc / cudaFree. Same arguments, results and asynchrony as
- * msfec_nedrt_build_device (identical K_H, F_H, reports), but every internal
- * buffer comes from one static device pool of 32 MiB per device that is part
- * of the library image; nothing is allocated on the device (host memory only
- * to format an error message). A batch whose cell table, basis Phi, Y = A Phi
- * and status (about 1.06 MB per depth-3 cell, 7.76 MB per depth-4 cell) do not
- * fit, or that holds more than 4096 cells, is rejected with
- * MSFEC_ERROR_INVALID_ARGUMENT and a message naming the bytes needed; split
- * it. Depth-4 cells also take 0.99 MB (mixed) / 1.75 MB (FP64) of MINRES
- * workspace per concurrent CTA from the pool, so fewer CTAs run when space is
- * short. The first call on each device looks up the pool's address (and may
- * load the library's module for it): make that first call before any stream
- * capture. The basis stays in the pool (msfec_nedrt_get_basis still returns
- * the last handle-owned build) and is overwritten by the next call. There is
- * one pool per device and process: calls that overlap in time on the same
- * device (other threads, handles or streams) race and corrupt each other's
- * results; serialise them on one stream.
+ * cudaMalloc / cudaFree. Same arguments, asynchrony, launch shape and
+ * preconditioner as msfec_nedrt_build_device on the same handle (the
+ * multilevel face preconditioner for depth >= 2 unless nedrt_precond = 1, the
+ * autotuned split / CTA choices), hence the same K_H, F_H and reports up to
+ * the last bits of the shared-memory atomic sums; but every internal buffer
+ * comes from one static device pool of 32 MiB per device that is part of the
+ * library image; nothing is allocated on the device (host memory only to
+ * format an error message). A batch whose cell table, multilevel data, basis
+ * Phi, Y = A Phi and status (about 1.06 MB per depth-3 cell, 7.82 MB per
+ * depth-4 cell) do not fit, or that holds more than 4096 cells, is rejected
+ * with MSFEC_ERROR_INVALID_ARGUMENT and a message naming the bytes needed;
+ * split it. Depth-4 cells also take 0.99 MB (mixed) / 1.75 MB (FP64) of
+ * MINRES workspace per concurrent CTA from the rest of the pool, so fewer
+ * CTAs run when space is short. Every call looks up the pool's address on
+ * the current device; the first call on a device may load the library's
+ * module for it: make that first call before any stream capture. The basis
+ * stays in the pool and is overwritten by the next call: msfec_nedrt_get_basis
+ * still returns the last handle-owned build, and msfec_nedrt_backward with
+ * reuse_basis set rebuilds the basis (it never reuses a pool basis or an older
+ * handle-owned one after this call). There is one pool per device and
+ * process: calls that overlap in time on the same device (other threads,
+ * handles or streams) race and corrupt each other's results; serialise them
+ * on one stream.
  */
 msfec_status msfec_nedrt_build_noalloc(msfec_handle *handle, int32_t ncells,
                                        const msfec_cell *cells,
@@ -480,6 +518,16 @@ msfec_status msfec_rtdq_get_basis(msfec_handle *handle, double *Phi,
 int64_t msfec_nedrt_basis_size(const msfec_handle *handle);
 msfec_status msfec_nedrt_get_basis(msfec_handle *handle, double *Phi,
                                    int64_t capacity);
+
+/* Copy the basis of cells [first, first + count) of the last handle-owned
+   Ned_RT build (batch cell order, 18 (NE + NF) doubles per cell, layout of
+   msfec_nedrt_get_basis) to host memory: the per-cell basis_solution of the
+   reference's NedRTBasis objects (source/Ned_RT/ned_rt_basis.h:99-153)
+   without copying the whole batch (16 GB at coarse 16^3 x depth 4).
+   capacity in doubles. */
+msfec_status msfec_nedrt_get_basis_cells(msfec_handle *handle, int32_t first,
+                                         int32_t count, double *Phi,
+                                         int64_t capacity);
 
 #ifdef __cplusplus
 }

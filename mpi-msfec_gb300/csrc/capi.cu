@@ -10,7 +10,6 @@
 #include <cstdio>
 #include <cmath>
 #include <cstring>
-#include <mutex>
 #include <string>
 #include <vector>
 
@@ -53,6 +52,14 @@ cudaError_t q1_adjoint_rhs_launch(const Q1Cell *cells, int ncells, const msfec_l
                                   cudaStream_t st);
 cudaError_t q1_gradient_launch(const Q1Cell *cells, int ncells, const double *a, const double *phi, const double *sol,
                                const double *U, const double *lam, double *grad, cudaStream_t st);
+cudaError_t q1g_solve_launch(bool fp64, bool has_r, int placement, const Q1GParams &prm, size_t smem, int grid,
+                             cudaStream_t st);
+cudaError_t q1g_solve_occupancy(bool fp64, bool has_r, int placement, size_t smem, int *blocks_per_sm);
+cudaError_t q1g_prepare_launch(const Q1Cell *cells, int ncells, const double *a, int gauss, const double *react,
+                               float *ed, int grid, cudaStream_t st);
+cudaError_t q1g_gradient_launch(const Q1Cell *cells, int ncells, const double *a, int gauss, const double *phi,
+                                const double *sol, const double *U, const double *lam, double *grad,
+                                cudaStream_t st);
 cudaError_t nedrt_solve_launch(bool fp64, bool ml, const NRParams &prm, size_t smem, int grid, cudaStream_t st);
 cudaError_t nedrt_solve_launch_split(bool ml, const NRParams &prm, size_t smem, int grid, cudaStream_t st);
 cudaError_t nedrt_ml_setup_launch(const NRCell *cells, int ncells, const double *ainv6, const double *bdiv,
@@ -173,6 +180,9 @@ struct msfec_handle {
   DevBuf<Q1Item> adj_items;
   DevBuf<Q1Unit> adj_units;
   DevBuf<Q1Cell> fs_cell;  // standard fine solve: the domain as one lattice
+  // tensor-coefficient Q1 solver: items, float element data per fine cell, global workspace
+  DevBuf<Q1GItem> q1g_items;
+  DevBuf<float> q1g_ed, q1g_scratch;
   // Ned_RT state of the last build
   DevBuf<NRCell> nr_cells;
   DevBuf<NRItem> nr_items;
@@ -184,6 +194,7 @@ struct msfec_handle {
   DevBuf<double> nr_ainv, nr_bdiv, nr_KH, nr_FH;
   int64_t nr_basis_doubles = 0;
   std::vector<msfec_cell> nr_h_cells;  // batch of the Ned_RT basis held in nr_phi
+  bool nr_basis_current = false;       // nr_phi holds the latest Ned_RT build (none came after it)
   // Ned_RT adjoint buffers
   DevBuf<double> nra_U, nra_lam, nra_comb, nra_b, nra_e, nra_work, nra_rhs, nra_x, nra_pts, nra_dJ, nra_ga, nra_gb,
       nra_floor;
@@ -214,8 +225,10 @@ struct msfec_handle {
   std::vector<Q1Cell> h_cells;
   // per-phase timing (CUDA events on the handle's stream)
   bool timing = false;
-  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  // ev: 0 start, 1 solver done, 2 Galerkin done, 3 end, 4 preconditioner setup done
+  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   bool ev_recorded = false;
+  bool ev_setup = false;  // ev[4] recorded by the last timed build (a setup kernel ran)
   int last_launches = 0;
   // CUDA-graph replay of the launch sequence (msfec_set_graph)
   bool graph_mode = false;
@@ -260,12 +273,19 @@ struct DeviceGuard {
   }
 };
 
+// Start event of a timed build; the setup event is recorded only by builds
+// that run a preconditioner setup kernel.
+cudaError_t record_start(msfec_handle *h, cudaStream_t st) {
+  h->ev_setup = false;
+  return cudaEventRecord(h->ev[0], st);
+}
+
 // Launches the instantiated graph of `gc` on the handle's stream; timing
 // events bracket the whole graph (solve_ms = total_ms, galerkin_ms = 0).
 msfec_status launch_graph(msfec_handle *h, GraphCache &gc) {
   cudaStream_t st = h->stream;
   cudaError_t e = cudaSuccess;
-  if (h->timing) e = cudaEventRecord(h->ev[0], st);
+  if (h->timing) e = record_start(h, st);
   if (e == cudaSuccess) e = cudaGraphLaunch(gc.exec, st);
   for (int i = 1; i < 4 && e == cudaSuccess && h->timing; ++i) e = cudaEventRecord(h->ev[i], st);
   if (e != cudaSuccess) {
@@ -465,9 +485,122 @@ BuildKey build_key(const msfec_handle *h, int kind, int ncells, const msfec_cell
   return k;
 }
 
+constexpr size_t kQ1GSmemLimit = 200 * 1024;
+
+// Q1 batch with a tensor coefficient (q1_coefficient TENSOR / GAUSS): element
+// data per fine cell, one persistent launch over the (cell, vertex) items
+// (deepest cells first), the Galerkin and report kernels of the scalar path.
+msfec_status q1g_build_impl(msfec_handle *h, int ncells, const msfec_cell *cells, const double *d_a,
+                            const double *d_react, const msfec_load *load, double *d_KH, double *d_FH,
+                            msfec_cell_report *d_rep) {
+  const bool fp64 = h->cfg.precision == MSFEC_PRECISION_FP64;
+  const bool has_r = d_react != nullptr;
+  const int gauss = h->cfg.q1_coefficient == MSFEC_Q1_COEF_GAUSS ? 1 : 0;
+  BuildKey key;
+  if (h->graph_mode) {
+    key = build_key(h, 3 + gauss, ncells, cells, d_a, d_react, load, d_KH, d_FH, d_rep);
+    msfec_status rs;
+    if (replay_graph(h, h->q1_graph, key, &rs)) return rs;
+  }
+  const Q1Plan plan = make_q1_plan(ncells, cells, fp64, has_r, false);  // cell table and node offsets
+  int nmax = 0;
+  for (int c = 0; c < ncells; ++c) nmax = std::max(nmax, 1 << cells[c].depth);
+  std::vector<int> order(ncells);
+  for (int c = 0; c < ncells; ++c) order[c] = c;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cells[x].depth > cells[y].depth; });
+  std::vector<Q1GItem> items;
+  items.reserve((size_t)ncells * 8);
+  for (int c : order)
+    for (int v = 0; v < 8; ++v) items.push_back(Q1GItem{c, v, 0, 0});
+  // workspace placement for the deepest cell: vectors (+ element data) in shared memory when they fit
+  const int ts = fp64 ? 8 : 4;
+  const size_t vec_bytes = 4 * q1g_vec_floats(nmax, ts);
+  const size_t ed_bytes = 4 * (size_t)nmax * nmax * nmax * q1g_ed_floats(gauss);
+  int placement = 0;
+  size_t smem = 0;
+  if (vec_bytes + ed_bytes <= kQ1GSmemLimit) {
+    placement = 2;
+    smem = vec_bytes + ed_bytes;
+  } else if (vec_bytes <= kQ1GSmemLimit) {
+    placement = 1;
+    smem = vec_bytes;
+  }
+  int occ = 0;
+  MSFEC_CUDA_TRY(h, q1g_solve_occupancy(fp64, has_r, placement, smem, &occ));
+  if (occ <= 0) return fail(h, MSFEC_ERROR_NOT_SUPPORTED, "tensor Q1 solver cannot be resident");
+  const int grid = std::min<int>((int)items.size(), occ * h->num_sms);
+  cudaStream_t st = h->stream;
+  MSFEC_CUDA_TRY(h, h->cells.reserve(plan.cells.size()));
+  MSFEC_CUDA_TRY(h, h->q1g_items.reserve(items.size()));
+  MSFEC_CUDA_TRY(h, h->queue.reserve(2));
+  MSFEC_CUDA_TRY(h, h->phi.reserve((size_t)plan.nodes * 8));
+  MSFEC_CUDA_TRY(h, h->y.reserve((size_t)plan.nodes * 8));
+  MSFEC_CUDA_TRY(h, h->stats.reserve((size_t)ncells * 8));
+  MSFEC_CUDA_TRY(h, h->q1g_ed.reserve((size_t)plan.fine * q1g_ed_floats(gauss)));
+  if (placement == 0) MSFEC_CUDA_TRY(h, h->q1g_scratch.reserve(q1g_vec_floats(nmax, ts) * grid));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->cells.ptr, plan.cells.data(), plan.cells.size() * sizeof(Q1Cell),
+                                    cudaMemcpyHostToDevice, st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->q1g_items.ptr, items.data(), items.size() * sizeof(Q1GItem),
+                                    cudaMemcpyHostToDevice, st));
+  Q1GParams prm{};
+  prm.cells = h->cells.ptr;
+  prm.items = h->q1g_items.ptr;
+  prm.n_items = (int)items.size();
+  prm.queue = h->queue.ptr;
+  prm.a = d_a;
+  prm.gauss = gauss;
+  prm.react = d_react;
+  prm.ed = h->q1g_ed.ptr;
+  prm.phi = h->phi.ptr;
+  prm.y = h->y.ptr;
+  prm.stats = h->stats.ptr;
+  prm.scratch = placement == 0 ? h->q1g_scratch.ptr : nullptr;
+  prm.scratch_floats = q1g_vec_floats(nmax, ts);
+  prm.rtol = h->cfg.rtol;
+  prm.inner_rtol = h->cfg.inner_rtol;
+  prm.max_iter = std::max(h->cfg.max_iter, 4 * nmax * nmax);  // Jacobi-PCG: O(n) .. O(n^2) iterations
+  prm.max_refine = h->cfg.max_refine;
+  if (h->cfg.verbose)
+    fprintf(stderr, "[msfec] q1 tensor plan: %d cells, %zu items, placement %d, smem %zu B, grid %d, %s, %s\n",
+            ncells, items.size(), placement, smem, grid, gauss ? "Gauss-point tensors" : "tensor per cell",
+            fp64 ? "fp64" : "mixed");
+  msfec_load ld;
+  if (load) {
+    ld = *load;
+  } else {
+    std::memset(&ld, 0, sizeof(ld));
+  }
+  auto seq = [&](bool timed) -> cudaError_t {
+    cudaError_t e = cudaMemsetAsync(h->queue.ptr, 0, sizeof(int), st);
+    if (e == cudaSuccess && timed) e = record_start(h, st);
+    if (e == cudaSuccess)
+      e = q1g_prepare_launch(h->cells.ptr, ncells, d_a, gauss, d_react, h->q1g_ed.ptr, std::min(ncells, 4 * h->num_sms),
+                             st);
+    if (e == cudaSuccess && timed) {
+      e = cudaEventRecord(h->ev[4], st);
+      h->ev_setup = true;
+    }
+    if (e == cudaSuccess) e = q1g_solve_launch(fp64, has_r, placement, prm, smem, grid, st);
+    if (e == cudaSuccess && timed) e = cudaEventRecord(h->ev[1], st);
+    if (e == cudaSuccess) e = q1_galerkin_launch(h->cells.ptr, ncells, h->phi.ptr, h->y.ptr, ld, d_KH, d_FH, st);
+    if (e == cudaSuccess && timed) e = cudaEventRecord(h->ev[2], st);
+    if (e == cudaSuccess && d_rep) e = q1_report_launch(h->stats.ptr, ncells, d_rep, st);
+    if (e == cudaSuccess && timed) e = cudaEventRecord(h->ev[3], st);
+    return e;
+  };
+  const msfec_status s = run_sequence(h, h->q1_graph, std::move(key), d_rep ? 4 : 3, seq);
+  if (s != MSFEC_SUCCESS) return s;
+  h->q1_ncells = ncells;
+  h->q1_basis_doubles = plan.nodes * 8;
+  h->h_cells = plan.cells;
+  return MSFEC_SUCCESS;
+}
+
 msfec_status q1_build_impl(msfec_handle *h, int ncells, const msfec_cell *cells, const double *d_a,
                            const double *d_react, const msfec_load *load, double *d_KH, double *d_FH,
                            msfec_cell_report *d_rep) {
+  if (h->cfg.q1_coefficient != MSFEC_Q1_COEF_SCALAR)
+    return q1g_build_impl(h, ncells, cells, d_a, d_react, load, d_KH, d_FH, d_rep);
   const bool fp64 = h->cfg.precision == MSFEC_PRECISION_FP64;
   const bool has_r = d_react != nullptr;
   BuildKey key;
@@ -564,7 +697,7 @@ msfec_status q1_build_impl(msfec_handle *h, int ncells, const msfec_cell *cells,
   }
   auto seq = [&](bool timed) -> cudaError_t {
     cudaError_t e = cudaMemsetAsync(h->queue.ptr, 0, 2 * sizeof(int), st);
-    if (e == cudaSuccess && timed) e = cudaEventRecord(h->ev[0], st);
+    if (e == cudaSuccess && timed) e = record_start(h, st);
     if (plan.split) {
       if (e == cudaSuccess) e = cudaEventRecord(h->ev_fork, st);
       if (e == cudaSuccess) e = cudaStreamWaitEvent(h->aux_stream, h->ev_fork, 0);
@@ -605,10 +738,102 @@ bool same_batch(const msfec_handle *h, int ncells, const msfec_cell *cells) {
 
 // Adjoint local problems (load bubble mu, observation bubble eta: source items
 // of the persistent solver, planes 0 and 1) and the per-fine-cell gradient.
+// Tensor layouts: the adjoint local problems as source items (coarse vertex
+// planes 0 and 1) of the tensor-coefficient solver, then its gradient kernel.
+msfec_status q1g_backward_impl(msfec_handle *h, int ncells, const msfec_cell *cells, const double *d_a,
+                               const double *d_react, const msfec_load *load, const double *d_U, const double *d_lam,
+                               int npoints, const int *d_cell_of, const double *d_pts, const double *d_gk,
+                               double *d_grad) {
+  const bool fp64 = h->cfg.precision == MSFEC_PRECISION_FP64;
+  const bool has_r = d_react != nullptr;
+  const int gauss = h->cfg.q1_coefficient == MSFEC_Q1_COEF_GAUSS ? 1 : 0;
+  const Q1Plan plan = make_q1_plan(ncells, cells, fp64, has_r, false);
+  int nmax = 0;
+  for (int c = 0; c < ncells; ++c) nmax = std::max(nmax, 1 << cells[c].depth);
+  std::vector<int> order(ncells);
+  for (int c = 0; c < ncells; ++c) order[c] = c;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cells[x].depth > cells[y].depth; });
+  std::vector<Q1GItem> items;
+  for (int c : order)
+    for (int v = 0; v < 2; ++v) items.push_back(Q1GItem{c, v, 1, 0});
+  const int ts = fp64 ? 8 : 4;
+  const size_t vec_bytes = 4 * q1g_vec_floats(nmax, ts);
+  const size_t ed_bytes = 4 * (size_t)nmax * nmax * nmax * q1g_ed_floats(gauss);
+  int placement = 0;
+  size_t smem = 0;
+  if (vec_bytes + ed_bytes <= kQ1GSmemLimit) {
+    placement = 2;
+    smem = vec_bytes + ed_bytes;
+  } else if (vec_bytes <= kQ1GSmemLimit) {
+    placement = 1;
+    smem = vec_bytes;
+  }
+  int occ = 0;
+  MSFEC_CUDA_TRY(h, q1g_solve_occupancy(fp64, has_r, placement, smem, &occ));
+  if (occ <= 0) return fail(h, MSFEC_ERROR_NOT_SUPPORTED, "tensor Q1 solver cannot be resident");
+  const int grid = std::min<int>((int)items.size(), occ * h->num_sms);
+  cudaStream_t st = h->stream;
+  const size_t planes = (size_t)plan.nodes * 8;
+  MSFEC_CUDA_TRY(h, h->adj_rhs.reserve(planes));
+  MSFEC_CUDA_TRY(h, h->adj_sol.reserve(planes));
+  MSFEC_CUDA_TRY(h, h->q1g_items.reserve(items.size()));
+  MSFEC_CUDA_TRY(h, h->q1g_ed.reserve((size_t)plan.fine * q1g_ed_floats(gauss)));
+  if (placement == 0) MSFEC_CUDA_TRY(h, h->q1g_scratch.reserve(q1g_vec_floats(nmax, ts) * grid));
+  MSFEC_CUDA_TRY(h, cudaMemsetAsync(h->adj_rhs.ptr, 0, planes * sizeof(double), st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->q1g_items.ptr, items.data(), items.size() * sizeof(Q1GItem),
+                                    cudaMemcpyHostToDevice, st));
+  MSFEC_CUDA_TRY(h, cudaMemsetAsync(h->queue.ptr, 0, sizeof(int), st));
+  msfec_load ld;
+  if (load) {
+    ld = *load;
+  } else {
+    std::memset(&ld, 0, sizeof(ld));
+  }
+  MSFEC_CUDA_TRY(h, q1_adjoint_rhs_launch(h->cells.ptr, ncells, ld, npoints, d_cell_of, d_pts, d_gk, h->adj_rhs.ptr, st));
+  MSFEC_CUDA_TRY(h, q1g_prepare_launch(h->cells.ptr, ncells, d_a, gauss, d_react, h->q1g_ed.ptr,
+                                       std::min(ncells, 4 * h->num_sms), st));
+  Q1GParams prm{};
+  prm.cells = h->cells.ptr;
+  prm.items = h->q1g_items.ptr;
+  prm.n_items = (int)items.size();
+  prm.queue = h->queue.ptr;
+  prm.a = d_a;
+  prm.gauss = gauss;
+  prm.react = d_react;
+  prm.ed = h->q1g_ed.ptr;
+  prm.phi = h->phi.ptr;
+  prm.y = h->y.ptr;
+  prm.src_rhs = h->adj_rhs.ptr;
+  prm.src_out = h->adj_sol.ptr;
+  prm.stats = h->stats.ptr;
+  prm.scratch = placement == 0 ? h->q1g_scratch.ptr : nullptr;
+  prm.scratch_floats = q1g_vec_floats(nmax, ts);
+  prm.rtol = h->cfg.rtol;
+  prm.inner_rtol = h->cfg.inner_rtol;
+  prm.max_iter = std::max(h->cfg.max_iter, 4 * nmax * nmax);
+  prm.max_refine = h->cfg.max_refine;
+  if (h->timing) MSFEC_CUDA_TRY(h, record_start(h, st));
+  MSFEC_CUDA_TRY(h, q1g_solve_launch(fp64, has_r, placement, prm, smem, grid, st));
+  if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[1], st));
+  MSFEC_CUDA_TRY(h, q1g_gradient_launch(h->cells.ptr, ncells, d_a, gauss, h->phi.ptr, h->adj_sol.ptr, d_U, d_lam,
+                                        d_grad, st));
+  if (h->timing) {
+    MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[2], st));
+    MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[3], st));
+    h->ev_recorded = true;
+  }
+  h->last_launches = 5;
+  h->last_graph = 0;
+  return MSFEC_SUCCESS;
+}
+
 msfec_status q1_backward_impl(msfec_handle *h, int ncells, const msfec_cell *cells, const double *d_a,
                               const double *d_react, const msfec_load *load, const double *d_U, const double *d_lam,
                               int npoints, const int *d_cell_of, const double *d_pts, const double *d_gk,
                               double *d_grad) {
+  if (h->cfg.q1_coefficient != MSFEC_Q1_COEF_SCALAR)
+    return q1g_backward_impl(h, ncells, cells, d_a, d_react, load, d_U, d_lam, npoints, d_cell_of, d_pts, d_gk,
+                             d_grad);
   const bool fp64 = h->cfg.precision == MSFEC_PRECISION_FP64;
   const bool has_r = d_react != nullptr;
   Q1Plan plan = make_q1_plan(ncells, cells, fp64, has_r);
@@ -676,7 +901,7 @@ msfec_status q1_backward_impl(msfec_handle *h, int ncells, const msfec_cell *cel
   int grid = plan.cluster > 1 ? std::min<int>((int)units.size(), occ) * plan.cluster
                               : std::min<int>((int)units.size(), occ * h->num_sms);
   grid = std::max(grid, plan.cluster);
-  if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[0], st));
+  if (h->timing) MSFEC_CUDA_TRY(h, record_start(h, st));
   MSFEC_CUDA_TRY(h, q1_solve_launch(fp64, plan.cluster, has_r, prm, plan.smem, grid, st));
   if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[1], st));
   MSFEC_CUDA_TRY(h, q1_gradient_launch(h->cells.ptr, ncells, d_a, h->phi.ptr, h->adj_sol.ptr, d_U, d_lam, d_grad, st));
@@ -695,6 +920,54 @@ constexpr size_t kNRSmemLimit = 200 * 1024;
 constexpr size_t kNRSmemTotalLimit = 224 * 1024;  // workspace + multilevel region (227 KB minus static)
 constexpr size_t kNRSplitSmemLimit = 108 * 1024;  // two CTAs per SM (228 KB, minus static shared memory)
 
+// Launch shape of the Ned_RT basis solver for a batch whose deepest cell has
+// n = nmax fine cells per edge: where the MINRES workspace lives (two 256-thread
+// CTAs per SM with the split workspace, one 512-thread CTA with the whole
+// workspace in shared memory, or one with a per-CTA global slot), the dynamic
+// shared memory including the multilevel region, and the grid. Shared by the
+// handle-owned build and the allocation-free one, so both make the same choice
+// (including the autotuner's) for the same batch.
+struct NRShape {
+  bool split = false, use_smem = false, ml = false;
+  size_t smem = 0, ws_floats = 0, ml_offset = 0;
+  int grid = 0;
+};
+
+msfec_status nr_shape(msfec_handle *h, int nmax, bool fp64, bool want_ml, size_t nitems, NRShape &s) {
+  int deepest = 0;
+  while ((1 << deepest) < nmax) ++deepest;
+  deepest = std::min(deepest, kNRMaxDepthCfg);
+  // mixed precision with a small enough item: two 256-thread CTAs per SM
+  // (split workspace) unless the autotuner chose the 512-thread CTA
+  const int split_sel = h->force_nr_split >= 0 ? h->force_nr_split : h->nr_split[deepest];
+  s.split = !fp64 && nr_split_smem_floats(nmax) * 4 <= kNRSplitSmemLimit && split_sel != 0;
+  s.ws_floats = nr_workspace_floats(nmax, fp64 ? 8 : 4);
+  s.use_smem = s.ws_floats * 4 <= kNRSmemLimit;
+  s.smem = s.use_smem ? s.ws_floats * 4 : 0;
+  s.grid = std::min<int>((int)nitems, h->num_sms);
+  if (s.split) {
+    s.smem = nr_split_smem_floats(nmax) * 4;
+    s.ws_floats = nr_split_global_floats(nmax);  // global slot per CTA
+    s.use_smem = true;
+  }
+  // the multilevel region follows the shared workspace (if any)
+  s.ml_offset = s.smem;
+  s.ml = want_ml;
+  const size_t ml_bytes = s.ml ? nr_ml_layout(nmax, fp64 ? 8 : 4).bytes : 0;
+  if (s.ml && s.smem + ml_bytes > (s.split ? kNRSplitSmemLimit : kNRSmemTotalLimit)) s.ml = false;
+  if (s.ml) s.smem += ml_bytes;
+  if (s.split) {
+    int occ = 0;
+    MSFEC_CUDA_TRY(h, nedrt_split_occupancy(s.ml, s.smem, &occ));
+    if (occ <= 0) return fail(h, MSFEC_ERROR_NOT_SUPPORTED, "split Ned_RT solver cannot be resident");
+    s.grid = std::min<int>((int)nitems, occ * h->num_sms);
+  } else if (!s.use_smem) {  // resident CTAs = workspace slots (L2 footprint), possibly autotuned
+    const int cap = h->force_ctas > 0 ? h->force_ctas : h->nr_ctas[fp64 ? 0 : 1][deepest];
+    if (cap > 0) s.grid = std::min(s.grid, cap);
+  }
+  return MSFEC_SUCCESS;
+}
+
 msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cells, const double *d_ainv,
                               const double *d_bdiv, const msfec_load *load, double *d_KH, double *d_FH,
                               msfec_cell_report *d_rep) {
@@ -704,7 +977,10 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
     key = build_key(h, 2, ncells, cells, d_ainv, d_bdiv, load, d_KH, d_FH, d_rep);
     msfec_status rs;
     if (replay_graph(h, h->nr_graph, key, &rs)) {
-      if (rs == MSFEC_SUCCESS) h->nr_basis_doubles = h->nr_graph_basis;
+      if (rs == MSFEC_SUCCESS) {
+        h->nr_basis_doubles = h->nr_graph_basis;
+        h->nr_basis_current = true;
+      }
       return rs;
     }
   }
@@ -748,39 +1024,18 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
   items.reserve((size_t)ncells * 18);
   for (int c : order)
     for (int b = 0; b < 18; ++b) items.push_back(NRItem{c, b, 0});
-  int deepest = 0;
-  while ((1 << deepest) < nmax) ++deepest;
-  deepest = std::min(deepest, kNRMaxDepthCfg);
-  // mixed precision with a small enough item: two 256-thread CTAs per SM
-  // (split workspace) unless the autotuner chose the 512-thread CTA
-  const int split_sel = h->force_nr_split >= 0 ? h->force_nr_split : h->nr_split[deepest];
-  const bool split = !fp64 && nr_split_smem_floats(nmax) * 4 <= kNRSplitSmemLimit && split_sel != 0;
-  size_t ws_floats = nr_workspace_floats(nmax, fp64 ? 8 : 4);
-  bool use_smem = ws_floats * 4 <= kNRSmemLimit;
-  size_t smem = use_smem ? ws_floats * 4 : 0;
-  cudaStream_t st = h->stream;
-  int grid = std::min<int>((int)items.size(), h->num_sms);
-  if (split) {
-    smem = nr_split_smem_floats(nmax) * 4;
-    ws_floats = nr_split_global_floats(nmax);  // global slot per CTA
-    use_smem = true;
+  NRShape shape;
+  {
+    const msfec_status ss = nr_shape(h, nmax, fp64, ml, items.size(), shape);
+    if (ss != MSFEC_SUCCESS) return ss;
   }
-  // the multilevel region follows the shared workspace (if any)
-  const size_t ml_offset = smem;
-  const size_t ml_bytes = ml ? nr_ml_layout(nmax, fp64 ? 8 : 4).bytes : 0;
-  if (ml && smem + ml_bytes > (split ? kNRSplitSmemLimit : kNRSmemTotalLimit)) ml = false;
+  const bool split = shape.split, use_smem = shape.use_smem;
+  const size_t smem = shape.smem, ws_floats = shape.ws_floats, ml_offset = shape.ml_offset;
+  const int grid = shape.grid;
+  ml = shape.ml;
   if (!ml)
     for (auto &q : hc) q.coarse_off = -1;
-  if (ml) smem += ml_bytes;
-  if (split) {
-    int occ = 0;
-    MSFEC_CUDA_TRY(h, nedrt_split_occupancy(ml, smem, &occ));
-    if (occ <= 0) return fail(h, MSFEC_ERROR_NOT_SUPPORTED, "split Ned_RT solver cannot be resident");
-    grid = std::min<int>((int)items.size(), occ * h->num_sms);
-  } else if (!use_smem) {  // resident CTAs = workspace slots (L2 footprint), possibly autotuned
-    const int cap = h->force_ctas > 0 ? h->force_ctas : h->nr_ctas[fp64 ? 0 : 1][deepest];
-    if (cap > 0) grid = std::min(grid, cap);
-  }
+  cudaStream_t st = h->stream;
   MSFEC_CUDA_TRY(h, h->nr_cells.reserve(ncells));
   MSFEC_CUDA_TRY(h, h->nr_items.reserve(items.size()));
   MSFEC_CUDA_TRY(h, h->queue.reserve(2));
@@ -830,10 +1085,14 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
   }
   auto seq = [&](bool timed) -> cudaError_t {
     cudaError_t e = cudaMemsetAsync(h->queue.ptr, 0, sizeof(int), st);
-    if (e == cudaSuccess && timed) e = cudaEventRecord(h->ev[0], st);
+    if (e == cudaSuccess && timed) e = record_start(h, st);
     if (e == cudaSuccess && ml)
       e = nedrt_ml_setup_launch(h->nr_cells.ptr, ncells, d_ainv, d_bdiv, h->nr_coarse.ptr, h->nr_mlscratch.ptr,
                                 ml_scratch, (size_t)nr_ml_data_floats(nmax) * 4, ml_grid, st);
+    if (e == cudaSuccess && timed && ml) {
+      e = cudaEventRecord(h->ev[4], st);
+      h->ev_setup = true;
+    }
     if (e == cudaSuccess)
       e = split ? nedrt_solve_launch_split(ml, prm, smem, grid, st)
                 : nedrt_solve_launch(fp64, ml, prm, smem, grid, st);
@@ -851,6 +1110,7 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
   h->nr_graph_basis = dofs * 18;
   h->nr_h_cells.assign(cells, cells + ncells);
   h->nr_basis_doubles = dofs * 18;
+  h->nr_basis_current = true;
   return MSFEC_SUCCESS;
 }
 
@@ -935,7 +1195,7 @@ msfec_status qned_build_impl(msfec_handle *h, int ncells, const msfec_cell *cell
   } else {
     std::memset(&ld, 0, sizeof(ld));
   }
-  if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[0], st));
+  if (h->timing) MSFEC_CUDA_TRY(h, record_start(h, st));
   MSFEC_CUDA_TRY(h, qned_solve_launch(fp64, two_per_sm, prm, smem, grid, st));
   if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[1], st));
   MSFEC_CUDA_TRY(h, qned_galerkin_launch(h->qn_cells.ptr, ncells, h->qn_phi.ptr, h->qn_y.ptr, ld, h->qn_eload.ptr,
@@ -1026,7 +1286,7 @@ msfec_status rtdq_build_impl(msfec_handle *h, int ncells, const msfec_cell *cell
   } else {
     std::memset(&ld, 0, sizeof(ld));
   }
-  if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[0], st));
+  if (h->timing) MSFEC_CUDA_TRY(h, record_start(h, st));
   MSFEC_CUDA_TRY(h, rtdq_solve_launch(fp64, two_per_sm, prm, smem, grid, st));
   if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[1], st));
   MSFEC_CUDA_TRY(h, rtdq_galerkin_launch(h->rt_cells.ptr, ncells, h->rt_phi.ptr, h->rt_y.ptr, ld, d_KH, d_FH, d_rep,
@@ -1070,10 +1330,26 @@ msfec_status tensor_coef_check(msfec_handle *h, const double *six, const double 
   return MSFEC_SUCCESS;
 }
 
-// Q1 coefficients per fine cell: a positive and finite, the reaction (if any) non-negative and finite.
+// Doubles of the Q1 diffusion coefficient per fine cell in the handle's layout.
+int64_t q1_coef_stride(const msfec_handle *h) {
+  return h->cfg.q1_coefficient == MSFEC_Q1_COEF_TENSOR ? 6 : (h->cfg.q1_coefficient == MSFEC_Q1_COEF_GAUSS ? 48 : 1);
+}
+
+// Q1 coefficients per fine cell: a positive and finite (or every tensor SPD and
+// finite), the reaction (if any) non-negative and finite.
 msfec_status q1_coef_check(msfec_handle *h, const double *a, const double *reaction, int64_t nfine) {
+  const int64_t stride = q1_coef_stride(h);
   for (int64_t e = 0; e < nfine; ++e) {
-    if (!(a[e] > 0.0) || !std::isfinite(a[e])) return fail(h, MSFEC_ERROR_NUMERICAL, "coefficient a not positive/finite");
+    if (stride == 1) {
+      if (!(a[e] > 0.0) || !std::isfinite(a[e]))
+        return fail(h, MSFEC_ERROR_NUMERICAL, "coefficient a not positive/finite");
+    } else {
+      for (int64_t q = 0; q < stride; q += 6)
+        if (!sym6_spd(a + e * stride + q))
+          return fail(h, MSFEC_ERROR_NUMERICAL, "tensor coefficient A not SPD / finite at fine cell " +
+                                                    std::to_string(e) + (stride == 48 ? ", Gauss point " +
+                                                    std::to_string(q / 6) : std::string()));
+    }
     if (reaction && (!(reaction[e] >= 0.0) || !std::isfinite(reaction[e])))
       return fail(h, MSFEC_ERROR_NUMERICAL, "reaction coefficient negative or non-finite");
   }
@@ -1128,7 +1404,8 @@ msfec_status msfec_create(msfec_handle **out, const msfec_config *cfg) {
     msfec_config_default(&c);
   if (c.precision != MSFEC_PRECISION_FP64 && c.precision != MSFEC_PRECISION_MIXED) return MSFEC_ERROR_INVALID_ARGUMENT;
   if (!(c.rtol > 0.0) || !(c.inner_rtol > 0.0) || c.inner_rtol >= 1.0 || c.max_iter < 1 || c.max_refine < 1 ||
-      !(c.nedrt_rtol > 0.0) || c.q1_launch < 0 || c.q1_launch > 2 || c.nedrt_precond < 0 || c.nedrt_precond > 1)
+      !(c.nedrt_rtol > 0.0) || c.q1_launch < 0 || c.q1_launch > 2 || c.nedrt_precond < 0 || c.nedrt_precond > 1 ||
+      c.q1_coefficient < MSFEC_Q1_COEF_SCALAR || c.q1_coefficient > MSFEC_Q1_COEF_GAUSS)
     return MSFEC_ERROR_INVALID_ARGUMENT;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || c.device < 0 || c.device >= ndev) return MSFEC_ERROR_CUDA;
@@ -1278,12 +1555,13 @@ msfec_status msfec_q1_build(msfec_handle *h, int32_t ncells, const msfec_cell *c
   if (ncells == 0) return msfec_q1_build_device(h, 0, cells, nullptr, nullptr, load, nullptr, nullptr, nullptr);
   DeviceGuard g(h->device);
   cudaStream_t st = h->stream;
-  MSFEC_CUDA_TRY(h, h->a.reserve(nfine));
+  const int64_t na = nfine * q1_coef_stride(h);
+  MSFEC_CUDA_TRY(h, h->a.reserve(na));
   if (reaction) MSFEC_CUDA_TRY(h, h->react.reserve(nfine));
   MSFEC_CUDA_TRY(h, h->KH.reserve((size_t)ncells * 64));
   MSFEC_CUDA_TRY(h, h->FH.reserve((size_t)ncells * 8));
   MSFEC_CUDA_TRY(h, h->rep.reserve(ncells));
-  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->a.ptr, a, nfine * sizeof(double), cudaMemcpyHostToDevice, st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->a.ptr, a, na * sizeof(double), cudaMemcpyHostToDevice, st));
   if (reaction)
     MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->react.ptr, reaction, nfine * sizeof(double), cudaMemcpyHostToDevice, st));
   msfec_status s = q1_build_impl(h, ncells, cells, h->a.ptr, reaction ? h->react.ptr : nullptr, load, h->KH.ptr,
@@ -1325,14 +1603,20 @@ msfec_status msfec_set_graph(msfec_handle *h, int32_t enable) {
 
 msfec_status msfec_get_timings(msfec_handle *h, msfec_timings *out) {
   if (!h || !out) return MSFEC_ERROR_INVALID_ARGUMENT;
-  out->solve_ms = out->galerkin_ms = out->total_ms = -1.0f;
+  out->solve_ms = out->galerkin_ms = out->total_ms = out->setup_ms = -1.0f;
   out->solve_launches = h->ev_recorded ? 1 : 0;
   out->kernel_launches = h->last_launches;
   out->graph = h->last_graph;
   if (!h->ev_recorded) return MSFEC_SUCCESS;
   DeviceGuard g(h->device);
   MSFEC_CUDA_TRY(h, cudaEventSynchronize(h->ev[3]));
-  MSFEC_CUDA_TRY(h, cudaEventElapsedTime(&out->solve_ms, h->ev[0], h->ev[1]));
+  out->setup_ms = 0.0f;
+  if (h->ev_setup) {
+    MSFEC_CUDA_TRY(h, cudaEventElapsedTime(&out->setup_ms, h->ev[0], h->ev[4]));
+    MSFEC_CUDA_TRY(h, cudaEventElapsedTime(&out->solve_ms, h->ev[4], h->ev[1]));
+  } else {
+    MSFEC_CUDA_TRY(h, cudaEventElapsedTime(&out->solve_ms, h->ev[0], h->ev[1]));
+  }
   MSFEC_CUDA_TRY(h, cudaEventElapsedTime(&out->galerkin_ms, h->ev[1], h->ev[2]));
   MSFEC_CUDA_TRY(h, cudaEventElapsedTime(&out->total_ms, h->ev[0], h->ev[3]));
   return MSFEC_SUCCESS;
@@ -1351,6 +1635,26 @@ msfec_status msfec_q1_get_basis(msfec_handle *h, double *Phi, int64_t capacity) 
   DeviceGuard g(h->device);
   MSFEC_CUDA_TRY(h, cudaMemcpyAsync(Phi, h->phi.ptr, h->q1_basis_doubles * sizeof(double), cudaMemcpyDeviceToHost,
                                     h->stream));
+  MSFEC_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  return MSFEC_SUCCESS;
+}
+
+msfec_status msfec_q1_get_basis_cells(msfec_handle *h, int32_t first, int32_t count, double *Phi, int64_t capacity) {
+  if (!h || (count > 0 && !Phi)) return MSFEC_ERROR_INVALID_ARGUMENT;
+  if (h->q1_basis_doubles <= 0) return fail(h, MSFEC_ERROR_INVALID_STATE, "no Q1 basis built yet");
+  const int ncells = (int)h->h_cells.size();
+  if (first < 0 || count < 0 || first > ncells || count > ncells - first)
+    return fail(h, MSFEC_ERROR_INVALID_ARGUMENT,
+                "cell range [" + std::to_string(first) + ", " + std::to_string((int64_t)first + count) +
+                    ") outside the batch of " + std::to_string(ncells) + " cells");
+  if (count == 0) return MSFEC_SUCCESS;
+  const int64_t off = 8 * (int64_t)h->h_cells[first].node_off;
+  const Q1Cell &last = h->h_cells[first + count - 1];
+  const int64_t n1 = last.n + 1;
+  const int64_t len = 8 * ((int64_t)last.node_off + n1 * n1 * n1) - off;
+  if (capacity < len) return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "capacity too small");
+  DeviceGuard g(h->device);
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(Phi, h->phi.ptr + off, len * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   MSFEC_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
   return MSFEC_SUCCESS;
 }
@@ -1407,9 +1711,10 @@ msfec_status msfec_q1_backward(msfec_handle *h, int32_t ncells, const msfec_cell
   }
   DeviceGuard g(h->device);
   cudaStream_t st = h->stream;
-  MSFEC_CUDA_TRY(h, h->a.reserve(nfine));
+  const int64_t na = nfine * q1_coef_stride(h);
+  MSFEC_CUDA_TRY(h, h->a.reserve(na));
   if (reaction) MSFEC_CUDA_TRY(h, h->react.reserve(nfine));
-  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->a.ptr, a, nfine * sizeof(double), cudaMemcpyHostToDevice, st));
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->a.ptr, a, na * sizeof(double), cudaMemcpyHostToDevice, st));
   if (reaction)
     MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->react.ptr, reaction, nfine * sizeof(double), cudaMemcpyHostToDevice, st));
   if (!(reuse_basis && same_batch(h, ncells, cells))) {
@@ -1455,6 +1760,8 @@ msfec_status msfec_q1_backward(msfec_handle *h, int32_t ncells, const msfec_cell
 msfec_status msfec_q1_fine_solve(msfec_handle *h, const msfec_cell *domain, const double *a, const double *reaction,
                                  const msfec_load *load, double *u, msfec_cell_report *report) {
   if (!h) return MSFEC_ERROR_INVALID_ARGUMENT;
+  if (h->cfg.q1_coefficient != MSFEC_Q1_COEF_SCALAR)
+    return fail(h, MSFEC_ERROR_NOT_SUPPORTED, "msfec_q1_fine_solve: scalar coefficient layout only");
   if (!domain || !a || !u) return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "null pointer");
   if (!cell_ok(*domain)) return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "domain box invalid (depth 1..5)");
   if (!load_ok(load) || (load && load->kind == MSFEC_LOAD_VEC_TRIG))
@@ -1528,7 +1835,7 @@ msfec_status msfec_q1_fine_solve(msfec_handle *h, const msfec_cell *domain, cons
   MSFEC_CUDA_TRY(h, q1_solve_occupancy(fp64, plan.cluster, has_r, plan.smem, &occ));
   if (occ <= 0) return fail(h, MSFEC_ERROR_NOT_SUPPORTED, "local solver kernel cannot be resident");
   const int grid = plan.cluster;  // one item: one CTA, or one cluster for a slab item
-  if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[0], st));
+  if (h->timing) MSFEC_CUDA_TRY(h, record_start(h, st));
   MSFEC_CUDA_TRY(h, q1_solve_launch(fp64, plan.cluster, has_r, prm, plan.smem, grid, st));
   if (h->timing) {
     MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[1], st));
@@ -1547,7 +1854,7 @@ msfec_status msfec_q1_fine_solve(msfec_handle *h, const msfec_cell *domain, cons
     report->iterations = stat.iters;
     report->refinements = stat.refinements;
     report->converged = ok ? 1 : 0;
-    report->reserved = 0;
+    report->iterations_sum = stat.iters;
     report->residual = stat.rel_residual;
   }
   if (!ok) return fail(h, MSFEC_ERROR_NOT_CONVERGED, "fine-scale solve missed rtol");
@@ -1613,7 +1920,7 @@ msfec_status msfec_nedrt_fine_solve(msfec_handle *h, const msfec_cell *domain, c
   } else {
     std::memset(&ld, 0, sizeof(ld));
   }
-  if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[0], st));
+  if (h->timing) MSFEC_CUDA_TRY(h, record_start(h, st));
   MSFEC_CUDA_TRY(h, nedrt_face_load_launch(h->nrf_cell.ptr, 1, ld, h->nrf_b.ptr, st));
   NRParams prm{};
   prm.cells = h->nrf_cell.ptr;
@@ -1655,7 +1962,7 @@ msfec_status msfec_nedrt_fine_solve(msfec_handle *h, const msfec_cell *domain, c
     report->iterations = stat.iters;
     report->refinements = stat.refinements;
     report->converged = ok ? 1 : 0;
-    report->reserved = 0;
+    report->iterations_sum = stat.iters;
     report->residual = stat.rel_residual;
   }
   if (!ok)
@@ -1733,6 +2040,11 @@ msfec_status msfec_autotune(msfec_handle *h, int32_t kind, int32_t ncells, const
   if ((kind != MSFEC_KIND_Q1 && kind != MSFEC_KIND_NEDRT) || ncells <= 0 || !cells || !coef0 ||
       (kind == MSFEC_KIND_NEDRT && !coef1) || !choice)
     return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "msfec_autotune: invalid kind, batch or output");
+  if (kind == MSFEC_KIND_Q1 && h->cfg.q1_coefficient != MSFEC_Q1_COEF_SCALAR) {  // one launch shape only
+    choice[0] = 0;
+    choice[1] = 1;
+    return MSFEC_SUCCESS;
+  }
   const bool fp64 = h->cfg.precision == MSFEC_PRECISION_FP64;
   int deepest = 0;
   for (int c = 0; c < ncells; ++c) deepest = std::max(deepest, (int)cells[c].depth);
@@ -1803,7 +2115,7 @@ msfec_status msfec_autotune(msfec_handle *h, int32_t kind, int32_t ncells, const
 }
 
 static bool nr_same_batch(const msfec_handle *h, int ncells, const msfec_cell *cells) {
-  if (h->nr_basis_doubles <= 0 || (int)h->nr_h_cells.size() != ncells) return false;
+  if (!h->nr_basis_current || h->nr_basis_doubles <= 0 || (int)h->nr_h_cells.size() != ncells) return false;
   for (int c = 0; c < ncells; ++c) {
     const msfec_cell &a = h->nr_h_cells[c], &b = cells[c];
     if (a.depth != b.depth) return false;
@@ -1893,7 +2205,7 @@ msfec_status msfec_nedrt_backward(msfec_handle *h, int32_t ncells, const msfec_c
   } else {
     std::memset(&ld, 0, sizeof(ld));
   }
-  if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[0], st));
+  if (h->timing) MSFEC_CUDA_TRY(h, record_start(h, st));
   MSFEC_CUDA_TRY(h, nedrt_adjoint_prepare_launch(h->nr_cells.ptr, ncells, h->nr_phi.ptr, h->nra_U.ptr, h->nra_lam.ptr,
                                                  ld, npoints, h->nra_cell.ptr, h->nra_pts.ptr, h->nra_dJ.ptr,
                                                  h->nr_ainv.ptr, h->nr_bdiv.ptr, h->nra_comb.ptr, h->nra_b.ptr,
@@ -2135,6 +2447,30 @@ msfec_status msfec_qned_get_basis(msfec_handle *h, double *Phi, int64_t capacity
 
 int64_t msfec_nedrt_basis_size(const msfec_handle *h) { return h ? h->nr_basis_doubles : 0; }
 
+msfec_status msfec_nedrt_get_basis_cells(msfec_handle *h, int32_t first, int32_t count, double *Phi,
+                                         int64_t capacity) {
+  if (!h || (count > 0 && !Phi)) return MSFEC_ERROR_INVALID_ARGUMENT;
+  if (h->nr_basis_doubles <= 0) return fail(h, MSFEC_ERROR_INVALID_STATE, "no Ned_RT basis built yet");
+  const int ncells = (int)h->nr_h_cells.size();
+  if (first < 0 || count < 0 || first > ncells || count > ncells - first)
+    return fail(h, MSFEC_ERROR_INVALID_ARGUMENT,
+                "cell range [" + std::to_string(first) + ", " + std::to_string((int64_t)first + count) +
+                    ") outside the batch of " + std::to_string(ncells) + " cells");
+  int64_t off = 0, len = 0;
+  for (int c = 0; c < first + count; ++c) {
+    int NEx, NFx, NE, NF;
+    nr_counts(1 << h->nr_h_cells[c].depth, NEx, NFx, NE, NF);
+    (c < first ? off : len) += 18 * (int64_t)(NE + NF);
+  }
+  if (capacity < len) return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "capacity too small");
+  if (len == 0) return MSFEC_SUCCESS;
+  DeviceGuard g(h->device);
+  MSFEC_CUDA_TRY(h, cudaMemcpyAsync(Phi, h->nr_phi.ptr + off, len * sizeof(double), cudaMemcpyDeviceToHost,
+                                    h->stream));
+  MSFEC_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  return MSFEC_SUCCESS;
+}
+
 msfec_status msfec_nedrt_get_basis(msfec_handle *h, double *Phi, int64_t capacity) {
   if (!h || !Phi) return MSFEC_ERROR_INVALID_ARGUMENT;
   if (h->nr_basis_doubles <= 0) return fail(h, MSFEC_ERROR_INVALID_STATE, "no Ned_RT basis built yet");
@@ -2168,30 +2504,20 @@ namespace {
 
 constexpr size_t kNRStaticPoolBytes = size_t(32) << 20;  // 32 MiB per device
 constexpr int kNRStaticMaxCells = 4096;
-constexpr int kNRStaticMaxDevices = 64;
 constexpr int kNRPlanThreads = 1024;
 
 static __device__ __align__(256) unsigned char g_nr_static_pool[kNRStaticPoolBytes];
 
-struct NRStaticPoolSlot {
-  std::mutex m;
-  unsigned char *ptr = nullptr;
-};
-NRStaticPoolSlot g_nr_static_slots[kNRStaticMaxDevices];
-
-// Device address of this device's pool, looked up once per device with that
-// device current (the caller holds a DeviceGuard). The first lookup may load
-// this module onto the device; later calls only read the cached pointer.
-cudaError_t nr_static_pool(int device, unsigned char **out) {
-  NRStaticPoolSlot &s = g_nr_static_slots[device];
-  std::lock_guard<std::mutex> lk(s.m);
-  if (!s.ptr) {
-    void *p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_nr_static_pool);
-    if (e != cudaSuccess) return e;
-    s.ptr = static_cast<unsigned char *>(p);
-  }
-  *out = s.ptr;
+// Device address of the pool on the current device (the caller holds a
+// DeviceGuard). Looked up on every call rather than cached: the address is
+// only valid for the context that loaded this module, and a cached copy would
+// outlive a context torn down and recreated (cudaDeviceReset). The first
+// lookup on a device may load this module onto it.
+cudaError_t nr_static_pool(unsigned char **out) {
+  void *p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_nr_static_pool);
+  if (e != cudaSuccess) return e;
+  *out = static_cast<unsigned char *>(p);
   return cudaSuccess;
 }
 
@@ -2199,15 +2525,17 @@ cudaError_t nr_static_pool(int device, unsigned char **out) {
 // msfec_cell list: the same NRCell offsets and the same deepest-first item
 // order (stable within a depth) as the host planner of nedrt_build_impl.
 // One block; each thread owns a contiguous run of cells, a block-wide
-// inclusive scan gives the fine-cell offset, the DoF offset and four packed
+// inclusive scan gives the fine-cell offset, the DoF offset, the offset of the
+// cell's multilevel data (cells of depth >= 2 when ml is set) and four packed
 // 16-bit per-depth counters (ncells <= 4096 < 2^16).
 __global__ void __launch_bounds__(kNRPlanThreads)
-    nr_static_plan_kernel(const msfec_cell *in, int ncells, NRCell *cells, NRItem *items, int *queue) {
-  __shared__ long long s_fine[kNRPlanThreads], s_dofs[kNRPlanThreads], s_cnt[kNRPlanThreads];
+    nr_static_plan_kernel(const msfec_cell *in, int ncells, int ml, NRCell *cells, NRItem *items, int *queue) {
+  __shared__ long long s_fine[kNRPlanThreads], s_dofs[kNRPlanThreads], s_cnt[kNRPlanThreads],
+      s_ml[kNRPlanThreads];
   const int t = threadIdx.x;
   const int per = (ncells + kNRPlanThreads - 1) / kNRPlanThreads;
   const int c0 = min(ncells, t * per), c1 = min(ncells, c0 + per);
-  long long f = 0, d = 0, k = 0;
+  long long f = 0, d = 0, k = 0, m = 0;
   for (int c = c0; c < c1; ++c) {
     const int dep = in[c].depth, n = 1 << dep;
     int NEx, NFx, NE, NF;
@@ -2215,25 +2543,29 @@ __global__ void __launch_bounds__(kNRPlanThreads)
     f += (long long)n * n * n;
     d += NE + NF;
     k += 1LL << (16 * (dep - 1));
+    if (ml && n >= 4) m += nr_ml_cell_floats(n);
   }
   s_fine[t] = f;
   s_dofs[t] = d;
   s_cnt[t] = k;
+  s_ml[t] = m;
   __syncthreads();
   for (int off = 1; off < kNRPlanThreads; off <<= 1) {
-    long long af = 0, ad = 0, ak = 0;
+    long long af = 0, ad = 0, ak = 0, am = 0;
     if (t >= off) {
       af = s_fine[t - off];
       ad = s_dofs[t - off];
       ak = s_cnt[t - off];
+      am = s_ml[t - off];
     }
     __syncthreads();
     s_fine[t] += af;
     s_dofs[t] += ad;
     s_cnt[t] += ak;
+    s_ml[t] += am;
     __syncthreads();
   }
-  long long pf = s_fine[t] - f, pd = s_dofs[t] - d, pk = s_cnt[t] - k;
+  long long pf = s_fine[t] - f, pd = s_dofs[t] - d, pk = s_cnt[t] - k, pm = s_ml[t] - m;
   const long long total = s_cnt[kNRPlanThreads - 1];
   long long first[5] = {0, 0, 0, 0, 0};  // first cell slot of each depth, deepest first
   long long acc = 0;
@@ -2253,7 +2585,11 @@ __global__ void __launch_bounds__(kNRPlanThreads)
     q.n = n;
     q.coef_off = pf;
     q.dof_off = pd;
-    q.coarse_off = -1;  // no multilevel data in the static pool: diagonal preconditioner
+    q.coarse_off = -1;  // diagonal preconditioner
+    if (ml && n >= 4) {
+      q.coarse_off = pm;
+      pm += nr_ml_cell_floats(n);
+    }
     cells[c] = q;
     const long long slot = first[dep] + ((pk >> (16 * (dep - 1))) & 0xFFFF);
     for (int b = 0; b < 18; ++b) items[slot * 18 + b] = NRItem{c, b, 0};
@@ -2282,8 +2618,6 @@ msfec_status msfec_nedrt_build_noalloc(msfec_handle *h, int32_t ncells, const ms
     return fail(h, MSFEC_ERROR_INVALID_ARGUMENT,
                 "msfec_nedrt_build_noalloc: " + std::to_string(ncells) + " cells exceed the static limit of " +
                     std::to_string(kNRStaticMaxCells) + "; split the batch");
-  if (h->device < 0 || h->device >= kNRStaticMaxDevices)
-    return fail(h, MSFEC_ERROR_NOT_SUPPORTED, "msfec_nedrt_build_noalloc: device ordinal beyond 63");
   int64_t dofs = 0;
   int nmax = 0;
   for (int c = 0; c < ncells; ++c) {
@@ -2298,9 +2632,26 @@ msfec_status msfec_nedrt_build_noalloc(msfec_handle *h, int32_t ncells, const ms
   if (!load_ok(load) || !nr_load_ok(load)) return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "invalid Ned_RT load");
   if (ncells == 0) return MSFEC_SUCCESS;
 
-  // pool layout, every block 256-byte aligned
+  DeviceGuard g(h->device);
+  // launch shape: the same choice as msfec_nedrt_build_device for this batch
   const bool fp64 = h->cfg.precision == MSFEC_PRECISION_FP64;
   const size_t nitems = (size_t)ncells * 18;
+  const bool want_ml = h->cfg.nedrt_precond == 0 && nmax >= 4;
+  NRShape shape;
+  {
+    const msfec_status ss = nr_shape(h, nmax, fp64, want_ml, nitems, shape);
+    if (ss != MSFEC_SUCCESS) return ss;
+  }
+  const bool ml = shape.ml;
+  int64_t coarse_floats = 0, n_ml = 0;
+  if (ml)
+    for (int c = 0; c < ncells; ++c)
+      if (cells[c].depth >= 2) {
+        coarse_floats += nr_ml_cell_floats(1 << cells[c].depth);
+        ++n_ml;
+      }
+  // pool layout, every block 256-byte aligned; the multilevel setup scratch and
+  // the MINRES workspace share the tail (the setup kernel finishes first, in stream order)
   size_t off = 0;
   auto take = [&off](size_t bytes) {
     const size_t o = off;
@@ -2312,26 +2663,31 @@ msfec_status msfec_nedrt_build_noalloc(msfec_handle *h, int32_t ncells, const ms
   const size_t o_cells = take((size_t)ncells * sizeof(NRCell));
   const size_t o_items = take(nitems * sizeof(NRItem));
   const size_t o_stats = take(nitems * sizeof(NRStat));
+  const size_t o_coarse = take((size_t)coarse_floats * sizeof(float));
   const size_t o_phi = take((size_t)dofs * 18 * sizeof(double));
   const size_t o_y = take((size_t)dofs * 18 * sizeof(double));
   const size_t o_ws = off;
-  const size_t ws_floats = nr_workspace_floats(nmax, fp64 ? 8 : 4);
-  const bool use_smem = ws_floats * 4 <= kNRSmemLimit;
-  const size_t smem = use_smem ? ws_floats * 4 : 0;
-  int grid = std::min<int>((int)nitems, h->num_sms);
-  if (o_ws <= kNRStaticPoolBytes && !use_smem)
-    grid = std::min<int>(grid, (int)((kNRStaticPoolBytes - o_ws) / (ws_floats * 4)));
-  if (o_ws > kNRStaticPoolBytes || grid < 1)
+  const size_t left = o_ws <= kNRStaticPoolBytes ? kNRStaticPoolBytes - o_ws : 0;
+  const bool global_ws = !shape.use_smem || shape.split;  // per-CTA slot in the pool
+  const size_t slot_bytes = nr_static_round(shape.ws_floats * 4);
+  int grid = shape.grid;
+  if (global_ws) grid = std::min<int>(grid, (int)std::min<size_t>(left / slot_bytes, (size_t)1 << 30));
+  int NEx0, NFx0, NE0, NF0;
+  nr_counts(nmax, NEx0, NFx0, NE0, NF0);
+  const size_t ml_scratch = 4 * (((size_t)NE0 + NF0 + 63) / 64 * 64);  // floats per setup CTA
+  int ml_grid = 0;
+  if (ml)
+    ml_grid = (int)std::min<size_t>(std::min<int64_t>(n_ml, h->num_sms), left / nr_static_round(ml_scratch * 4));
+  if (o_ws > kNRStaticPoolBytes || grid < 1 || (ml && ml_grid < 1))
     return fail(h, MSFEC_ERROR_INVALID_ARGUMENT,
                 "msfec_nedrt_build_noalloc: the batch needs " + std::to_string(o_ws) + " bytes" +
-                    (use_smem ? std::string() : " + " + std::to_string(ws_floats * 4) + " per CTA workspace") +
+                    (global_ws ? " + " + std::to_string(slot_bytes) + " per CTA workspace" : std::string()) +
                     " of static scratch but the pool holds " + std::to_string(kNRStaticPoolBytes) +
                     " bytes per device; split the batch");
 
-  DeviceGuard g(h->device);
   unsigned char *pool = nullptr;
   {
-    const cudaError_t e = nr_static_pool(h->device, &pool);
+    const cudaError_t e = nr_static_pool(&pool);
     if (e != cudaSuccess) return cuda_fail(h, e, "cudaGetSymbolAddress(static Ned_RT pool)");
   }
   cudaStream_t st = h->stream;
@@ -2339,8 +2695,9 @@ msfec_status msfec_nedrt_build_noalloc(msfec_handle *h, int32_t ncells, const ms
   msfec_cell *d_in = reinterpret_cast<msfec_cell *>(pool + o_in);
   NRCell *d_cells = reinterpret_cast<NRCell *>(pool + o_cells);
   NRItem *d_items = reinterpret_cast<NRItem *>(pool + o_items);
+  float *d_coarse = reinterpret_cast<float *>(pool + o_coarse);
   MSFEC_CUDA_TRY(h, cudaMemcpyAsync(d_in, cells, (size_t)ncells * sizeof(msfec_cell), cudaMemcpyHostToDevice, st));
-  nr_static_plan_kernel<<<1, kNRPlanThreads, 0, st>>>(d_in, ncells, d_cells, d_items, queue);
+  nr_static_plan_kernel<<<1, kNRPlanThreads, 0, st>>>(d_in, ncells, ml ? 1 : 0, d_cells, d_items, queue);
   MSFEC_CUDA_TRY(h, cudaGetLastError());
   NRParams prm{};
   prm.cells = d_cells;
@@ -2352,15 +2709,27 @@ msfec_status msfec_nedrt_build_noalloc(msfec_handle *h, int32_t ncells, const ms
   prm.phi = reinterpret_cast<double *>(pool + o_phi);
   prm.y = reinterpret_cast<double *>(pool + o_y);
   prm.stats = reinterpret_cast<NRStat *>(pool + o_stats);
-  prm.scratch = use_smem ? nullptr : reinterpret_cast<float *>(pool + o_ws);
-  prm.scratch_floats = ws_floats;
-  prm.use_smem = use_smem ? 1 : 0;
+  prm.scratch = global_ws ? reinterpret_cast<float *>(pool + o_ws) : nullptr;
+  prm.scratch_floats = slot_bytes / 4;
+  prm.use_smem = shape.use_smem ? 1 : 0;
   prm.rtol = h->cfg.nedrt_rtol;
   prm.inner_rtol = h->cfg.inner_rtol;
   prm.max_iter = std::max(h->cfg.max_iter, 8000);
   prm.max_refine = h->cfg.max_refine;
-  if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[0], st));
-  MSFEC_CUDA_TRY(h, nedrt_solve_launch(fp64, false, prm, smem, grid, st));  // diagonal preconditioner
+  prm.coarse = ml ? d_coarse : nullptr;
+  prm.ml_offset = shape.ml_offset;
+  if (h->timing) MSFEC_CUDA_TRY(h, record_start(h, st));
+  if (ml)
+    MSFEC_CUDA_TRY(h, nedrt_ml_setup_launch(d_cells, ncells, d_ainv6, d_bdiv, d_coarse,
+                                            reinterpret_cast<float *>(pool + o_ws),
+                                            nr_static_round(ml_scratch * 4) / 4,
+                                            (size_t)nr_ml_data_floats(nmax) * 4, ml_grid, st));
+  if (h->timing && ml) {
+    MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[4], st));
+    h->ev_setup = true;
+  }
+  MSFEC_CUDA_TRY(h, shape.split ? nedrt_solve_launch_split(ml, prm, shape.smem, grid, st)
+                                : nedrt_solve_launch(fp64, ml, prm, shape.smem, grid, st));
   if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[1], st));
   msfec_load ld;
   if (load) {
@@ -2374,7 +2743,10 @@ msfec_status msfec_nedrt_build_noalloc(msfec_handle *h, int32_t ncells, const ms
     MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[3], st));
     h->ev_recorded = true;
   }
-  h->last_launches = d_reports ? 4 : 3;
+  // the handle's own basis no longer matches the latest build: a later
+  // msfec_nedrt_backward with reuse_basis set rebuilds instead of reusing it
+  h->nr_basis_current = false;
+  h->last_launches = (d_reports ? 4 : 3) + (ml ? 1 : 0);
   h->last_graph = 0;
   return MSFEC_SUCCESS;
 }

@@ -1370,7 +1370,14 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
 }
 
 // ML: multilevel face preconditioner (cells with coarse data), else diagonal.
-template <typename T, int NT, bool ML>
+// PLACE: where the MINRES workspace lives, one kernel per placement so that
+// each gets its own register allocation (fewer spills than one kernel that
+// branches between them): 1 shared memory, 0 this CTA's global slot (NT = 256
+// is the split workspace of the two-CTAs-per-SM variant). Keeping only the
+// apply's accumulation vector in shared memory for the global placement was
+// measured slower (3917 vs 3659 ms on 512 depth-4 cells): its 108 KB take L1
+// from the apply's scattered global gathers.
+template <typename T, int NT, bool ML, int PLACE>
 __global__ void __launch_bounds__(NT, 512 / NT) nedrt_solve_kernel(NRParams prm) {
   __shared__ NRShared sh;
   for (;;) {
@@ -1378,14 +1385,10 @@ __global__ void __launch_bounds__(NT, 512 / NT) nedrt_solve_kernel(NRParams prm)
     __syncthreads();
     const int item = sh.item;
     if (item >= prm.n_items) break;
-    if constexpr (NT == 256) {
+    if constexpr (NT == 256)
       solve_item<T, true, 256, ML>(prm, sh, item);  // split workspace: shared vectors + global x / coefficients
-    } else {
-      if (prm.use_smem)
-        solve_item<T, true, NT, ML>(prm, sh, item);
-      else
-        solve_item<T, false, NT, ML>(prm, sh, item);
-    }
+    else
+      solve_item<T, PLACE == 1, NT, ML>(prm, sh, item);
   }
 }
 
@@ -1518,11 +1521,12 @@ __global__ void nedrt_report_kernel(const NRStat *__restrict__ stats, int ncells
   r.iterations = 0;
   r.refinements = 0;
   r.converged = 1;
-  r.reserved = 0;
+  r.iterations_sum = 0;
   r.residual = 0.0;
   for (int v = 0; v < 18; ++v) {
     const NRStat s = stats[(size_t)c * 18 + v];
     r.iterations = max(r.iterations, s.iters);
+    r.iterations_sum += s.iters;
     r.refinements = max(r.refinements, s.refinements);
     r.converged = r.converged && s.converged && !(s.flags & 1);
     r.residual = fmax(r.residual, s.rel_residual);
@@ -2074,9 +2078,9 @@ __global__ void __launch_bounds__(kMLSetupThreads) nr_ml_setup_kernel(const NRCe
 
 }  // namespace nrimpl
 
-template <typename T, int NT, bool ML>
-static cudaError_t launch_solve(const NRParams &prm, size_t smem, int grid, cudaStream_t st, bool carveout) {
-  auto k = nrimpl::nedrt_solve_kernel<T, NT, ML>;
+template <typename T, int NT, bool ML, int PLACE>
+static cudaError_t launch_solve_p(const NRParams &prm, size_t smem, int grid, cudaStream_t st, bool carveout) {
+  auto k = nrimpl::nedrt_solve_kernel<T, NT, ML, PLACE>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   if (carveout) {
@@ -2085,6 +2089,16 @@ static cudaError_t launch_solve(const NRParams &prm, size_t smem, int grid, cuda
   }
   k<<<grid, NT, smem, st>>>(prm);
   return cudaGetLastError();
+}
+
+template <typename T, int NT, bool ML>
+static cudaError_t launch_solve(const NRParams &prm, size_t smem, int grid, cudaStream_t st, bool carveout) {
+  if constexpr (NT == 256) {
+    return launch_solve_p<T, NT, ML, 1>(prm, smem, grid, st, carveout);
+  } else {
+    if (prm.use_smem) return launch_solve_p<T, NT, ML, 1>(prm, smem, grid, st, carveout);
+    return launch_solve_p<T, NT, ML, 0>(prm, smem, grid, st, carveout);
+  }
 }
 
 // ml: the multilevel variant (prm.coarse set); smem includes its region.
@@ -2103,7 +2117,7 @@ cudaError_t nedrt_solve_launch_split(bool ml, const NRParams &prm, size_t smem, 
 }
 
 cudaError_t nedrt_split_occupancy(bool ml, size_t smem, int *blocks_per_sm) {
-  auto k = ml ? nrimpl::nedrt_solve_kernel<float, 256, true> : nrimpl::nedrt_solve_kernel<float, 256, false>;
+  auto k = ml ? nrimpl::nedrt_solve_kernel<float, 256, true, 1> : nrimpl::nedrt_solve_kernel<float, 256, false, 1>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);

@@ -118,4 +118,51 @@ __host__ __device__ inline Q1Smem q1_smem_layout(int n, int R, int nslab, bool h
   return s;
 }
 
+// ---- tensor-coefficient Q1 solver (q1g_solve.cu): one (cell, coarse vertex)
+// item per CTA, cell-wise quadrature apply.
+struct Q1GItem {
+  int cell;
+  int vertex;  // coarse vertex 0..7 (basis mode) / right-hand side plane (source mode)
+  int mode;    // 0 basis function, 1 source: zero Dirichlet data, right-hand side from src_rhs
+  int pad;
+};
+
+struct Q1GParams {
+  const Q1Cell *cells;
+  const Q1GItem *items;
+  int n_items;
+  int *queue;
+  const double *a;  // 6 (tensor) or 48 (Gauss points) doubles per fine cell
+  int gauss;
+  const double *react;  // per fine cell or null
+  const float *ed;      // element data per fine cell, q1g_ed_floats(gauss) floats (q1g_prepare_kernel)
+  double *phi;          // basis mode: [cell][8][(n+1)^3] at 8 node_off
+  double *y;            // K phi, same layout
+  const double *src_rhs;  // source mode: [cell][8][(n+1)^3] right-hand sides
+  double *src_out;        // source mode: solutions, same layout
+  Q1Stat *stats;          // [cell][8]
+  float *scratch;         // per-CTA global workspace (vectors that exceed shared memory)
+  size_t scratch_floats;
+  double rtol;
+  double inner_rtol;
+  int max_iter;
+  int max_refine;
+};
+
+constexpr int kQ1GThreads = 256;
+constexpr int kQ1GWarps = kQ1GThreads / 32;
+
+// Floats of element data per fine cell: the scaled tensor(s) B (6 per point,
+// one point for a tensor per cell, 8 Gauss points), r |e|, pad to 16 bytes.
+__host__ __device__ inline int q1g_ed_floats(int gauss) { return gauss ? 52 : 8; }
+
+// Workspace (floats) of one item: Jacobi scaling (float) + x, r, p, q of
+// precision T over the padded node set; ed_floats more when the cell's element
+// data is staged too.
+__host__ __device__ inline size_t q1g_vec_floats(int n, int tsize) {
+  const size_t nn = (size_t)(n + 1) * (n + 1) * (n + 1);
+  const size_t Np = (nn + 63) / 64 * 64;
+  return Np + 4 * Np * (size_t)(tsize / 4);
+}
+
 }  // namespace msfec

@@ -103,11 +103,12 @@ __global__ void q1_report_kernel(const Q1Stat *__restrict__ stats, int ncells, m
   r.iterations = 0;
   r.refinements = 0;
   r.converged = 1;
-  r.reserved = 0;
+  r.iterations_sum = 0;
   r.residual = 0.0;
   for (int v = 0; v < 8; ++v) {
     const Q1Stat s = stats[(size_t)c * 8 + v];
     r.iterations = max(r.iterations, s.iters);
+    r.iterations_sum += s.iters;
     r.refinements = max(r.refinements, s.refinements);
     r.converged = r.converged && s.converged && !(s.flags & 1);
     r.residual = fmax(r.residual, s.rel_residual);

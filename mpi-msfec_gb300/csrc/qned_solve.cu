@@ -912,11 +912,12 @@ __global__ void qned_report_kernel(const NRStat *__restrict__ stats, int ncells,
   r.iterations = 0;
   r.refinements = 0;
   r.converged = 1;
-  r.reserved = 0;
+  r.iterations_sum = 0;
   r.residual = 0.0;
   for (int b = 0; b < kQNBases; ++b) {
     const NRStat s = stats[(size_t)c * kQNBases + b];
     r.iterations = max(r.iterations, s.iters);
+    r.iterations_sum += s.iters;
     r.refinements = max(r.refinements, s.refinements);
     r.converged = r.converged && s.converged && !(s.flags & 1);
     r.residual = fmax(r.residual, s.rel_residual);

@@ -14,11 +14,12 @@ static void check(msfec_handle *h, msfec_status s, const char *where) {
     throw BasisError(s, std::string(where) + ": " + msfec_status_string(s) + ": " + (h ? msfec_last_error(h) : ""));
 }
 
-BasisBatch::BasisBatch(int device, int precision) {
+BasisBatch::BasisBatch(int device, int precision, int q1_coefficient) {
   msfec_config cfg;
   msfec_config_default(&cfg);
   cfg.device = device;
   cfg.precision = precision;
+  cfg.q1_coefficient = q1_coefficient;
   check(nullptr, msfec_create(&handle_, &cfg), "msfec_create");
 }
 
@@ -44,6 +45,21 @@ static void for_each_fine_centre(const msfec_cell &c, F &&f) {
       for (int i = 0; i < n; ++i)
         f(Point{c.origin[0] + (i + 0.5) * c.size[0] / n, c.origin[1] + (j + 0.5) * c.size[1] / n,
                 c.origin[2] + (k + 0.5) * c.size[2] / n});
+}
+
+// The 2x2x2 Gauss points (x fastest) of every fine cell of a coarse cell,
+// fine cells in the ABI's lexicographic order.
+template <typename F>
+static void for_each_fine_gauss_point(const msfec_cell &c, F &&f) {
+  const int n = 1 << c.depth;
+  const double g = 0.5 / std::sqrt(3.0);
+  const double xi[2] = {0.5 - g, 0.5 + g};
+  for (int k = 0; k < n; ++k)
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i)
+        for (int q = 0; q < 8; ++q)
+          f(Point{c.origin[0] + (i + xi[q & 1]) * c.size[0] / n, c.origin[1] + (j + xi[(q >> 1) & 1]) * c.size[1] / n,
+                  c.origin[2] + (k + xi[q >> 2]) * c.size[2] / n});
 }
 
 namespace Q {
@@ -86,7 +102,9 @@ double QBasis::global_solution_value(const Point &x) const {
   return batch_->evaluate(slot_, global_weights_, x);
 }
 
-Q1Batch::Q1Batch(Q1Coefficients coeff, int device, int precision) : coeff_(std::move(coeff)), gpu_(device, precision) {}
+Q1Batch::Q1Batch(Q1Coefficients coeff, int device, int precision)
+    : coeff_(std::move(coeff)),
+      gpu_(device, precision, coeff_.diffusion_tensor ? MSFEC_Q1_COEF_GAUSS : MSFEC_Q1_COEF_SCALAR) {}
 
 int Q1Batch::enqueue(const CoarseCell &cell, unsigned depth) {
   if (built_) {  // a new cell after a build starts a new batch
@@ -100,11 +118,18 @@ int Q1Batch::enqueue(const CoarseCell &cell, unsigned depth) {
 void Q1Batch::flush() {
   if (built_) return;
   std::vector<double> a, r;
-  for (const msfec_cell &c : cells_)
+  for (const msfec_cell &c : cells_) {
+    if (coeff_.diffusion_tensor) {
+      for_each_fine_gauss_point(c, [&](const Point &p) {  // a00 a11 a22 a01 a02 a12 of the symmetric part
+        const std::array<double, 9> m = coeff_.diffusion_tensor(p);
+        a.insert(a.end(), {m[0], m[4], m[8], 0.5 * (m[1] + m[3]), 0.5 * (m[2] + m[6]), 0.5 * (m[5] + m[7])});
+      });
+    }
     for_each_fine_centre(c, [&](const Point &p) {
-      a.push_back(coeff_.diffusion(p));
+      if (!coeff_.diffusion_tensor) a.push_back(coeff_.diffusion(p));
       if (coeff_.reaction) r.push_back(coeff_.reaction(p));
     });
+  }
   const int nc = (int)cells_.size();
   std::vector<double> KH((size_t)nc * 64), FH((size_t)nc * 8);
   reports_.assign(nc, msfec_cell_report{});
@@ -154,6 +179,8 @@ QStd::QStd(const ParametersStd &parameters, Q1Coefficients coeff)
     : parameters_(parameters), coeff_(std::move(coeff)), gpu_(parameters.device, parameters.precision) {}
 
 void QStd::run() {
+  if (!coeff_.diffusion)
+    throw BasisError(MSFEC_ERROR_NOT_SUPPORTED, "QStd: the standard fine solve takes a scalar diffusion callback");
   const msfec_cell dom = unit_cube(parameters_.n_refine);
   std::vector<double> a, r;
   for_each_fine_centre(dom, [&](const Point &p) {

@@ -92,7 +92,8 @@ struct ParametersStd {
 // One GPU handle and the pending cells of one batch.
 class BasisBatch {
  public:
-  explicit BasisBatch(int device = 0, int precision = MSFEC_PRECISION_MIXED);
+  explicit BasisBatch(int device = 0, int precision = MSFEC_PRECISION_MIXED,
+                      int q1_coefficient = MSFEC_Q1_COEF_SCALAR);
   ~BasisBatch();
   BasisBatch(const BasisBatch &) = delete;
   BasisBatch &operator=(const BasisBatch &) = delete;
@@ -104,10 +105,15 @@ class BasisBatch {
 
 namespace Q {
 
-// Scalar diffusion a(x) > 0, reaction r(x) >= 0 (r may be empty = zero, the
-// reference's ReactionRate), load f as an msfec_load.
+// Diffusion: either a scalar a(x) > 0, sampled at fine-cell centres, or the
+// reference's tensor coefficient (Diffusion_A::value, row-major 3x3, SPD),
+// evaluated like the reference's assembly at the 2x2x2 Gauss points of every
+// fine cell (Diffusion_A::value_list, source/Q/q_basis.cc:218-231); the
+// tensor, when set, takes precedence. Reaction r(x) >= 0 (may be empty =
+// zero, the reference's ReactionRate), load f as an msfec_load.
 struct Q1Coefficients {
   std::function<double(const Point &)> diffusion;
+  std::function<std::array<double, 9>(const Point &)> diffusion_tensor;
   std::function<double(const Point &)> reaction;
   msfec_load load{MSFEC_LOAD_ZERO, 0, {0, 0, 0, 0}};
 };

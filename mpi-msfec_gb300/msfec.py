@@ -24,6 +24,7 @@ ERROR_NOT_SUPPORTED = 5
 ERROR_NUMERICAL = 6
 ERROR_INVALID_STATE = 7
 KIND_Q1, KIND_NEDRT = 1, 2
+Q1_COEF_SCALAR, Q1_COEF_TENSOR, Q1_COEF_GAUSS = 0, 1, 2  # msfec_config.q1_coefficient
 
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
@@ -38,6 +39,7 @@ EXPORTED = [
     "msfec_q1_basis_device", "msfec_q1_eval_fine", "msfec_set_timing", "msfec_get_timings",
     "msfec_nedrt_build", "msfec_nedrt_build_device", "msfec_nedrt_basis_size",
     "msfec_nedrt_get_basis", "msfec_q1_backward", "msfec_nedrt_build_noalloc",
+    "msfec_q1_get_basis_cells", "msfec_nedrt_get_basis_cells",
     "msfec_set_graph", "msfec_autotune", "msfec_q1_fine_solve", "msfec_nedrt_backward",
     "msfec_qned_build", "msfec_qned_build_device", "msfec_qned_basis_size", "msfec_qned_get_basis",
     "msfec_rtdq_build", "msfec_rtdq_build_device", "msfec_rtdq_basis_size", "msfec_rtdq_get_basis",
@@ -50,7 +52,7 @@ class Config(ctypes.Structure):
                 ("inner_rtol", ctypes.c_double), ("max_iter", ctypes.c_int32),
                 ("max_refine", ctypes.c_int32), ("verbose", ctypes.c_int32),
                 ("q1_launch", ctypes.c_int32), ("nedrt_rtol", ctypes.c_double),
-                ("nedrt_precond", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("nedrt_precond", ctypes.c_int32), ("q1_coefficient", ctypes.c_int32)]
 
 
 class Cell(ctypes.Structure):
@@ -65,20 +67,21 @@ class Load(ctypes.Structure):
 
 class CellReport(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int32), ("refinements", ctypes.c_int32),
-                ("converged", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("converged", ctypes.c_int32), ("iterations_sum", ctypes.c_int32),
                 ("residual", ctypes.c_double)]
 
 
 class Timings(ctypes.Structure):
     _fields_ = [("solve_ms", ctypes.c_float), ("galerkin_ms", ctypes.c_float),
                 ("total_ms", ctypes.c_float), ("solve_launches", ctypes.c_int32),
-                ("kernel_launches", ctypes.c_int32), ("graph", ctypes.c_int32)]
+                ("kernel_launches", ctypes.c_int32), ("graph", ctypes.c_int32),
+                ("setup_ms", ctypes.c_float)]
 
 
 CELL_DTYPE = np.dtype([("origin", "<f8", (3,)), ("size", "<f8", (3,)), ("depth", "<i4"),
                        ("reserved", "<i4")])
 REPORT_DTYPE = np.dtype([("iterations", "<i4"), ("refinements", "<i4"), ("converged", "<i4"),
-                         ("reserved", "<i4"), ("residual", "<f8")])
+                         ("iterations_sum", "<i4"), ("residual", "<f8")])
 assert CELL_DTYPE.itemsize == ctypes.sizeof(Cell)
 assert REPORT_DTYPE.itemsize == ctypes.sizeof(CellReport)
 
@@ -132,6 +135,9 @@ def load_library(path: str = LIB_PATH):
     L.msfec_nedrt_basis_size.restype = ctypes.c_int64
     L.msfec_nedrt_get_basis.argtypes = [_vp, _dp, ctypes.c_int64]
     L.msfec_nedrt_get_basis.restype = ctypes.c_int
+    for name in ("msfec_q1_get_basis_cells", "msfec_nedrt_get_basis_cells"):
+        getattr(L, name).argtypes = [_vp, ctypes.c_int32, ctypes.c_int32, _dp, ctypes.c_int64]
+        getattr(L, name).restype = ctypes.c_int
     L.msfec_q1_backward.argtypes = [_vp, ctypes.c_int32, _vp, _dp, _dp, ctypes.POINTER(Load), ctypes.c_int32,
                                     _dp, _dp, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32), _dp, _dp, _dp]
     L.msfec_q1_backward.restype = ctypes.c_int
@@ -202,7 +208,8 @@ class Handle:
     """One msfec handle (device buffers + stream)."""
 
     def __init__(self, precision=PRECISION_MIXED, device=0, rtol=None, inner_rtol=None,
-                 max_iter=None, max_refine=None, verbose=0, nedrt_rtol=None, q1_launch=0, nedrt_precond=0):
+                 max_iter=None, max_refine=None, verbose=0, nedrt_rtol=None, q1_launch=0, nedrt_precond=0,
+                 q1_coefficient=0):
         L = load_library()
         cfg = Config()
         L.msfec_config_default(ctypes.byref(cfg))
@@ -221,6 +228,7 @@ class Handle:
         cfg.verbose = int(verbose or os.environ.get("MSFEC_VERBOSE", "0"))
         cfg.q1_launch = int(q1_launch)
         cfg.nedrt_precond = int(nedrt_precond)
+        cfg.q1_coefficient = int(q1_coefficient)
         self.cfg = cfg
         h = _vp()
         st = L.msfec_create(ctypes.byref(h), ctypes.byref(cfg))
@@ -354,7 +362,7 @@ class Handle:
         self.check(self._lib.msfec_get_timings(self._h, ctypes.byref(t)))
         return {"solve_ms": t.solve_ms, "galerkin_ms": t.galerkin_ms, "total_ms": t.total_ms,
                 "solve_launches": t.solve_launches, "kernel_launches": t.kernel_launches,
-                "graph": t.graph}
+                "graph": t.graph, "setup_ms": t.setup_ms}
 
     def q1_backward(self, cells, a, reaction, load, U, lam, cell_of, points, dJ_du, reuse_basis=True):
         """dJ/d log a per fine cell (msfec_q1_backward)."""
@@ -469,6 +477,25 @@ class Handle:
         out = np.zeros(n)
         self.check(self._lib.msfec_q1_get_basis(self._h, _d(out), n))
         return out
+
+    def q1_basis_cells(self, cells, first, count):
+        """Basis of cells [first, first + count) of the last Q1 build `cells`:
+        a list of [8, (n+1)^3] arrays."""
+        n1 = (1 << cells["depth"][first:first + count].astype(np.int64)) + 1
+        out = np.zeros(int(np.sum(8 * n1 ** 3)))
+        self.check(self._lib.msfec_q1_get_basis_cells(self._h, first, count, _d(out), out.size))
+        sizes = np.cumsum(np.concatenate([[0], 8 * n1 ** 3]))
+        return [out[sizes[i]:sizes[i + 1]].reshape(8, -1) for i in range(count)]
+
+    def nedrt_basis_cells(self, cells, first, count):
+        """Basis of cells [first, first + count) of the last Ned_RT build
+        `cells`: a list of [18, NE + NF] arrays."""
+        n = 1 << cells["depth"][first:first + count].astype(np.int64)
+        nd = 3 * n * (n + 1) ** 2 + 3 * n * n * (n + 1)
+        out = np.zeros(int(np.sum(18 * nd)))
+        self.check(self._lib.msfec_nedrt_get_basis_cells(self._h, first, count, _d(out), out.size))
+        sizes = np.cumsum(np.concatenate([[0], 18 * nd]))
+        return [out[sizes[i]:sizes[i + 1]].reshape(18, -1) for i in range(count)]
 
     def q1_eval_fine(self, weights, cell_of, points):
         weights = np.ascontiguousarray(weights, dtype=np.float64)

@@ -93,6 +93,60 @@ def q1_uneven(m=16, seed=3, eps=1.0 / 64.0, depths=(2, 3, 4, 5)):
     return cells, a, None, load
 
 
+GAUSS_2 = np.array([0.5 - 0.5 / np.sqrt(3.0), 0.5 + 0.5 / np.sqrt(3.0)])
+
+
+def gauss_points(cells):
+    """The 2x2x2 Gauss points (x fastest) of every fine cell: [sum n^3, 8, 3]."""
+    out = []
+    for c in cells:
+        n = 1 << int(c["depth"])
+        h = c["size"] / n
+        t = np.arange(n)
+        k, j, i = np.meshgrid(t, t, t, indexing="ij")
+        base = np.stack([i.ravel(), j.ravel(), k.ravel()], 1).astype(np.float64)
+        q = np.array([[GAUSS_2[g & 1], GAUSS_2[(g >> 1) & 1], GAUSS_2[g >> 2]] for g in range(8)])
+        out.append(c["origin"][None, None, :] + (base[:, None, :] + q[None, :, :]) * h[None, None, :])
+    return np.concatenate(out, axis=0)
+
+
+def euler_rotation(alpha=np.pi / 3, beta=np.pi / 6, gamma=np.pi / 4):
+    """The fixed rotation of the reference's Diffusion_A
+    (source/equation_data/eqn_coeff_A.cc:25-42; Euler angles pi/3, pi/6, pi/4)."""
+    ca, sa, cb, sb, cg, sg = np.cos(alpha), np.sin(alpha), np.cos(beta), np.sin(beta), np.cos(gamma), np.sin(gamma)
+    return np.array([[ca * cg - sa * cb * sg, -ca * sg - sa * cb * cg, sa * sb],
+                     [sa * cg + ca * cb * sg, -sa * sg + ca * cb * cg, -ca * sb],
+                     [sb * sg, sb * cg, cb]])
+
+
+def reference_diffusion(points, freq=(17, 16, 15), alpha=(0.9, 0.9, 0.9), scale=(1.0, 1.0, 1.0), rotate=True):
+    """The reference's Q1 diffusion tensor at points [..., 3]
+    (Diffusion_A::value_list, eqn_coeff_A.cc:162-191): diag(scale_d (1 - alpha_d
+    sin(2 pi k_d x_d))), rotated by R . R^T; defaults of
+    example_parameters/prm_q_test-01.prm (frequencies 17/16/15, alpha 0.9,
+    rotate = true). Returns [..., 6] (a00 a11 a22 a01 a02 a12)."""
+    x = np.asarray(points, dtype=np.float64)
+    d = np.stack([scale[q] * (1.0 - alpha[q] * np.sin(2.0 * np.pi * freq[q] * x[..., q])) for q in range(3)], -1)
+    R = euler_rotation() if rotate else np.eye(3)
+    A = np.einsum("ij,...j,kj->...ik", R, d, R)
+    return np.stack([A[..., 0, 0], A[..., 1, 1], A[..., 2, 2], A[..., 0, 1], A[..., 0, 2], A[..., 1, 2]], -1)
+
+
+def q1_reference_tensor(m=2, depth=3, gauss=True, freq=(17, 16, 15)):
+    """Q1 workload with the reference's example coefficient (rotated
+    oscillatory Diffusion_A of prm_q_test-01.prm) on coarse m^3 cells of the
+    unit cube: the tensor at each fine cell's Gauss points (gauss=True, 48 per
+    fine cell) or at its centre (6 per fine cell); no reaction; the
+    example's load f = sin(2 pi x) sin(2 pi y) sin(2 pi z)."""
+    cells = coarse_grid(m, depth)
+    if gauss:
+        a = reference_diffusion(gauss_points(cells), freq=freq).reshape(-1, 48)
+    else:
+        a = reference_diffusion(fine_centres(cells), freq=freq)
+    load = make_load(LOAD_SIN_PRODUCT, (1.0, 2.0, 0.0, 0.0))
+    return cells, a, None, load
+
+
 def haar_rotations(rng, count):
     """Haar-random rotations: QR of Gaussian 3x3 with the sign of diag(R) fixed, det +1."""
     G = rng.standard_normal((count, 3, 3))
@@ -111,10 +165,14 @@ def nedrt_tensor(m=8, depth=3, seed=2, kb=14.0):
     cells = coarse_grid(m, depth)
     nf = int(np.sum(fine_counts(cells)[0]))
     g = rng.standard_normal((nf, 3))
-    Rr = haar_rotations(rng, nf)
-    ainv = np.einsum("cij,cj,ckj->cik", Rr, np.exp(-g), Rr)
-    ainv6 = np.stack([ainv[:, 0, 0], ainv[:, 1, 1], ainv[:, 2, 2], ainv[:, 0, 1], ainv[:, 0, 2],
-                      ainv[:, 1, 2]], 1)
+    ainv6 = np.empty((nf, 6))
+    chunk = 1 << 20  # rotations drawn in chunks: the same stream as one draw, less memory
+    for lo in range(0, nf, chunk):
+        hi = min(nf, lo + chunk)
+        Rr = haar_rotations(rng, hi - lo)
+        ainv = np.einsum("cij,cj,ckj->cik", Rr, np.exp(-g[lo:hi]), Rr)
+        ainv6[lo:hi] = np.stack([ainv[:, 0, 0], ainv[:, 1, 1], ainv[:, 2, 2], ainv[:, 0, 1], ainv[:, 0, 2],
+                                 ainv[:, 1, 2]], 1)
     x = fine_centres(cells)[:, 0]
     bdiv = 1.0 - 0.9 * np.sin(2 * np.pi * kb * x)
     load = make_load(LOAD_VEC_TRIG, (1.0, 1.0, 0.0, 0.0))

@@ -44,17 +44,22 @@ def global_rhs(m, FH):
 
 
 class MisfitProblem:
-    def __init__(self, msfec, cells, m, load, cell_of, points, data, precision, rtol=None):
+    """theta per fine cell: a = exp(theta) (scalar layout), or A_e = exp(theta_e)
+    base_e for a tensor coefficient base (layout TENSOR: [fine, 6], GAUSS:
+    [fine, 48])."""
+
+    def __init__(self, msfec, cells, m, load, cell_of, points, data, precision, rtol=None, base=None, layout=0):
         self.msfec, self.cells, self.m, self.load = msfec, cells, m, load
         self.cell_of = np.asarray(cell_of, dtype=np.int32)
         self.points = np.asarray(points, dtype=np.float64)
         self.data = np.asarray(data, dtype=np.float64)
-        self.h = msfec.Handle(precision=precision, rtol=rtol)
+        self.base = None if base is None else np.asarray(base, dtype=np.float64)
+        self.h = msfec.Handle(precision=precision, rtol=rtol, q1_coefficient=layout)
         self.nodes = cell_nodes(m)
 
     def forward(self, theta):
         """J and the state needed by the gradient."""
-        a = np.exp(theta)
+        a = np.exp(theta) if self.base is None else self.base * np.exp(theta)[:, None]
         KH, FH, rep, st = self.h.q1_build(self.cells, a, None, self.load)
         K, I = coarse_system(self.m, KH)
         Kii = spla.splu(K[I][:, I].tocsc())

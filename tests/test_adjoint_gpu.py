@@ -47,6 +47,30 @@ def test_gradient_matches_central_differences(gpu, precision):
             assert abs(fd - ad) <= 1e-6 * abs(fd), (t, fd, ad)
 
 
+def test_gradient_at_adjoint_benchmark_scale(gpu):
+    """The adjoint benchmark's size: coarse 8^3 x depth 4 (2.1 M fine cells),
+    log a ~ N(0,1) i.i.d. per fine cell (seed 4), 512 seeded observation
+    points, data from a second seeded coefficient; central differences
+    (h = 1e-6) along 16 seeded random directions against grad . d, with the
+    stated tolerance 1e-6 of sum |g_i d_i| (over 2 M parameters a random
+    direction cancels the directional derivative by ~1/sqrt(N), so it is the
+    only scale that measures the gradient's error)."""
+    prob, theta = _problem(gpu, "mixed", m=8, depth=4, npts=512, seed=4, rtol=1e-14)
+    J, state = prob.forward(theta)
+    grad = prob.gradient(theta, state)
+    rng = np.random.default_rng(16)
+    h = 1e-6
+    worst = 0.0
+    for t in range(16):
+        d = rng.standard_normal(theta.shape)
+        fd = (prob.forward(theta + h * d)[0] - prob.forward(theta - h * d)[0]) / (2 * h)
+        ad = float(grad @ d)
+        scale = float(np.abs(grad * d).sum())
+        worst = max(worst, abs(fd - ad) / scale)
+        assert abs(fd - ad) <= 1e-6 * scale, (t, fd, ad, scale)
+    print(f"config-4 scale: 16 directions, max |fd - g.d| / sum|g d| = {worst:.2e}")
+
+
 def test_mixed_gradient_matches_fp64_gradient(gpu):
     pm, theta = _problem(gpu, "mixed")
     pf, _ = _problem(gpu, "fp64")

@@ -76,6 +76,27 @@ def test_qbasis_shim_example_driver(gpu):
     assert res["coarse_cg_iterations"] > 0 and np.isfinite(res["u_centre"])
 
 
+def test_qbasis_shim_reference_tensor_coefficient(gpu, oracle_lib):
+    """The shim driver with the reference's own Q1 coefficient (rotated
+    Diffusion_A of prm_q_test-01.prm as a tensor callback, evaluated by the
+    shim at the Gauss points): its K_H equals the C ABI's GAUSS-layout build
+    and the oracle's quadrature assembly to 1e-10."""
+    import msfec_build
+    out = subprocess.run([msfec_build.EXAMPLE, "2", "2", "reference"], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    res = json.loads(out.stdout.strip().splitlines()[-1])
+    KHs = np.array(res["KH"]).reshape(-1, 8, 8)
+    cells, a, r, load = workloads.q1_reference_tensor(m=2, depth=2, gauss=True)
+    h = gpu.Handle(q1_coefficient=gpu.Q1_COEF_GAUSS)
+    KH, FH, rep, st = h.q1_build(cells, a, r, load)
+    ref = oracle_lib.q1_build(cells["origin"], cells["size"], cells["depth"], a, r, load_kind=load.kind,
+                              load_params=list(load.params), want_phi=False, coef_mode=oracle_lib.COEF_GAUSS)
+    for c in range(len(cells)):
+        scale = np.abs(ref["KH"][c]).max()
+        assert np.abs(KHs[c] - KH[c]).max() <= 1e-10 * scale
+        assert np.abs(KH[c] - ref["KH"][c]).max() <= 1e-10 * scale
+
+
 def test_nedrtbasis_shim_example_driver(gpu):
     """The C++ NedRTBasis-compatible shim driver (run, getters, host coarse
     solve, set_global_weights, fine sigma/u) against the same build through the
