@@ -92,7 +92,11 @@ typedef struct msfec_config {
      items: 0 = autotuned (msfec_autotune) or else one fused launch,
      1 = one fused launch, 2 = split cluster / non-cluster launches. */
   int32_t q1_launch;
-  /* Ned_RT local solves stop when ||r||_2 <= nedrt_rtol * ||f_I - A_IB g||_2.
+  /* The mixed local solves (Ned_RT, Q_Ned, RT_DQ) stop when
+     ||r||_P <= nedrt_rtol * ||f_I - A_IB g||_P, ||v||_P^2 = v^T P v with P the
+     solver's (block-diagonal) preconditioner: the norm MINRES minimises, and
+     one that weighs the edge and face rows alike whatever the fine mesh size
+     (the face rows of the unscaled system outweigh the edge rows by ~h^-2).
      The mixed local system has condition number ~1e4 at depth 3, so 1e-14
      is needed for a 1e-10 basis error. */
   double nedrt_rtol;
@@ -424,8 +428,9 @@ msfec_status msfec_autotune(msfec_handle *handle, int32_t kind, int32_t ncells,
  *   grad_a, grad_b  [fine cells] outputs
  * Four adjoint local problems per cell (edge / face bases x lambda / U
  * weights) run as source items of the batched MINRES solver (A^T = S A S, S
- * = -1 on face rows), to max(nedrt_rtol, 1e-11) relative residual, taken
- * relative to max(||f||, 1e-3 of the cell's adjoint source scale) (the
+ * = -1 on face rows), to max(nedrt_rtol, 1e-11) relative residual (in the
+ * preconditioner's norm), taken relative to max(||f||_P, 1e-3 of the P-norm
+ * of the cell's adjoint source scale) (the
  * right-hand sides are projections and differences that can cancel to
  * rounding); the basis is rebuilt unless reuse_basis != 0 and the
  * last Ned_RT build on this handle is the same batch. Coefficients are

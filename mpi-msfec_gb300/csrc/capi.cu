@@ -80,7 +80,7 @@ cudaError_t nedrt_adjoint_prepare_launch(const NRCell *cells, int ncells, const 
                                          const double *lam, const msfec_load &load, int npoints, const int *cell_of,
                                          const double *pts, const double *dJdu, const double *ainv6,
                                          const double *bdiv, double *comb, double *bload, double *e, double *work,
-                                         double *rhs, double *floor_out, cudaStream_t st);
+                                         double *rhs, double *scale2_out, cudaStream_t st);
 cudaError_t nedrt_adjoint_gradient_launch(const NRCell *cells, int ncells, const double *ainv6, const double *bdiv,
                                           const double *comb, const double *work, const double *xsol, double *ga,
                                           double *gb, cudaStream_t st);
@@ -197,13 +197,13 @@ struct msfec_handle {
   bool nr_basis_current = false;       // nr_phi holds the latest Ned_RT build (none came after it)
   // Ned_RT adjoint buffers
   DevBuf<double> nra_U, nra_lam, nra_comb, nra_b, nra_e, nra_work, nra_rhs, nra_x, nra_pts, nra_dJ, nra_ga, nra_gb,
-      nra_floor;
+      nra_scale2;
   DevBuf<int> nra_cell;
   DevBuf<NRItem> nra_items;
   // Ned_RT standard fine solve: the domain as one cell
   DevBuf<NRCell> nrf_cell;
   DevBuf<NRItem> nrf_item;
-  DevBuf<double> nrf_b, nrf_x, nrf_floor;
+  DevBuf<double> nrf_b, nrf_x;
   DevBuf<NRStat> nrf_stats;
   DevBuf<float> nrf_scratch;
   // Q_Ned state of the last build
@@ -808,7 +808,10 @@ msfec_status q1g_backward_impl(msfec_handle *h, int ncells, const msfec_cell *ce
   prm.stats = h->stats.ptr;
   prm.scratch = placement == 0 ? h->q1g_scratch.ptr : nullptr;
   prm.scratch_floats = q1g_vec_floats(nmax, ts);
-  prm.rtol = h->cfg.rtol;
+  // the adjoint right-hand sides (load and observation bubbles) stop at
+  // max(rtol, 1e-12): their FP64 residual floor at depth >= 4 can sit above 1e-14,
+  // and 1e-12 already puts the gradient far inside its 1e-6 finite-difference check
+  prm.rtol = std::max(h->cfg.rtol, 1e-12);
   prm.inner_rtol = h->cfg.inner_rtol;
   prm.max_iter = std::max(h->cfg.max_iter, 4 * nmax * nmax);
   prm.max_refine = h->cfg.max_refine;
@@ -891,7 +894,10 @@ msfec_status q1_backward_impl(msfec_handle *h, int ncells, const msfec_cell *cel
   prm.src_rhs = h->adj_rhs.ptr;
   prm.src_out = h->adj_sol.ptr;
   prm.stats = h->stats.ptr;
-  prm.rtol = h->cfg.rtol;
+  // the adjoint right-hand sides (load and observation bubbles) stop at
+  // max(rtol, 1e-12): their FP64 residual floor at depth >= 4 can sit above 1e-14,
+  // and 1e-12 already puts the gradient far inside its 1e-6 finite-difference check
+  prm.rtol = std::max(h->cfg.rtol, 1e-12);
   prm.inner_rtol = h->cfg.inner_rtol;
   prm.max_iter = h->cfg.max_iter;
   prm.max_refine = h->cfg.max_refine;
@@ -1468,7 +1474,7 @@ void msfec_destroy(msfec_handle *h) {
     h->nr_KH.release();
     h->nr_FH.release();
     for (DevBuf<double> *b : {&h->nra_U, &h->nra_lam, &h->nra_comb, &h->nra_b, &h->nra_e, &h->nra_work, &h->nra_rhs,
-                              &h->nra_x, &h->nra_pts, &h->nra_dJ, &h->nra_ga, &h->nra_gb, &h->nra_floor})
+                              &h->nra_x, &h->nra_pts, &h->nra_dJ, &h->nra_ga, &h->nra_gb, &h->nra_scale2})
       b->release();
     h->nra_cell.release();
     h->nra_items.release();
@@ -1476,7 +1482,6 @@ void msfec_destroy(msfec_handle *h) {
     h->nrf_item.release();
     h->nrf_b.release();
     h->nrf_x.release();
-    h->nrf_floor.release();
     h->nrf_stats.release();
     h->nrf_scratch.release();
     h->qn_cells.release();
@@ -1901,7 +1906,6 @@ msfec_status msfec_nedrt_fine_solve(msfec_handle *h, const msfec_cell *domain, c
   MSFEC_CUDA_TRY(h, h->nrf_item.reserve(1));
   MSFEC_CUDA_TRY(h, h->nrf_b.reserve(kNRSrcRhs * N));
   MSFEC_CUDA_TRY(h, h->nrf_x.reserve(kNRSrcRhs * N));
-  MSFEC_CUDA_TRY(h, h->nrf_floor.reserve(1));
   MSFEC_CUDA_TRY(h, h->nrf_stats.reserve(18));
   MSFEC_CUDA_TRY(h, h->queue.reserve(2));
   if (!use_smem) MSFEC_CUDA_TRY(h, h->nrf_scratch.reserve(ws_floats));
@@ -1911,7 +1915,6 @@ msfec_status msfec_nedrt_fine_solve(msfec_handle *h, const msfec_cell *domain, c
   MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->nrf_item.ptr, &item, sizeof(NRItem), cudaMemcpyHostToDevice, st));
   MSFEC_CUDA_TRY(h, cudaMemsetAsync(h->nrf_b.ptr, 0, N * sizeof(double), st));
   MSFEC_CUDA_TRY(h, cudaMemsetAsync(h->nrf_x.ptr, 0, N * sizeof(double), st));
-  MSFEC_CUDA_TRY(h, cudaMemsetAsync(h->nrf_floor.ptr, 0, sizeof(double), st));
   MSFEC_CUDA_TRY(h, cudaMemsetAsync(h->nrf_stats.ptr, 0, 18 * sizeof(NRStat), st));
   MSFEC_CUDA_TRY(h, cudaMemsetAsync(h->queue.ptr, 0, sizeof(int), st));
   msfec_load ld;
@@ -1934,7 +1937,7 @@ msfec_status msfec_nedrt_fine_solve(msfec_handle *h, const msfec_cell *domain, c
   prm.stats = h->nrf_stats.ptr;
   prm.src_rhs = h->nrf_b.ptr;
   prm.src_out = h->nrf_x.ptr;
-  prm.src_floor = h->nrf_floor.ptr;
+  prm.src_scale2 = nullptr;  // no floor: the load is the whole right-hand side
   prm.scratch = use_smem ? nullptr : h->nrf_scratch.ptr;
   prm.scratch_floats = ws_floats;
   prm.use_smem = use_smem ? 1 : 0;
@@ -2183,7 +2186,7 @@ msfec_status msfec_nedrt_backward(msfec_handle *h, int32_t ncells, const msfec_c
   MSFEC_CUDA_TRY(h, h->nra_pts.reserve((size_t)std::max(npoints, 1) * 3));
   MSFEC_CUDA_TRY(h, h->nra_dJ.reserve((size_t)std::max(npoints, 1) * 3));
   MSFEC_CUDA_TRY(h, h->nra_cell.reserve(std::max(npoints, 1)));
-  MSFEC_CUDA_TRY(h, h->nra_floor.reserve(ncells));
+  MSFEC_CUDA_TRY(h, h->nra_scale2.reserve(nd));
   MSFEC_CUDA_TRY(h, h->nra_ga.reserve(nfine));
   MSFEC_CUDA_TRY(h, h->nra_gb.reserve(nfine));
   MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->nra_U.ptr, U, (size_t)ncells * 18 * sizeof(double), cudaMemcpyHostToDevice, st));
@@ -2209,7 +2212,7 @@ msfec_status msfec_nedrt_backward(msfec_handle *h, int32_t ncells, const msfec_c
   MSFEC_CUDA_TRY(h, nedrt_adjoint_prepare_launch(h->nr_cells.ptr, ncells, h->nr_phi.ptr, h->nra_U.ptr, h->nra_lam.ptr,
                                                  ld, npoints, h->nra_cell.ptr, h->nra_pts.ptr, h->nra_dJ.ptr,
                                                  h->nr_ainv.ptr, h->nr_bdiv.ptr, h->nra_comb.ptr, h->nra_b.ptr,
-                                                 h->nra_e.ptr, h->nra_work.ptr, h->nra_rhs.ptr, h->nra_floor.ptr, st));
+                                                 h->nra_e.ptr, h->nra_work.ptr, h->nra_rhs.ptr, h->nra_scale2.ptr, st));
   // four source-mode solves per cell on the batched solver, deepest cells first
   std::vector<int> order(ncells);
   for (int c = 0; c < ncells; ++c) order[c] = c;
@@ -2245,7 +2248,7 @@ msfec_status msfec_nedrt_backward(msfec_handle *h, int32_t ncells, const msfec_c
   prm.stats = h->nr_stats.ptr;
   prm.src_rhs = h->nra_rhs.ptr;
   prm.src_out = h->nra_x.ptr;
-  prm.src_floor = h->nra_floor.ptr;
+  prm.src_scale2 = h->nra_scale2.ptr;
   prm.scratch = use_smem ? nullptr : h->nr_scratch.ptr;
   prm.scratch_floats = ws_floats;
   prm.use_smem = use_smem ? 1 : 0;

@@ -57,7 +57,8 @@ struct NRParams {
   NRStat *stats;        // [cell][18]
   const double *src_rhs;  // source mode: [cell][kNRSrcRhs][ndof] at kNRSrcRhs * dof_off
   double *src_out;        // source mode: solutions, same layout
-  const double *src_floor;  // source mode: [cell] lower bound of the ||f|| the stopping test scales
+  const double *src_scale2;  // source mode: [dof_off + d] squared scale of the terms the right-hand side
+                             // is a difference of; 1e-3 of its P-norm floors ||f||_P in the stopping test (null: none)
   float *scratch;       // global workspace when the item does not fit shared memory
   size_t scratch_floats;  // per CTA
   const float *coarse;    // multilevel preconditioner data (per cell at coarse_off); null: diagonal only

@@ -879,7 +879,7 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
       }
       __syncthreads();
     }
-    double part[2] = {0.0, 0.0};
+    double part[3] = {0.0, 0.0, 0.0};
     for (int pass = (ir == 0 ? 0 : 1); pass < 2; ++pass) {
       // pass 0: lift of the boundary data only (scale of the stopping test)
       // accumulator starts at -f for a source item (r = f - A phi)
@@ -931,11 +931,18 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
         }
       }
       __syncthreads();
-      // r = -(A phi - f) on interior DoFs (boundary: 0), kept in vA
+      // r = -(A phi - f) on interior DoFs (boundary: 0), kept in vA. Its size is
+      // measured in the preconditioner's norm ||r||_P^2 = r^T P r (the norm MINRES
+      // minimises): the face rows of the local system outweigh the edge rows by
+      // ~(1/h)^2 (div-div ~ h^-3 against edge mass ~ h), so a plain 2-norm would
+      // leave the edge block unresolved on small cells; the P-norm is invariant
+      // to that block scaling.
       for (int d = tid; d < (int)Np; d += NT) {
         const bool interior = pd[d] > 0.0f;  // false on the pad [N, Np)
         const double r = interior ? -(fp32_res ? (double)facc[d] : dacc[d]) : 0.0;
-        part[pass] += r * r;
+        part[pass] += (double)pd[d] * r * r;
+        if (ir == 0 && pass == 1 && src && prm.src_scale2 && interior)
+          part[2] += (double)pd[d] * prm.src_scale2[Cc.dof_off + d];
         // MINRES runs on the symmetric form S A (S = +1 on edges, -1 on faces):
         // [M -C; -C^T -D] x = S r. vA is disjoint from the accumulator.
         if (pass == 1) vA[d] = (T)(d < g.NE ? r : -r);
@@ -943,12 +950,13 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
       __syncthreads();
     }
     {
-      double tot[2];
-      block_sum<double, 2, NW>(sh, part, tot);
+      double tot[3];
+      block_sum<double, 3, NW>(sh, part, tot);
       if (ir == 0) bnorm2 = tot[0];
       // a source right-hand side that cancelled to rounding is solved to rtol of
-      // its cell's adjoint scale, not of its own (noise-level) norm
-      if (ir == 0 && src) bnorm2 = fmax(bnorm2, prm.src_floor[it.cell] * prm.src_floor[it.cell]);
+      // 1e-3 of its cell's adjoint source scale (in the same norm), not of its own
+      // noise-level norm
+      if (ir == 0 && src) bnorm2 = fmax(bnorm2, 1e-6 * tot[2]);
       rnorm2 = tot[1];
     }
     ++nref;
@@ -1669,7 +1677,7 @@ __global__ void __launch_bounds__(kAdjThreads) nr_adj_rhs_kernel(const NRCell *_
                                                                  const double *__restrict__ bload,
                                                                  const double *__restrict__ e,
                                                                  double *__restrict__ work, double *__restrict__ rhs,
-                                                                 double *__restrict__ floor_out) {
+                                                                 double *__restrict__ scale2_out) {
   __shared__ NRFactors<double> F;
   const int c = blockIdx.x;
   const NRCell C = cells[c];
@@ -1725,17 +1733,9 @@ __global__ void __launch_bounds__(kAdjThreads) nr_adj_rhs_kernel(const NRCell *_
     r[(size_t)N + d] = r1;
     r[2 * (size_t)N + d] = r2;
     r[3 * (size_t)N + d] = r3;
-    if (!bnd) scale2 += as[d] * as[d] + at * at + bl[d] * bl[d] + ee[d] * ee[d];
-  }
-  // floor of the stopping scale: 1e-3 of the cell's adjoint source scale
-  __shared__ double red[kAdjThreads / 32];
-  for (int off = 16; off >= 1; off >>= 1) scale2 += __shfl_xor_sync(0xffffffffu, scale2, off);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = scale2;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int w = 0; w < kAdjThreads / 32; ++w) t += red[w];
-    floor_out[c] = 1e-3 * sqrt(t);
+    // squared scale of the terms whose difference the right-hand sides are
+    // (the solver weights it with its preconditioner into the stopping floor)
+    scale2_out[C.dof_off + d] = bnd ? 0.0 : as[d] * as[d] + at * at + bl[d] * bl[d] + ee[d] * ee[d];
   }
 }
 
@@ -2153,14 +2153,14 @@ cudaError_t nedrt_adjoint_prepare_launch(const NRCell *cells, int ncells, const 
                                          const double *lam, const msfec_load &load, int npoints, const int *cell_of,
                                          const double *pts, const double *dJdu, const double *ainv6,
                                          const double *bdiv, double *comb, double *bload, double *e, double *work,
-                                         double *rhs, double *floor_out, cudaStream_t st) {
+                                         double *rhs, double *scale2_out, cudaStream_t st) {
   if (ncells <= 0) return cudaSuccess;
   nrimpl::nr_adj_combine_kernel<<<ncells, nrimpl::kAdjThreads, 0, st>>>(cells, phi, U, lam, comb);
   nrimpl::nr_adj_face_load_kernel<<<ncells, nrimpl::kAdjThreads, 0, st>>>(cells, load, bload);
   if (npoints > 0)
     nrimpl::nr_adj_point_kernel<<<(npoints + 127) / 128, 128, 0, st>>>(cells, npoints, cell_of, pts, dJdu, e);
   nrimpl::nr_adj_rhs_kernel<<<ncells, nrimpl::kAdjThreads, 0, st>>>(cells, ainv6, bdiv, comb, bload, e, work, rhs,
-                                                                     floor_out);
+                                                                     scale2_out);
   return cudaGetLastError();
 }
 

@@ -585,7 +585,9 @@ __device__ void solve_item(const QNParams &prm, QNShared &sh, int item_id) {
       for (int d = tid; d < N; d += NT) {
         const bool interior = pd[d] > 0.0f;
         const double r = interior ? -(fp32_res ? (double)facc[d] : dacc[d]) : 0.0;
-        part[pass] += r * r;
+        // measured in the preconditioner's norm r^T P r: invariant to the h-scaling
+        // of the blocks (mass ~ h^3, curl-curl ~ 1/h), which a plain 2-norm is not
+        part[pass] += (double)pd[d] * r * r;
         // symmetric form S A (S = +1 on vertices, -1 on edges)
         if (pass == 1) vA[d] = (T)(d < g.NV ? r : -r);
       }

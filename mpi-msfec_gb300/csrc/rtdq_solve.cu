@@ -350,7 +350,9 @@ __device__ void solve_item(const RTParams &prm, RTShared &sh, int item_id) {
       for (int d = tid; d < N; d += NT) {
         const bool interior = pd[d] > 0.0f;
         const double r = interior ? -(fp32_res ? (double)facc[d] : dacc[d]) - (d >= NF ? mean : 0.0) : 0.0;
-        part[pass] += r * r;
+        // measured in the preconditioner's norm r^T P r: invariant to the h-scaling
+        // of the blocks (RT mass ~ 1/h against the unit cell rows)
+        part[pass] += (double)pd[d] * r * r;
         // symmetric form S A (S = +1 on faces, -1 on cells)
         if (pass == 1) vA[d] = (T)(d < NF ? r : -r);
       }
