@@ -309,6 +309,21 @@ def time_oracle(wl, sel, nthreads):
 
 
 # --------------------------------------------------------------------------- GPU
+def shape_names(kind, ncand, sms=152):
+    """Names of msfec_autotune's candidates, in its order (include/msfec_cuda.h)."""
+    if ncand <= 1:
+        return ["default"]
+    if kind == "q1":
+        return ["fused cluster launch", "split cluster + non-cluster launches"]
+    if kind in ("qned", "rtdq") or (kind == "nedrt" and ncand == 2):
+        return ["1 x 512-thread CTA per SM", "2 x 256-thread CTAs per SM"]
+    ctas = [sms] + [max(1, sms * q // 8) for q in (7, 6, 5, 4)]
+    out = [f"{c} resident CTAs, plain coefficient loads" for c in ctas]
+    if ncand == 10:
+        out += [f"{c} resident CTAs, coefficient tiles staged by bulk copies" for c in ctas]
+    return out
+
+
 def gpu_run(wl, lo, hi, precision, steps, warmup, local, stream, barrier, tune_info=None, batches=None):
     """Device-resident builds of this rank's cells [lo, hi), one batch per step
     (the steps cycle through `batches`, default batches_of(wl, lo, hi)).
@@ -352,17 +367,22 @@ def gpu_run(wl, lo, hi, precision, steps, warmup, local, stream, barrier, tune_i
         else:
             h.q1_build_device(c, x, y, wl.load, *out)
 
-    if tune_info is not None and nc > 0 and wl.kind not in ("qned", "rtdq"):
+    if tune_info is not None and nc > 0:
         import sharding
-        k = min(nc, 64 if wl.kind == "nedrt" else 512)  # several waves of items, seconds of trials
+        k = min(nc, 64 if wl.kind in ("nedrt", "qned", "rtdq") else 512)  # several waves of items
         f = int(sharding.fine_offsets(cells)[k])
         if wl.kind == "nedrt":
             c0, c1, kind = sh["ainv6"][:f], sh["bdiv"][:f], msfec.KIND_NEDRT
+        elif wl.kind == "qned":
+            c0, c1, kind = sh["a6"][:f], sh["binv"][:f], msfec.KIND_QNED
+        elif wl.kind == "rtdq":
+            c0, c1, kind = sh["ainv6"][:f], None, msfec.KIND_RTDQ
         else:
             c0, c1, kind = sh["a"][:f], None if sh["r"] is None else sh["r"][:f], msfec.KIND_Q1
         choice, ncand, times = h.autotune(kind, cells[:k], c0, c1, wl.load)
-        tune_info.update({"sample_cells": k, "candidates": ncand, "choice": choice,
-                          "times_ms": [round(t, 3) for t in times]})
+        names = shape_names(wl.kind, ncand)
+        tune_info.update({"sample_cells": k, "shapes": names, "times_ms": [round(t, 2) for t in times],
+                          "choice": names[choice] if choice < len(names) else choice})
     for i in range(warmup):
         build(*batches[i % len(batches)])
     barrier()
@@ -723,7 +743,8 @@ def run_ours(args):
             extras[name] = {"value": ex["value"], "ms_per_step": ex["ms_per_step"], "converged": ex["converged"],
                             "max_iterations": ex["max_iterations"], "work_dof_rhs": ex["work_dof_rhs"],
                             "solve_launch_ms": rf["launch_ms"], "hbm_frac": rf["frac"],
-                            "fp32_tflops": rf["onchip"]["achieved_tflops"]}
+                            "fp32_tflops": rf["onchip"]["achieved_tflops"],
+                            "autotune": ex["autotune"].get("choice")}
             if "fp64_path" in ex:
                 extras[name]["fp64_value"] = ex["fp64_path"]["value"]
                 extras[name]["mixed_over_fp64"] = ex["fp64_path"]["mixed_over_fp64"]

@@ -112,6 +112,12 @@ typedef struct msfec_config {
      reference's Diffusion_A::value_list gives its assembly
      (source/equation_data/eqn_coeff_A.cc:162-191, q_basis.cc:218-231). */
   int32_t q1_coefficient;
+  /* Ned_RT cells whose MINRES workspace is in global memory (depth 4, mixed
+     precision): 1 = the operator apply reads its coefficient tiles from shared
+     memory, put there two rounds ahead by bulk (TMA) copies; 0 = plain global
+     loads. Same results either way. */
+  int32_t nedrt_stage;
+  int32_t reserved;
 } msfec_config;
 
 typedef enum msfec_q1_coefficient {
@@ -391,24 +397,37 @@ msfec_status msfec_nedrt_build_noalloc(msfec_handle *handle, int32_t ncells,
                                        msfec_cell_report *d_reports);
 
 /* Problem kinds (msfec_autotune). */
-typedef enum msfec_kind { MSFEC_KIND_Q1 = 1, MSFEC_KIND_NEDRT = 2 } msfec_kind;
+typedef enum msfec_kind {
+  MSFEC_KIND_Q1 = 1,
+  MSFEC_KIND_NEDRT = 2,
+  MSFEC_KIND_QNED = 3,
+  MSFEC_KIND_RTDQ = 4
+} msfec_kind;
 
 /*
- * Autotuner for launch shapes. Builds the given batch (host buffers, as
- * msfec_q1_build / msfec_nedrt_build: coef0 = a or ainv6, coef1 = reaction
- * (may be NULL) or bdiv) twice per candidate in the handle's precision,
- * times the second build on the device, and keeps the fastest candidate for
- * later builds of that kind on this handle. Pass a representative sample
- * (e.g. one or two GPU waves of cells); the call costs 2 builds per
- * candidate. choice[0] = index of the chosen candidate, choice[1] = number of
- * candidates; times_ms (NULL or >= 8 floats) receives each candidate's time.
+ * Autotuner for launch shapes. Builds the given batch (host buffers, as the
+ * kind's build entry point: Q1 coef0 = a, coef1 = reaction or NULL; Ned_RT
+ * coef0 = ainv6, coef1 = bdiv; Q_Ned coef0 = a6, coef1 = binv; RT_DQ coef0 =
+ * ainv6, coef1 unused) twice per candidate in the handle's precision, times
+ * the second build on the device, and keeps the fastest candidate for later
+ * builds of that kind on this handle. Pass a representative sample (e.g. one
+ * or two GPU waves of cells); the call costs 2 builds per candidate.
+ * choice[0] = index of the chosen candidate, choice[1] = number of
+ * candidates; times_ms (NULL or >= 16 floats) receives each candidate's time.
+ * Candidates, in order:
  *   Q1 (per precision and reaction on/off), when the batch mixes cluster
  *     (z-slab) items with independent ones: 0 = one launch of the cluster
  *     kernel over all items, 1 = the cluster kernel over the slab items and
  *     a non-cluster kernel over the rest, concurrently on two streams.
- *   Ned_RT (per precision and deepest depth), when the MINRES workspace is
- *     in global memory (depth 4, or FP64): the number of resident CTAs, i.e.
- *     of workspace slots in L2: the SM count times 1, 7/8, 6/8, 5/8, 4/8.
+ *   Ned_RT (per precision and deepest depth): with the MINRES workspace in
+ *     shared memory (mixed, depth <= 3): 0 = one 512-thread CTA per SM,
+ *     1 = two 256-thread CTAs per SM (split workspace). With it in global
+ *     memory (depth 4, or FP64): the number of resident CTAs, i.e. of
+ *     workspace slots in L2, the SM count times 1, 7/8, 6/8, 5/8, 4/8, first
+ *     with plain coefficient loads, then (mixed only) with the apply's
+ *     coefficient tiles staged by bulk copies (nedrt_stage): 10 candidates.
+ *   Q_Ned, RT_DQ (per deepest depth, mixed): 0 = one 512-thread CTA per SM,
+ *     1 = two 256-thread CTAs per SM (when the workspace fits twice).
  * Batches with a single candidate return at once (choice = {0, 1}).
  */
 msfec_status msfec_autotune(msfec_handle *handle, int32_t kind, int32_t ncells,

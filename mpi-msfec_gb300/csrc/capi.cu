@@ -238,7 +238,11 @@ struct msfec_handle {
   int q1_split[2][2] = {{-1, -1}, {-1, -1}};  // [precision][has reaction]: 1 = split launches
   int nr_ctas[2][kNRMaxDepthCfg + 1] = {};    // [precision][deepest depth]: resident CTAs
   int nr_split[kNRMaxDepthCfg + 1] = {-1, -1, -1, -1, -1};  // [deepest depth] mixed: 1 = two 256-thread CTAs/SM
+  int nr_stage[kNRMaxDepthCfg + 1] = {-1, -1, -1, -1, -1};  // [deepest depth] mixed, global workspace: staged tiles
+  int qn_two[kNRMaxDepthCfg + 1] = {-1, -1, -1, -1, -1};    // [deepest depth] Q_Ned mixed: 1 = two CTAs/SM
+  int rt_two[kNRMaxDepthCfg + 1] = {-1, -1, -1, -1, -1};    // [deepest depth] RT_DQ mixed: 1 = two CTAs/SM
   int force_split = -1, force_ctas = 0, force_nr_split = -1;  // candidate under trial
+  int force_stage = -1, force_two = -1;
   cudaStream_t aux_stream = nullptr;          // second stream of the split Q1 launch
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int last_graph = 0;  // 0 direct launches, 1 captured a new graph, 2 replayed
@@ -934,8 +938,8 @@ constexpr size_t kNRSplitSmemLimit = 108 * 1024;  // two CTAs per SM (228 KB, mi
 // handle-owned build and the allocation-free one, so both make the same choice
 // (including the autotuner's) for the same batch.
 struct NRShape {
-  bool split = false, use_smem = false, ml = false;
-  size_t smem = 0, ws_floats = 0, ml_offset = 0;
+  bool split = false, use_smem = false, ml = false, stage = false;
+  size_t smem = 0, ws_floats = 0, ml_offset = 0, stage_offset = 0;
   int grid = 0;
 };
 
@@ -962,6 +966,18 @@ msfec_status nr_shape(msfec_handle *h, int nmax, bool fp64, bool want_ml, size_t
   const size_t ml_bytes = s.ml ? nr_ml_layout(nmax, fp64 ? 8 : 4).bytes : 0;
   if (s.ml && s.smem + ml_bytes > (s.split ? kNRSplitSmemLimit : kNRSmemTotalLimit)) s.ml = false;
   if (s.ml) s.smem += ml_bytes;
+  // global workspace (mixed): the apply's coefficient tiles staged by bulk copies
+  // (nedrt_stage), two 1 KB stages per warp after the multilevel region
+  const int stage_sel = h->force_stage >= 0 ? h->force_stage : h->nr_stage[deepest];
+  if ((stage_sel >= 0 ? stage_sel != 0 : h->cfg.nedrt_stage != 0) && !s.use_smem && !s.split && !fp64) {
+    const size_t off = (s.smem + 127) / 128 * 128;
+    const size_t bytes = (size_t)kNRThreads / 32 * 2 * 1024;
+    if (off + bytes <= kNRSmemTotalLimit) {
+      s.stage = true;
+      s.stage_offset = off;
+      s.smem = off + bytes;
+    }
+  }
   if (s.split) {
     int occ = 0;
     MSFEC_CUDA_TRY(h, nedrt_split_occupancy(s.ml, s.smem, &occ));
@@ -1079,6 +1095,8 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
   prm.max_refine = h->cfg.max_refine;
   prm.coarse = ml ? h->nr_coarse.ptr : nullptr;
   prm.ml_offset = ml_offset;
+  prm.stage = shape.stage ? 1 : 0;
+  prm.stage_offset = shape.stage_offset;
   if (h->cfg.verbose)
     fprintf(stderr, "[msfec] nedrt plan: %d cells, %zu items, workspace %zu floats (%s), grid %d, %s, %s\n", ncells,
             items.size(), ws_floats, split ? "split, 2 CTAs/SM" : (use_smem ? "shared" : "global"), grid,
@@ -1158,7 +1176,10 @@ msfec_status qned_build_impl(msfec_handle *h, int ncells, const msfec_cell *cell
   const bool use_smem = ws_floats * 4 <= kNRSmemLimit;
   const size_t smem = use_smem ? ws_floats * 4 : 0;
   // mixed precision with a workspace that fits twice per SM: two 256-thread CTAs per SM
-  const bool two_per_sm = !fp64 && use_smem && smem <= kNRSplitSmemLimit;
+  int deepest_q = 0;
+  while ((1 << deepest_q) < nmax) ++deepest_q;
+  const int two_sel = h->force_two >= 0 ? h->force_two : h->qn_two[std::min(deepest_q, kNRMaxDepthCfg)];
+  const bool two_per_sm = !fp64 && use_smem && smem <= kNRSplitSmemLimit && two_sel != 0;
   const int grid = std::min<int>((int)items.size(), (two_per_sm ? 2 : 1) * h->num_sms);
   cudaStream_t st = h->stream;
   MSFEC_CUDA_TRY(h, h->qn_cells.reserve(ncells));
@@ -1252,7 +1273,10 @@ msfec_status rtdq_build_impl(msfec_handle *h, int ncells, const msfec_cell *cell
   const size_t ws_floats = rt_workspace_floats(nmax, fp64 ? 8 : 4);
   const bool use_smem = ws_floats * 4 <= kNRSmemLimit;
   const size_t smem = use_smem ? ws_floats * 4 : 0;
-  const bool two_per_sm = !fp64 && use_smem && smem <= kNRSplitSmemLimit;
+  int deepest_r = 0;
+  while ((1 << deepest_r) < nmax) ++deepest_r;
+  const int two_sel = h->force_two >= 0 ? h->force_two : h->rt_two[std::min(deepest_r, kNRMaxDepthCfg)];
+  const bool two_per_sm = !fp64 && use_smem && smem <= kNRSplitSmemLimit && two_sel != 0;
   const int grid = std::min<int>((int)items.size(), (two_per_sm ? 2 : 1) * h->num_sms);
   cudaStream_t st = h->stream;
   MSFEC_CUDA_TRY(h, h->rt_cells.reserve(ncells));
@@ -1411,7 +1435,8 @@ msfec_status msfec_create(msfec_handle **out, const msfec_config *cfg) {
   if (c.precision != MSFEC_PRECISION_FP64 && c.precision != MSFEC_PRECISION_MIXED) return MSFEC_ERROR_INVALID_ARGUMENT;
   if (!(c.rtol > 0.0) || !(c.inner_rtol > 0.0) || c.inner_rtol >= 1.0 || c.max_iter < 1 || c.max_refine < 1 ||
       !(c.nedrt_rtol > 0.0) || c.q1_launch < 0 || c.q1_launch > 2 || c.nedrt_precond < 0 || c.nedrt_precond > 1 ||
-      c.q1_coefficient < MSFEC_Q1_COEF_SCALAR || c.q1_coefficient > MSFEC_Q1_COEF_GAUSS)
+      c.q1_coefficient < MSFEC_Q1_COEF_SCALAR || c.q1_coefficient > MSFEC_Q1_COEF_GAUSS || c.nedrt_stage < 0 ||
+      c.nedrt_stage > 1)
     return MSFEC_ERROR_INVALID_ARGUMENT;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || c.device < 0 || c.device >= ndev) return MSFEC_ERROR_CUDA;
@@ -2040,60 +2065,94 @@ msfec_status msfec_autotune(msfec_handle *h, int32_t kind, int32_t ncells, const
                             const double *coef0, const double *coef1, const msfec_load *load, int32_t *choice,
                             float *times_ms) {
   if (!h) return MSFEC_ERROR_INVALID_ARGUMENT;
-  if ((kind != MSFEC_KIND_Q1 && kind != MSFEC_KIND_NEDRT) || ncells <= 0 || !cells || !coef0 ||
-      (kind == MSFEC_KIND_NEDRT && !coef1) || !choice)
+  if (kind < MSFEC_KIND_Q1 || kind > MSFEC_KIND_RTDQ || ncells <= 0 || !cells || !coef0 ||
+      ((kind == MSFEC_KIND_NEDRT || kind == MSFEC_KIND_QNED) && !coef1) || !choice)
     return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "msfec_autotune: invalid kind, batch or output");
-  if (kind == MSFEC_KIND_Q1 && h->cfg.q1_coefficient != MSFEC_Q1_COEF_SCALAR) {  // one launch shape only
-    choice[0] = 0;
-    choice[1] = 1;
-    return MSFEC_SUCCESS;
-  }
+  for (int c = 0; c < ncells; ++c)
+    if (!cell_ok(cells[c])) return fail(h, MSFEC_ERROR_INVALID_ARGUMENT, "msfec_autotune: invalid cell");
+  choice[0] = 0;
+  choice[1] = 1;
+  if (kind == MSFEC_KIND_Q1 && h->cfg.q1_coefficient != MSFEC_Q1_COEF_SCALAR) return MSFEC_SUCCESS;  // one shape
   const bool fp64 = h->cfg.precision == MSFEC_PRECISION_FP64;
   int deepest = 0;
   for (int c = 0; c < ncells; ++c) deepest = std::max(deepest, (int)cells[c].depth);
-  // candidates
-  std::vector<int> cand;
-  bool nr_split_tune = false;
+  const int dcfg = std::min(deepest, kNRMaxDepthCfg);
+  const int nmax = 1 << dcfg;
+  // candidate launch shapes (one knob each, or resident CTAs x coefficient staging)
+  struct Cand {
+    int split = -1, ctas = 0, nr_split = -1, stage = -1, two = -1;
+  };
+  std::vector<Cand> cand;
+  bool nr_split_tune = false, nr_global = false;
   if (kind == MSFEC_KIND_Q1) {
     const Q1Plan p = make_q1_plan(ncells, cells, fp64, coef1 != nullptr, true);
-    cand = p.split ? std::vector<int>{0, 1} : std::vector<int>{0};
-  } else {
-    const int nmax = 1 << std::min(deepest, kNRMaxDepthCfg);
+    cand.push_back(Cand{});
+    cand.back().split = 0;
+    if (p.split) {
+      cand.push_back(Cand{});
+      cand.back().split = 1;
+    }
+  } else if (kind == MSFEC_KIND_NEDRT) {
     const bool smem_ws = nr_workspace_floats(nmax, fp64 ? 8 : 4) * 4 <= kNRSmemLimit;
     nr_split_tune = !fp64 && nr_split_smem_floats(nmax) * 4 <= kNRSplitSmemLimit;
-    if (nr_split_tune) {
-      cand = {0, 1};  // one 512-thread CTA per SM, two 256-thread CTAs per SM
+    if (nr_split_tune) {  // one 512-thread CTA per SM, two 256-thread CTAs per SM
+      for (int v : {0, 1}) {
+        cand.push_back(Cand{});
+        cand.back().nr_split = v;
+      }
     } else {
-      cand.push_back(h->num_sms);
+      nr_global = !smem_ws;
+      std::vector<int> ctas{h->num_sms};
       if (!smem_ws)
-        for (int k : {7, 6, 5, 4}) cand.push_back(std::max(1, h->num_sms * k / 8));
+        for (int k : {7, 6, 5, 4}) ctas.push_back(std::max(1, h->num_sms * k / 8));
+      const std::vector<int> stages = (!fp64 && !smem_ws) ? std::vector<int>{0, 1} : std::vector<int>{-1};
+      for (int st : stages)
+        for (int c : ctas) {
+          cand.push_back(Cand{});
+          cand.back().ctas = c;
+          cand.back().stage = st;
+        }
+    }
+  } else {  // Q_Ned / RT_DQ: one 512-thread CTA per SM, or two 256-thread CTAs when the workspace fits twice
+    const size_t ws = kind == MSFEC_KIND_QNED ? qn_workspace_floats(nmax, fp64 ? 8 : 4) : rt_workspace_floats(nmax, fp64 ? 8 : 4);
+    const bool two_ok = !fp64 && ws * 4 <= kNRSmemLimit && ws * 4 <= kNRSplitSmemLimit;
+    cand.push_back(Cand{});
+    cand.back().two = 0;
+    if (two_ok) {
+      cand.push_back(Cand{});
+      cand.back().two = 1;
     }
   }
-  choice[0] = 0;
   choice[1] = (int32_t)cand.size();
   if (cand.size() == 1) return MSFEC_SUCCESS;
   const bool timing0 = h->timing, graph0 = h->graph_mode;
   msfec_status s = msfec_set_timing(h, 1);
   if (s != MSFEC_SUCCESS) return s;
   h->graph_mode = false;
-  std::vector<double> KH((size_t)ncells * 324), FH((size_t)ncells * 18);
+  std::vector<double> KH((size_t)ncells * 400), FH((size_t)ncells * 20);
   float best = 0.0f;
   for (size_t k = 0; k < cand.size() && s == MSFEC_SUCCESS; ++k) {
-    if (kind == MSFEC_KIND_Q1)
-      h->force_split = cand[k];
-    else if (nr_split_tune)
-      h->force_nr_split = cand[k];
-    else
-      h->force_ctas = cand[k];
+    h->force_split = cand[k].split;
+    h->force_ctas = cand[k].ctas;
+    h->force_nr_split = cand[k].nr_split;
+    h->force_stage = cand[k].stage;
+    h->force_two = cand[k].two;
     msfec_timings t{};
     for (int rep = 0; rep < 2 && s == MSFEC_SUCCESS; ++rep) {  // second run timed (first warms)
-      s = kind == MSFEC_KIND_Q1
-              ? msfec_q1_build(h, ncells, cells, coef0, coef1, load, KH.data(), FH.data(), nullptr)
-              : msfec_nedrt_build(h, ncells, cells, coef0, coef1, load, KH.data(), FH.data(), nullptr);
+      switch (kind) {
+        case MSFEC_KIND_Q1: s = msfec_q1_build(h, ncells, cells, coef0, coef1, load, KH.data(), FH.data(), nullptr); break;
+        case MSFEC_KIND_NEDRT:
+          s = msfec_nedrt_build(h, ncells, cells, coef0, coef1, load, KH.data(), FH.data(), nullptr);
+          break;
+        case MSFEC_KIND_QNED:
+          s = msfec_qned_build(h, ncells, cells, coef0, coef1, load, KH.data(), FH.data(), nullptr);
+          break;
+        default: s = msfec_rtdq_build(h, ncells, cells, coef0, load, KH.data(), FH.data(), nullptr); break;
+      }
       if (s == MSFEC_SUCCESS) s = msfec_get_timings(h, &t);
     }
     if (s != MSFEC_SUCCESS) break;
-    if (times_ms) times_ms[k] = t.total_ms;
+    if (times_ms && k < 16) times_ms[k] = t.total_ms;
     if (k == 0 || t.total_ms < best) {
       best = t.total_ms;
       choice[0] = (int32_t)k;
@@ -2102,15 +2161,26 @@ msfec_status msfec_autotune(msfec_handle *h, int32_t kind, int32_t ncells, const
   h->force_split = -1;
   h->force_ctas = 0;
   h->force_nr_split = -1;
+  h->force_stage = -1;
+  h->force_two = -1;
   h->graph_mode = graph0;
   msfec_set_timing(h, timing0 ? 1 : 0);
   if (s != MSFEC_SUCCESS) return s;
-  if (kind == MSFEC_KIND_Q1)
-    h->q1_split[fp64 ? 0 : 1][coef1 ? 1 : 0] = cand[choice[0]];
-  else if (nr_split_tune)
-    h->nr_split[std::min(deepest, kNRMaxDepthCfg)] = cand[choice[0]];
-  else
-    h->nr_ctas[fp64 ? 0 : 1][std::min(deepest, kNRMaxDepthCfg)] = cand[choice[0]] == h->num_sms ? 0 : cand[choice[0]];
+  const Cand &w = cand[choice[0]];
+  if (kind == MSFEC_KIND_Q1) {
+    h->q1_split[fp64 ? 0 : 1][coef1 ? 1 : 0] = w.split;
+  } else if (kind == MSFEC_KIND_NEDRT) {
+    if (nr_split_tune) {
+      h->nr_split[dcfg] = w.nr_split;
+    } else {
+      h->nr_ctas[fp64 ? 0 : 1][dcfg] = w.ctas == h->num_sms ? 0 : w.ctas;
+      if (nr_global && !fp64) h->nr_stage[dcfg] = w.stage;
+    }
+  } else if (kind == MSFEC_KIND_QNED) {
+    h->qn_two[dcfg] = w.two;
+  } else {
+    h->rt_two[dcfg] = w.two;
+  }
   if (h->cfg.verbose)
     fprintf(stderr, "[msfec] autotune kind %d depth %d %s: candidate %d of %zu\n", kind, deepest,
             fp64 ? "fp64" : "mixed", choice[0], cand.size());
@@ -2290,7 +2360,7 @@ msfec_status msfec_nedrt_backward(msfec_handle *h, int32_t ncells, const msfec_c
   for (int c = 0; c < ncells; ++c)
     for (int k = 0; k < kNRSrcRhs; ++k) {
       const NRStat &q = stats[(size_t)c * 18 + k];
-      if (!q.converged || (q.flags & 1))
+      if (!q.converged || (q.flags & 5))
         return fail(h, MSFEC_ERROR_NOT_CONVERGED,
                     "Ned_RT adjoint local solve missed its tolerance (cell " + std::to_string(c) + ", rhs " +
                         std::to_string(k) + ", relative residual " + std::to_string(q.rel_residual) + ", " +
@@ -2721,6 +2791,8 @@ msfec_status msfec_nedrt_build_noalloc(msfec_handle *h, int32_t ncells, const ms
   prm.max_refine = h->cfg.max_refine;
   prm.coarse = ml ? d_coarse : nullptr;
   prm.ml_offset = shape.ml_offset;
+  prm.stage = shape.stage ? 1 : 0;
+  prm.stage_offset = shape.stage_offset;
   if (h->timing) MSFEC_CUDA_TRY(h, record_start(h, st));
   if (ml)
     MSFEC_CUDA_TRY(h, nedrt_ml_setup_launch(d_cells, ncells, d_ainv6, d_bdiv, d_coarse,

@@ -64,6 +64,10 @@ struct NRParams {
   const float *coarse;    // multilevel preconditioner data (per cell at coarse_off); null: diagonal only
   size_t ml_offset;       // byte offset of the multilevel region in the dynamic shared memory
   int use_smem;
+  // global workspace, mixed precision: the apply's coefficient tiles staged by
+  // bulk copies into the dynamic shared memory at this byte offset (32 KB)
+  int stage;
+  size_t stage_offset;
   double rtol;
   double inner_rtol;
   int max_iter;

@@ -23,7 +23,7 @@ ERROR_NOT_CONVERGED = 4
 ERROR_NOT_SUPPORTED = 5
 ERROR_NUMERICAL = 6
 ERROR_INVALID_STATE = 7
-KIND_Q1, KIND_NEDRT = 1, 2
+KIND_Q1, KIND_NEDRT, KIND_QNED, KIND_RTDQ = 1, 2, 3, 4
 Q1_COEF_SCALAR, Q1_COEF_TENSOR, Q1_COEF_GAUSS = 0, 1, 2  # msfec_config.q1_coefficient
 
 PRECISION_FP64 = 0
@@ -52,7 +52,8 @@ class Config(ctypes.Structure):
                 ("inner_rtol", ctypes.c_double), ("max_iter", ctypes.c_int32),
                 ("max_refine", ctypes.c_int32), ("verbose", ctypes.c_int32),
                 ("q1_launch", ctypes.c_int32), ("nedrt_rtol", ctypes.c_double),
-                ("nedrt_precond", ctypes.c_int32), ("q1_coefficient", ctypes.c_int32)]
+                ("nedrt_precond", ctypes.c_int32), ("q1_coefficient", ctypes.c_int32),
+                ("nedrt_stage", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 class Cell(ctypes.Structure):
@@ -209,7 +210,7 @@ class Handle:
 
     def __init__(self, precision=PRECISION_MIXED, device=0, rtol=None, inner_rtol=None,
                  max_iter=None, max_refine=None, verbose=0, nedrt_rtol=None, q1_launch=0, nedrt_precond=0,
-                 q1_coefficient=0):
+                 q1_coefficient=0, nedrt_stage=None):
         L = load_library()
         cfg = Config()
         L.msfec_config_default(ctypes.byref(cfg))
@@ -229,6 +230,8 @@ class Handle:
         cfg.q1_launch = int(q1_launch)
         cfg.nedrt_precond = int(nedrt_precond)
         cfg.q1_coefficient = int(q1_coefficient)
+        if nedrt_stage is not None:
+            cfg.nedrt_stage = int(nedrt_stage)
         self.cfg = cfg
         h = _vp()
         st = L.msfec_create(ctypes.byref(h), ctypes.byref(cfg))
@@ -346,7 +349,7 @@ class Handle:
         c0 = np.ascontiguousarray(coef0, dtype=np.float64)
         c1 = None if coef1 is None else np.ascontiguousarray(coef1, dtype=np.float64)
         ch = (ctypes.c_int32 * 2)()
-        tm = (ctypes.c_float * 8)()
+        tm = (ctypes.c_float * 16)()
         st = self._lib.msfec_autotune(self._h, int(kind), cells.shape[0], cells.ctypes.data_as(_vp),
                                       c0.ctypes.data_as(_vp), None if c1 is None else c1.ctypes.data_as(_vp),
                                       ctypes.byref(load), ch, tm)

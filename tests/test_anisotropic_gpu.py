@@ -2,7 +2,7 @@
 pairings against the FP64 oracle: the element operators take the fine-cell
 sides from the cell record and the multilevel setup probes the Schur operator
 through them. Tolerances as in the pairings' own parity tests (K_H, F_H
-<= 1e-9 relative; Ned_RT with both face preconditioners)."""
+<= 1e-10 relative; Ned_RT with both face preconditioners)."""
 import numpy as np
 import pytest
 
@@ -12,7 +12,7 @@ from oracle import qned_oracle as Q
 from oracle import rtdq_oracle as RQ
 
 pytestmark = pytest.mark.gpu
-TOL = 1e-9
+TOL = 1e-10
 SIZE = (1.0, 0.45, 1.7)
 
 

@@ -69,3 +69,41 @@ def test_nedrt_autotune_global_workspace(gpu):
     assert st2 == gpu.SUCCESS and rep2["converged"].all()
     for c in range(len(cells)):
         assert _rel(KH2[c], KH20[c]) <= 1e-11
+
+
+def test_nedrt_autotune_depth4_ctas_and_staging(gpu):
+    """Mixed depth 4 (global MINRES workspace): 10 candidates, resident CTAs x
+    coefficient staging; the tuned build's K_H equals the default build's."""
+    cells, ainv6, bdiv, load = workloads.nedrt_tensor(m=1, depth=4, seed=6)
+    h = gpu.Handle()
+    choice, ncand, times = h.autotune(gpu.KIND_NEDRT, cells, ainv6, bdiv, load)
+    assert ncand == 10 and 0 <= choice < 10 and all(t > 0 for t in times), (choice, times)
+    print("nedrt autotune (mixed, depth 4): plain", [f"{t:.1f}" for t in times[:5]], "staged",
+          [f"{t:.1f}" for t in times[5:]], "->", choice)
+    KH, FH, rep, st = h.nedrt_build(cells, ainv6, bdiv, load)
+    assert st == gpu.SUCCESS and rep["converged"].all()
+    KH0, FH0, _, _ = gpu.Handle().nedrt_build(cells, ainv6, bdiv, load)
+    assert _rel(KH[0], KH0[0]) <= 1e-11 and _rel(FH[0], FH0[0]) <= 1e-11
+
+
+@pytest.mark.parametrize("kind", ["qned", "rtdq"])
+def test_mixed_pairings_autotune_cta_shape(gpu, kind):
+    """Q_Ned and RT_DQ (mixed, depth 3): one 512-thread CTA or two 256-thread
+    CTAs per SM; both shapes give the same K_H (shared-memory atomics aside)."""
+    if kind == "qned":
+        cells, a6, binv, load = workloads.qned_tensor(m=2, depth=3, seed=2)
+        c0, c1, k = a6, binv, gpu.KIND_QNED
+        build = lambda h: h.qned_build(cells, a6, binv, load)  # noqa: E731
+    else:
+        cells, ainv6, load = workloads.rtdq_tensor(m=2, depth=3, seed=2)
+        c0, c1, k = ainv6, None, gpu.KIND_RTDQ
+        build = lambda h: h.rtdq_build(cells, ainv6, load)  # noqa: E731
+    h = gpu.Handle()
+    choice, ncand, times = h.autotune(k, cells, c0, c1, load)
+    assert ncand == 2 and choice in (0, 1) and all(t > 0 for t in times), (choice, times)
+    print(f"{kind} autotune: 512x1 {times[0]:.1f} ms, 256x2 {times[1]:.1f} ms -> {choice}")
+    KH, FH, rep, st = build(h)
+    KH0, FH0, _, _ = build(gpu.Handle())
+    assert st == gpu.SUCCESS and rep["converged"].all()
+    for c in range(len(cells)):
+        assert _rel(KH[c], KH0[c]) <= 1e-11

@@ -1,10 +1,10 @@
 """GPU parity of the Ned_RT basis build against the FP64 oracle (C ABI).
 
-The local mixed system is ill-conditioned (kappa ~ 1e4 at depth 3), so even
-the sparse-direct oracle carries errors of order 1e-11 in the basis. Stated,
-measured tolerances (both precisions; mixed = FP32 MINRES + FP64 refinement):
-  K_H, F_H   max abs error <= 1e-9 * max |entry| of the cell
-  basis      max|phi - phi_oracle| <= 1e-8 * max|phi_oracle| per function
+Tolerances, the 1e-10 bar of the FP64 path, for both precisions (mixed =
+FP32 MINRES + FP64 refinement); the oracle's sparse-direct solves are refined
+in FP64 to well below it:
+  K_H, F_H   max abs error <= 1e-10 * max |entry| of the cell
+  basis      max|phi - phi_oracle| <= 1e-10 * max|phi_oracle| per function
 """
 import os
 
@@ -16,8 +16,8 @@ from oracle import nedrt_oracle as N
 
 pytestmark = pytest.mark.gpu
 HERE = os.path.dirname(os.path.abspath(__file__))
-TOL_KH = 1e-9
-TOL_PHI = 1e-8
+TOL_KH = 1e-10
+TOL_PHI = 1e-10
 PRECISIONS = ("mixed", "fp64")
 
 
@@ -159,3 +159,26 @@ def test_constant_diagonal_coefficients_give_the_standard_basis(gpu, precision, 
     for b in range(18):
         blk = slice(0, NE) if b < 12 else slice(NE, NE + NF)
         assert _rel(phi[b, blk], S[b, blk]) <= TOL_PHI, (b, _rel(phi[b, blk], S[b, blk]))
+
+
+def test_staged_coefficient_tiles_match_plain_loads(gpu):
+    """Cells with the global MINRES workspace (a depth-4 cell in the batch,
+    mixed precision): the apply that reads its coefficient tiles from shared
+    memory, put there by bulk copies (nedrt_stage 1), gives the plain-load
+    build's K_H and F_H up to the rounding of the apply's atomics, on depths
+    4, 3, 2, 1 (full, single-round and partly empty warps)."""
+    parts = [workloads.nedrt_tensor(m=1, depth=d, seed=40 + d) for d in (4, 3, 2, 1)]
+    cells = np.concatenate([p[0] for p in parts])
+    ainv6 = np.concatenate([p[1] for p in parts])
+    bdiv = np.concatenate([p[2] for p in parts])
+    load = parts[0][3]
+    out = {}
+    for st in (0, 1):
+        h = gpu.Handle(nedrt_stage=st)
+        KH, FH, rep, status = h.nedrt_build(cells, ainv6, bdiv, load)
+        assert status == gpu.SUCCESS and rep["converged"].all(), (st, rep)
+        out[st] = (KH, FH, rep)
+    for c in range(len(cells)):
+        assert _rel(out[1][0][c], out[0][0][c]) <= 1e-11, c
+        assert _rel(out[1][1][c], out[0][1][c]) <= 1e-11, c
+    print(f"staged: iterations {out[1][2]['iterations'].max()} (plain {out[0][2]['iterations'].max()})")

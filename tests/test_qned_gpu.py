@@ -1,7 +1,7 @@
 """GPU parity of the Q_Ned (Q1 sigma x Nedelec u) basis build against the FP64
 oracle (C ABI). Stated tolerances (both precisions; mixed = FP32 MINRES +
-FP64 refinement): K_H, F_H max abs error <= 1e-9 * max |entry| of the cell;
-basis max|phi - phi_oracle| <= 1e-8 * max|phi_oracle| per function."""
+FP64 refinement): K_H, F_H max abs error <= 1e-10 * max |entry| of the cell;
+basis max|phi - phi_oracle| <= 1e-10 * max|phi_oracle| per function."""
 import numpy as np
 import pytest
 
@@ -10,8 +10,8 @@ from oracle import nedrt_oracle as NR
 from oracle import qned_oracle as Q
 
 pytestmark = pytest.mark.gpu
-TOL_KH = 1e-9
-TOL_PHI = 1e-8
+TOL_KH = 1e-10
+TOL_PHI = 1e-10
 
 
 def _rel(a, b):
