@@ -318,9 +318,11 @@ def shape_names(kind, ncand, sms=152):
     if kind in ("qned", "rtdq") or (kind == "nedrt" and ncand == 2):
         return ["1 x 512-thread CTA per SM", "2 x 256-thread CTAs per SM"]
     ctas = [sms] + [max(1, sms * q // 8) for q in (7, 6, 5, 4)]
-    out = [f"{c} resident CTAs, plain coefficient loads" for c in ctas]
-    if ncand == 10:
-        out += [f"{c} resident CTAs, coefficient tiles staged by bulk copies" for c in ctas]
+    out = [f"{c} x 512-thread CTAs, plain coefficient loads" for c in ctas]
+    if ncand >= 10:
+        out += [f"{c} x 512-thread CTAs, coefficient tiles staged by bulk copies" for c in ctas]
+    if ncand == 11:
+        out.append(f"{2 * sms} x 256-thread CTAs (2 per SM), plain coefficient loads")
     return out
 
 
@@ -380,9 +382,9 @@ def gpu_run(wl, lo, hi, precision, steps, warmup, local, stream, barrier, tune_i
         else:
             c0, c1, kind = sh["a"][:f], None if sh["r"] is None else sh["r"][:f], msfec.KIND_Q1
         choice, ncand, times = h.autotune(kind, cells[:k], c0, c1, wl.load)
-        names = shape_names(wl.kind, ncand)
-        tune_info.update({"sample_cells": k, "shapes": names, "times_ms": [round(t, 2) for t in times],
-                          "choice": names[choice] if choice < len(names) else choice})
+        shapes = shape_names(wl.kind, ncand)
+        tune_info.update({"sample_cells": k, "shapes": shapes, "times_ms": [round(t, 2) for t in times],
+                          "choice": shapes[choice] if choice < len(shapes) else choice})
     for i in range(warmup):
         build(*batches[i % len(batches)])
     barrier()

@@ -117,7 +117,14 @@ typedef struct msfec_config {
      memory, put there two rounds ahead by bulk (TMA) copies; 0 = plain global
      loads. Same results either way. */
   int32_t nedrt_stage;
-  int32_t reserved;
+  /* CTAs per SM of the mixed local solvers (Ned_RT, Q_Ned, RT_DQ): 0 = the
+     autotuned choice (msfec_autotune) or else the default (two 256-thread
+     CTAs per SM where the shared workspace fits twice, one 512-thread CTA
+     otherwise); 1 = one 512-thread CTA per SM; 2 = two 256-thread CTAs per SM
+     where the workspace allows (shared workspace split between shared memory
+     and a global slot, or, for Ned_RT cells with a global workspace, two
+     global slots per SM). Same results either way. */
+  int32_t nedrt_ctas_per_sm;
 } msfec_config;
 
 typedef enum msfec_q1_coefficient {
@@ -425,7 +432,8 @@ typedef enum msfec_kind {
  *     memory (depth 4, or FP64): the number of resident CTAs, i.e. of
  *     workspace slots in L2, the SM count times 1, 7/8, 6/8, 5/8, 4/8, first
  *     with plain coefficient loads, then (mixed only) with the apply's
- *     coefficient tiles staged by bulk copies (nedrt_stage): 10 candidates.
+ *     coefficient tiles staged by bulk copies (nedrt_stage), then (mixed
+ *     only) two 256-thread CTAs per SM with a global slot each: 11 candidates.
  *   Q_Ned, RT_DQ (per deepest depth, mixed): 0 = one 512-thread CTA per SM,
  *     1 = two 256-thread CTAs per SM (when the workspace fits twice).
  * Batches with a single candidate return at once (choice = {0, 1}).

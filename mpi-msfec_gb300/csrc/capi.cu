@@ -62,6 +62,8 @@ cudaError_t q1g_gradient_launch(const Q1Cell *cells, int ncells, const double *a
                                 cudaStream_t st);
 cudaError_t nedrt_solve_launch(bool fp64, bool ml, const NRParams &prm, size_t smem, int grid, cudaStream_t st);
 cudaError_t nedrt_solve_launch_split(bool ml, const NRParams &prm, size_t smem, int grid, cudaStream_t st);
+cudaError_t nedrt_cell_prep_launch(const NRCell *cells, int ncells, const double *ainv6, const double *bdiv,
+                                   const float *coarse, float *prep, int grid, cudaStream_t st);
 cudaError_t nedrt_ml_setup_launch(const NRCell *cells, int ncells, const double *ainv6, const double *bdiv,
                                   float *coarse, float *scratch, size_t scratch_floats, size_t smem, int grid,
                                   cudaStream_t st);
@@ -75,7 +77,7 @@ cudaError_t rtdq_solve_launch(bool fp64, bool two_per_sm, const RTParams &prm, s
 cudaError_t rtdq_galerkin_launch(const NRCell *cells, int ncells, const double *phi, const double *y,
                                  const msfec_load &load, double *KH, double *FH, msfec_cell_report *rep,
                                  const NRStat *stats, cudaStream_t st);
-cudaError_t nedrt_split_occupancy(bool ml, size_t smem, int *blocks_per_sm);
+cudaError_t nedrt_split_occupancy(bool ml, bool use_smem, size_t smem, int *blocks_per_sm);
 cudaError_t nedrt_adjoint_prepare_launch(const NRCell *cells, int ncells, const double *phi, const double *U,
                                          const double *lam, const msfec_load &load, int npoints, const int *cell_of,
                                          const double *pts, const double *dJdu, const double *ainv6,
@@ -190,6 +192,7 @@ struct msfec_handle {
   DevBuf<NRStat> nr_stats;
   DevBuf<float> nr_scratch;
   DevBuf<float> nr_coarse, nr_mlscratch;  // multilevel preconditioner data per cell, setup workspace
+  DevBuf<float> nr_prep;                  // global workspace: per-cell preconditioner + float coefficients
   bool nr_ml_valid = false;               // the last Ned_RT build left multilevel data for its cells
   DevBuf<double> nr_ainv, nr_bdiv, nr_KH, nr_FH;
   int64_t nr_basis_doubles = 0;
@@ -239,10 +242,11 @@ struct msfec_handle {
   int nr_ctas[2][kNRMaxDepthCfg + 1] = {};    // [precision][deepest depth]: resident CTAs
   int nr_split[kNRMaxDepthCfg + 1] = {-1, -1, -1, -1, -1};  // [deepest depth] mixed: 1 = two 256-thread CTAs/SM
   int nr_stage[kNRMaxDepthCfg + 1] = {-1, -1, -1, -1, -1};  // [deepest depth] mixed, global workspace: staged tiles
+  int nr_two[kNRMaxDepthCfg + 1] = {-1, -1, -1, -1, -1};    // [deepest depth] mixed, global workspace: 2 CTAs/SM
   int qn_two[kNRMaxDepthCfg + 1] = {-1, -1, -1, -1, -1};    // [deepest depth] Q_Ned mixed: 1 = two CTAs/SM
   int rt_two[kNRMaxDepthCfg + 1] = {-1, -1, -1, -1, -1};    // [deepest depth] RT_DQ mixed: 1 = two CTAs/SM
   int force_split = -1, force_ctas = 0, force_nr_split = -1;  // candidate under trial
-  int force_stage = -1, force_two = -1;
+  int force_stage = -1, force_two = -1, force_nr_two = -1;
   cudaStream_t aux_stream = nullptr;          // second stream of the split Q1 launch
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int last_graph = 0;  // 0 direct launches, 1 captured a new graph, 2 replayed
@@ -933,23 +937,28 @@ constexpr size_t kNRSplitSmemLimit = 108 * 1024;  // two CTAs per SM (228 KB, mi
 // Launch shape of the Ned_RT basis solver for a batch whose deepest cell has
 // n = nmax fine cells per edge: where the MINRES workspace lives (two 256-thread
 // CTAs per SM with the split workspace, one 512-thread CTA with the whole
-// workspace in shared memory, or one with a per-CTA global slot), the dynamic
-// shared memory including the multilevel region, and the grid. Shared by the
-// handle-owned build and the allocation-free one, so both make the same choice
-// (including the autotuner's) for the same batch.
+// workspace in shared memory, or a per-CTA global slot for one 512-thread CTA
+// or two 256-thread CTAs per SM), the dynamic shared memory including the
+// multilevel region, and the grid. split = 256-thread CTAs (use_smem: the split
+// workspace; else the global slot). Shared by the handle-owned build and the
+// allocation-free one, so both make the same choice (including the
+// autotuner's) for the same batch.
 struct NRShape {
-  bool split = false, use_smem = false, ml = false, stage = false;
+  bool split = false, use_smem = false, ml = false, stage = false, prep = false;
   size_t smem = 0, ws_floats = 0, ml_offset = 0, stage_offset = 0;
   int grid = 0;
 };
 
-msfec_status nr_shape(msfec_handle *h, int nmax, bool fp64, bool want_ml, size_t nitems, NRShape &s) {
+msfec_status nr_shape(msfec_handle *h, int nmax, bool fp64, bool want_ml, size_t nitems, NRShape &s,
+                      bool allow_prep = false) {
   int deepest = 0;
   while ((1 << deepest) < nmax) ++deepest;
   deepest = std::min(deepest, kNRMaxDepthCfg);
   // mixed precision with a small enough item: two 256-thread CTAs per SM
   // (split workspace) unless the autotuner chose the 512-thread CTA
-  const int split_sel = h->force_nr_split >= 0 ? h->force_nr_split : h->nr_split[deepest];
+  const int cps = h->cfg.nedrt_ctas_per_sm;  // 0: tuned or default, 1 / 2: explicit
+  const int split_sel =
+      h->force_nr_split >= 0 ? h->force_nr_split : (cps ? (cps == 2 ? 1 : 0) : h->nr_split[deepest]);
   s.split = !fp64 && nr_split_smem_floats(nmax) * 4 <= kNRSplitSmemLimit && split_sel != 0;
   s.ws_floats = nr_workspace_floats(nmax, fp64 ? 8 : 4);
   s.use_smem = s.ws_floats * 4 <= kNRSmemLimit;
@@ -959,6 +968,11 @@ msfec_status nr_shape(msfec_handle *h, int nmax, bool fp64, bool want_ml, size_t
     s.smem = nr_split_smem_floats(nmax) * 4;
     s.ws_floats = nr_split_global_floats(nmax);  // global slot per CTA
     s.use_smem = true;
+  } else if (!s.use_smem && !fp64) {
+    // global workspace: two 256-thread CTAs per SM (two items overlap each
+    // other's barriers and reductions) when the autotuner chose them
+    const int two_sel = h->force_nr_two >= 0 ? h->force_nr_two : (cps ? (cps == 2 ? 1 : 0) : h->nr_two[deepest]);
+    s.split = two_sel > 0;
   }
   // the multilevel region follows the shared workspace (if any)
   s.ml_offset = s.smem;
@@ -966,6 +980,12 @@ msfec_status nr_shape(msfec_handle *h, int nmax, bool fp64, bool want_ml, size_t
   const size_t ml_bytes = s.ml ? nr_ml_layout(nmax, fp64 ? 8 : 4).bytes : 0;
   if (s.ml && s.smem + ml_bytes > (s.split ? kNRSplitSmemLimit : kNRSmemTotalLimit)) s.ml = false;
   if (s.ml) s.smem += ml_bytes;
+  // global workspace: the cell's preconditioner and float coefficients shared
+  // by its items (NRParams::prep), the slot holding only Krylov vectors
+  if (allow_prep && !s.use_smem) {
+    s.prep = true;
+    s.ws_floats = nr_prep_slot_floats(nmax, fp64 ? 8 : 4, s.ml);
+  }
   // global workspace (mixed): the apply's coefficient tiles staged by bulk copies
   // (nedrt_stage), two 1 KB stages per warp after the multilevel region
   const int stage_sel = h->force_stage >= 0 ? h->force_stage : h->nr_stage[deepest];
@@ -980,7 +1000,7 @@ msfec_status nr_shape(msfec_handle *h, int nmax, bool fp64, bool want_ml, size_t
   }
   if (s.split) {
     int occ = 0;
-    MSFEC_CUDA_TRY(h, nedrt_split_occupancy(s.ml, s.smem, &occ));
+    MSFEC_CUDA_TRY(h, nedrt_split_occupancy(s.ml, s.use_smem, s.smem, &occ));
     if (occ <= 0) return fail(h, MSFEC_ERROR_NOT_SUPPORTED, "split Ned_RT solver cannot be resident");
     s.grid = std::min<int>((int)nitems, occ * h->num_sms);
   } else if (!s.use_smem) {  // resident CTAs = workspace slots (L2 footprint), possibly autotuned
@@ -1048,7 +1068,7 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
     for (int b = 0; b < 18; ++b) items.push_back(NRItem{c, b, 0});
   NRShape shape;
   {
-    const msfec_status ss = nr_shape(h, nmax, fp64, ml, items.size(), shape);
+    const msfec_status ss = nr_shape(h, nmax, fp64, ml, items.size(), shape, true);
     if (ss != MSFEC_SUCCESS) return ss;
   }
   const bool split = shape.split, use_smem = shape.use_smem;
@@ -1057,6 +1077,11 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
   ml = shape.ml;
   if (!ml)
     for (auto &q : hc) q.coarse_off = -1;
+  int64_t prep_floats = 0;
+  for (auto &q : hc) {
+    q.prep_off = shape.prep ? prep_floats : -1;
+    if (shape.prep) prep_floats += (int64_t)nr_prep_floats(q.n);
+  }
   cudaStream_t st = h->stream;
   MSFEC_CUDA_TRY(h, h->nr_cells.reserve(ncells));
   MSFEC_CUDA_TRY(h, h->nr_items.reserve(items.size()));
@@ -1073,6 +1098,7 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
     MSFEC_CUDA_TRY(h, h->nr_coarse.reserve((size_t)coarse_floats));
     MSFEC_CUDA_TRY(h, h->nr_mlscratch.reserve(ml_scratch * ml_grid));
   }
+  if (shape.prep) MSFEC_CUDA_TRY(h, h->nr_prep.reserve((size_t)prep_floats));
   MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->nr_cells.ptr, hc.data(), hc.size() * sizeof(NRCell), cudaMemcpyHostToDevice, st));
   MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->nr_items.ptr, items.data(), items.size() * sizeof(NRItem),
                                     cudaMemcpyHostToDevice, st));
@@ -1094,12 +1120,14 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
   prm.max_iter = std::max(h->cfg.max_iter, 8000);  // per refinement step (MINRES, kappa ~ 1e4)
   prm.max_refine = h->cfg.max_refine;
   prm.coarse = ml ? h->nr_coarse.ptr : nullptr;
+  prm.prep = shape.prep ? h->nr_prep.ptr : nullptr;
   prm.ml_offset = ml_offset;
   prm.stage = shape.stage ? 1 : 0;
   prm.stage_offset = shape.stage_offset;
   if (h->cfg.verbose)
     fprintf(stderr, "[msfec] nedrt plan: %d cells, %zu items, workspace %zu floats (%s), grid %d, %s, %s\n", ncells,
-            items.size(), ws_floats, split ? "split, 2 CTAs/SM" : (use_smem ? "shared" : "global"), grid,
+            items.size(), ws_floats,
+            split ? (use_smem ? "split, 2 CTAs/SM" : "global, 2 CTAs/SM") : (use_smem ? "shared" : "global"), grid,
             fp64 ? "fp64" : "mixed", ml ? "multilevel" : "diagonal");
   msfec_load ld;
   if (load) {
@@ -1113,7 +1141,10 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
     if (e == cudaSuccess && ml)
       e = nedrt_ml_setup_launch(h->nr_cells.ptr, ncells, d_ainv, d_bdiv, h->nr_coarse.ptr, h->nr_mlscratch.ptr,
                                 ml_scratch, (size_t)nr_ml_data_floats(nmax) * 4, ml_grid, st);
-    if (e == cudaSuccess && timed && ml) {
+    if (e == cudaSuccess && shape.prep)
+      e = nedrt_cell_prep_launch(h->nr_cells.ptr, ncells, d_ainv, d_bdiv, ml ? h->nr_coarse.ptr : nullptr,
+                                 h->nr_prep.ptr, std::min(ncells, h->num_sms), st);
+    if (e == cudaSuccess && timed && (ml || shape.prep)) {
       e = cudaEventRecord(h->ev[4], st);
       h->ev_setup = true;
     }
@@ -1128,7 +1159,8 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
     if (e == cudaSuccess && timed) e = cudaEventRecord(h->ev[3], st);
     return e;
   };
-  const msfec_status s = run_sequence(h, h->nr_graph, std::move(key), (d_rep ? 3 : 2) + (ml ? 1 : 0), seq);
+  const msfec_status s =
+      run_sequence(h, h->nr_graph, std::move(key), (d_rep ? 3 : 2) + (ml ? 1 : 0) + (shape.prep ? 1 : 0), seq);
   if (s != MSFEC_SUCCESS) return s;
   h->nr_ml_valid = ml;
   h->nr_graph_basis = dofs * 18;
@@ -1178,7 +1210,9 @@ msfec_status qned_build_impl(msfec_handle *h, int ncells, const msfec_cell *cell
   // mixed precision with a workspace that fits twice per SM: two 256-thread CTAs per SM
   int deepest_q = 0;
   while ((1 << deepest_q) < nmax) ++deepest_q;
-  const int two_sel = h->force_two >= 0 ? h->force_two : h->qn_two[std::min(deepest_q, kNRMaxDepthCfg)];
+  const int cps = h->cfg.nedrt_ctas_per_sm;
+  const int two_sel = h->force_two >= 0 ? h->force_two
+                                        : (cps ? (cps == 2 ? 1 : 0) : h->qn_two[std::min(deepest_q, kNRMaxDepthCfg)]);
   const bool two_per_sm = !fp64 && use_smem && smem <= kNRSplitSmemLimit && two_sel != 0;
   const int grid = std::min<int>((int)items.size(), (two_per_sm ? 2 : 1) * h->num_sms);
   cudaStream_t st = h->stream;
@@ -1275,7 +1309,9 @@ msfec_status rtdq_build_impl(msfec_handle *h, int ncells, const msfec_cell *cell
   const size_t smem = use_smem ? ws_floats * 4 : 0;
   int deepest_r = 0;
   while ((1 << deepest_r) < nmax) ++deepest_r;
-  const int two_sel = h->force_two >= 0 ? h->force_two : h->rt_two[std::min(deepest_r, kNRMaxDepthCfg)];
+  const int cps = h->cfg.nedrt_ctas_per_sm;
+  const int two_sel = h->force_two >= 0 ? h->force_two
+                                        : (cps ? (cps == 2 ? 1 : 0) : h->rt_two[std::min(deepest_r, kNRMaxDepthCfg)]);
   const bool two_per_sm = !fp64 && use_smem && smem <= kNRSplitSmemLimit && two_sel != 0;
   const int grid = std::min<int>((int)items.size(), (two_per_sm ? 2 : 1) * h->num_sms);
   cudaStream_t st = h->stream;
@@ -1436,7 +1472,7 @@ msfec_status msfec_create(msfec_handle **out, const msfec_config *cfg) {
   if (!(c.rtol > 0.0) || !(c.inner_rtol > 0.0) || c.inner_rtol >= 1.0 || c.max_iter < 1 || c.max_refine < 1 ||
       !(c.nedrt_rtol > 0.0) || c.q1_launch < 0 || c.q1_launch > 2 || c.nedrt_precond < 0 || c.nedrt_precond > 1 ||
       c.q1_coefficient < MSFEC_Q1_COEF_SCALAR || c.q1_coefficient > MSFEC_Q1_COEF_GAUSS || c.nedrt_stage < 0 ||
-      c.nedrt_stage > 1)
+      c.nedrt_stage > 1 || c.nedrt_ctas_per_sm < 0 || c.nedrt_ctas_per_sm > 2)
     return MSFEC_ERROR_INVALID_ARGUMENT;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || c.device < 0 || c.device >= ndev) return MSFEC_ERROR_CUDA;
@@ -2111,7 +2147,13 @@ msfec_status msfec_autotune(msfec_handle *h, int32_t kind, int32_t ncells, const
           cand.push_back(Cand{});
           cand.back().ctas = c;
           cand.back().stage = st;
+          cand.back().two = 0;
         }
+      if (!fp64 && !smem_ws) {  // two 256-thread CTAs per SM, global workspace
+        cand.push_back(Cand{});
+        cand.back().two = 1;
+        cand.back().stage = 0;
+      }
     }
   } else {  // Q_Ned / RT_DQ: one 512-thread CTA per SM, or two 256-thread CTAs when the workspace fits twice
     const size_t ws = kind == MSFEC_KIND_QNED ? qn_workspace_floats(nmax, fp64 ? 8 : 4) : rt_workspace_floats(nmax, fp64 ? 8 : 4);
@@ -2137,6 +2179,7 @@ msfec_status msfec_autotune(msfec_handle *h, int32_t kind, int32_t ncells, const
     h->force_nr_split = cand[k].nr_split;
     h->force_stage = cand[k].stage;
     h->force_two = cand[k].two;
+    h->force_nr_two = kind == MSFEC_KIND_NEDRT ? cand[k].two : -1;
     msfec_timings t{};
     for (int rep = 0; rep < 2 && s == MSFEC_SUCCESS; ++rep) {  // second run timed (first warms)
       switch (kind) {
@@ -2163,6 +2206,7 @@ msfec_status msfec_autotune(msfec_handle *h, int32_t kind, int32_t ncells, const
   h->force_nr_split = -1;
   h->force_stage = -1;
   h->force_two = -1;
+  h->force_nr_two = -1;
   h->graph_mode = graph0;
   msfec_set_timing(h, timing0 ? 1 : 0);
   if (s != MSFEC_SUCCESS) return s;
@@ -2173,8 +2217,11 @@ msfec_status msfec_autotune(msfec_handle *h, int32_t kind, int32_t ncells, const
     if (nr_split_tune) {
       h->nr_split[dcfg] = w.nr_split;
     } else {
-      h->nr_ctas[fp64 ? 0 : 1][dcfg] = w.ctas == h->num_sms ? 0 : w.ctas;
-      if (nr_global && !fp64) h->nr_stage[dcfg] = w.stage;
+      h->nr_ctas[fp64 ? 0 : 1][dcfg] = (w.ctas == h->num_sms || w.ctas == 0) ? 0 : w.ctas;
+      if (nr_global && !fp64) {
+        h->nr_stage[dcfg] = w.stage;
+        h->nr_two[dcfg] = w.two;
+      }
     }
   } else if (kind == MSFEC_KIND_QNED) {
     h->qn_two[dcfg] = w.two;

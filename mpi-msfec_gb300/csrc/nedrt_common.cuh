@@ -26,6 +26,7 @@ struct NRCell {
   long long coef_off;  // first fine cell in ainv6 / bdiv
   long long dof_off;   // sum of previous cells' DoF counts; Phi base = 18 * dof_off
   long long coarse_off;  // first float of the cell's multilevel preconditioner data, -1: none
+  long long prep_off;    // first float of the cell's shared preconditioner + coefficients (NRParams::prep)
 };
 
 struct NRItem {
@@ -59,6 +60,11 @@ struct NRParams {
   double *src_out;        // source mode: solutions, same layout
   const double *src_scale2;  // source mode: [dof_off + d] squared scale of the terms the right-hand side
                              // is a difference of; 1e-3 of its P-norm floors ||f||_P in the stopping test (null: none)
+  // global workspace: per cell at NRCell::prep_off, the preconditioner diagonal
+  // (Np floats) and the float coefficients (8 per fine cell), built once by
+  // nr_cell_prep_kernel and read by the cell's 18 items, whose global slots then
+  // hold only Krylov vectors; null: every item builds its own in its slot
+  float *prep;
   float *scratch;       // global workspace when the item does not fit shared memory
   size_t scratch_floats;  // per CTA
   const float *coarse;    // multilevel preconditioner data (per cell at coarse_off); null: diagonal only
@@ -92,6 +98,26 @@ __host__ __device__ inline size_t nr_workspace_floats(int n, int tsize) {
   const size_t Np = (N + al - 1) / al * al;
   const size_t nc = (size_t)n * n * n;
   return Np + 7 * Np * (size_t)(tsize / 4) + (8 * nc + al - 1) / al * al;
+}
+
+// Per-cell shared data of the global workspace (NRParams::prep): the
+// preconditioner diagonal over the padded DoFs and 8 float coefficients per
+// fine cell, 64-float aligned.
+__host__ __device__ inline size_t nr_prep_floats(int n) {
+  int NEx, NFx, NE, NF;
+  nr_counts(n, NEx, NFx, NE, NF);
+  const size_t Np = ((size_t)NE + NF + 63) / 64 * 64;
+  return Np + (8 * (size_t)n * n * n + 63) / 64 * 64;
+}
+// Global slot of one item when the cell's data is shared (NRParams::prep):
+// the Krylov vectors z~, v~ (2), w (2), x, and the apply's accumulation vector
+// for the diagonal-preconditioner path only (the multilevel path accumulates
+// the apply into the spent Lanczos vector).
+__host__ __device__ inline size_t nr_prep_slot_floats(int n, int tsize, bool multilevel) {
+  int NEx, NFx, NE, NF;
+  nr_counts(n, NEx, NFx, NE, NF);
+  const size_t Np = ((size_t)NE + NF + 63) / 64 * 64;
+  return (multilevel ? 6 : 7) * Np * (size_t)(tsize / 4);
 }
 
 // Split workspace of the two-CTAs-per-SM mixed variant (256 threads): the

@@ -72,14 +72,15 @@ def test_nedrt_autotune_global_workspace(gpu):
 
 
 def test_nedrt_autotune_depth4_ctas_and_staging(gpu):
-    """Mixed depth 4 (global MINRES workspace): 10 candidates, resident CTAs x
-    coefficient staging; the tuned build's K_H equals the default build's."""
+    """Mixed depth 4 (global MINRES workspace): 11 candidates, resident
+    512-thread CTAs x coefficient staging, then two 256-thread CTAs per SM; the
+    tuned build's K_H equals the default build's."""
     cells, ainv6, bdiv, load = workloads.nedrt_tensor(m=1, depth=4, seed=6)
     h = gpu.Handle()
     choice, ncand, times = h.autotune(gpu.KIND_NEDRT, cells, ainv6, bdiv, load)
-    assert ncand == 10 and 0 <= choice < 10 and all(t > 0 for t in times), (choice, times)
+    assert ncand == 11 and 0 <= choice < 11 and all(t > 0 for t in times[:11]), (choice, times)
     print("nedrt autotune (mixed, depth 4): plain", [f"{t:.1f}" for t in times[:5]], "staged",
-          [f"{t:.1f}" for t in times[5:]], "->", choice)
+          [f"{t:.1f}" for t in times[5:10]], "2 CTAs/SM", f"{times[10]:.1f}", "->", choice)
     KH, FH, rep, st = h.nedrt_build(cells, ainv6, bdiv, load)
     assert st == gpu.SUCCESS and rep["converged"].all()
     KH0, FH0, _, _ = gpu.Handle().nedrt_build(cells, ainv6, bdiv, load)

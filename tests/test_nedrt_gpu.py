@@ -21,16 +21,16 @@ TOL_PHI = 1e-10
 PRECISIONS = ("mixed", "fp64")
 
 
-def _handle(gpu, precision):
-    return gpu.Handle(precision=gpu.PRECISION_MIXED if precision == "mixed" else gpu.PRECISION_FP64)
+def _handle(gpu, precision, **kw):
+    return gpu.Handle(precision=gpu.PRECISION_MIXED if precision == "mixed" else gpu.PRECISION_FP64, **kw)
 
 
 def _rel(a, b):
     return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
 
 
-def _check(gpu, precision, cells, ainv6, bdiv, load, basis=True):
-    h = _handle(gpu, precision)
+def _check(gpu, precision, cells, ainv6, bdiv, load, basis=True, **kw):
+    h = _handle(gpu, precision, **kw)
     KH, FH, rep, st = h.nedrt_build(cells, ainv6, bdiv, load)
     assert st == gpu.SUCCESS and rep["converged"].all(), rep
     ref = N.build(cells, N.sym6_to_ainv(ainv6), bdiv, load.kind, list(load.params), want_phi=basis)
@@ -73,10 +73,12 @@ def test_depth3_basis_matches_oracle(gpu, precision):
            np.concatenate([bdiv, b2]), load)
 
 
-@pytest.mark.parametrize("precision", PRECISIONS)
-def test_depth4_global_workspace(gpu, precision):
+@pytest.mark.parametrize("precision,ctas_per_sm", [("mixed", 1), ("fp64", 0), ("mixed", 2)])
+def test_depth4_global_workspace(gpu, precision, ctas_per_sm):
+    """Depth 4 (MINRES workspace in a per-CTA global slot): one 512-thread CTA
+    per SM, or (mixed) two 256-thread CTAs per SM."""
     cells, ainv6, bdiv, load = workloads.nedrt_tensor(m=1, depth=4, seed=6)
-    _check(gpu, precision, cells, ainv6, bdiv, load, basis=False)
+    _check(gpu, precision, cells, ainv6, bdiv, load, basis=False, nedrt_ctas_per_sm=ctas_per_sm)
 
 
 def test_invalid_tensor_rejected(gpu):
@@ -182,3 +184,26 @@ def test_staged_coefficient_tiles_match_plain_loads(gpu):
         assert _rel(out[1][0][c], out[0][0][c]) <= 1e-11, c
         assert _rel(out[1][1][c], out[0][1][c]) <= 1e-11, c
     print(f"staged: iterations {out[1][2]['iterations'].max()} (plain {out[0][2]['iterations'].max()})")
+
+
+def test_two_ctas_per_sm_global_workspace_match_one(gpu):
+    """A batch whose deepest cell has depth 4 runs every item from a global
+    workspace slot; two 256-thread CTAs per SM (nedrt_ctas_per_sm 2) give the
+    512-thread build's K_H, F_H and basis up to the rounding of the apply's
+    atomics, on depths 4, 3, 2, 1 (full, single-round and partly empty warps)."""
+    parts = [workloads.nedrt_tensor(m=1, depth=d, seed=50 + d) for d in (4, 3, 2, 1)]
+    cells = np.concatenate([p[0] for p in parts])
+    ainv6 = np.concatenate([p[1] for p in parts])
+    bdiv = np.concatenate([p[2] for p in parts])
+    load = parts[0][3]
+    out = {}
+    for cps in (1, 2):
+        h = gpu.Handle(nedrt_ctas_per_sm=cps)
+        KH, FH, rep, status = h.nedrt_build(cells, ainv6, bdiv, load)
+        assert status == gpu.SUCCESS and rep["converged"].all(), (cps, rep)
+        out[cps] = (KH, FH, rep, h.nedrt_basis())
+    for c in range(len(cells)):
+        assert _rel(out[2][0][c], out[1][0][c]) <= 1e-11, c
+        assert _rel(out[2][1][c], out[1][1][c]) <= 1e-11, c
+    assert np.abs(out[2][3] - out[1][3]).max() <= 1e-10 * np.abs(out[1][3]).max()
+    print(f"2 CTAs/SM: iterations {out[2][2]['iterations'].max()} (1 CTA/SM {out[1][2]['iterations'].max()})")
