@@ -468,8 +468,10 @@ def e2e_run(wl, lo, hi, local, stream, barrier, steps):
 # (profiles/nedrt_solve_kernel_L3_traffic.md), 358.2 MB / 256 cells; traffic grows with the cells.
 NEDRT_L3_TRAFFIC_PER_CELL = 358.2e6 / 256
 # The same for depth-4 cells (global MINRES workspace): ncu DRAM bytes of
-# `bench.py --probe nedrt_depth4_8cells` per cell (profiles/nedrt_solve_kernel_L4_8cells.md).
-NEDRT_L4_TRAFFIC_PER_CELL = None
+# `bench.py --probe nedrt_depth4_8cells` (one wave: 144 items), 20.05 GB read + 61.07 GB written
+# per 8 cells (profiles/nedrt_solve_kernel_L4_8cells.md); every item streams its own workspace, so
+# the traffic grows with the items.
+NEDRT_L4_TRAFFIC_PER_CELL = (20.05e9 + 61.07e9) / 8
 
 
 def roofline(wl, lo, hi, solve_ms, setup_ms, gal_ms, rep, kind):
