@@ -100,9 +100,14 @@ typedef struct msfec_config {
      The mixed local system has condition number ~1e4 at depth 3, so 1e-14
      is needed for a 1e-10 basis error. */
   double nedrt_rtol;
-  /* Face (Schur) block preconditioner of the mixed local solvers (Ned_RT):
-     0 = multilevel (diagonal + coarse RT levels n/2 .. 4 + exact level 2),
-     1 = diagonal only. */
+  /* Preconditioner of the Ned_RT local solver:
+     0 = face (Schur) block multilevel (diagonal + coarse RT levels n/2 .. 4 +
+         exact level 2); edge block, for cells whose MINRES workspace is in
+         global memory (depth 4, or the FP64 path), the additive Schwarz
+         operator over fine-cell patches (the inverse of the edge mass on each
+         fine cell's 12 edges), else diag(M)^-1;
+     1 = diagonal only (both blocks);
+     2 = multilevel face block, diagonal edge block. */
   int32_t nedrt_precond;
   /* Layout of the Q1 diffusion coefficient `a` (msfec_q1_coefficient):
      SCALAR one value per fine cell (default); TENSOR a symmetric positive

@@ -21,26 +21,33 @@
 
 namespace msfec {
 cudaError_t q1_solve_launch_f32_c1(bool has_r, const Q1Params &prm, size_t smem, int grid, cudaStream_t st);
-cudaError_t q1_solve_launch_f32_c8(bool has_r, const Q1Params &prm, size_t smem, int grid, cudaStream_t st);
+cudaError_t q1_solve_launch_f32_c8(bool has_r, bool slab_only, const Q1Params &prm, size_t smem, int grid,
+                                   cudaStream_t st);
 cudaError_t q1_solve_launch_f64_c1(bool has_r, const Q1Params &prm, size_t smem, int grid, cudaStream_t st);
-cudaError_t q1_solve_launch_f64_c8(bool has_r, const Q1Params &prm, size_t smem, int grid, cudaStream_t st);
+cudaError_t q1_solve_launch_f64_c8(bool has_r, bool slab_only, const Q1Params &prm, size_t smem, int grid,
+                                   cudaStream_t st);
 cudaError_t q1_solve_occupancy_f32_c1(bool has_r, size_t smem, int *out);
-cudaError_t q1_solve_occupancy_f32_c8(bool has_r, size_t smem, int *out);
+cudaError_t q1_solve_occupancy_f32_c8(bool has_r, bool slab_only, size_t smem, int *out);
 cudaError_t q1_solve_occupancy_f64_c1(bool has_r, size_t smem, int *out);
-cudaError_t q1_solve_occupancy_f64_c8(bool has_r, size_t smem, int *out);
+cudaError_t q1_solve_occupancy_f64_c8(bool has_r, bool slab_only, size_t smem, int *out);
 
+// slab_only (cluster launches whose units are all z-slab items): the cluster
+// kernel variant without the independent-item paths.
 static cudaError_t q1_solve_launch(bool fp64, int cluster, bool has_r, const Q1Params &prm, size_t smem, int grid,
-                                   cudaStream_t st) {
+                                   cudaStream_t st, bool slab_only = false) {
   if (fp64)
-    return cluster > 1 ? q1_solve_launch_f64_c8(has_r, prm, smem, grid, st)
+    return cluster > 1 ? q1_solve_launch_f64_c8(has_r, slab_only, prm, smem, grid, st)
                        : q1_solve_launch_f64_c1(has_r, prm, smem, grid, st);
-  return cluster > 1 ? q1_solve_launch_f32_c8(has_r, prm, smem, grid, st)
+  return cluster > 1 ? q1_solve_launch_f32_c8(has_r, slab_only, prm, smem, grid, st)
                      : q1_solve_launch_f32_c1(has_r, prm, smem, grid, st);
 }
-static cudaError_t q1_solve_occupancy(bool fp64, int cluster, bool has_r, size_t smem, int *out) {
+static cudaError_t q1_solve_occupancy(bool fp64, int cluster, bool has_r, size_t smem, int *out,
+                                      bool slab_only = false) {
   if (fp64)
-    return cluster > 1 ? q1_solve_occupancy_f64_c8(has_r, smem, out) : q1_solve_occupancy_f64_c1(has_r, smem, out);
-  return cluster > 1 ? q1_solve_occupancy_f32_c8(has_r, smem, out) : q1_solve_occupancy_f32_c1(has_r, smem, out);
+    return cluster > 1 ? q1_solve_occupancy_f64_c8(has_r, slab_only, smem, out)
+                       : q1_solve_occupancy_f64_c1(has_r, smem, out);
+  return cluster > 1 ? q1_solve_occupancy_f32_c8(has_r, slab_only, smem, out)
+                     : q1_solve_occupancy_f32_c1(has_r, smem, out);
 }
 cudaError_t q1_galerkin_launch(const Q1Cell *cells, int ncells, const double *phi, const double *y,
                                const msfec_load &load, double *KH, double *FH, cudaStream_t stream);
@@ -63,7 +70,7 @@ cudaError_t q1g_gradient_launch(const Q1Cell *cells, int ncells, const double *a
 cudaError_t nedrt_solve_launch(bool fp64, bool ml, const NRParams &prm, size_t smem, int grid, cudaStream_t st);
 cudaError_t nedrt_solve_launch_split(bool ml, const NRParams &prm, size_t smem, int grid, cudaStream_t st);
 cudaError_t nedrt_cell_prep_launch(const NRCell *cells, int ncells, const double *ainv6, const double *bdiv,
-                                   const float *coarse, float *prep, int grid, cudaStream_t st);
+                                   const float *coarse, float *prep, int edge_patch, int grid, cudaStream_t st);
 cudaError_t nedrt_ml_setup_launch(const NRCell *cells, int ncells, const double *ainv6, const double *bdiv,
                                   float *coarse, float *scratch, size_t scratch_floats, size_t smem, int grid,
                                   cudaStream_t st);
@@ -675,7 +682,7 @@ msfec_status q1_build_impl(msfec_handle *h, int ncells, const msfec_cell *cells,
     smem_a = plan.smem_slab;
   }
   int occ = 0;
-  MSFEC_CUDA_TRY(h, q1_solve_occupancy(fp64, cluster_a, has_r, smem_a, &occ));
+  MSFEC_CUDA_TRY(h, q1_solve_occupancy(fp64, cluster_a, has_r, smem_a, &occ, plan.split));
   if (occ <= 0) return fail(h, MSFEC_ERROR_NOT_SUPPORTED, "local solver kernel cannot be resident");
   int grid;
   if (cluster_a > 1) {
@@ -709,7 +716,7 @@ msfec_status q1_build_impl(msfec_handle *h, int ncells, const msfec_cell *cells,
     if (plan.split) {
       if (e == cudaSuccess) e = cudaEventRecord(h->ev_fork, st);
       if (e == cudaSuccess) e = cudaStreamWaitEvent(h->aux_stream, h->ev_fork, 0);
-      if (e == cudaSuccess) e = q1_solve_launch(fp64, cluster_a, has_r, prm, smem_a, grid, st);
+      if (e == cudaSuccess) e = q1_solve_launch(fp64, cluster_a, has_r, prm, smem_a, grid, st, true);
       if (e == cudaSuccess) e = q1_solve_launch(fp64, 1, has_r, prm_b, plan.smem_indep, grid_b, h->aux_stream);
       if (e == cudaSuccess) e = cudaEventRecord(h->ev_join, h->aux_stream);
       if (e == cudaSuccess) e = cudaStreamWaitEvent(st, h->ev_join, 0);
@@ -1046,8 +1053,8 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
     dofs += NE + NF;
     nmax = std::max(nmax, n);
   }
-  // multilevel face preconditioner for every cell of depth >= 2 (nedrt_precond 0)
-  bool ml = h->cfg.nedrt_precond == 0 && nmax >= 4;
+  // multilevel face preconditioner for every cell of depth >= 2 (nedrt_precond 0, 2)
+  bool ml = h->cfg.nedrt_precond != 1 && nmax >= 4;
   int64_t coarse_floats = 0;
   int n_ml = 0;
   for (int c = 0; c < ncells; ++c) {
@@ -1121,6 +1128,7 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
   prm.max_refine = h->cfg.max_refine;
   prm.coarse = ml ? h->nr_coarse.ptr : nullptr;
   prm.prep = shape.prep ? h->nr_prep.ptr : nullptr;
+  prm.edge_patch = (shape.prep && ml && h->cfg.nedrt_precond == 0) ? 1 : 0;
   prm.ml_offset = ml_offset;
   prm.stage = shape.stage ? 1 : 0;
   prm.stage_offset = shape.stage_offset;
@@ -1143,7 +1151,7 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
                                 ml_scratch, (size_t)nr_ml_data_floats(nmax) * 4, ml_grid, st);
     if (e == cudaSuccess && shape.prep)
       e = nedrt_cell_prep_launch(h->nr_cells.ptr, ncells, d_ainv, d_bdiv, ml ? h->nr_coarse.ptr : nullptr,
-                                 h->nr_prep.ptr, std::min(ncells, h->num_sms), st);
+                                 h->nr_prep.ptr, prm.edge_patch, std::min(ncells, h->num_sms), st);
     if (e == cudaSuccess && timed && (ml || shape.prep)) {
       e = cudaEventRecord(h->ev[4], st);
       h->ev_setup = true;
@@ -1470,7 +1478,7 @@ msfec_status msfec_create(msfec_handle **out, const msfec_config *cfg) {
     msfec_config_default(&c);
   if (c.precision != MSFEC_PRECISION_FP64 && c.precision != MSFEC_PRECISION_MIXED) return MSFEC_ERROR_INVALID_ARGUMENT;
   if (!(c.rtol > 0.0) || !(c.inner_rtol > 0.0) || c.inner_rtol >= 1.0 || c.max_iter < 1 || c.max_refine < 1 ||
-      !(c.nedrt_rtol > 0.0) || c.q1_launch < 0 || c.q1_launch > 2 || c.nedrt_precond < 0 || c.nedrt_precond > 1 ||
+      !(c.nedrt_rtol > 0.0) || c.q1_launch < 0 || c.q1_launch > 2 || c.nedrt_precond < 0 || c.nedrt_precond > 2 ||
       c.q1_coefficient < MSFEC_Q1_COEF_SCALAR || c.q1_coefficient > MSFEC_Q1_COEF_GAUSS || c.nedrt_stage < 0 ||
       c.nedrt_stage > 1 || c.nedrt_ctas_per_sm < 0 || c.nedrt_ctas_per_sm > 2)
     return MSFEC_ERROR_INVALID_ARGUMENT;
@@ -2756,7 +2764,7 @@ msfec_status msfec_nedrt_build_noalloc(msfec_handle *h, int32_t ncells, const ms
   // launch shape: the same choice as msfec_nedrt_build_device for this batch
   const bool fp64 = h->cfg.precision == MSFEC_PRECISION_FP64;
   const size_t nitems = (size_t)ncells * 18;
-  const bool want_ml = h->cfg.nedrt_precond == 0 && nmax >= 4;
+  const bool want_ml = h->cfg.nedrt_precond != 1 && nmax >= 4;
   NRShape shape;
   {
     const msfec_status ss = nr_shape(h, nmax, fp64, want_ml, nitems, shape);

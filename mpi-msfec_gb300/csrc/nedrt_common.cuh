@@ -65,6 +65,10 @@ struct NRParams {
   // nr_cell_prep_kernel and read by the cell's 18 items, whose global slots then
   // hold only Krylov vectors; null: every item builds its own in its slot
   float *prep;
+  // with prep and the multilevel face preconditioner: the edge block of the
+  // preconditioner is the additive Schwarz operator over fine-cell patches,
+  // sum_c R_c^T (M restricted to cell c's 12 edges)^-1 R_c, instead of diag(M)^-1
+  int edge_patch;
   float *scratch;       // global workspace when the item does not fit shared memory
   size_t scratch_floats;  // per CTA
   const float *coarse;    // multilevel preconditioner data (per cell at coarse_off); null: diagonal only
@@ -100,10 +104,20 @@ __host__ __device__ inline size_t nr_workspace_floats(int n, int tsize) {
   return Np + 7 * Np * (size_t)(tsize / 4) + (8 * nc + al - 1) / al * al;
 }
 
-// Per-cell shared data of the global workspace (NRParams::prep): the
-// preconditioner diagonal over the padded DoFs and 8 float coefficients per
-// fine cell, 64-float aligned.
+// Per-cell shared data of the global workspace (NRParams::prep), 64-float
+// aligned parts: the preconditioner diagonal over the padded DoFs, 8 float
+// coefficients per fine cell, and the cell-patch factors of the edge
+// preconditioner (kNRPatchFloats 32-bit words per fine cell, structure of
+// arrays: word t of fine cell c at t * n^3 + c).
+constexpr int kNRPatchFloats = 39;  // L^-1 of a 12 x 12 Cholesky factor: 78 FP16 entries, 2 per word
 __host__ __device__ inline size_t nr_prep_floats(int n) {
+  int NEx, NFx, NE, NF;
+  nr_counts(n, NEx, NFx, NE, NF);
+  const size_t Np = ((size_t)NE + NF + 63) / 64 * 64;
+  const size_t nc = (size_t)n * n * n;
+  return Np + (8 * nc + 63) / 64 * 64 + (kNRPatchFloats * nc + 63) / 64 * 64;
+}
+__host__ __device__ inline size_t nr_prep_patch_offset(int n) {
   int NEx, NFx, NE, NF;
   nr_counts(n, NEx, NFx, NE, NF);
   const size_t Np = ((size_t)NE + NF + 63) / 64 * 64;

@@ -1,6 +1,8 @@
 // Ned_RT multilevel setup, Galerkin, report and adjoint kernels, and the
 // dispatch of the persistent solver over its per-precision translation
 // units (the solver itself: nedrt_solver.cuh).
+#include <cuda_fp16.h>
+
 #include "nedrt_solver.cuh"
 
 namespace msfec {
@@ -691,22 +693,108 @@ __global__ void __launch_bounds__(kMLSetupThreads) nr_ml_setup_kernel(const NRCe
 __global__ void __launch_bounds__(kNRThreads) nr_cell_prep_kernel(const NRCell *__restrict__ cells, int ncells,
                                                                   const double *__restrict__ ainv6,
                                                                   const double *__restrict__ bdiv,
-                                                                  const float *__restrict__ coarse, float *prep) {
+                                                                  const float *__restrict__ coarse, float *prep,
+                                                                  int edge_patch) {
   __shared__ NRShared sh;
-  for (int c = blockIdx.x; c < ncells; c += gridDim.x) {
-    const NRCell C = cells[c];
+  for (int cell = blockIdx.x; cell < ncells; cell += gridDim.x) {
+    const NRCell C = cells[cell];
     NRGeom g;
     g.n = C.n;
     g.L = C.depth;
     nr_counts(g.n, g.NEx, g.NFx, g.NE, g.NF);
     g.N = g.NE + g.NF;
+    const int n = g.n, nc = n * n * n;
     const int Np = (g.N + 63) / 64 * 64;
     float *pd = prep + C.prep_off;
     float *cf = pd + Np;
-    nr_float_coefficients<kNRThreads>(ainv6 + 6 * C.coef_off, bdiv + C.coef_off, g.n * g.n * g.n,
+    nr_float_coefficients<kNRThreads>(ainv6 + 6 * C.coef_off, bdiv + C.coef_off, nc,
                                       1.0 / (C.h[0] * C.h[1] * C.h[2]), cf);
     nr_precond_diag<kNRThreads>(g, C, cf, pd, Np, sh, false,
                                 (coarse && C.coarse_off >= 0) ? coarse + C.coarse_off + nr_ml_data_floats(C.n) : nullptr);
+    if (!edge_patch || !coarse || C.coarse_off < 0) continue;  // block-uniform
+    // Cell-patch factors of the edge preconditioner: per fine cell the
+    // assembled edge mass on its 12 edges, M_lm = sum over the fine cells that
+    // hold both edges of A^-1_pq G_pq(l4', m4') (positions in that cell), with
+    // Dirichlet edges (pd = 0) replaced by identity rows, factorised M = L L^T
+    // in FP64; L^-1 is stored.
+    float *X = prep + C.prep_off + nr_prep_patch_offset(n);
+    for (int c = threadIdx.x; c < nc; c += kNRThreads) {
+      const int ci = c & (n - 1), cj = (c >> g.L) & (n - 1), ck = c >> (2 * g.L);
+      int e[12], f[6];
+      cell_dofs(g, c, e, f);
+      double Mb[12][12];
+      bool in[12];
+#pragma unroll
+      for (int l = 0; l < 12; ++l) {
+        in[l] = pd[e[l]] > 0.0f;
+#pragma unroll
+        for (int m = 0; m < 12; ++m) Mb[l][m] = 0.0;
+      }
+      for (int l = 0; l < 12; ++l) {
+        if (!in[l]) continue;
+        const int p = l >> 2;
+        int x, y, z;
+        nr_edge_line(l, ci, cj, ck, x, y, z);
+        for (int s = 0; s < 4; ++s) {  // the 4 fine cells around edge l
+          const int a = s & 1, b = s >> 1;
+          const int qi = p == 0 ? x : x - 1 + a;
+          const int qj = p == 1 ? y : (p == 0 ? y - 1 + a : y - 1 + b);
+          const int qk = p == 2 ? z : z - 1 + b;
+          if (qi < 0 || qj < 0 || qk < 0 || qi >= n || qj >= n || qk >= n) continue;
+          const float *ca = cf + 8 * (size_t)((qk * n + qj) * n + qi);
+          const int l4 = nr_edge_pos_in(p, x, y, z, qi, qj, qk);
+          for (int m = l; m < 12; ++m) {
+            if (!in[m]) continue;
+            const int q = m >> 2;
+            int xm, ym, zm;
+            nr_edge_line(m, ci, cj, ck, xm, ym, zm);
+            const int m4 = nr_edge_pos_in(q, xm, ym, zm, qi, qj, qk);
+            if (m4 < 0) continue;
+            Mb[l][m] += (double)nr_ainv_pq(ca, p, q) * (double)sh.Gf[p][q][l4][m4];
+          }
+        }
+      }
+      for (int l = 0; l < 12; ++l) {
+        for (int m = 0; m < l; ++m) Mb[l][m] = Mb[m][l];
+        if (!in[l]) Mb[l][l] = 1.0;
+      }
+      // Cholesky M = L L^T in place (lower), then L^-1 in place, X = L^-T L^-1
+      for (int j = 0; j < 12; ++j) {
+        double d = Mb[j][j];
+        for (int k = 0; k < j; ++k) d -= Mb[j][k] * Mb[j][k];
+        d = sqrt(fmax(d, 1e-300));
+        Mb[j][j] = d;
+        for (int i = j + 1; i < 12; ++i) {
+          double v = Mb[i][j];
+          for (int k = 0; k < j; ++k) v -= Mb[i][k] * Mb[j][k];
+          Mb[i][j] = v / d;
+        }
+      }
+      for (int j = 0; j < 12; ++j) {
+        Mb[j][j] = 1.0 / Mb[j][j];
+        for (int i = j + 1; i < 12; ++i) {
+          double v = 0.0;
+          for (int k = j; k < i; ++k) v -= Mb[i][k] * Mb[k][j];
+          Mb[i][j] = v / Mb[i][i];
+        }
+      }
+      // store L^-1 (lower triangle, row by row: entries (l, 0..l)) in FP16
+      // pairs; X = L^-T L^-1 is then symmetric positive definite whatever the
+      // rounding of the stored entries (a Gram matrix). Dirichlet edges have
+      // identity rows and columns in M and a zero v, so they add nothing.
+      __half2 *X2 = reinterpret_cast<__half2 *>(X);
+      float pend = 0.0f;
+      int t = 0;
+      for (int l = 0; l < 12; ++l)
+        for (int m = 0; m <= l; ++m, ++t) {
+          const float v = (float)Mb[l][m];
+          if (t & 1)
+            X2[(size_t)(t >> 1) * nc + c] = __floats2half2_rn(pend, v);
+          else
+            pend = v;
+        }
+    }
+    __syncthreads();  // sh tables are rewritten for the next cell
   }
 }
 
@@ -739,11 +827,12 @@ cudaError_t nedrt_split_occupancy(bool ml, bool use_smem, size_t smem, int *bloc
 }
 
 // Shared per-cell preconditioner + float coefficients (NRParams::prep) of
-// every cell, at its prep_off; coarse: the multilevel data (null: none).
+// every cell, at its prep_off; coarse: the multilevel data (null: none);
+// edge_patch: also the cell-patch edge-mass inverses of multilevel cells.
 cudaError_t nedrt_cell_prep_launch(const NRCell *cells, int ncells, const double *ainv6, const double *bdiv,
-                                   const float *coarse, float *prep, int grid, cudaStream_t st) {
+                                   const float *coarse, float *prep, int edge_patch, int grid, cudaStream_t st) {
   if (ncells <= 0 || grid <= 0) return cudaSuccess;
-  nrimpl::nr_cell_prep_kernel<<<grid, kNRThreads, 0, st>>>(cells, ncells, ainv6, bdiv, coarse, prep);
+  nrimpl::nr_cell_prep_kernel<<<grid, kNRThreads, 0, st>>>(cells, ncells, ainv6, bdiv, coarse, prep, edge_patch);
   return cudaGetLastError();
 }
 

@@ -26,6 +26,7 @@
 // sigma of an edge basis, u of a face basis) for the Galerkin product of
 // NedRTBasis::assemble_global_element_matrix (ned_rt_basis.cc:849-948).
 #pragma once
+#include <cuda_fp16.h>
 #include "../../include/msfec_cuda.h"
 #include "nedrt_common.cuh"
 
@@ -750,6 +751,28 @@ __device__ __forceinline__ T ml_coarse(NRShared &sh, const NRGeom &g, const T *v
 
 extern __shared__ __align__(256) unsigned char nr_dyn_smem[];
 
+// Edge l (direction p = l / 4, position l4 = l % 4, as in cell_dofs) of fine
+// cell (ci, cj, ck) as its grid line: direction p through lattice point
+// (x, y, z), i.e. the edge from (x, y, z) to (x, y, z) + unit_p.
+__device__ __forceinline__ void nr_edge_line(int l, int ci, int cj, int ck, int &x, int &y, int &z) {
+  const int p = l >> 2, a = l & 1, b = (l >> 1) & 1;
+  x = ci + (p == 0 ? 0 : a);
+  y = cj + (p == 1 ? 0 : (p == 0 ? a : b));
+  z = ck + (p == 2 ? 0 : b);
+}
+// Position (0..3) of the grid line (p, x, y, z) among fine cell (ci, cj, ck)'s
+// edges of direction p, or -1 when the cell does not have it.
+__device__ __forceinline__ int nr_edge_pos_in(int p, int x, int y, int z, int ci, int cj, int ck) {
+  const int dx = x - ci, dy = y - cj, dz = z - ck;
+  if (p == 0) return (dx == 0 && (dy | dz) >= 0 && dy <= 1 && dz <= 1) ? dy + 2 * dz : -1;
+  if (p == 1) return (dy == 0 && (dx | dz) >= 0 && dx <= 1 && dz <= 1) ? dx + 2 * dz : -1;
+  return (dz == 0 && (dx | dy) >= 0 && dx <= 1 && dy <= 1) ? dx + 2 * dy : -1;
+}
+// A^-1_pq from a cell's float coefficients (a00 a11 a22 a01 a02 a12).
+__device__ __forceinline__ float nr_ainv_pq(const float *a, int p, int q) {
+  return p == q ? a[p] : a[p + q + 2];  // (0,1) -> 3, (0,2) -> 4, (1,2) -> 5
+}
+
 // Block-Jacobi part of the preconditioner of one cell into pd[0, Np): diag(M)^-1
 // on the edges and, on the faces, the inverse of the lumped Schur diagonal
 // D_ff + sum_l C_lf^2 / M_ll (cell-local approximation) or, where the
@@ -962,6 +985,50 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
     __syncthreads();
   }
 
+  // ---- cell-patch edge preconditioner (shared per-cell data, multilevel items):
+  // z_E += sum_c R_c^T X_c R_c v over the fine cells, X_c = L_c^-T L_c^-1 the
+  // inverse of the assembled edge mass restricted to cell c's edges (M_c =
+  // L_c L_c^T, Dirichlet edges decoupled; v is zero on them), L_c^-1 stored in
+  // FP16 pairs, row-packed lower triangle, word t of cell c at pX[t * nc + c].
+  // Per cell t = L^-1 v_c, z += L^-T t; returns this thread's share of
+  // v_E^T z_E = sum_c |t|^2.
+  const bool epatch = prep && prm.edge_patch && ml;
+  const __half2 *pX =
+      prep ? reinterpret_cast<const __half2 *>(prm.prep + Cc.prep_off + nr_prep_patch_offset(n)) : nullptr;
+  auto patch_pass = [&](const T *vsrc) -> T {
+    T qf = T(0);
+    for (int c = tid; c < nc; c += NT) {
+      int e[12], f[6];
+      cell_dofs(g, c, e, f);
+      float L[78];
+#pragma unroll
+      for (int w = 0; w < 39; ++w) {
+        const float2 p2 = __half22float2(pX[(size_t)w * nc + c]);
+        L[2 * w] = p2.x;
+        L[2 * w + 1] = p2.y;
+      }
+      T vl[12], tl[12];
+#pragma unroll
+      for (int l = 0; l < 12; ++l) vl[l] = vsrc[e[l]];
+#pragma unroll
+      for (int l = 0; l < 12; ++l) {
+        T a = T(0);
+#pragma unroll
+        for (int m = 0; m <= l; ++m) a += (T)L[l * (l + 1) / 2 + m] * vl[m];
+        tl[l] = a;
+        qf += a * a;
+      }
+#pragma unroll
+      for (int m = 0; m < 12; ++m) {
+        T a = T(0);
+#pragma unroll
+        for (int l = m; l < 12; ++l) a += (T)L[l * (l + 1) / 2 + m] * tl[l];
+        atomicAdd(zt + e[m], a);
+      }
+    }
+    return qf;
+  };
+
   double bnorm2 = 0.0, rnorm2 = 0.0;
   int conv = 0, its = 0, flags = 0, nref = 0;
   static_assert(!STAGE || (sizeof(T) == 4 && !SMEM && NT == 512), "staged apply: mixed, global workspace");
@@ -1145,12 +1212,16 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
       {
         T p1[1] = {T(0)};
         for (int d = tid; d < (int)Np; d += NT) {
-          const T z = (T)pd[d] * vc[d];
+          const T z = (epatch && d < g.NE) ? T(0) : (T)pd[d] * vc[d];  // patch edges: accumulated below
           zt[d] = z;
           p1[0] += z * vc[d];
         }
+        if (epatch) {
+          __syncthreads();
+          p1[0] += patch_pass(vc);
+        }
         T t1[1];
-        block_sum<T, 1, NW>(sh, p1, t1);  // its barriers also complete vc
+        block_sum<T, 1, NW>(sh, p1, t1);  // its barriers also complete vc and the patch atomics
         const T gc = ml_coarse<T, NW>(sh, g, vc, ml_rr, ml_y, ml_wk, ml_dat, ml_lcodes);
         gam = sqrt(fmax(t1[0] + gc, T(0)));
         for (int d = g.NE + tid; d < N; d += NT) zt[d] += ml_code_prolong(ml_codes[d - g.NE], ml_y, m2);
@@ -1192,7 +1263,62 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
         const T delta = slot_total<T, NW>(sh, 0) * gi_c * gi_c;
         // ---- phase 2: v~_{j+1} = (S B - delta~ v~_j) / g_j in place of B
         T gpart = T(0);
-        if constexpr (kMixed) {  // 4 DoFs per access; face quads start at NE (NE % 4 == 0 for n >= 4)
+        const T a2 = ss * delta + c_prev * cc * gam;
+        const T a3 = s_prev * gam;
+        if (epatch) {
+          // with the patch edge block z~_{j+1} needs a cell pass, so z~_j is
+          // consumed here: the direction w_j = (z~_j / g_j - a3 w_{j-2} - a2 w_{j-1}) / a1
+          // is formed up to its 1 / a1 (which needs gamma_{j+1}) in w_{j-2}'s slot,
+          // and zt takes the face part of z~_{j+1} (edges 0, accumulated by the pass)
+          if constexpr (kMixed) {
+            const float4 *pd4 = reinterpret_cast<const float4 *>(pd);
+            const float4 *vc4 = reinterpret_cast<const float4 *>(vc);
+            float4 *vp4 = reinterpret_cast<float4 *>(vp);
+            float4 *zt4 = reinterpret_cast<float4 *>(zt);
+            float4 *wo4 = reinterpret_cast<float4 *>(wo);
+            const float4 *wc4 = reinterpret_cast<const float4 *>(wc);
+            for (int q = tid; q < (int)(Np / 4); q += NT) {
+              const float4 pv = pd4[q], b = vp4[q], c = vc4[q], z = zt4[q], a = wo4[q], bw = wc4[q];
+              const bool face = 4 * q >= g.NE;
+              const float sg = face ? -1.0f : 1.0f;
+              auto lane = [&](float pdd, float bd, float cd) {
+                return pdd > 0.0f ? (sg * bd - delta * cd) * gi_c : 0.0f;
+              };
+              float4 vn, wt, nz = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+              vn.x = lane(pv.x, b.x, c.x);
+              vn.y = lane(pv.y, b.y, c.y);
+              vn.z = lane(pv.z, b.z, c.z);
+              vn.w = lane(pv.w, b.w, c.w);
+              wt.x = z.x * gi_c - a3 * a.x - a2 * bw.x;
+              wt.y = z.y * gi_c - a3 * a.y - a2 * bw.y;
+              wt.z = z.z * gi_c - a3 * a.z - a2 * bw.z;
+              wt.w = z.w * gi_c - a3 * a.w - a2 * bw.w;
+              if (face) {
+                nz = make_float4(pv.x * vn.x, pv.y * vn.y, pv.z * vn.z, pv.w * vn.w);
+                gpart += nz.x * vn.x + nz.y * vn.y + nz.z * vn.z + nz.w * vn.w;
+              }
+              vp4[q] = vn;
+              wo4[q] = wt;
+              zt4[q] = nz;
+            }
+          } else {
+            for (int d = tid; d < (int)Np; d += NT) {
+              const float pdd = pd[d];
+              T vn = T(0);
+              if (pdd > 0.0f) {
+                const T b = d < g.NE ? vp[d] : -vp[d];
+                vn = (b - delta * vc[d]) * gi_c;
+              }
+              vp[d] = vn;
+              wo[d] = zt[d] * gi_c - a3 * wo[d] - a2 * wc[d];
+              const T nz = d < g.NE ? T(0) : (T)pdd * vn;
+              zt[d] = nz;
+              gpart += nz * vn;
+            }
+          }
+          __syncthreads();
+          gpart += patch_pass(vp);
+        } else if constexpr (kMixed) {  // 4 DoFs per access; face quads start at NE (NE % 4 == 0 for n >= 4)
           const float4 *pd4 = reinterpret_cast<const float4 *>(pd);
           const float4 *vc4 = reinterpret_cast<const float4 *>(vc);
           float4 *vp4 = reinterpret_cast<float4 *>(vp);
@@ -1229,8 +1355,6 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
         const T gnew = sqrt(fmax(slot_total<T, NW>(sh, 1) + gc, T(0)));
         const T a0 = cc * delta - c_prev * ss * gam;
         const T a1 = sqrt(a0 * a0 + gnew * gnew);
-        const T a2 = ss * delta + c_prev * cc * gam;
-        const T a3 = s_prev * gam;
         if (!(a1 > T(0)) || !isfinite(a1)) {
           flags |= 1;
           break;
@@ -1239,7 +1363,48 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
         const T step = cn * eta, ia1 = T(1) / a1;
         // ---- phase 3 (pre: the prefill scale gamma_{j+1}^2 / g_j of v~_j's slot)
         const T pre = gnew * gnew * gi_c;
-        if constexpr (kMixed) {
+        if (epatch) {  // w_j = w~ / a1, x += c eta w_j, faces of z~_{j+1} += P_{n/2} y, prefill
+          if constexpr (kMixed) {
+            float4 *vc4 = reinterpret_cast<float4 *>(vc);
+            float4 *zt4 = reinterpret_cast<float4 *>(zt);
+            float4 *wo4 = reinterpret_cast<float4 *>(wo);
+            float4 *xk4 = reinterpret_cast<float4 *>(xk);
+            for (int q = tid; q < (int)(Np / 4); q += NT) {
+              const float4 a = wo4[q], vo = vc4[q];
+              float4 x = xk4[q], wn;
+              wn.x = a.x * ia1;
+              wn.y = a.y * ia1;
+              wn.z = a.z * ia1;
+              wn.w = a.w * ia1;
+              x.x += step * wn.x;
+              x.y += step * wn.y;
+              x.z += step * wn.z;
+              x.w += step * wn.w;
+              const bool face = 4 * q >= g.NE;
+              if (face) {
+                float4 nz = zt4[q];
+                const uint2 cw = reinterpret_cast<const uint2 *>(ml_codes)[q - g.NE / 4];
+                nz.x += ml_code_prolong(cw.x & 0xFFFFu, (const float *)ml_y, m2);
+                nz.y += ml_code_prolong(cw.x >> 16, (const float *)ml_y, m2);
+                nz.z += ml_code_prolong(cw.y & 0xFFFFu, (const float *)ml_y, m2);
+                nz.w += ml_code_prolong(cw.y >> 16, (const float *)ml_y, m2);
+                zt4[q] = nz;
+              }
+              const float ps = face ? (float)pre : -(float)pre;  // -S pre
+              wo4[q] = wn;
+              xk4[q] = x;
+              vc4[q] = make_float4(ps * vo.x, ps * vo.y, ps * vo.z, ps * vo.w);
+            }
+          } else {
+            for (int d = tid; d < (int)Np; d += NT) {
+              const T wn = wo[d] * ia1;
+              wo[d] = wn;
+              xk[d] += step * wn;
+              if (d >= g.NE) zt[d] += ml_code_prolong(ml_codes[d - g.NE], ml_y, m2);
+              vc[d] = (d < g.NE ? -pre : pre) * vc[d];
+            }
+          }
+        } else if constexpr (kMixed) {
           const float4 *pd4 = reinterpret_cast<const float4 *>(pd);
           const float4 *vp4 = reinterpret_cast<const float4 *>(vp);
           float4 *vc4 = reinterpret_cast<float4 *>(vc);

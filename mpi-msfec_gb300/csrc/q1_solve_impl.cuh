@@ -235,6 +235,17 @@ __device__ __forceinline__ void column_apply_f64(const double *__restrict__ ps, 
   }
 }
 
+// The FP64 refinement residual as a call: it runs once per refinement step,
+// and out of line it gets its own register allocation instead of raising
+// the pressure (and the spills) of the FP32 Krylov loop in the same kernel.
+template <int R, int PMAX, bool HAS_R>
+__device__ __noinline__ void column_residual_f64(const double *__restrict__ vs, const double *__restrict__ ag,
+                                                 const double *__restrict__ rg, int n, int rho, int i, int j, int P,
+                                                 const double (&c)[8], const double (&mm)[8], double (&q)[PMAX],
+                                                 double (&ctr)[PMAX]) {
+  column_apply_f64<R, PMAX, HAS_R>(vs, ag, rg, n, rho, i, j, P, c, mm, q, ctr);
+}
+
 // Residual-pass apply at one node for all R right-hand sides: y = K v, and
 // (BND) yb = the part of K v coming from lattice-boundary neighbours (K_IB g
 // when v carries the Dirichlet data). GUARD: lattice-boundary node, the
@@ -492,12 +503,6 @@ __device__ void solve_item(const Q1Params &prm, Q1Shared &sh, unsigned char *sme
     }
   };
 
-  T r[UMAX][PMAX], q[UMAX][PMAX];
-#pragma unroll
-  for (int s = 0; s < UMAX; ++s)
-#pragma unroll
-    for (int pk = 0; pk < PMAX; ++pk) r[s][pk] = q[s][pk] = T(0);
-
   // State of this thread's rhs.
   double bnorm2 = 0.0, rnorm2 = 0.0;
   int conv = 0, its = 0, flags = 0, nref = 0;
@@ -524,7 +529,7 @@ __device__ void solve_item(const Q1Params &prm, Q1Shared &sh, unsigned char *sme
         for (int s = 0; s < UMAX; ++s) {
           if (!cval[s]) continue;
           double q[PMAX], ctr[PMAX];
-          column_apply_f64<R, PMAX, HAS_R>(slab_d, ag, rg, n, rho, ci[s], cj[s], P, cd, mmd, q, ctr);
+          column_residual_f64<R, PMAX, HAS_R>(slab_d, ag, rg, n, rho, ci[s], cj[s], P, cd, mmd, q, ctr);
 #pragma unroll
           for (int pk = 0; pk < PMAX; ++pk)
             if (pk < P) {
@@ -601,12 +606,17 @@ __device__ void solve_item(const Q1Params &prm, Q1Shared &sh, unsigned char *sme
     const double target2 = kMixed ? fmax(prm.inner_rtol * prm.inner_rtol * rnorm2, 0.01 * tol_abs2) : 0.25 * tol_abs2;
     bool active = !conv && (rnorm2 > target2);
     const T target2t = (T)target2;
-    // r into registers; x = p = s = 0; u-slab = 0 (boundary and halo planes stay zero)
+    // r into registers (K u of the iteration in q); x = p = s = 0; u-slab = 0
+    // (boundary and halo planes stay zero). Scoped to this phase, so that
+    // nothing stays live across the FP64 residual phase (fewer spills).
+    T r[UMAX][PMAX], q[UMAX][PMAX];
 #pragma unroll
     for (int s = 0; s < UMAX; ++s)
 #pragma unroll
-      for (int pk = 0; pk < PMAX; ++pk)
-        if (cval[s] && pk < P) r[s][pk] = xs[own_idx(s, pk) * R + rho];
+      for (int pk = 0; pk < PMAX; ++pk) {
+        r[s][pk] = (cval[s] && pk < P) ? xs[own_idx(s, pk) * R + rho] : T(0);
+        q[s][pk] = T(0);
+      }
     __syncthreads();
     for (size_t e = tid; e < own_nodes * R; e += kQ1Threads) xs[e] = ps[e] = ss[e] = T(0);
     for (size_t e = tid; e < slab_nodes * R; e += kQ1Threads) slab_t[e] = T(0);
@@ -792,7 +802,10 @@ __device__ void solve_item(const Q1Params &prm, Q1Shared &sh, unsigned char *sme
 // CTA x 2 rhs (15-node columns); depth 5 z-slabs of 4 planes x 1 rhs.
 // FP64: depth <= 3 one CTA x 8 rhs; depth 4 z-slabs (2 planes) x 2 rhs;
 // depth 5 z-slabs of 4 planes x 1 rhs.
-template <typename T, int CL, bool HAS_R>
+// SLAB_ONLY (cluster launches that carry only slab units, e.g. the cluster
+// half of a split launch): the independent-item paths are compiled out, so
+// the register allocation is the slab path's alone (fewer spills).
+template <typename T, int CL, bool HAS_R, bool SLAB_ONLY = false>
 __global__ void __launch_bounds__(kQ1Threads, 1) q1_solve_kernel(Q1Params prm) {
   extern __shared__ __align__(256) unsigned char smem[];
   __shared__ Q1Shared sh;
@@ -821,7 +834,7 @@ __global__ void __launch_bounds__(kQ1Threads, 1) q1_solve_kernel(Q1Params prm) {
           if (depth == 4) solve_item<T, 2, 1, 2, HAS_R, true>(prm, sh, smem, U.first_item, rank, CL);
         }
       }
-    } else if (rank < U.n_items) {
+    } else if (!SLAB_ONLY && rank < U.n_items) {
       const int item = U.first_item + rank;
       const int depth = prm.cells[prm.items[item].cell].depth;
       switch (depth) {
@@ -843,9 +856,9 @@ __global__ void __launch_bounds__(kQ1Threads, 1) q1_solve_kernel(Q1Params prm) {
   }
 }
 
-template <typename T, int CL, bool HAS_R>
+template <typename T, int CL, bool HAS_R, bool SLAB_ONLY = false>
 cudaError_t launch(const Q1Params &prm, size_t smem_bytes, int grid, cudaStream_t stream) {
-  auto kern = q1_solve_kernel<T, CL, HAS_R>;
+  auto kern = q1_solve_kernel<T, CL, HAS_R, SLAB_ONLY>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
   if (e != cudaSuccess) return e;
   cudaLaunchConfig_t cfg = {};
@@ -863,9 +876,9 @@ cudaError_t launch(const Q1Params &prm, size_t smem_bytes, int grid, cudaStream_
   return cudaLaunchKernelEx(&cfg, kern, prm);
 }
 
-template <typename T, int CL, bool HAS_R>
+template <typename T, int CL, bool HAS_R, bool SLAB_ONLY = false>
 cudaError_t occupancy(size_t smem_bytes, int *out) {
-  auto kern = q1_solve_kernel<T, CL, HAS_R>;
+  auto kern = q1_solve_kernel<T, CL, HAS_R, SLAB_ONLY>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
   if (e != cudaSuccess) return e;
   if (CL == 1) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, kern, kQ1Threads, smem_bytes);

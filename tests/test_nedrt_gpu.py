@@ -207,3 +207,30 @@ def test_two_ctas_per_sm_global_workspace_match_one(gpu):
         assert _rel(out[2][1][c], out[1][1][c]) <= 1e-11, c
     assert np.abs(out[2][3] - out[1][3]).max() <= 1e-10 * np.abs(out[1][3]).max()
     print(f"2 CTAs/SM: iterations {out[2][2]['iterations'].max()} (1 CTA/SM {out[1][2]['iterations'].max()})")
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_patch_edge_preconditioner_matches_diagonal_edges(gpu, precision):
+    """Cells with a global MINRES workspace (depth 4 in the batch, or the FP64
+    path at depth 3): the cell-patch edge preconditioner (nedrt_precond 0, the
+    default) and diag(M)^-1 on the edges (nedrt_precond 2) give the same K_H,
+    F_H and basis, on depths 4, 3, 2, 1, and the patch version needs fewer
+    MINRES iterations on the deepest cell."""
+    parts = [workloads.nedrt_tensor(m=1, depth=d, seed=60 + d) for d in (4, 3, 2, 1)]
+    cells = np.concatenate([p[0] for p in parts])
+    ainv6 = np.concatenate([p[1] for p in parts])
+    bdiv = np.concatenate([p[2] for p in parts])
+    load = parts[0][3]
+    out = {}
+    for pc in (2, 0):
+        h = _handle(gpu, precision, nedrt_precond=pc)
+        KH, FH, rep, status = h.nedrt_build(cells, ainv6, bdiv, load)
+        assert status == gpu.SUCCESS and rep["converged"].all(), (pc, rep)
+        out[pc] = (KH, FH, rep, h.nedrt_basis())
+    for c in range(len(cells)):
+        assert _rel(out[0][0][c], out[2][0][c]) <= 1e-11, c
+        assert _rel(out[0][1][c], out[2][1][c]) <= 1e-11, c
+    assert np.abs(out[0][3] - out[2][3]).max() <= 1e-10 * np.abs(out[2][3]).max()
+    it0, it2 = out[0][2]["iterations_sum"][0], out[2][2]["iterations_sum"][0]
+    print(f"{precision} patch edge block: depth-4 iterations {it0} (diagonal edges {it2})")
+    assert it0 < it2

@@ -110,13 +110,14 @@ def _high_contrast(ncells, depth, seed, sigma=2.0):
 
 
 def test_noalloc_high_contrast_depth4_converges(gpu):
-    """Three depth-4 cells at contrast e^+-6: the multilevel preconditioner
-    (same as the device build) converges, iteration counts close to the device
-    build's, K_H within the tolerance."""
+    """Three depth-4 cells at contrast e^+-6: the multilevel face
+    preconditioner converges, iteration counts close to the device build's
+    with the same preconditioner (diagonal edge block: nedrt_precond 2), K_H
+    within the tolerance."""
     import torch
     cells, ainv6, bdiv, load = _high_contrast(3, 4, seed=11)
     n = len(cells)
-    h = gpu.Handle(precision=gpu.PRECISION_MIXED)
+    h = gpu.Handle(precision=gpu.PRECISION_MIXED, nedrt_precond=2)
     h.set_stream(torch.cuda.current_stream().cuda_stream)
     d_a, d_b = _device_inputs(ainv6, bdiv)
     ref_out, out = _outputs(n), _outputs(n)
