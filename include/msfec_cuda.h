@@ -103,9 +103,9 @@ typedef struct msfec_config {
   /* Preconditioner of the Ned_RT local solver:
      0 = face (Schur) block multilevel (diagonal + coarse RT levels n/2 .. 4 +
          exact level 2); edge block, for cells whose MINRES workspace is in
-         global memory (depth 4, or the FP64 path), the additive Schwarz
-         operator over fine-cell patches (the inverse of the edge mass on each
-         fine cell's 12 edges), else diag(M)^-1;
+         global memory (depth 4, or the FP64 path at depth 3), the additive
+         Schwarz operator over fine-cell patches (the inverse of the assembled
+         edge mass on each fine cell's 12 edges), else diag(M)^-1;
      1 = diagonal only (both blocks);
      2 = multilevel face block, diagonal edge block. */
   int32_t nedrt_precond;

@@ -1084,10 +1084,15 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
   ml = shape.ml;
   if (!ml)
     for (auto &q : hc) q.coarse_off = -1;
+  // per-cell data of a global workspace (shape.prep): the shared
+  // preconditioner + coefficients and, with the multilevel preconditioner
+  // (nedrt_precond 0), the cell-patch edge factors
+  const bool edge_patch = shape.prep && ml && h->cfg.nedrt_precond == 0;
+  const bool cell_data = shape.prep;
   int64_t prep_floats = 0;
   for (auto &q : hc) {
-    q.prep_off = shape.prep ? prep_floats : -1;
-    if (shape.prep) prep_floats += (int64_t)nr_prep_floats(q.n);
+    q.prep_off = cell_data ? prep_floats : -1;
+    if (cell_data) prep_floats += (int64_t)nr_prep_floats(q.n);
   }
   cudaStream_t st = h->stream;
   MSFEC_CUDA_TRY(h, h->nr_cells.reserve(ncells));
@@ -1105,7 +1110,7 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
     MSFEC_CUDA_TRY(h, h->nr_coarse.reserve((size_t)coarse_floats));
     MSFEC_CUDA_TRY(h, h->nr_mlscratch.reserve(ml_scratch * ml_grid));
   }
-  if (shape.prep) MSFEC_CUDA_TRY(h, h->nr_prep.reserve((size_t)prep_floats));
+  if (cell_data) MSFEC_CUDA_TRY(h, h->nr_prep.reserve((size_t)prep_floats));
   MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->nr_cells.ptr, hc.data(), hc.size() * sizeof(NRCell), cudaMemcpyHostToDevice, st));
   MSFEC_CUDA_TRY(h, cudaMemcpyAsync(h->nr_items.ptr, items.data(), items.size() * sizeof(NRItem),
                                     cudaMemcpyHostToDevice, st));
@@ -1127,8 +1132,8 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
   prm.max_iter = std::max(h->cfg.max_iter, 8000);  // per refinement step (MINRES, kappa ~ 1e4)
   prm.max_refine = h->cfg.max_refine;
   prm.coarse = ml ? h->nr_coarse.ptr : nullptr;
-  prm.prep = shape.prep ? h->nr_prep.ptr : nullptr;
-  prm.edge_patch = (shape.prep && ml && h->cfg.nedrt_precond == 0) ? 1 : 0;
+  prm.prep = cell_data ? h->nr_prep.ptr : nullptr;
+  prm.edge_patch = edge_patch ? 1 : 0;
   prm.ml_offset = ml_offset;
   prm.stage = shape.stage ? 1 : 0;
   prm.stage_offset = shape.stage_offset;
@@ -1149,10 +1154,10 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
     if (e == cudaSuccess && ml)
       e = nedrt_ml_setup_launch(h->nr_cells.ptr, ncells, d_ainv, d_bdiv, h->nr_coarse.ptr, h->nr_mlscratch.ptr,
                                 ml_scratch, (size_t)nr_ml_data_floats(nmax) * 4, ml_grid, st);
-    if (e == cudaSuccess && shape.prep)
+    if (e == cudaSuccess && cell_data)
       e = nedrt_cell_prep_launch(h->nr_cells.ptr, ncells, d_ainv, d_bdiv, ml ? h->nr_coarse.ptr : nullptr,
                                  h->nr_prep.ptr, prm.edge_patch, std::min(ncells, h->num_sms), st);
-    if (e == cudaSuccess && timed && (ml || shape.prep)) {
+    if (e == cudaSuccess && timed && (ml || cell_data)) {
       e = cudaEventRecord(h->ev[4], st);
       h->ev_setup = true;
     }
@@ -1168,7 +1173,7 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
     return e;
   };
   const msfec_status s =
-      run_sequence(h, h->nr_graph, std::move(key), (d_rep ? 3 : 2) + (ml ? 1 : 0) + (shape.prep ? 1 : 0), seq);
+      run_sequence(h, h->nr_graph, std::move(key), (d_rep ? 3 : 2) + (ml ? 1 : 0) + (cell_data ? 1 : 0), seq);
   if (s != MSFEC_SUCCESS) return s;
   h->nr_ml_valid = ml;
   h->nr_graph_basis = dofs * 18;

@@ -992,39 +992,41 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
   // FP16 pairs, row-packed lower triangle, word t of cell c at pX[t * nc + c].
   // Per cell t = L^-1 v_c, z += L^-T t; returns this thread's share of
   // v_E^T z_E = sum_c |t|^2.
-  const bool epatch = prep && prm.edge_patch && ml;
-  const __half2 *pX =
-      prep ? reinterpret_cast<const __half2 *>(prm.prep + Cc.prep_off + nr_prep_patch_offset(n)) : nullptr;
+  // Global-workspace items only: compiled out of the shared-memory variants,
+  // where the extra pass cost about what the fewer iterations saved (depth 3,
+  // 512 cells: 190 ms with it, 189 ms without) and its code slowed the rest.
+  const bool epatch = !SMEM && prm.prep != nullptr && prm.edge_patch && ml;
+  const __half2 *pX = epatch ? reinterpret_cast<const __half2 *>(prm.prep + Cc.prep_off + nr_prep_patch_offset(n))
+                             : nullptr;
   auto patch_pass = [&](const T *vsrc) -> T {
     T qf = T(0);
     for (int c = tid; c < nc; c += NT) {
       int e[12], f[6];
       cell_dofs(g, c, e, f);
-      float L[78];
+      __half2 Lw[39];  // kept packed: half the registers of the unpacked factor
 #pragma unroll
-      for (int w = 0; w < 39; ++w) {
-        const float2 p2 = __half22float2(pX[(size_t)w * nc + c]);
-        L[2 * w] = p2.x;
-        L[2 * w + 1] = p2.y;
+      for (int w = 0; w < 39; ++w) Lw[w] = pX[(size_t)w * nc + c];
+      auto Lv = [&](int idx) -> T {
+        return (T)((idx & 1) ? __high2float(Lw[idx >> 1]) : __low2float(Lw[idx >> 1]));
+      };
+      T vl[12], y[12];
+#pragma unroll
+      for (int l = 0; l < 12; ++l) {
+        vl[l] = vsrc[e[l]];
+        y[l] = T(0);
       }
-      T vl[12], tl[12];
-#pragma unroll
-      for (int l = 0; l < 12; ++l) vl[l] = vsrc[e[l]];
+      // row l of L^-1 gives t_l, then at once its share t_l L^-1_lm of (L^-T t)_m
 #pragma unroll
       for (int l = 0; l < 12; ++l) {
         T a = T(0);
 #pragma unroll
-        for (int m = 0; m <= l; ++m) a += (T)L[l * (l + 1) / 2 + m] * vl[m];
-        tl[l] = a;
+        for (int m = 0; m <= l; ++m) a += Lv(l * (l + 1) / 2 + m) * vl[m];
         qf += a * a;
+#pragma unroll
+        for (int m = 0; m <= l; ++m) y[m] += Lv(l * (l + 1) / 2 + m) * a;
       }
 #pragma unroll
-      for (int m = 0; m < 12; ++m) {
-        T a = T(0);
-#pragma unroll
-        for (int l = m; l < 12; ++l) a += (T)L[l * (l + 1) / 2 + m] * tl[l];
-        atomicAdd(zt + e[m], a);
-      }
+      for (int m = 0; m < 12; ++m) atomicAdd(zt + e[m], y[m]);
     }
     return qf;
   };
