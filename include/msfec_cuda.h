@@ -376,11 +376,14 @@ msfec_status msfec_nedrt_build_device(msfec_handle *handle, int32_t ncells,
  * callers that must not allocate device memory while they build: a solver
  * whose pooling allocator already holds nearly all of HBM, or a rank whose
  * other streams must not be stalled by the device-wide synchronisation of
- * cudaMalloc / cudaFree. Same arguments, asynchrony, launch shape and
- * preconditioner as msfec_nedrt_build_device on the same handle (the
- * multilevel face preconditioner for depth >= 2 unless nedrt_precond = 1, the
- * autotuned split / CTA choices), hence the same K_H, F_H and reports up to
- * the last bits of the shared-memory atomic sums; but every internal buffer
+ * cudaMalloc / cudaFree. Same arguments, asynchrony and launch shape as
+ * msfec_nedrt_build_device on the same handle (the autotuned split / CTA
+ * choices) and the same face preconditioner (multilevel for depth >= 2 unless
+ * nedrt_precond = 1); the edge block is diag(M)^-1 throughout (the handle's
+ * build uses the cell-patch edge block on cells with a global workspace), so
+ * K_H, F_H agree with that build within the solver tolerance, and with a
+ * build at nedrt_precond = 2 up to the last bits of the shared-memory atomic
+ * sums; but every internal buffer
  * comes from one static device pool of 32 MiB per device that is part of the
  * library image; nothing is allocated on the device (host memory only to
  * format an error message). A batch whose cell table, multilevel data, basis

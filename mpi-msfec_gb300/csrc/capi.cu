@@ -386,6 +386,7 @@ struct Q1Plan {
   // split: slab units (units[0, n_slab_units)) run in the cluster kernel,
   // the independent single-item units after them in a non-cluster kernel
   bool split = false;
+  bool all_slab = false;  // every item is a z-slab item (e.g. only depth-5 cells)
   int n_slab_units = 0;
   size_t smem_slab = 0, smem_indep = 0;
   int64_t nodes = 0;   // sum (n+1)^3
@@ -445,6 +446,7 @@ Q1Plan make_q1_plan(int ncells, const msfec_cell *cells, bool fp64, bool has_r, 
   bool any_indep = false;
   for (const Q1Item &it : p.items) any_indep = any_indep || !it.slab;
   p.split = split && any_slab && any_indep;
+  p.all_slab = any_slab && !any_indep;
   // units: slab items alone; independent items grouped by `cluster` (same
   // depth), or one per unit for the non-cluster kernel of a split launch.
   // Slab items come first (deepest first), so slab units precede the rest.
@@ -682,7 +684,9 @@ msfec_status q1_build_impl(msfec_handle *h, int ncells, const msfec_cell *cells,
     smem_a = plan.smem_slab;
   }
   int occ = 0;
-  MSFEC_CUDA_TRY(h, q1_solve_occupancy(fp64, cluster_a, has_r, smem_a, &occ, plan.split));
+  // the cluster kernel without the independent-item paths when it runs only slab units
+  const bool slab_only = plan.split || plan.all_slab;
+  MSFEC_CUDA_TRY(h, q1_solve_occupancy(fp64, cluster_a, has_r, smem_a, &occ, slab_only));
   if (occ <= 0) return fail(h, MSFEC_ERROR_NOT_SUPPORTED, "local solver kernel cannot be resident");
   int grid;
   if (cluster_a > 1) {
@@ -721,7 +725,7 @@ msfec_status q1_build_impl(msfec_handle *h, int ncells, const msfec_cell *cells,
       if (e == cudaSuccess) e = cudaEventRecord(h->ev_join, h->aux_stream);
       if (e == cudaSuccess) e = cudaStreamWaitEvent(st, h->ev_join, 0);
     } else if (e == cudaSuccess) {
-      e = q1_solve_launch(fp64, cluster_a, has_r, prm, smem_a, grid, st);
+      e = q1_solve_launch(fp64, cluster_a, has_r, prm, smem_a, grid, st, slab_only);
     }
     if (e == cudaSuccess && timed) e = cudaEventRecord(h->ev[1], st);
     if (e == cudaSuccess) e = q1_galerkin_launch(h->cells.ptr, ncells, h->phi.ptr, h->y.ptr, ld, d_KH, d_FH, st);
@@ -917,13 +921,15 @@ msfec_status q1_backward_impl(msfec_handle *h, int ncells, const msfec_cell *cel
   prm.max_iter = h->cfg.max_iter;
   prm.max_refine = h->cfg.max_refine;
   int occ = 0;
-  MSFEC_CUDA_TRY(h, q1_solve_occupancy(fp64, plan.cluster, has_r, plan.smem, &occ));
+  bool only_slabs = plan.cluster > 1;  // the slab-only cluster kernel when every item is a slab
+  for (const Q1Item &q : items) only_slabs = only_slabs && q.slab;
+  MSFEC_CUDA_TRY(h, q1_solve_occupancy(fp64, plan.cluster, has_r, plan.smem, &occ, only_slabs));
   if (occ <= 0) return fail(h, MSFEC_ERROR_NOT_SUPPORTED, "local solver kernel cannot be resident");
   int grid = plan.cluster > 1 ? std::min<int>((int)units.size(), occ) * plan.cluster
                               : std::min<int>((int)units.size(), occ * h->num_sms);
   grid = std::max(grid, plan.cluster);
   if (h->timing) MSFEC_CUDA_TRY(h, record_start(h, st));
-  MSFEC_CUDA_TRY(h, q1_solve_launch(fp64, plan.cluster, has_r, prm, plan.smem, grid, st));
+  MSFEC_CUDA_TRY(h, q1_solve_launch(fp64, plan.cluster, has_r, prm, plan.smem, grid, st, only_slabs));
   if (h->timing) MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[1], st));
   MSFEC_CUDA_TRY(h, q1_gradient_launch(h->cells.ptr, ncells, d_a, h->phi.ptr, h->adj_sol.ptr, d_U, d_lam, d_grad, st));
   if (h->timing) {
@@ -1911,11 +1917,13 @@ msfec_status msfec_q1_fine_solve(msfec_handle *h, const msfec_cell *domain, cons
   prm.max_iter = h->cfg.max_iter;
   prm.max_refine = h->cfg.max_refine;
   int occ = 0;
-  MSFEC_CUDA_TRY(h, q1_solve_occupancy(fp64, plan.cluster, has_r, plan.smem, &occ));
+  bool only_slabs = plan.cluster > 1;  // the slab-only cluster kernel when every item is a slab
+  for (const Q1Item &q : items) only_slabs = only_slabs && q.slab;
+  MSFEC_CUDA_TRY(h, q1_solve_occupancy(fp64, plan.cluster, has_r, plan.smem, &occ, only_slabs));
   if (occ <= 0) return fail(h, MSFEC_ERROR_NOT_SUPPORTED, "local solver kernel cannot be resident");
   const int grid = plan.cluster;  // one item: one CTA, or one cluster for a slab item
   if (h->timing) MSFEC_CUDA_TRY(h, record_start(h, st));
-  MSFEC_CUDA_TRY(h, q1_solve_launch(fp64, plan.cluster, has_r, prm, plan.smem, grid, st));
+  MSFEC_CUDA_TRY(h, q1_solve_launch(fp64, plan.cluster, has_r, prm, plan.smem, grid, st, only_slabs));
   if (h->timing) {
     MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[1], st));
     MSFEC_CUDA_TRY(h, cudaEventRecord(h->ev[2], st));
