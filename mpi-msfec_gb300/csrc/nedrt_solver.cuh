@@ -437,6 +437,51 @@ __device__ __forceinline__ TA cell_apply_s(const TV *__restrict__ z, TO *out, co
 
 // Warp-reduce v and store the warp's partial in slot set `slot`; the block
 // total is read with slot_total after the next __syncthreads.
+// Accumulate a cell's 12 edge contributions y into out with the apply's warp
+// merge (full warps of complete x-rows, n >= 4): the 4 edges on the plane
+// x = i are summed with the left neighbour's right-plane values by a shuffle,
+// then the x-edges and the z-edge of the plane y = j with the row below's
+// top values; each shared edge is written once per warp. ~6.5 atomics per
+// cell instead of 12.
+template <typename TA, typename TO>
+__device__ __forceinline__ void edge_scatter_merged(TO *out, const TA (&y)[12], const int (&e)[12], int c, int L) {
+  const int n = 1 << L, lane = threadIdx.x & 31;
+  const int i = c & (n - 1), j = (c >> L) & (n - 1);
+  TA lf[4] = {y[4], y[6], y[8], y[10]};  // plane x = i: ey(k), ey(k+1), ez(j), ez(j+1)
+  const TA rt[4] = {y[5], y[7], y[9], y[11]};
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    const TA v = __shfl_up_sync(0xffffffffu, rt[t], 1);
+    if (i > 0) lf[t] += v;
+  }
+  if (i == n - 1) {
+    atomicAdd(out + e[5], (TO)rt[0]);
+    atomicAdd(out + e[7], (TO)rt[1]);
+    atomicAdd(out + e[9], (TO)rt[2]);
+    atomicAdd(out + e[11], (TO)rt[3]);
+  }
+  atomicAdd(out + e[4], (TO)lf[0]);
+  atomicAdd(out + e[6], (TO)lf[1]);
+  // plane y = j: ex(k), ex(k+1), ez(i) and the same edges of plane y = j+1
+  TA bt[3] = {y[0], y[2], lf[2]};
+  const TA tp[3] = {y[1], y[3], lf[3]};
+  const bool below = lane >= n && j > 0;
+  const bool above = lane + n < 32 && j < n - 1;
+#pragma unroll
+  for (int t = 0; t < 3; ++t) {
+    const TA v = __shfl_up_sync(0xffffffffu, tp[t], n);
+    if (below) bt[t] += v;
+  }
+  if (!above) {
+    atomicAdd(out + e[1], (TO)tp[0]);
+    atomicAdd(out + e[3], (TO)tp[1]);
+    atomicAdd(out + e[10], (TO)tp[2]);
+  }
+  atomicAdd(out + e[0], (TO)bt[0]);
+  atomicAdd(out + e[2], (TO)bt[1]);
+  atomicAdd(out + e[8], (TO)bt[2]);
+}
+
 template <typename VT>
 __device__ __forceinline__ void warp_publish(NRShared &sh, int slot, VT v) {
 #pragma unroll
@@ -1025,8 +1070,7 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
 #pragma unroll
         for (int m = 0; m <= l; ++m) y[m] += Lv(l * (l + 1) / 2 + m) * a;
       }
-#pragma unroll
-      for (int m = 0; m < 12; ++m) atomicAdd(zt + e[m], y[m]);
+      edge_scatter_merged<T, T>(zt, y, e, c, g.L);  // n >= 4 (multilevel items): full warps of x-rows
     }
     return qf;
   };
@@ -1238,6 +1282,10 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
       const double outer = (kMixed ? 0.1 : 0.01) * tol_abs / fmax(sqrt(rnorm2), 1e-300);
       const T target = (T)((kMixed ? fmax(prm.inner_rtol, outer) : outer) * (double)eta0);
       bool active = gam > T(0) && isfinite(gam);
+      // patch path: the 1 / a1 scale of w_j and the x update of iteration j
+      // are applied in the Lanczos pass of iteration j + 1 (pending)
+      bool pending = false;
+      T p_step = T(0), p_ia1 = T(0);
       for (int iter = 0; active && iter < prm.max_iter; ++iter) {
         // ---- phase 1
         T dpart = T(0);
@@ -1271,16 +1319,34 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
           // with the patch edge block z~_{j+1} needs a cell pass, so z~_j is
           // consumed here: the direction w_j = (z~_j / g_j - a3 w_{j-2} - a2 w_{j-1}) / a1
           // is formed up to its 1 / a1 (which needs gamma_{j+1}) in w_{j-2}'s slot,
-          // and zt takes the face part of z~_{j+1} (edges 0, accumulated by the pass)
+          // and zt takes the face part of z~_{j+1} (edges 0, accumulated by the
+          // pass). The pending scale of w_{j-1} (still unscaled in its slot) and
+          // x += c eta w_{j-1} of the previous iteration are applied on the way.
+          const T sc = pending ? p_ia1 : T(1), st = pending ? p_step : T(0);
           if constexpr (kMixed) {
             const float4 *pd4 = reinterpret_cast<const float4 *>(pd);
             const float4 *vc4 = reinterpret_cast<const float4 *>(vc);
             float4 *vp4 = reinterpret_cast<float4 *>(vp);
             float4 *zt4 = reinterpret_cast<float4 *>(zt);
             float4 *wo4 = reinterpret_cast<float4 *>(wo);
-            const float4 *wc4 = reinterpret_cast<const float4 *>(wc);
+            float4 *wc4 = reinterpret_cast<float4 *>(wc);
+            float4 *xk4 = reinterpret_cast<float4 *>(xk);
             for (int q = tid; q < (int)(Np / 4); q += NT) {
-              const float4 pv = pd4[q], b = vp4[q], c = vc4[q], z = zt4[q], a = wo4[q], bw = wc4[q];
+              const float4 pv = pd4[q], b = vp4[q], c = vc4[q], z = zt4[q], a = wo4[q];
+              float4 bw = wc4[q];
+              if (pending) {
+                float4 x = xk4[q];
+                bw.x *= sc;
+                bw.y *= sc;
+                bw.z *= sc;
+                bw.w *= sc;
+                x.x += st * bw.x;
+                x.y += st * bw.y;
+                x.z += st * bw.z;
+                x.w += st * bw.w;
+                wc4[q] = bw;
+                xk4[q] = x;
+              }
               const bool face = 4 * q >= g.NE;
               const float sg = face ? -1.0f : 1.0f;
               auto lane = [&](float pdd, float bd, float cd) {
@@ -1312,12 +1378,19 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
                 vn = (b - delta * vc[d]) * gi_c;
               }
               vp[d] = vn;
-              wo[d] = zt[d] * gi_c - a3 * wo[d] - a2 * wc[d];
+              T bw = wc[d];
+              if (pending) {
+                bw *= sc;
+                wc[d] = bw;
+                xk[d] += st * bw;
+              }
+              wo[d] = zt[d] * gi_c - a3 * wo[d] - a2 * bw;
               const T nz = d < g.NE ? T(0) : (T)pdd * vn;
               zt[d] = nz;
               gpart += nz * vn;
             }
           }
+          pending = false;
           __syncthreads();
           gpart += patch_pass(vp);
         } else if constexpr (kMixed) {  // 4 DoFs per access; face quads start at NE (NE % 4 == 0 for n >= 4)
@@ -1365,23 +1438,12 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
         const T step = cn * eta, ia1 = T(1) / a1;
         // ---- phase 3 (pre: the prefill scale gamma_{j+1}^2 / g_j of v~_j's slot)
         const T pre = gnew * gnew * gi_c;
-        if (epatch) {  // w_j = w~ / a1, x += c eta w_j, faces of z~_{j+1} += P_{n/2} y, prefill
+        if (epatch) {  // faces of z~_{j+1} += P_{n/2} y, prefill; w_j / x are pending
           if constexpr (kMixed) {
             float4 *vc4 = reinterpret_cast<float4 *>(vc);
             float4 *zt4 = reinterpret_cast<float4 *>(zt);
-            float4 *wo4 = reinterpret_cast<float4 *>(wo);
-            float4 *xk4 = reinterpret_cast<float4 *>(xk);
             for (int q = tid; q < (int)(Np / 4); q += NT) {
-              const float4 a = wo4[q], vo = vc4[q];
-              float4 x = xk4[q], wn;
-              wn.x = a.x * ia1;
-              wn.y = a.y * ia1;
-              wn.z = a.z * ia1;
-              wn.w = a.w * ia1;
-              x.x += step * wn.x;
-              x.y += step * wn.y;
-              x.z += step * wn.z;
-              x.w += step * wn.w;
+              const float4 vo = vc4[q];
               const bool face = 4 * q >= g.NE;
               if (face) {
                 float4 nz = zt4[q];
@@ -1393,19 +1455,17 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
                 zt4[q] = nz;
               }
               const float ps = face ? (float)pre : -(float)pre;  // -S pre
-              wo4[q] = wn;
-              xk4[q] = x;
               vc4[q] = make_float4(ps * vo.x, ps * vo.y, ps * vo.z, ps * vo.w);
             }
           } else {
             for (int d = tid; d < (int)Np; d += NT) {
-              const T wn = wo[d] * ia1;
-              wo[d] = wn;
-              xk[d] += step * wn;
               if (d >= g.NE) zt[d] += ml_code_prolong(ml_codes[d - g.NE], ml_y, m2);
               vc[d] = (d < g.NE ? -pre : pre) * vc[d];
             }
           }
+          pending = true;
+          p_step = step;
+          p_ia1 = ia1;
         } else if constexpr (kMixed) {
           const float4 *pd4 = reinterpret_cast<const float4 *>(pd);
           const float4 *vp4 = reinterpret_cast<const float4 *>(vp);
@@ -1474,6 +1534,8 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
         ss = sn;
         if (fabs(eta) <= target || gnew == T(0)) active = false;
       }
+      if (pending)  // the last direction (unscaled, in wc after the swap) and its x update
+        for (int d = tid; d < (int)Np; d += NT) xk[d] += p_step * (wc[d] * p_ia1);
       __syncthreads();
     } else {
       // ---------------- MINRES on A_II d = r, precision T ----------------
