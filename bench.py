@@ -468,10 +468,10 @@ def e2e_run(wl, lo, hi, local, stream, barrier, steps):
 # (profiles/nedrt_solve_kernel_L3_traffic.md), 358.2 MB / 256 cells; traffic grows with the cells.
 NEDRT_L3_TRAFFIC_PER_CELL = 358.2e6 / 256
 # The same for depth-4 cells (global MINRES workspace): ncu DRAM bytes of
-# `bench.py --probe nedrt_depth4_8cells` (one wave: 144 items), 22.63 GB read + 43.86 GB written
+# `bench.py --probe nedrt_depth4_8cells` (one wave: 144 items), 27.01 GB read + 48.86 GB written
 # per 8 cells (profiles/nedrt_solve_kernel_L4_8cells.md); every item streams its own workspace, so
 # the traffic grows with the items.
-NEDRT_L4_TRAFFIC_PER_CELL = (22.63e9 + 43.86e9) / 8
+NEDRT_L4_TRAFFIC_PER_CELL = (27.01e9 + 48.86e9) / 8
 
 
 def roofline(wl, lo, hi, solve_ms, setup_ms, gal_ms, rep, kind):
@@ -487,9 +487,9 @@ def roofline(wl, lo, hi, solve_ms, setup_ms, gal_ms, rep, kind):
         nrhs, coef_bytes = 18, 7 * 8
         # FP32 flops of one MINRES iteration of one item: tensor-product cell operator
         # fused with the delta dot product (~330 per fine cell) + recurrences (~20 per DoF)
-        # + the cell-patch edge block on depth >= 2 (L^-1 v and L^-T t, 2 x 78 FMAs, and
-        # |t|^2: ~324 per fine cell)
-        flops_iter = (330 + np.where(n >= 4, 324, 0)) * n ** 3 + 20 * (3 * n * (n + 1) ** 2 + 3 * n * n * (n + 1))
+        # + the cell-patch edge block of the global-workspace items (depth 4, mixed: L^-1 v and
+        # L^-T t, 2 x 78 FMAs, and |t|^2: ~324 per fine cell)
+        flops_iter = (330 + np.where(n >= 16, 324, 0)) * n ** 3 + 20 * (3 * n * (n + 1) ** 2 + 3 * n * n * (n + 1))
     elif wl.kind == "qned":
         ndof = int(np.sum((n + 1) ** 3 + 3 * n * (n + 1) ** 2))
         nrhs, coef_bytes = 20, 7 * 8

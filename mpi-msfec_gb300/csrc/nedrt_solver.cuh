@@ -1424,7 +1424,10 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
           }
         }
         warp_publish<T>(sh, 1, gpart);
-        __syncthreads();
+        // the coarse step reads v~_{j+1}: complete after the Lanczos pass's
+        // barrier on the patch path (the patch pass only adds to zt's edges and
+        // the coarse step's own barriers publish slot 1), else after this one
+        if (!epatch) __syncthreads();
         // ---- coarse step (reads v~_{j+1}, now in vp)
         const T gc = ml_coarse<T, NW>(sh, g, vp, ml_rr, ml_y, ml_wk, ml_dat, ml_lcodes);
         const T gnew = sqrt(fmax(slot_total<T, NW>(sh, 1) + gc, T(0)));
