@@ -303,26 +303,28 @@ def time_oracle(wl, sel, nthreads):
             pool.map(worker, chunks)
             dt = time.perf_counter() - t0
         nb = {"nedrt": 18, "qned": 20, "rtdq": 6}[wl.kind]
-        desc = f"sparse direct (SuperLU, one factorisation per cell, {nb} solves), process per core"
+        desc = f"SuperLU per cell ({nb} solves), process per core"
     work = int(np.sum(wl.per_cell_work()[sel]))
     return work / dt, dt, f"{len(sel)} of {len(wl.cells)} cells (every depth); {desc}; {dt:.1f} s"
 
 
 # --------------------------------------------------------------------------- GPU
 def shape_names(kind, ncand, sms=152):
-    """Names of msfec_autotune's candidates, in its order (include/msfec_cuda.h)."""
+    """Short names of msfec_autotune's candidates, in its order (include/msfec_cuda.h):
+    Q1 fused / split launch; CTAs x threads per CTA, "+stage" = the apply's coefficient
+    tiles staged by bulk copies."""
     if ncand <= 1:
         return ["default"]
     if kind == "q1":
-        return ["fused cluster launch", "split cluster + non-cluster launches"]
+        return ["fused", "split"]
     if kind in ("qned", "rtdq") or (kind == "nedrt" and ncand == 2):
-        return ["1 x 512-thread CTA per SM", "2 x 256-thread CTAs per SM"]
+        return [f"{sms}x512", f"{2 * sms}x256"]
     ctas = [sms] + [max(1, sms * q // 8) for q in (7, 6, 5, 4)]
-    out = [f"{c} x 512-thread CTAs, plain coefficient loads" for c in ctas]
+    out = [f"{c}x512" for c in ctas]
     if ncand >= 10:
-        out += [f"{c} x 512-thread CTAs, coefficient tiles staged by bulk copies" for c in ctas]
+        out += [f"{c}x512+stage" for c in ctas]
     if ncand == 11:
-        out.append(f"{2 * sms} x 256-thread CTAs (2 per SM), plain coefficient loads")
+        out.append(f"{2 * sms}x256")
     return out
 
 
@@ -383,7 +385,7 @@ def gpu_run(wl, lo, hi, precision, steps, warmup, local, stream, barrier, tune_i
             c0, c1, kind = sh["a"][:f], None if sh["r"] is None else sh["r"][:f], msfec.KIND_Q1
         choice, ncand, times = h.autotune(kind, cells[:k], c0, c1, wl.load)
         shapes = shape_names(wl.kind, ncand)
-        tune_info.update({"sample_cells": k, "shapes": shapes, "times_ms": [round(t, 2) for t in times],
+        tune_info.update({"cells": k, "ms": dict(zip(shapes, [round(t, 1) for t in times])),
                           "choice": shapes[choice] if choice < len(shapes) else choice})
     for i in range(warmup):
         build(*batches[i % len(batches)])
@@ -558,9 +560,8 @@ def adjoint_timing(local, stream, steps=3):
     recompute = time.perf_counter() - t0
     h.close()
     f, b = float(np.median(fw)), float(np.median(bw))
-    return {"workload": "q1_lognormal_coarse8^3_L4, 512 observation points", "forward_ms": f * 1e3,
-            "backward_ms": b * 1e3, "bwd_over_fwd": b / f, "backward_recompute_basis_ms": recompute * 1e3,
-            "note": "host-buffer C ABI for both; backward = 2 adjoint local problems per cell + gradient kernel"}
+    return {"forward_ms": f * 1e3, "backward_ms": b * 1e3, "bwd_over_fwd": b / f,
+            "backward_recompute_basis_ms": recompute * 1e3}
 
 
 def adjoint_timing_nedrt(local, stream, wl=None, lo=0, hi=None, steps=2):
@@ -575,12 +576,12 @@ def adjoint_timing_nedrt(local, stream, wl=None, lo=0, hi=None, steps=2):
     import workloads
     if wl is None:
         cells, ainv6, bdiv, load = workloads.nedrt_tensor(m=8, depth=3, seed=2)
-        name = "nedrt_tensor_coarse8^3_L3"
+        name = "8^3 x L3"
     else:
         hi = len(wl.cells) if hi is None else hi
         f0, f1 = int(wl.foff[lo]), int(wl.foff[hi])
         cells, ainv6, bdiv, load = wl.cells[lo:hi], wl.ainv6[f0:f1], wl.bdiv[f0:f1], wl.load
-        name = f"{wl.cfg['workload']} cells [{lo}, {hi})"
+        name = f"[{lo}, {hi})"
     rng = np.random.default_rng(7)
     npts = 512
     cell_of = rng.integers(0, len(cells), npts).astype(np.int32)
@@ -606,9 +607,8 @@ def adjoint_timing_nedrt(local, stream, wl=None, lo=0, hi=None, steps=2):
         br.append(t3 - t2)
     h.close()
     f, b, r = float(np.median(fw)), float(np.median(bw)), float(np.median(br))
-    return {"workload": f"{name}, 512 observation points", "forward_ms": f * 1e3,
-            "backward_recompute_basis_ms": r * 1e3, "bwd_recompute_over_fwd": r / f,
-            "backward_reuse_basis_ms": b * 1e3, "bwd_reuse_over_fwd": b / f}
+    return {"cells": name, "forward_ms": f * 1e3, "backward_recompute_basis_ms": r * 1e3,
+            "bwd_recompute_over_fwd": r / f, "backward_reuse_basis_ms": b * 1e3, "bwd_reuse_over_fwd": b / f}
 
 
 def _r(x, digits=4):
@@ -747,9 +747,7 @@ def run_ours(args):
             ex = measure(Workload(name), max(3, min(args.steps, 5)), 3, 0 if args.skip_fp64 else 2, False)
             rf = ex["roofline"]
             extras[name] = {"value": ex["value"], "ms_per_step": ex["ms_per_step"], "converged": ex["converged"],
-                            "max_iterations": ex["max_iterations"], "work_dof_rhs": ex["work_dof_rhs"],
-                            "solve_launch_ms": rf["launch_ms"], "hbm_frac": rf["frac"],
-                            "fp32_tflops": rf["onchip"]["achieved_tflops"],
+                            "max_iterations": ex["max_iterations"], "fp32_tflops": rf["onchip"]["achieved_tflops"],
                             "autotune": ex["autotune"].get("choice")}
             if "fp64_path" in ex:
                 extras[name]["fp64_value"] = ex["fp64_path"]["value"]
@@ -778,11 +776,10 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
             "config": dict(wl.cfg, batch_cells=wl.batch_cells, batches=nb,
-                           step=(f"one batch of {wl.batch_cells} cells, cycling through the {nb} batches"
-                                 if nb > 1 else "the whole batch"),
-                           precision="mixed (FP32 Krylov + FP64 refinement)",
-                           l2="inputs + basis exceed L2 (129 MB): Phi and K*Phi are written fresh every step",
-                           parallelism=f"{world} GPU(s), the whole workload on each (weak)"),
+                           step=(f"1 batch of {wl.batch_cells} cells, {nb} batches cycled" if nb > 1 else "whole batch"),
+                           precision="FP32 Krylov in FP64 refinement",
+                           l2="inputs, outputs > L2; Phi, K*Phi written each step",
+                           parallelism=f"{world} GPU(s), whole workload each (weak)"),
             "roofline": head["roofline"], "cpu_baseline": cpu,
             "e2e": {"value": e2e_work * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
