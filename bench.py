@@ -237,12 +237,13 @@ def _nedrt_oracle_chunk(args):
 def cpu_sample(wl, target_s, nthreads, lo=0, hi=None):
     """Stratified sample of cells [lo, hi) (every depth represented) sized for
     ~target_s of wall time on nthreads workers (at least one cell per worker
-    when the cells are that many)."""
+    when the cells are that many; cells of a second or more each, whole rounds
+    of one cell per worker, so that no round runs on a few cores)."""
     hi = len(wl.cells) if hi is None else hi
     depth = wl.cells["depth"][lo:hi]
     depths = sorted(set(int(d) for d in depth))
     if wl.kind in ("nedrt", "qned"):
-        per_cell = {1: 5e-3, 2: 3e-2, 3: 0.6, 4: 7.0}
+        per_cell = {1: 5e-3, 2: 3e-2, 3: 0.6, 4: 10.0}
     elif wl.kind == "rtdq":
         per_cell = {1: 2e-3, 2: 2e-2, 3: 0.25, 4: 5.0}
     else:
@@ -252,6 +253,8 @@ def cpu_sample(wl, target_s, nthreads, lo=0, hi=None):
     for d in depths:
         cand = lo + np.where(depth == d)[0]
         k = int(max(1, min(len(cand), max(per_depth / per_cell.get(d, 1.0), nthreads / len(depths)))))
+        if per_cell.get(d, 1.0) >= 1.0 and len(cand) >= nthreads:  # whole rounds of one cell per worker
+            k = max(nthreads, int(round(k / nthreads)) * nthreads)
         idx.extend(cand[np.round(np.linspace(0, len(cand) - 1, k)).astype(int)].tolist())
     return np.array(sorted(set(idx)))
 
