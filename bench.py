@@ -470,8 +470,8 @@ def e2e_run(wl, lo, hi, local, stream, barrier, steps):
 
 # DRAM bytes per coarse cell of one Ned_RT depth-3 solve launch (mixed precision, multilevel
 # preconditioner): ncu dram__bytes_read.sum + dram__bytes_write.sum of `bench.py --probe nedrt_256cells`
-# (profiles/nedrt_solve_kernel_L3_traffic.md), 358.2 MB / 256 cells; traffic grows with the cells.
-NEDRT_L3_TRAFFIC_PER_CELL = 358.2e6 / 256
+# (profiles/nedrt_solve_kernel_L3_traffic.md), 371.0 MB / 256 cells; traffic grows with the cells.
+NEDRT_L3_TRAFFIC_PER_CELL = 371.0e6 / 256
 # The same for depth-4 cells (global MINRES workspace): ncu DRAM bytes of
 # `bench.py --probe nedrt_depth4_8cells` (one wave: 144 items), 27.01 GB read + 48.86 GB written
 # per 8 cells (profiles/nedrt_solve_kernel_L4_8cells.md); every item streams its own workspace, so
