@@ -107,9 +107,10 @@ __host__ __device__ inline size_t nr_workspace_floats(int n, int tsize) {
 // Per-cell shared data of the global workspace (NRParams::prep), 64-float
 // aligned parts: the preconditioner diagonal over the padded DoFs, 8 float
 // coefficients per fine cell, and the cell-patch factors of the edge
-// preconditioner (kNRPatchFloats 32-bit words per fine cell, structure of
-// arrays: word t of fine cell c at t * n^3 + c).
-constexpr int kNRPatchFloats = 39;  // L^-1 of a 12 x 12 Cholesky factor: 78 FP16 entries, 2 per word
+// preconditioner (kNRPatchFloats 32-bit words per fine cell in 16-byte groups,
+// structure of arrays by group: word t of fine cell c at (t / 4 * n^3 + c) * 4
+// + t % 4).
+constexpr int kNRPatchFloats = 40;  // L^-1 of a 12 x 12 Cholesky factor: 78 FP16 entries, 2 per word, 1 pad word
 __host__ __device__ inline size_t nr_prep_floats(int n) {
   int NEx, NFx, NE, NF;
   nr_counts(n, NEx, NFx, NE, NF);

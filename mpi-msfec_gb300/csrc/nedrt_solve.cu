@@ -782,17 +782,20 @@ __global__ void __launch_bounds__(kNRThreads) nr_cell_prep_kernel(const NRCell *
       // pairs; X = L^-T L^-1 is then symmetric positive definite whatever the
       // rounding of the stored entries (a Gram matrix). Dirichlet edges have
       // identity rows and columns in M and a zero v, so they add nothing.
-      __half2 *X2 = reinterpret_cast<__half2 *>(X);
+      __half2 *X2 = reinterpret_cast<__half2 *>(X);  // word w of cell c at (w / 4 * nc + c) * 4 + w % 4
       float pend = 0.0f;
       int t = 0;
       for (int l = 0; l < 12; ++l)
         for (int m = 0; m <= l; ++m, ++t) {
           const float v = (float)Mb[l][m];
-          if (t & 1)
-            X2[(size_t)(t >> 1) * nc + c] = __floats2half2_rn(pend, v);
-          else
+          if (t & 1) {
+            const int w = t >> 1;
+            X2[((size_t)(w >> 2) * nc + c) * 4 + (w & 3)] = __floats2half2_rn(pend, v);
+          } else {
             pend = v;
+          }
         }
+      X2[((size_t)9 * nc + c) * 4 + 3] = __floats2half2_rn(0.0f, 0.0f);  // pad word 39
     }
     __syncthreads();  // sh tables are rewritten for the next cell
   }

@@ -1034,7 +1034,8 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
   // z_E += sum_c R_c^T X_c R_c v over the fine cells, X_c = L_c^-T L_c^-1 the
   // inverse of the assembled edge mass restricted to cell c's edges (M_c =
   // L_c L_c^T, Dirichlet edges decoupled; v is zero on them), L_c^-1 stored in
-  // FP16 pairs, row-packed lower triangle, word t of cell c at pX[t * nc + c].
+  // FP16 pairs, row-packed lower triangle, in 16-byte groups: word t of cell c
+  // at pX[(t / 4 * nc + c) * 4 + t % 4].
   // Per cell t = L^-1 v_c, z += L^-T t; returns this thread's share of
   // v_E^T z_E = sum_c |t|^2.
   // Global-workspace items only: compiled out of the shared-memory variants,
@@ -1048,9 +1049,16 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
     for (int c = tid; c < nc; c += NT) {
       int e[12], f[6];
       cell_dofs(g, c, e, f);
-      __half2 Lw[39];  // kept packed: half the registers of the unpacked factor
+      __half2 Lw[40];  // kept packed: half the registers of the unpacked factor
+      const uint4 *pX4 = reinterpret_cast<const uint4 *>(pX);
 #pragma unroll
-      for (int w = 0; w < 39; ++w) Lw[w] = pX[(size_t)w * nc + c];
+      for (int g4 = 0; g4 < 10; ++g4) {  // 16-byte groups of 4 words, coalesced over the warp's cells
+        const uint4 q = pX4[(size_t)g4 * nc + c];
+        Lw[4 * g4] = *reinterpret_cast<const __half2 *>(&q.x);
+        Lw[4 * g4 + 1] = *reinterpret_cast<const __half2 *>(&q.y);
+        Lw[4 * g4 + 2] = *reinterpret_cast<const __half2 *>(&q.z);
+        Lw[4 * g4 + 3] = *reinterpret_cast<const __half2 *>(&q.w);
+      }
       auto Lv = [&](int idx) -> T {
         return (T)((idx & 1) ? __high2float(Lw[idx >> 1]) : __low2float(Lw[idx >> 1]));
       };
