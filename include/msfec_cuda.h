@@ -130,6 +130,14 @@ typedef struct msfec_config {
      and a global slot, or, for Ned_RT cells with a global workspace, two
      global slots per SM). Same results either way. */
   int32_t nedrt_ctas_per_sm;
+  /* Ned_RT cells whose MINRES workspace is in global memory (depth 4, mixed
+     precision, multilevel face preconditioner, one 512-thread CTA per SM, not
+     staged): where the preconditioned Lanczos vector z~ lives. 0 = the default
+     (shared memory), 1 = shared memory after the multilevel region (the
+     operator apply gathers it and the edge patch pass accumulates into it on
+     the SM), 2 = the CTA's global slot with the other Krylov vectors. Same
+     results either way (to the order of the floating-point sums). */
+  int32_t nedrt_zt_place;
 } msfec_config;
 
 typedef enum msfec_q1_coefficient {

@@ -957,8 +957,8 @@ constexpr size_t kNRSplitSmemLimit = 108 * 1024;  // two CTAs per SM (228 KB, mi
 // allocation-free one, so both make the same choice (including the
 // autotuner's) for the same batch.
 struct NRShape {
-  bool split = false, use_smem = false, ml = false, stage = false, prep = false;
-  size_t smem = 0, ws_floats = 0, ml_offset = 0, stage_offset = 0;
+  bool split = false, use_smem = false, ml = false, stage = false, prep = false, zsh = false;
+  size_t smem = 0, ws_floats = 0, ml_offset = 0, stage_offset = 0, zt_offset = 0;
   int grid = 0;
 };
 
@@ -1008,6 +1008,20 @@ msfec_status nr_shape(msfec_handle *h, int nmax, bool fp64, bool want_ml, size_t
     if (off + bytes <= kNRSmemTotalLimit) {
       s.stage = true;
       s.stage_offset = off;
+      s.smem = off + bytes;
+    }
+  }
+  // global workspace with the per-cell data, mixed, multilevel, one 512-thread
+  // CTA per SM, not staged: z~ in shared memory after the multilevel region
+  // (nedrt_zt_place 0 / 1)
+  if (s.prep && s.ml && !fp64 && !s.use_smem && !s.split && !s.stage && h->cfg.nedrt_zt_place != 2) {
+    int NEx, NFx, NE, NF;
+    nr_counts(nmax, NEx, NFx, NE, NF);
+    const size_t off = (s.smem + 127) / 128 * 128;
+    const size_t bytes = ((size_t)NE + NF + 63) / 64 * 64 * 4;
+    if (off + bytes <= kNRSmemTotalLimit) {
+      s.zsh = true;
+      s.zt_offset = off;
       s.smem = off + bytes;
     }
   }
@@ -1143,10 +1157,14 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
   prm.ml_offset = ml_offset;
   prm.stage = shape.stage ? 1 : 0;
   prm.stage_offset = shape.stage_offset;
+  prm.zt_smem = shape.zsh ? 1 : 0;
+  prm.zt_offset = shape.zt_offset;
   if (h->cfg.verbose)
     fprintf(stderr, "[msfec] nedrt plan: %d cells, %zu items, workspace %zu floats (%s), grid %d, %s, %s\n", ncells,
             items.size(), ws_floats,
-            split ? (use_smem ? "split, 2 CTAs/SM" : "global, 2 CTAs/SM") : (use_smem ? "shared" : "global"), grid,
+            split ? (use_smem ? "split, 2 CTAs/SM" : "global, 2 CTAs/SM")
+                  : (use_smem ? "shared" : (shape.zsh ? "global, z~ shared" : "global")),
+            grid,
             fp64 ? "fp64" : "mixed", ml ? "multilevel" : "diagonal");
   msfec_load ld;
   if (load) {
@@ -1491,7 +1509,8 @@ msfec_status msfec_create(msfec_handle **out, const msfec_config *cfg) {
   if (!(c.rtol > 0.0) || !(c.inner_rtol > 0.0) || c.inner_rtol >= 1.0 || c.max_iter < 1 || c.max_refine < 1 ||
       !(c.nedrt_rtol > 0.0) || c.q1_launch < 0 || c.q1_launch > 2 || c.nedrt_precond < 0 || c.nedrt_precond > 2 ||
       c.q1_coefficient < MSFEC_Q1_COEF_SCALAR || c.q1_coefficient > MSFEC_Q1_COEF_GAUSS || c.nedrt_stage < 0 ||
-      c.nedrt_stage > 1 || c.nedrt_ctas_per_sm < 0 || c.nedrt_ctas_per_sm > 2)
+      c.nedrt_stage > 1 || c.nedrt_ctas_per_sm < 0 || c.nedrt_ctas_per_sm > 2 || c.nedrt_zt_place < 0 ||
+      c.nedrt_zt_place > 2)
     return MSFEC_ERROR_INVALID_ARGUMENT;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || c.device < 0 || c.device >= ndev) return MSFEC_ERROR_CUDA;
@@ -2861,6 +2880,8 @@ msfec_status msfec_nedrt_build_noalloc(msfec_handle *h, int32_t ncells, const ms
   prm.ml_offset = shape.ml_offset;
   prm.stage = shape.stage ? 1 : 0;
   prm.stage_offset = shape.stage_offset;
+  prm.zt_smem = shape.zsh ? 1 : 0;
+  prm.zt_offset = shape.zt_offset;
   if (h->timing) MSFEC_CUDA_TRY(h, record_start(h, st));
   if (ml)
     MSFEC_CUDA_TRY(h, nedrt_ml_setup_launch(d_cells, ncells, d_ainv6, d_bdiv, d_coarse,

@@ -78,6 +78,11 @@ struct NRParams {
   // bulk copies into the dynamic shared memory at this byte offset (32 KB)
   int stage;
   size_t stage_offset;
+  // global workspace, mixed precision, multilevel with prep: z~ (the apply's
+  // operand, the patch pass's accumulator) in the dynamic shared memory at this
+  // byte offset instead of the slot; the slot's other vectors stay in L2
+  int zt_smem;
+  size_t zt_offset;
   double rtol;
   double inner_rtol;
   int max_iter;

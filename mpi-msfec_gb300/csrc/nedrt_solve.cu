@@ -806,15 +806,19 @@ __global__ void __launch_bounds__(kNRThreads) nr_cell_prep_kernel(const NRCell *
 // Per-precision translation units of the persistent solver (one kernel per
 // variant; compiled in parallel). place: 0 = per-CTA global workspace slot,
 // 1 = shared memory (for 256 threads: the split workspace), 2 = global slot
-// with the apply's coefficient tiles staged by bulk copies (FP32 only).
+// with the apply's coefficient tiles staged by bulk copies (FP32 only);
+// nedrt_solve_f32_zs: the global slot with z~ in shared memory (FP32,
+// multilevel, prep).
 cudaError_t nedrt_solve_f64(bool ml, int place, const NRParams &prm, size_t smem, int grid, cudaStream_t st);
 cudaError_t nedrt_solve_f32(bool ml, int place, const NRParams &prm, size_t smem, int grid, cudaStream_t st);
+cudaError_t nedrt_solve_f32_zs(const NRParams &prm, size_t smem, int grid, cudaStream_t st);
 cudaError_t nedrt_solve_f32_256(bool ml, int place, const NRParams &prm, size_t smem, int grid, cudaStream_t st);
 cudaError_t nedrt_solve_f32_256_occupancy(bool ml, int place, size_t smem, int *blocks_per_sm);
 
 // ml: the multilevel variant (prm.coarse set); smem includes its region.
 cudaError_t nedrt_solve_launch(bool fp64, bool ml, const NRParams &prm, size_t smem, int grid, cudaStream_t st) {
   if (fp64) return nedrt_solve_f64(ml, prm.use_smem ? 1 : 0, prm, smem, grid, st);
+  if (prm.zt_smem) return ml ? nedrt_solve_f32_zs(prm, smem, grid, st) : cudaErrorInvalidValue;
   return nedrt_solve_f32(ml, prm.use_smem ? 1 : (prm.stage ? 2 : 0), prm, smem, grid, st);
 }
 

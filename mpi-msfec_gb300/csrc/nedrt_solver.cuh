@@ -899,8 +899,12 @@ __device__ __forceinline__ void nr_float_coefficients(const double *ag, const do
 // STAGE (global workspace, mixed precision): the apply reads each warp's 32
 // cells of coefficients from shared memory, where a bulk copy issued two rounds
 // earlier put them.
-template <typename T, bool SMEM, int NT, bool ML, bool STAGE = false>
+// ZSH (global workspace with prep, mixed precision): z~ lives in the dynamic
+// shared memory at NRParams::zt_offset, so the apply's 18 gathers per fine
+// cell and the patch pass's atomics stay on the SM.
+template <typename T, bool SMEM, int NT, bool ML, bool STAGE = false, bool ZSH = false>
 __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
+  static_assert(!ZSH || (sizeof(T) == 4 && !SMEM && !STAGE), "z~ in shared memory: mixed, global workspace");
   // NT = 256 with the shared workspace (two CTAs per SM, mixed precision):
   // the correction x and the float coefficients live in this CTA's global
   // slot so that the shared part (preconditioner + 6 vectors) fits twice per
@@ -934,7 +938,7 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
   // and the float coefficients are the cell's shared copy, and the slot holds
   // zt, vA, vB, wA, wB, xk, then az (present only when the host sized the slot
   // for the diagonal path).
-  const bool prep = !SMEM && prm.prep != nullptr;
+  const bool prep = ZSH || (!SMEM && prm.prep != nullptr);  // ZSH: z~ is a shared-memory pointer only
   float *gws = prm.scratch + (size_t)blockIdx.x * prm.scratch_floats;  // split workspace only
   float *pd, *cf;
   T *zt, *az, *vA, *vB, *wA, *wB, *xk;
@@ -942,8 +946,10 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
   if (prep) {
     pd = prm.prep + Cc.prep_off;
     cf = pd + Np;
-    zt = reinterpret_cast<T *>(ws);
-    vA = zt + Np;
+    // with ZSH the slot's first Np floats are left unused (the host guarantees
+    // prep for ZSH launches)
+    zt = ZSH ? reinterpret_cast<T *>(nr_dyn_smem + prm.zt_offset) : reinterpret_cast<T *>(ws);
+    vA = reinterpret_cast<T *>(ws) + Np;
     vB = vA + Np;
     wA = vB + Np;
     wB = wA + Np;
@@ -1787,7 +1793,8 @@ __device__ void solve_item(const NRParams &prm, NRShared &sh, int item_id) {
 // each gets its own register allocation (fewer spills than one kernel that
 // branches between them): 1 shared memory (NT = 256: the split workspace of
 // the two-CTAs-per-SM variant), 0 this CTA's global slot, 2 the global slot
-// with the apply's coefficient tiles staged by bulk copies. Keeping only the
+// with the apply's coefficient tiles staged by bulk copies, 3 the global slot
+// with z~ in shared memory. Keeping only the
 // apply's accumulation vector in shared memory for the global placement was
 // measured slower (3917 vs 3659 ms on 512 depth-4 cells): its 108 KB take L1
 // from the apply's scattered global gathers.
@@ -1808,7 +1815,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) nedrt_solve_kernel(NRParams prm)
     __syncthreads();
     const int item = sh.item;
     if (item >= prm.n_items) break;
-    solve_item<T, PLACE == 1, NT, ML, PLACE == 2>(prm, sh, item);
+    solve_item<T, PLACE == 1, NT, ML, PLACE == 2, PLACE == 3>(prm, sh, item);
   }
 }
 

@@ -53,7 +53,8 @@ class Config(ctypes.Structure):
                 ("max_refine", ctypes.c_int32), ("verbose", ctypes.c_int32),
                 ("q1_launch", ctypes.c_int32), ("nedrt_rtol", ctypes.c_double),
                 ("nedrt_precond", ctypes.c_int32), ("q1_coefficient", ctypes.c_int32),
-                ("nedrt_stage", ctypes.c_int32), ("nedrt_ctas_per_sm", ctypes.c_int32)]
+                ("nedrt_stage", ctypes.c_int32), ("nedrt_ctas_per_sm", ctypes.c_int32),
+                ("nedrt_zt_place", ctypes.c_int32)]
 
 
 class Cell(ctypes.Structure):
@@ -210,7 +211,7 @@ class Handle:
 
     def __init__(self, precision=PRECISION_MIXED, device=0, rtol=None, inner_rtol=None,
                  max_iter=None, max_refine=None, verbose=0, nedrt_rtol=None, q1_launch=0, nedrt_precond=0,
-                 q1_coefficient=0, nedrt_stage=None, nedrt_ctas_per_sm=0):
+                 q1_coefficient=0, nedrt_stage=None, nedrt_ctas_per_sm=0, nedrt_zt_place=0):
         L = load_library()
         cfg = Config()
         L.msfec_config_default(ctypes.byref(cfg))
@@ -233,6 +234,7 @@ class Handle:
         if nedrt_stage is not None:
             cfg.nedrt_stage = int(nedrt_stage)
         cfg.nedrt_ctas_per_sm = int(nedrt_ctas_per_sm)
+        cfg.nedrt_zt_place = int(nedrt_zt_place)
         self.cfg = cfg
         h = _vp()
         st = L.msfec_create(ctypes.byref(h), ctypes.byref(cfg))

@@ -234,3 +234,33 @@ def test_patch_edge_preconditioner_matches_diagonal_edges(gpu, precision):
     it0, it2 = out[0][2]["iterations_sum"][0], out[2][2]["iterations_sum"][0]
     print(f"{precision} patch edge block: depth-4 iterations {it0} (diagonal edges {it2})")
     assert it0 < it2
+
+
+def test_zt_in_shared_memory_matches_global_slot(gpu):
+    """Mixed path, depths 4, 3, 2, 1 in one batch (global workspace, multilevel,
+    patch edge block): z~ in shared memory (nedrt_zt_place 1) and in the CTA's
+    global slot (2) give the same K_H, F_H and basis (to the order of the
+    floating-point sums) and the same iteration counts within a few, and the
+    shared-memory placement matches the FP64 oracle on the depth-3 cell."""
+    parts = [workloads.nedrt_tensor(m=1, depth=d, seed=70 + d) for d in (4, 3, 2, 1)]
+    cells = np.concatenate([p[0] for p in parts])
+    ainv6 = np.concatenate([p[1] for p in parts])
+    bdiv = np.concatenate([p[2] for p in parts])
+    load = parts[0][3]
+    out = {}
+    for zp in (2, 1):
+        h = _handle(gpu, "mixed", nedrt_zt_place=zp)
+        KH, FH, rep, status = h.nedrt_build(cells, ainv6, bdiv, load)
+        assert status == gpu.SUCCESS and rep["converged"].all(), (zp, rep)
+        out[zp] = (KH, FH, rep, h.nedrt_basis())
+    for c in range(len(cells)):
+        assert _rel(out[1][0][c], out[2][0][c]) <= 1e-11, c
+        assert _rel(out[1][1][c], out[2][1][c]) <= 1e-11, c
+    assert np.abs(out[1][3] - out[2][3]).max() <= 1e-10 * np.abs(out[2][3]).max()
+    it1, it2 = out[1][2]["iterations_sum"], out[2][2]["iterations_sum"]
+    assert np.abs(it1.astype(np.int64) - it2.astype(np.int64)).max() <= 0.02 * it2.max() + 4, (it1, it2)
+    # the depth-3 cell ran through the same launch (z~ in shared memory, sized for depth 4)
+    f0 = 8 ** 4
+    ref = N.build(cells[1:2], N.sym6_to_ainv(ainv6[f0:f0 + 8 ** 3]), bdiv[f0:f0 + 8 ** 3], load.kind,
+                  list(load.params), want_phi=False)
+    assert _rel(out[1][0][1], ref["KH"][0]) <= TOL_KH
