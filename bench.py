@@ -473,10 +473,10 @@ def e2e_run(wl, lo, hi, local, stream, barrier, steps):
 # (profiles/nedrt_solve_kernel_L3_traffic.md), 371.0 MB / 256 cells; traffic grows with the cells.
 NEDRT_L3_TRAFFIC_PER_CELL = 371.0e6 / 256
 # The same for depth-4 cells (global MINRES workspace): ncu DRAM bytes of
-# `bench.py --probe nedrt_depth4_8cells` (one wave: 144 items), 27.01 GB read + 48.86 GB written
+# `bench.py --probe nedrt_depth4_8cells` (one wave: 144 items), 8.15 GB read + 32.26 GB written
 # per 8 cells (profiles/nedrt_solve_kernel_L4_8cells.md); every item streams its own workspace, so
 # the traffic grows with the items.
-NEDRT_L4_TRAFFIC_PER_CELL = (27.01e9 + 48.86e9) / 8
+NEDRT_L4_TRAFFIC_PER_CELL = (8.15e9 + 32.26e9) / 8
 
 
 def roofline(wl, lo, hi, solve_ms, setup_ms, gal_ms, rep, kind):

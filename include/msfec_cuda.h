@@ -138,6 +138,11 @@ typedef struct msfec_config {
      the SM), 2 = the CTA's global slot with the other Krylov vectors. Same
      results either way (to the order of the floating-point sums). */
   int32_t nedrt_zt_place;
+  /* MIXED: relative residual reduction asked of the FP32 Krylov solve in each
+     FP64 refinement step of the Ned_RT basis solves (the last step asks only
+     what nedrt_rtol still needs); 0 = inner_rtol. Default 3e-6: fewer MINRES
+     iterations in total than 1e-6 for the same final residual. */
+  double nedrt_inner_rtol;
 } msfec_config;
 
 typedef enum msfec_q1_coefficient {

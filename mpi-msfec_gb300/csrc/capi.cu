@@ -942,6 +942,11 @@ msfec_status q1_backward_impl(msfec_handle *h, int ncells, const msfec_cell *cel
   return MSFEC_SUCCESS;
 }
 
+// Inner (FP32 Krylov) tolerance of the Ned_RT basis solves.
+inline double nr_inner_rtol(const msfec_handle *h) {
+  return h->cfg.nedrt_inner_rtol > 0.0 ? h->cfg.nedrt_inner_rtol : h->cfg.inner_rtol;
+}
+
 constexpr int kNRMaxDepth = 4;
 constexpr size_t kNRSmemLimit = 200 * 1024;
 constexpr size_t kNRSmemTotalLimit = 224 * 1024;  // workspace + multilevel region (227 KB minus static)
@@ -1148,7 +1153,7 @@ msfec_status nedrt_build_impl(msfec_handle *h, int ncells, const msfec_cell *cel
   prm.scratch_floats = ws_floats;
   prm.use_smem = use_smem ? 1 : 0;
   prm.rtol = h->cfg.nedrt_rtol;
-  prm.inner_rtol = h->cfg.inner_rtol;
+  prm.inner_rtol = nr_inner_rtol(h);
   prm.max_iter = std::max(h->cfg.max_iter, 8000);  // per refinement step (MINRES, kappa ~ 1e4)
   prm.max_refine = h->cfg.max_refine;
   prm.coarse = ml ? h->nr_coarse.ptr : nullptr;
@@ -1479,6 +1484,7 @@ void msfec_config_default(msfec_config *cfg) {
   cfg->max_refine = 6;
   cfg->verbose = 0;
   cfg->nedrt_rtol = 1e-14;
+  cfg->nedrt_inner_rtol = 3e-6;
 }
 
 const char *msfec_status_string(msfec_status s) {
@@ -1510,7 +1516,7 @@ msfec_status msfec_create(msfec_handle **out, const msfec_config *cfg) {
       !(c.nedrt_rtol > 0.0) || c.q1_launch < 0 || c.q1_launch > 2 || c.nedrt_precond < 0 || c.nedrt_precond > 2 ||
       c.q1_coefficient < MSFEC_Q1_COEF_SCALAR || c.q1_coefficient > MSFEC_Q1_COEF_GAUSS || c.nedrt_stage < 0 ||
       c.nedrt_stage > 1 || c.nedrt_ctas_per_sm < 0 || c.nedrt_ctas_per_sm > 2 || c.nedrt_zt_place < 0 ||
-      c.nedrt_zt_place > 2)
+      c.nedrt_zt_place > 2 || !(c.nedrt_inner_rtol >= 0.0) || c.nedrt_inner_rtol >= 1.0)
     return MSFEC_ERROR_INVALID_ARGUMENT;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || c.device < 0 || c.device >= ndev) return MSFEC_ERROR_CUDA;
@@ -2414,7 +2420,7 @@ msfec_status msfec_nedrt_backward(msfec_handle *h, int32_t ncells, const msfec_c
   // rounding: they stop at max(nedrt_rtol, 1e-11) relative to max(||f||, the
   // cell's floor from nr_adj_rhs_kernel) (the basis solves keep nedrt_rtol).
   prm.rtol = std::max(h->cfg.nedrt_rtol, 1e-11);
-  prm.inner_rtol = h->cfg.inner_rtol;
+  prm.inner_rtol = nr_inner_rtol(h);
   prm.max_iter = std::max(h->cfg.max_iter, 8000);
   prm.max_refine = h->cfg.max_refine;
   // the forward build's multilevel data serves the transposed solves (same cells, same S A S form)
@@ -2873,7 +2879,7 @@ msfec_status msfec_nedrt_build_noalloc(msfec_handle *h, int32_t ncells, const ms
   prm.scratch_floats = slot_bytes / 4;
   prm.use_smem = shape.use_smem ? 1 : 0;
   prm.rtol = h->cfg.nedrt_rtol;
-  prm.inner_rtol = h->cfg.inner_rtol;
+  prm.inner_rtol = nr_inner_rtol(h);
   prm.max_iter = std::max(h->cfg.max_iter, 8000);
   prm.max_refine = h->cfg.max_refine;
   prm.coarse = ml ? d_coarse : nullptr;

@@ -54,7 +54,7 @@ class Config(ctypes.Structure):
                 ("q1_launch", ctypes.c_int32), ("nedrt_rtol", ctypes.c_double),
                 ("nedrt_precond", ctypes.c_int32), ("q1_coefficient", ctypes.c_int32),
                 ("nedrt_stage", ctypes.c_int32), ("nedrt_ctas_per_sm", ctypes.c_int32),
-                ("nedrt_zt_place", ctypes.c_int32)]
+                ("nedrt_zt_place", ctypes.c_int32), ("nedrt_inner_rtol", ctypes.c_double)]
 
 
 class Cell(ctypes.Structure):
@@ -211,7 +211,8 @@ class Handle:
 
     def __init__(self, precision=PRECISION_MIXED, device=0, rtol=None, inner_rtol=None,
                  max_iter=None, max_refine=None, verbose=0, nedrt_rtol=None, q1_launch=0, nedrt_precond=0,
-                 q1_coefficient=0, nedrt_stage=None, nedrt_ctas_per_sm=0, nedrt_zt_place=0):
+                 q1_coefficient=0, nedrt_stage=None, nedrt_ctas_per_sm=0, nedrt_zt_place=0,
+                 nedrt_inner_rtol=None):
         L = load_library()
         cfg = Config()
         L.msfec_config_default(ctypes.byref(cfg))
@@ -235,6 +236,8 @@ class Handle:
             cfg.nedrt_stage = int(nedrt_stage)
         cfg.nedrt_ctas_per_sm = int(nedrt_ctas_per_sm)
         cfg.nedrt_zt_place = int(nedrt_zt_place)
+        if nedrt_inner_rtol is not None:
+            cfg.nedrt_inner_rtol = nedrt_inner_rtol
         self.cfg = cfg
         h = _vp()
         st = L.msfec_create(ctypes.byref(h), ctypes.byref(cfg))
